@@ -1,0 +1,357 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 MLS-MPM substep.
+
+Workload (one GPU): the liquid throughput scene — 1,000,000 weakly compressible
+liquid particles uniform in [0.1,0.5]x[0.1,0.7]x[0.1,0.9], N=32, dt=1e-4, cell
+sort every 16 substeps.  A step is one substep of all particles.
+
+Prints one JSON line (rank 0):
+  value        particle-substeps/s over the timed steps (CUDA events on the
+               launching stream, device time of the substeps; the L2 is flushed
+               by a 512 MiB write between steps, outside the events)
+  roofline     the fused substep kernel: algorithmic bytes (128 B per
+               particle-substep + 32 B per grid node) / its mean launch time,
+               against the measured HBM copy bandwidth
+  e2e          the same metric through the C ABI with pinned host buffers:
+               upload of the state, one substep, readback of the state
+  cpu_baseline the CPU restatement of the reference substep (oracle, FP32,
+               all host threads) on a bounded sample of the same scene
+
+--impl reference: the reference's substep has no CPU implementation and cannot
+be built here, so the arm times the oracle's CPU restatement of it (all host
+threads) on the same scene.
+Multi-GPU (torchrun): a single scene does not shard, so each rank runs an
+independent replica ("replicas only"); value = all ranks' particle-substeps /
+the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+B_ALG = {"liquid": 128.0, "snow": 200.0, "elastic": 200.0, "fixed_corotated": 200.0}
+GRID_BYTES_PER_NODE = 32.0  # one float4 read + one float4 written per grid node and substep
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--warmup", type=int, default=8)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="liquid", choices=["liquid", "snow", "elastic"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    return ap.parse_args()
+
+
+def make_cfg(name):
+    from mpm_gb300 import scenes
+
+    if name == "liquid":
+        return scenes.config_liquid(), "liquid_1M_N32"
+    if name == "snow":
+        return scenes.config_snow(), "snow_500k_N64"
+    return scenes.config_elastic(), "elastic_10k_N16"
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(workload):
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", f"fused_step_{workload}.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch")
+    return None
+
+
+def cpu_baseline(cfg, budget_s=12.0, max_particles=None):
+    """The oracle's FP32 restatement on all host threads over a bounded sample."""
+    import oracle
+
+    mats = [m.derived() for m in cfg["materials"]]
+    st = cfg["state"]
+    n = st["x"].shape[0]
+    if max_particles and n > max_particles:
+        st = {k: v[:max_particles] for k, v in st.items()}
+        n = max_particles
+    threads = oracle.max_threads()
+    t1 = oracle.time_f32(st, cfg["params"], mats, 1, threads)
+    steps = int(max(1, min(50, budget_s / max(t1, 1e-6))))
+    t = oracle.time_f32(st, cfg["params"], mats, steps, threads)
+    return {"value": n * steps / t, "unit": "particle-substeps/s", "cores": threads, "kind": "port",
+            "sample": f"{n} particles x {steps} substeps of the same scene (FP32 oracle, {threads} threads, "
+                      f"{t:.1f} s)"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    from oracle import build as ob
+
+    ob.build_oracle()
+    import oracle
+
+    cfg, workload = make_cfg(args.config)
+    mats = [m.derived() for m in cfg["materials"]]
+    st = cfg["state"]
+    n_full = st["x"].shape[0]
+    threads = oracle.max_threads()
+    # size the per-step sample so the whole run stays within a few minutes
+    t1 = oracle.time_f32(st, cfg["params"], mats, 1, threads)
+    total_steps = args.steps + args.warmup
+    budget = 150.0
+    n = n_full
+    if t1 * total_steps > budget:
+        n = max(10_000, int(n_full * budget / (t1 * total_steps)))
+    sample = {k: v[:n] for k, v in st.items()}
+    for _ in range(args.warmup):
+        oracle.time_f32(sample, cfg["params"], mats, 1, threads)
+    times = [oracle.time_f32(sample, cfg["params"], mats, 1, threads) for _ in range(args.steps)]
+    tot = sum(times)
+    value = n * args.steps / tot
+    line = {
+        "impl": "reference", "metric": "particle-substeps/s", "value": value, "unit": "particle-substeps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload, "particles": n_full, "N": cfg["params"]["N"], "sample_particles": n},
+        "cpu_baseline": {"value": value, "unit": "particle-substeps/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} of {n_full} particles, one substep per step (the reference has no CPU "
+                                   f"substep and does not build here; oracle FP32 restatement)"},
+        "e2e": {"value": value, "unit": "particle-substeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    world, rank, local = dist_setup(args)
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from mpm_gb300 import build
+
+    if rank == 0 or world == 1:
+        build.build()
+    if world > 1:
+        torch.distributed.barrier()
+    from mpm_gb300.simulation import Simulation
+
+    cfg, workload = make_cfg(args.config)
+    n = cfg["state"]["x"].shape[0]
+    N = cfg["params"]["N"]
+    stream = torch.cuda.current_stream()
+    sim = Simulation.from_config(cfg)
+    sim.L.mpm_set_stream(sim.ctx, stream.cuda_stream)
+    sim.upload(cfg["state"])
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        sim.advance(1)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    pure = []
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    launches0 = sim.launches
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        l0 = sim.launches
+        starts[k].record(stream)
+        sim.advance(1)
+        ends[k].record(stream)
+        pure.append(sim.launches - l0 == 1)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = sim.launches - launches0
+    clocks = sampler.stop()
+    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    sim.sync()
+    dev_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([dev_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    ms_per_step = dev_ms / args.steps
+    value = world * n * args.steps / (dev_ms * 1e-3)
+
+    fused_ms = [m for m, p in zip(ms, pure) if p]
+    kernel_ms = statistics.mean(fused_ms) if fused_ms else ms_per_step
+    peak, peak_kind = measured_peaks()
+    bytes_per_launch = B_ALG[cfg["materials"][0].name if cfg["materials"][0].name in B_ALG else "liquid"] * n \
+        + GRID_BYTES_PER_NODE * N ** 3
+    achieved = bytes_per_launch / (kernel_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": profile_traffic(workload), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "kernel": "mpm::step_kernel (fused G2P + P2G)", "kernel_ms": kernel_ms,
+                "bytes_per_launch": bytes_per_launch}
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(sim, cfg, args.e2e_steps, world)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(cfg, max_particles=None if args.config != "liquid" else 1_000_000)
+    sim.close()
+    if rank == 0:
+        line = {
+            "metric": "particle-substeps/s", "value": value, "unit": "particle-substeps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload, "particles": n, "N": N, "material": cfg["materials"][0].name,
+                       "dt": cfg["params"]["dt"], "sort_interval": cfg["params"].get("sort_interval", 0),
+                       "l2": "flushed between steps (512 MiB write, outside the timed events)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+            "wall_s_timed_region": wall,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(sim, cfg, steps, world):
+    """Per step through the C ABI: pinned host state -> device, one substep,
+    device -> pinned host state; wall clock around the blocking calls."""
+    import ctypes
+
+    import torch
+
+    st = cfg["state"]
+    n = st["x"].shape[0]
+    liquid = cfg["materials"][0].kind == 3
+    fields = {"x": 3, "v": 3, "C": 9, "Jp": 1} if liquid else {"x": 3, "v": 3, "C": 9, "F": 9, "Jp": 1}
+    host = {k: torch.from_numpy(np.ascontiguousarray(np.asarray(st[k], np.float32).reshape(n, w))).pin_memory()
+            for k, w in fields.items()}
+    out = {k: torch.empty((n, w), dtype=torch.float32).pin_memory() for k, w in fields.items()}
+    P = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+    L = sim.L
+    times = []
+    for k in range(steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = L.mpm_upload_soa(sim.ctx, n, P(host["x"]), P(host["v"]), P(host["C"]), P(host.get("F")),
+                              P(host["Jp"]), None)
+        rc |= L.mpm_substep(sim.ctx, 1)
+        rc |= L.mpm_download_soa(sim.ctx, P(out["x"]), P(out["v"]), P(out["C"]), P(out.get("F")), P(out["Jp"]),
+                                 None)
+        t1 = time.perf_counter()
+        if rc != 0:
+            raise RuntimeError("e2e C ABI call failed")
+        if k > 0:
+            times.append(t1 - t0)
+    per = statistics.median(times)
+    nbytes = 4 * n * sum(fields.values())
+    return {"value": world * n / per, "unit": "particle-substeps/s", "h2d_bytes_per_step": nbytes,
+            "d2h_bytes_per_step": nbytes, "ms_per_step": 1e3 * per,
+            "path": "mpm_upload_soa + mpm_substep(1) + mpm_download_soa, pinned host buffers"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+/*
+ * mpm_gb300 — C ABI of the GB300 (sm_103a) MLS-MPM substep.
+ *
+ * Drop-in boundary for the substep of kekeblom/mpm.  The reference has no C ABI:
+ * its host class `Simulation` (include/mpm.cuh:44-106, src/mpm.cu:180-329) owns
+ * device memory, uploads an AoS particle array and launches three kernels per
+ * `advance()`.  Each entry point below names the reference member it replaces.
+ *
+ * Conventions
+ *   - Every call returns an mpm_status (0 = MPM_OK).  The message of the last
+ *     failure on a context is available from mpm_last_error().
+ *   - The context owns every device buffer; the caller owns host buffers.
+ *   - Work is enqueued on the context's stream (mpm_set_stream, default: a
+ *     stream created by mpm_create).  Calls on one context are not re-entrant;
+ *     use one context per host thread.
+ *   - Host particle arrays are per-particle interleaved: x[3n], v[3n],
+ *     C[9n] and F[9n] row-major (C[9p + 3r + c]), Jp[n], mat[n] (material index).
+ *   - Kernels never trap: a non-finite particle, a bad index or an expired wait
+ *     sets a device status word that mpm_sync() returns (MPM_ERR_STATE /
+ *     MPM_ERR_TIMEOUT).
+ */
+#ifndef MPM_GB300_H
+#define MPM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mpm_status {
+  MPM_OK = 0,
+  MPM_ERR_INVALID = 1,     /* bad argument or call order */
+  MPM_ERR_CUDA = 2,        /* CUDA runtime error (message in mpm_last_error) */
+  MPM_ERR_STATE = 3,       /* device status word: non-finite particle / index out of range */
+  MPM_ERR_TIMEOUT = 4,     /* a bounded device-side wait expired */
+  MPM_ERR_NOMEM = 5,       /* device allocation failed */
+  MPM_ERR_UNSUPPORTED = 6  /* configuration not supported by this build */
+} mpm_status;
+
+/* Material kinds. MMSnow is the only model the reference instantiates
+ * (include/mpm.cuh:25); "elastic" and the reference's "liquid" are MMSnow with
+ * hardening 0 and clamps [0, 1e30] / [0.975, 0.975] (scenes/*.toml). */
+enum {
+  MPM_MAT_SNOW = 0,            /* MMSnow            include/MaterialModel.cuh:67-116 */
+  MPM_MAT_FIXED_COROTATED = 1, /* MMFixedCorotated  include/MaterialModel.cuh:40-62 */
+  MPM_MAT_JELLY = 2,           /* MMJelly           include/MaterialModel.cuh:119-150 */
+  MPM_MAT_LIQUID = 3           /* weakly compressible liquid, P F^T = K (J-1) J I,
+                                  J <- J det(I + dt C), F = J^(1/3) I (not in the reference) */
+};
+
+/* Boundary rule of the grid operation. */
+enum {
+  MPM_BOUNDARY_REF_FRACTION = 0,  /* src/mpm.cu:92-105: idx/N < 0.05 or > 0.95 sticky on
+                                     x, z and the top; separating floor (v_y >= 0) */
+  MPM_BOUNDARY_STICKY_CELLS = 1,  /* all six walls sticky within boundary_cells cells */
+  MPM_BOUNDARY_SEPARATE_CELLS = 2 /* reference structure with a cell-count thickness */
+};
+
+#define MPM_MAX_MATERIALS 16
+
+/* Simulation parameters.  dt and N are the reference's CLI options
+ * (include/options.h:19-21, SimulationParameters in include/TransferScheme.h:6-29). */
+typedef struct mpm_params {
+  float dt;               /* substep length (reference default 1e-4) */
+  uint32_t N;             /* grid cells per dimension over the unit cube */
+  float gravity;          /* y acceleration; the reference hard-codes -9.81 (src/mpm.cu:6) */
+  int32_t boundary_mode;  /* MPM_BOUNDARY_* */
+  int32_t boundary_cells; /* wall thickness for the *_CELLS modes */
+  int32_t g2p_guard;      /* 1: only particles with original index <= N^3 run G2P, as
+                             src/mpm.cu:114 does; 0: every particle (default) */
+  int32_t sort_interval;  /* re-sort particles by cell every k substeps (0 = never) */
+  int32_t check_finite;   /* 1: flag non-finite positions in the device status word */
+} mpm_params;
+
+/* Constructor arguments of MMSnow(volume, density, E, Nu, hardening, lo, hi)
+ * (include/MaterialModel.cuh:74-83); particle_volume is 1/particle-count
+ * (src/main.cu:36).  mu0, lambda0 and the particle mass are derived in float
+ * exactly as the reference constructors do. */
+typedef struct mpm_material {
+  int32_t kind;            /* MPM_MAT_* */
+  float particle_volume;
+  float density;
+  float E;
+  float nu;
+  float hardening;
+  float clamp_lo;          /* plast_clamp_lower */
+  float clamp_hi;          /* plast_clamp_higher */
+  float bulk;              /* MPM_MAT_LIQUID bulk modulus K */
+} mpm_material;
+
+typedef struct mpm_ctx mpm_ctx;
+
+/* Simulation::Simulation + Simulation::initCuda (src/mpm.cu:180-207): allocates the
+ * triple-buffered grid and a stream; particles come with mpm_upload_*. */
+mpm_status mpm_create(const mpm_params* params, mpm_ctx** out);
+/* Simulation::~Simulation (src/mpm.cu:190-195). */
+mpm_status mpm_destroy(mpm_ctx* ctx);
+/* Use a caller-owned cudaStream_t for all subsequent work (NULL: the context's own). */
+mpm_status mpm_set_stream(mpm_ctx* ctx, void* cuda_stream);
+/* Change dt / gravity / boundary / sort interval (N must stay the same). */
+mpm_status mpm_set_params(mpm_ctx* ctx, const mpm_params* params);
+/* The material table the reference copies to the device in initCuda
+ * (src/mpm.cu:199-201); particles index it with their material byte. */
+mpm_status mpm_set_materials(mpm_ctx* ctx, const mpm_material* materials, int32_t count);
+
+/* Simulation::particlesToDevice (src/mpm.cu:278-286), SoA host arrays.  mat may be
+ * NULL (all particles use material 0).  Replaces all particles. */
+mpm_status mpm_upload_soa(mpm_ctx* ctx, int64_t n, const float* x, const float* v, const float* C,
+                          const float* F, const float* Jp, const uint8_t* mat);
+/* Same, from the reference's AoS MLS_APIC_Particle records (104 bytes: u8 material,
+ * Vec x, Vec v, Mat F, Mat C, real Jp; Eigen column-major matrices;
+ * include/types.h:24-35, include/TransferScheme.h:46-54). */
+mpm_status mpm_upload_aos(mpm_ctx* ctx, const void* particles, int64_t n);
+
+/* Simulation::advance (src/mpm.cu:323-329) repeated nsteps times; asynchronous. */
+mpm_status mpm_substep(mpm_ctx* ctx, int32_t nsteps);
+/* Wait for the context's stream and return the device status word. */
+mpm_status mpm_sync(mpm_ctx* ctx);
+
+/* Simulation::particlesToHost / syncDevice (src/mpm.cu:209-211, 288-306): blocking
+ * copy of all particles, in upload order.  Any pointer may be NULL to skip it. */
+mpm_status mpm_download_soa(mpm_ctx* ctx, float* x, float* v, float* C, float* F, float* Jp,
+                            uint8_t* mat);
+mpm_status mpm_download_aos(mpm_ctx* ctx, void* particles);
+
+/* Grid of the last completed substep (N^3 x 4 floats, index N*(N*i+j)+k):
+ * which = 0: after P2G (m v, m); which = 1: after the grid operation, with the
+ * reference's mass slot (1 wherever m > 0, src/mpm.cu:86-88). Blocking. */
+mpm_status mpm_get_grid(mpm_ctx* ctx, int32_t which, float* out);
+
+/* Re-sort particles by cell now (also done every sort_interval substeps). */
+mpm_status mpm_sort(mpm_ctx* ctx);
+
+/* Simulation::getFullParticleCount (src/mpm.cu:253-259). */
+int64_t mpm_particle_count(const mpm_ctx* ctx);
+/* Number of substeps advanced since the last upload. */
+int64_t mpm_substep_count(const mpm_ctx* ctx);
+/* Copy the last error message (NUL-terminated, truncated to len). */
+mpm_status mpm_last_error(const mpm_ctx* ctx, char* buf, size_t len);
+/* Kernel launches issued by this context since creation (for accounting). */
+int64_t mpm_launch_count(const mpm_ctx* ctx);
+
+/* Tuning knobs of the fused substep kernel (0 = keep the current value):
+ * steps_per_warp (particles per lane per chunk), tile_nodes (shared-memory grid
+ * tile capacity), waves (chunks per SM). */
+mpm_status mpm_set_tuning(mpm_ctx* ctx, int32_t steps_per_warp, int32_t tile_nodes, int32_t waves);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPM_GB300_H */

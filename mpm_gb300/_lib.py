@@ -1,0 +1,101 @@
+"""ctypes binding of ``libmpm_gb300.so`` (the C ABI declared in include/mpm_gb300.h).
+
+The library is built in-tree by :mod:`mpm_gb300.build`.  There is no fallback:
+if the library cannot be loaded, :func:`lib` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libmpm_gb300.so")
+
+MPM_MAX_MATERIALS = 16
+STATUS_NAMES = {0: "MPM_OK", 1: "MPM_ERR_INVALID", 2: "MPM_ERR_CUDA", 3: "MPM_ERR_STATE", 4: "MPM_ERR_TIMEOUT",
+                5: "MPM_ERR_NOMEM", 6: "MPM_ERR_UNSUPPORTED"}
+
+
+class MpmParams(ctypes.Structure):
+    _fields_ = [
+        ("dt", ctypes.c_float),
+        ("N", ctypes.c_uint32),
+        ("gravity", ctypes.c_float),
+        ("boundary_mode", ctypes.c_int32),
+        ("boundary_cells", ctypes.c_int32),
+        ("g2p_guard", ctypes.c_int32),
+        ("sort_interval", ctypes.c_int32),
+        ("check_finite", ctypes.c_int32),
+    ]
+
+
+class MpmMaterial(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("particle_volume", ctypes.c_float),
+        ("density", ctypes.c_float),
+        ("E", ctypes.c_float),
+        ("nu", ctypes.c_float),
+        ("hardening", ctypes.c_float),
+        ("clamp_lo", ctypes.c_float),
+        ("clamp_hi", ctypes.c_float),
+        ("bulk", ctypes.c_float),
+    ]
+
+
+# (name, restype, argtypes) for every entry point of include/mpm_gb300.h
+P = ctypes.c_void_p
+I32, I64 = ctypes.c_int32, ctypes.c_int64
+SIGNATURES = [
+    ("mpm_create", I32, [ctypes.POINTER(MpmParams), ctypes.POINTER(P)]),
+    ("mpm_destroy", I32, [P]),
+    ("mpm_set_stream", I32, [P, P]),
+    ("mpm_set_params", I32, [P, ctypes.POINTER(MpmParams)]),
+    ("mpm_set_materials", I32, [P, ctypes.POINTER(MpmMaterial), I32]),
+    ("mpm_upload_soa", I32, [P, I64, P, P, P, P, P, P]),
+    ("mpm_upload_aos", I32, [P, P, I64]),
+    ("mpm_substep", I32, [P, I32]),
+    ("mpm_sync", I32, [P]),
+    ("mpm_download_soa", I32, [P, P, P, P, P, P, P]),
+    ("mpm_download_aos", I32, [P, P]),
+    ("mpm_get_grid", I32, [P, I32, P]),
+    ("mpm_sort", I32, [P]),
+    ("mpm_particle_count", I64, [P]),
+    ("mpm_substep_count", I64, [P]),
+    ("mpm_last_error", I32, [P, ctypes.c_char_p, ctypes.c_size_t]),
+    ("mpm_launch_count", I64, [P]),
+    ("mpm_set_tuning", I32, [P, I32, I32, I32]),
+]
+
+_lib = None
+
+
+class MpmError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+def lib() -> ctypes.CDLL:
+    """Load the CUDA library (raises if it is missing: there is no CPU fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing; run mpm_gb300.build.build() (needs nvcc)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(code: int, ctx=None) -> None:
+    if code != 0:
+        msg = ""
+        if ctx:
+            buf = ctypes.create_string_buffer(512)
+            lib().mpm_last_error(ctx, buf, 512)
+            msg = buf.value.decode(errors="replace")
+        raise MpmError(code, msg)

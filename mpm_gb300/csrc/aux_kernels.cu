@@ -1,0 +1,251 @@
+// Auxiliary kernels: periodic cell sort, host-layout conversion, grid-op readback.
+#include "mpm_internal.h"
+
+namespace mpm {
+
+// ---------------------------------------------------------------------------
+// Cell sort: counting sort of particles by the linear index of their base cell
+// (keys < N^3).  histogram (warp-aggregated atomics) -> exclusive scan -> scatter.
+// Order inside a cell is not stable; the substep does not depend on it.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t cell_key(const float* s, int64_t st, int64_t p, float dx_inv, int N) {
+  int b[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int v = QuadraticInterpolationKernel::base_cell(s[(kX + d) * st + p], dx_inv);
+    b[d] = min(max(v, 0), N - 1);
+  }
+  return (uint32_t)(((int64_t)b[0] * N + b[1]) * N + b[2]);
+}
+
+__global__ void sort_histogram(SortArgs a) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < a.n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = base + threadIdx.x;
+    const bool valid = p < a.n;
+    uint32_t key = valid ? cell_key(a.sA, a.stride, p, a.dx_inv, a.N) : 0xffffffffu;
+    if (valid) a.keys[p] = key;
+    const unsigned same = __match_any_sync(kFull, key);
+    if (valid && lane == __ffs(same) - 1) atomicAdd(a.counts + key, __popc(same));
+  }
+}
+
+constexpr int kScanItems = 8;  // per thread; a block scans kThreads * kScanItems counts
+
+// In-place exclusive scan of counts[] in blocks; block totals to block_sums[].
+__global__ void scan_blocks(int* counts, int64_t m, int* block_sums) {
+  __shared__ int warp_tot[kWarps];
+  const int64_t off = (int64_t)blockIdx.x * kThreads * kScanItems + (int64_t)threadIdx.x * kScanItems;
+  int v[kScanItems];
+  int sum = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = (off + i < m) ? counts[off + i] : 0;
+    sum += v[i];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int inc = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) warp_tot[warp] = inc;
+  __syncthreads();
+  int wpre = 0, tot = 0;
+  for (int w = 0; w < kWarps; ++w) {
+    if (w < warp) wpre += warp_tot[w];
+    tot += warp_tot[w];
+  }
+  int run = wpre + inc - sum;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (off + i < m) counts[off + i] = run;
+    run += v[i];
+  }
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+
+// Exclusive scan of the block totals by one CTA (loops over tiles of 256).
+__global__ void scan_block_sums(int* block_sums, int nb) {
+  __shared__ int warp_tot[kWarps];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int base = 0; base < nb; base += kThreads) {
+    const int i = base + threadIdx.x;
+    const int v = i < nb ? block_sums[i] : 0;
+    int inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(kFull, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_tot[warp] = inc;
+    __syncthreads();
+    int wpre = 0, tot = 0;
+    for (int w = 0; w < kWarps; ++w) {
+      if (w < warp) wpre += warp_tot[w];
+      tot += warp_tot[w];
+    }
+    if (i < nb) block_sums[i] = carry + wpre + inc - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+}
+
+__global__ void scan_add(int* counts, int64_t m, const int* block_sums) {
+  const int64_t off = (int64_t)blockIdx.x * kThreads * kScanItems;
+  const int add = block_sums[blockIdx.x];
+  for (int i = threadIdx.x; i < kThreads * kScanItems; i += kThreads)
+    if (off + i < m) counts[off + i] += add;
+}
+
+__global__ void sort_scatter(SortArgs a) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < a.n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = base + threadIdx.x;
+    const bool valid = p < a.n;
+    const uint32_t key = valid ? a.keys[p] : 0xffffffffu;
+    const unsigned same = __match_any_sync(kFull, key);
+    const int leader = __ffs(same) - 1;
+    int start = 0;
+    if (valid && lane == leader) start = atomicAdd(a.counts + key, __popc(same));
+    start = __shfl_sync(kFull, start, leader);
+    if (!valid) continue;
+    const int64_t q = (int64_t)start + __popc(same & ((1u << lane) - 1u));
+    for (int c = 0; c < a.ncomp; ++c) {
+      const int k = a.comp_list[c];
+      a.sB[k * a.stride + q] = a.sA[k * a.stride + p];
+    }
+    if (a.matA) a.matB[q] = a.matA[p];
+    a.idB[q] = a.idA[p];
+  }
+}
+
+cudaError_t launch_sort(const SortArgs& a, int num_sms, cudaStream_t st, int64_t* launches) {
+  if (a.n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(a.counts, 0, sizeof(int) * a.cells, st);
+  if (e != cudaSuccess) return e;
+  int blocks = (int)std::min<int64_t>((a.n + kThreads - 1) / kThreads, (int64_t)num_sms * 8);
+  sort_histogram<<<blocks, kThreads, 0, st>>>(a);
+  const int per = kThreads * kScanItems;
+  const int nb = (int)((a.cells + per - 1) / per);
+  scan_blocks<<<nb, kThreads, 0, st>>>(a.counts, a.cells, a.block_sums);
+  scan_block_sums<<<1, kThreads, 0, st>>>(a.block_sums, nb);
+  scan_add<<<nb, kThreads, 0, st>>>(a.counts, a.cells, a.block_sums);
+  sort_scatter<<<blocks, kThreads, 0, st>>>(a);
+  if (launches) *launches += 5;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Host layout (per-particle interleaved x[3n] v[3n] C[9n] F[9n] Jp[n], staged
+// contiguously in that order) <-> component-major device layout.
+// ---------------------------------------------------------------------------
+__global__ void deinterleave_kernel(const float* stage, float* s, int64_t st, int64_t n, int has_v, int has_C,
+                                    int has_F, int has_Jp) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const float* xs = stage;
+    const float* vs = xs + 3 * n;
+    const float* Cs = vs + 3 * n;
+    const float* Fs = Cs + 9 * n;
+    const float* Js = Fs + 9 * n;
+    for (int d = 0; d < 3; ++d) {
+      s[(kX + d) * st + p] = xs[3 * p + d];
+      s[(kV + d) * st + p] = has_v ? vs[3 * p + d] : 0.f;
+    }
+    for (int i = 0; i < 9; ++i) {
+      s[(kC + i) * st + p] = has_C ? Cs[9 * p + i] : 0.f;
+      s[(kF + i) * st + p] = has_F ? Fs[9 * p + i] : ((i % 4 == 0) ? 1.f : 0.f);
+    }
+    s[kJp * st + p] = has_Jp ? Js[p] : 1.f;
+  }
+}
+
+__global__ void interleave_kernel(const float* s, int64_t st, const uint32_t* id, int64_t n, float* stage,
+                                  int liquid_layout) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = id[p];
+    float* xs = stage;
+    float* vs = xs + 3 * n;
+    float* Cs = vs + 3 * n;
+    float* Fs = Cs + 9 * n;
+    float* Js = Fs + 9 * n;
+    for (int d = 0; d < 3; ++d) {
+      xs[3 * q + d] = s[(kX + d) * st + p];
+      vs[3 * q + d] = s[(kV + d) * st + p];
+    }
+    const float J = s[kJp * st + p];
+    const float cr = liquid_layout ? cbrtf(J) : 0.f;
+    for (int i = 0; i < 9; ++i) {
+      Cs[9 * q + i] = s[(kC + i) * st + p];
+      Fs[9 * q + i] = liquid_layout ? ((i % 4 == 0) ? cr : 0.f) : s[(kF + i) * st + p];
+    }
+    Js[q] = J;
+  }
+}
+
+__global__ void iota_kernel(uint32_t* id, int64_t n) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+    id[p] = (uint32_t)p;
+}
+
+__global__ void scatter_u8_kernel(const uint8_t* src, const uint32_t* id, int64_t n, uint8_t* dst) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+    dst[id[p]] = src[p];
+}
+
+static int grid_for(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 4096)); }
+
+cudaError_t launch_deinterleave(const float* stage, float* s, int64_t stride, int64_t n, int has_v, int has_C,
+                                int has_F, int has_Jp, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  deinterleave_kernel<<<grid_for(n), 256, 0, st>>>(stage, s, stride, n, has_v, has_C, has_F, has_Jp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_interleave(const float* s, int64_t stride, const uint32_t* id, int64_t n, float* stage,
+                              int liquid_layout, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  interleave_kernel<<<grid_for(n), 256, 0, st>>>(s, stride, id, n, stage, liquid_layout);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_iota(uint32_t* id, int64_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  iota_kernel<<<grid_for(n), 256, 0, st>>>(id, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_u8(const uint8_t* src, const uint32_t* id, int64_t n, uint8_t* dst, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  scatter_u8_kernel<<<grid_for(n), 256, 0, st>>>(src, id, n, dst);
+  return cudaGetLastError();
+}
+
+// gridOpKernel (src/mpm.cu:76-107) over the whole grid, for readback: nodes with
+// mass > 0 get the operated velocity and mass slot 1 (the reference divides all four
+// components by the mass); others keep their raw value.
+__global__ void grid_op_kernel(const float4* in, float4* out, SimConsts K) {
+  const int N = K.N;
+  const int64_t cells = (int64_t)N * N * N;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c / ((int64_t)N * N));
+    const int j = (int)((c / N) % N);
+    const int k = (int)(c % N);
+    const float4 g = in[c];
+    const float3 v = grid_node_velocity(g, i, j, k, K);
+    out[c] = make_float4(v.x, v.y, v.z, g.w > 0.f ? g.w / g.w : g.w);
+  }
+}
+
+cudaError_t launch_grid_op(const float4* in, float4* out, SimConsts K, cudaStream_t st) {
+  const int64_t cells = (int64_t)K.N * K.N * K.N;
+  grid_op_kernel<<<grid_for(cells), 256, 0, st>>>(in, out, K);
+  return cudaGetLastError();
+}
+
+}  // namespace mpm

@@ -1,0 +1,596 @@
+// C ABI of the GB300 MLS-MPM substep: context, buffers, launch sequencing.
+//
+// Replaces the reference's host class Simulation (include/mpm.cuh:44-106,
+// src/mpm.cu:180-329).  Grid buffers rotate through three slots so that a substep
+// is one fused launch (see substep.cu); particles are component-major SoA sorted by
+// cell every `sort_interval` substeps.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mpm_gb300.h"
+#include "mpm_internal.h"
+
+using namespace mpm;
+
+struct mpm_ctx {
+  mpm_params params{};
+  SimConsts K{};
+  int n_materials = 0;
+  mpm_material mats[MPM_MAX_MATERIALS]{};
+  bool liquid_layout = false;
+
+  int device = 0;
+  int num_sms = 1;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+
+  // particles
+  int64_t n = 0, stride = 0, capacity = 0;
+  float* sA = nullptr;
+  float* sB = nullptr;
+  uint8_t* matA = nullptr;
+  uint8_t* matB = nullptr;
+  uint32_t* idA = nullptr;
+  uint32_t* idB = nullptr;
+  uint32_t* keys = nullptr;
+  bool have_mat = false;
+
+  // grid: three rotating buffers
+  float4* grid[3] = {nullptr, nullptr, nullptr};
+  int64_t cells = 0;
+  int cur = 0;            // slot holding the P2G grid of the next substep (when pending)
+  int prev = -1;          // slot the last completed substep's G2P read
+  bool pending = false;
+
+  // sort scratch
+  int* counts = nullptr;
+  int* block_sums = nullptr;
+  int* comp_list = nullptr;
+
+  // staging
+  float* stage = nullptr;
+  size_t stage_bytes = 0;
+  int* status = nullptr;
+
+  int64_t substeps = 0;
+  int64_t since_sort = 0;
+  int64_t launches = 0;
+  int steps_per_warp = 8;
+  int tile_cap = 4096;
+  int waves = 0;
+  std::string last_error;
+};
+
+namespace {
+
+mpm_status fail(mpm_ctx* c, mpm_status code, const std::string& msg) {
+  if (c) c->last_error = msg;
+  return code;
+}
+
+#define MPM_CUDA(ctx, call)                                                                          \
+  do {                                                                                               \
+    cudaError_t _e = (call);                                                                         \
+    if (_e != cudaSuccess)                                                                           \
+      return fail((ctx), _e == cudaErrorMemoryAllocation ? MPM_ERR_NOMEM : MPM_ERR_CUDA,             \
+                  std::string(#call) + ": " + cudaGetErrorString(_e));                               \
+  } while (0)
+
+bool valid_params(const mpm_params* p, std::string& why) {
+  if (!p) {
+    why = "params is NULL";
+    return false;
+  }
+  if (p->N < 4 || p->N > 1000) {
+    why = "N must be in [4, 1000]";
+    return false;
+  }
+  if (!(p->dt > 0.f) || !std::isfinite(p->dt)) {
+    why = "dt must be positive and finite";
+    return false;
+  }
+  if (p->boundary_mode < 0 || p->boundary_mode > 2) {
+    why = "unknown boundary_mode";
+    return false;
+  }
+  if (p->boundary_cells < 0 || (uint32_t)p->boundary_cells * 2 > p->N) {
+    why = "boundary_cells out of range";
+    return false;
+  }
+  if (p->sort_interval < 0) {
+    why = "sort_interval must be >= 0";
+    return false;
+  }
+  return true;
+}
+
+void derive_consts(mpm_ctx* c) {
+  SimConsts& K = c->K;
+  const mpm_params& p = c->params;
+  K.N = (int)p.N;
+  K.dt = p.dt;
+  // SimulationParameters: dx = 1.0/N (double, stored as float), dx_inv = 1.0/dx
+  // (include/TransferScheme.h:22-28); D_inv_const = I * 4.0 * dx_inv * dx_inv.
+  const float dx = (float)(1.0 / (double)p.N);
+  const float dxi = (float)(1.0 / (double)dx);
+  K.dx = dx;
+  K.dx_inv = dxi;
+  K.dinv = (4.0f * dxi) * dxi;
+  K.dtg = p.dt * p.gravity;
+  K.boundary_mode = p.boundary_mode;
+  K.boundary_cells = p.boundary_cells;
+  K.n_materials = c->n_materials;
+  for (int i = 0; i < c->n_materials; ++i) {
+    const mpm_material& m = c->mats[i];
+    DevMaterial& d = K.mat[i];
+    d.kind = m.kind;
+    d.vol = m.particle_volume;
+    d.mass = m.density * m.particle_volume;                       // MaterialModelBase
+    d.mu0 = m.E / (2.f * (1.f + m.nu));                            // MMFixedCorotated
+    d.lambda0 = m.E * m.nu / ((1.f + m.nu) * (1.f - 2.f * m.nu));
+    d.hardening = m.hardening;
+    d.clamp_lo = m.clamp_lo;
+    d.clamp_hi = m.clamp_hi;
+    d.bulk = m.bulk;
+  }
+}
+
+// The compact liquid layout (x, v, C, J) is used when the table is a single liquid.
+bool all_liquid(const mpm_ctx* c) { return c->n_materials == 1 && c->mats[0].kind == MPM_MAT_LIQUID; }
+
+mpm_status ensure_stage(mpm_ctx* c, size_t bytes) {
+  if (c->stage_bytes >= bytes) return MPM_OK;
+  if (c->stage) cudaFree(c->stage);
+  c->stage = nullptr;
+  c->stage_bytes = 0;
+  MPM_CUDA(c, cudaMalloc(&c->stage, bytes));
+  c->stage_bytes = bytes;
+  return MPM_OK;
+}
+
+void free_particles(mpm_ctx* c) {
+  cudaFree(c->sA);
+  cudaFree(c->sB);
+  cudaFree(c->matA);
+  cudaFree(c->matB);
+  cudaFree(c->idA);
+  cudaFree(c->idB);
+  cudaFree(c->keys);
+  c->sA = c->sB = nullptr;
+  c->matA = c->matB = nullptr;
+  c->idA = c->idB = nullptr;
+  c->keys = nullptr;
+  c->capacity = 0;
+}
+
+mpm_status ensure_particles(mpm_ctx* c, int64_t n) {
+  if (n <= c->capacity && c->sA) return MPM_OK;
+  free_particles(c);
+  const int64_t cap = std::max<int64_t>(64, (n + 63) / 64 * 64);
+  const size_t fbytes = sizeof(float) * (size_t)kNumComps * cap;
+  MPM_CUDA(c, cudaMalloc(&c->sA, fbytes));
+  MPM_CUDA(c, cudaMalloc(&c->sB, fbytes));
+  MPM_CUDA(c, cudaMalloc(&c->matA, cap));
+  MPM_CUDA(c, cudaMalloc(&c->matB, cap));
+  MPM_CUDA(c, cudaMalloc(&c->idA, sizeof(uint32_t) * cap));
+  MPM_CUDA(c, cudaMalloc(&c->idB, sizeof(uint32_t) * cap));
+  MPM_CUDA(c, cudaMalloc(&c->keys, sizeof(uint32_t) * cap));
+  c->capacity = cap;
+  c->stride = cap;
+  return MPM_OK;
+}
+
+StepArgs make_step_args(mpm_ctx* c) {
+  StepArgs a{};
+  a.s = c->sA;
+  a.stride = c->stride;
+  a.mat = c->have_mat ? c->matA : nullptr;
+  a.id = c->idA;
+  a.n = c->n;
+  a.grid_cells = c->cells;
+  a.tile_cap = c->tile_cap;
+  a.guard_limit = (int64_t)c->params.N * c->params.N * c->params.N;
+  a.check_finite = c->params.check_finite;
+  a.status = c->status;
+  a.K = c->K;
+  return a;
+}
+
+// Chunk size: about steps_per_warp particles per lane, rounded so the chunks split
+// evenly over the resident CTAs.
+void launch_shape(mpm_ctx* c, StepKind kind, bool guard, int& chunk, int& blocks) {
+  const size_t smem = (kind == kStepP2GOnly) ? 0 : (size_t)c->tile_cap * sizeof(float4);
+  const int bps = step_blocks_per_sm(kind, c->liquid_layout, guard, smem);
+  const int64_t resident = (int64_t)c->num_sms * bps;
+  const int64_t target = (int64_t)kThreads * c->steps_per_warp;
+  int64_t waves = c->waves > 0 ? c->waves : std::max<int64_t>(1, (c->n + resident * target / 2) / (resident * target));
+  int64_t steps = (c->n + resident * waves * kThreads - 1) / (resident * waves * kThreads);
+  steps = std::max<int64_t>(1, std::min<int64_t>(steps, 64));
+  chunk = (int)(steps * kThreads);
+  const int64_t nchunks = (c->n + chunk - 1) / chunk;
+  blocks = (int)std::max<int64_t>(1, std::min<int64_t>(nchunks, resident));
+}
+
+mpm_status run_step(mpm_ctx* c, StepKind kind) {
+  StepArgs a = make_step_args(c);
+  const bool guard = c->params.g2p_guard != 0;
+  int chunk, blocks;
+  launch_shape(c, kind, guard, chunk, blocks);
+  a.chunk = chunk;
+  const int r = c->cur;
+  a.grid_in = (kind == kStepP2GOnly) ? nullptr : c->grid[r];
+  a.grid_out = c->grid[(r + 1) % 3];
+  a.grid_zero = c->grid[(r + 2) % 3];
+  MPM_CUDA(c, launch_step(a, kind, c->liquid_layout, guard, blocks, c->stream));
+  c->launches += 1;
+  if (kind == kStepFused) c->prev = r;
+  c->cur = (r + 1) % 3;
+  c->pending = true;
+  return MPM_OK;
+}
+
+mpm_status run_sort(mpm_ctx* c) {
+  if (c->n == 0) return MPM_OK;
+  SortArgs s{};
+  s.sA = c->sA;
+  s.sB = c->sB;
+  s.stride = c->stride;
+  s.n = c->n;
+  s.matA = c->have_mat ? c->matA : nullptr;
+  s.matB = c->matB;
+  s.idA = c->idA;
+  s.idB = c->idB;
+  s.keys = c->keys;
+  s.counts = c->counts;
+  s.block_sums = c->block_sums;
+  s.cells = c->cells;
+  s.N = (int)c->params.N;
+  s.dx_inv = c->K.dx_inv;
+  // liquid layout: x, v, C, J (16 components); general: all 25
+  s.ncomp = c->liquid_layout ? kLiquidComps : kNumComps;
+  s.comp_list = c->liquid_layout ? c->comp_list : c->comp_list + kLiquidComps;
+  MPM_CUDA(c, launch_sort(s, c->num_sms, c->stream, &c->launches));
+  std::swap(c->sA, c->sB);
+  std::swap(c->matA, c->matB);
+  std::swap(c->idA, c->idB);
+  c->since_sort = 0;
+  return MPM_OK;
+}
+
+mpm_status check_ready(mpm_ctx* c) {
+  if (!c) return MPM_ERR_INVALID;
+  if (c->n_materials == 0) return fail(c, MPM_ERR_INVALID, "no materials set (mpm_set_materials)");
+  return MPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mpm_status mpm_create(const mpm_params* params, mpm_ctx** out) {
+  if (!out) return MPM_ERR_INVALID;
+  *out = nullptr;
+  std::string why;
+  if (!valid_params(params, why)) return MPM_ERR_INVALID;
+  mpm_ctx* c = new mpm_ctx();
+  c->params = *params;
+  derive_consts(c);
+  mpm_status st = MPM_OK;
+  auto bail = [&](mpm_status s) {
+    mpm_destroy(c);
+    return s;
+  };
+  if (cudaGetDevice(&c->device) != cudaSuccess) return bail(MPM_ERR_CUDA);
+  if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
+    return bail(MPM_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) return bail(MPM_ERR_CUDA);
+  c->stream = c->own_stream;
+  c->cells = (int64_t)params->N * params->N * params->N;
+  for (int i = 0; i < 3; ++i) {
+    if (cudaMalloc(&c->grid[i], sizeof(float4) * c->cells) != cudaSuccess) return bail(MPM_ERR_NOMEM);
+    if (cudaMemsetAsync(c->grid[i], 0, sizeof(float4) * c->cells, c->stream) != cudaSuccess)
+      return bail(MPM_ERR_CUDA);
+  }
+  const int per = kThreads * 8;
+  const int64_t nb = (c->cells + per - 1) / per;
+  if (cudaMalloc(&c->counts, sizeof(int) * c->cells) != cudaSuccess) return bail(MPM_ERR_NOMEM);
+  if (cudaMalloc(&c->block_sums, sizeof(int) * std::max<int64_t>(nb, 1)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
+  if (cudaMalloc(&c->status, sizeof(int)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
+  if (cudaMemsetAsync(c->status, 0, sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
+  // component lists for the sort: liquid layout = x, v, C, J; general = all
+  int comps[kNumComps];
+  for (int i = 0; i < kNumComps; ++i) comps[i] = i;
+  int liq[kLiquidComps];
+  for (int i = 0; i < 15; ++i) liq[i] = i;
+  liq[15] = kJp;
+  if (cudaMalloc(&c->comp_list, sizeof(int) * 2 * kNumComps) != cudaSuccess) return bail(MPM_ERR_NOMEM);
+  (void)comps;
+  if (cudaMemcpy(c->comp_list, liq, sizeof(liq), cudaMemcpyHostToDevice) != cudaSuccess) return bail(MPM_ERR_CUDA);
+  if (cudaMemcpy(c->comp_list + kLiquidComps, comps, sizeof(comps), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(MPM_ERR_CUDA);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
+  (void)st;
+  *out = c;
+  return MPM_OK;
+}
+
+mpm_status mpm_destroy(mpm_ctx* c) {
+  if (!c) return MPM_ERR_INVALID;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_particles(c);
+  for (auto& g : c->grid) cudaFree(g);
+  cudaFree(c->counts);
+  cudaFree(c->block_sums);
+  cudaFree(c->comp_list);
+  cudaFree(c->stage);
+  cudaFree(c->status);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return MPM_OK;
+}
+
+mpm_status mpm_set_stream(mpm_ctx* c, void* stream) {
+  if (!c) return MPM_ERR_INVALID;
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return MPM_OK;
+}
+
+mpm_status mpm_set_params(mpm_ctx* c, const mpm_params* p) {
+  if (!c) return MPM_ERR_INVALID;
+  std::string why;
+  if (!valid_params(p, why)) return fail(c, MPM_ERR_INVALID, why);
+  if (p->N != c->params.N) return fail(c, MPM_ERR_INVALID, "N cannot change on a live context");
+  c->params = *p;
+  derive_consts(c);
+  c->pending = false;  // the prefetched P2G used the old dt
+  return MPM_OK;
+}
+
+mpm_status mpm_set_materials(mpm_ctx* c, const mpm_material* m, int32_t count) {
+  if (!c) return MPM_ERR_INVALID;
+  if (!m || count <= 0 || count > MPM_MAX_MATERIALS) return fail(c, MPM_ERR_INVALID, "material count out of range");
+  for (int i = 0; i < count; ++i) {
+    if (m[i].kind < 0 || m[i].kind > MPM_MAT_LIQUID) return fail(c, MPM_ERR_INVALID, "unknown material kind");
+    if (!(m[i].particle_volume > 0.f) || !(m[i].density > 0.f))
+      return fail(c, MPM_ERR_INVALID, "particle_volume and density must be positive");
+  }
+  const bool was_liquid = c->liquid_layout;
+  for (int i = 0; i < count; ++i) c->mats[i] = m[i];
+  c->n_materials = count;
+  const bool liq = all_liquid(c);
+  if (c->n > 0 && liq != was_liquid)
+    return fail(c, MPM_ERR_INVALID, "material table change would switch the particle layout; set materials before upload");
+  c->liquid_layout = liq;
+  derive_consts(c);
+  c->pending = false;
+  return MPM_OK;
+}
+
+mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v, const float* C, const float* F,
+                          const float* Jp, const uint8_t* mat) {
+  mpm_status st = check_ready(c);
+  if (st != MPM_OK) return st;
+  if (n < 0 || (n > 0 && !x)) return fail(c, MPM_ERR_INVALID, "x is required");
+  if (n > (int64_t)0xffffffffLL) return fail(c, MPM_ERR_INVALID, "too many particles");
+  if (mat)
+    for (int64_t p = 0; p < n; ++p)
+      if (mat[p] >= c->n_materials) return fail(c, MPM_ERR_INVALID, "material index out of range");
+  st = ensure_particles(c, n);
+  if (st != MPM_OK) return st;
+  c->n = n;
+  c->pending = false;
+  c->prev = -1;
+  c->substeps = 0;
+  c->since_sort = c->params.sort_interval;  // sort before the first substep
+  if (n == 0) return MPM_OK;
+  const size_t per = 25 * sizeof(float);
+  st = ensure_stage(c, per * (size_t)n);
+  if (st != MPM_OK) return st;
+  float* xs = c->stage;
+  float* vs = xs + 3 * n;
+  float* Cs = vs + 3 * n;
+  float* Fs = Cs + 9 * n;
+  float* Js = Fs + 9 * n;
+  MPM_CUDA(c, cudaMemcpyAsync(xs, x, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+  if (v) MPM_CUDA(c, cudaMemcpyAsync(vs, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+  if (C) MPM_CUDA(c, cudaMemcpyAsync(Cs, C, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, c->stream));
+  if (F) MPM_CUDA(c, cudaMemcpyAsync(Fs, F, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, c->stream));
+  if (Jp) MPM_CUDA(c, cudaMemcpyAsync(Js, Jp, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+  MPM_CUDA(c, launch_deinterleave(c->stage, c->sA, c->stride, n, v != nullptr, C != nullptr, F != nullptr,
+                                  Jp != nullptr, c->stream));
+  MPM_CUDA(c, launch_iota(c->idA, n, c->stream));
+  c->launches += 2;
+  c->have_mat = !c->liquid_layout && c->n_materials > 1;
+  if (c->have_mat) {
+    if (mat) {
+      MPM_CUDA(c, cudaMemcpyAsync(c->matA, mat, n, cudaMemcpyHostToDevice, c->stream));
+    } else {
+      MPM_CUDA(c, cudaMemsetAsync(c->matA, 0, n, c->stream));
+    }
+  } else if (mat) {
+    for (int64_t p = 0; p < n; ++p)
+      if (mat[p] != 0) {
+        c->have_mat = true;
+        break;
+      }
+    if (c->have_mat) MPM_CUDA(c, cudaMemcpyAsync(c->matA, mat, n, cudaMemcpyHostToDevice, c->stream));
+  }
+  // Host buffers may be reused by the caller as soon as we return.
+  MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+mpm_status mpm_upload_aos(mpm_ctx* c, const void* particles, int64_t n) {
+  mpm_status st = check_ready(c);
+  if (st != MPM_OK) return st;
+  if (n < 0 || (n > 0 && !particles)) return fail(c, MPM_ERR_INVALID, "particles is NULL");
+  std::vector<float> x(3 * n), v(3 * n), C(9 * n), F(9 * n), J(n);
+  std::vector<uint8_t> mat(n);
+  const uint8_t* b = (const uint8_t*)particles;
+  for (int64_t p = 0; p < n; ++p) {
+    const uint8_t* r = b + 104 * p;
+    float f[25];
+    std::memcpy(f, r + 4, sizeof(f));
+    mat[p] = r[0];
+    for (int d = 0; d < 3; ++d) {
+      x[3 * p + d] = f[d];
+      v[3 * p + d] = f[3 + d];
+    }
+    // Eigen matrices are column-major: element (row, col) at col * 3 + row
+    for (int rr = 0; rr < 3; ++rr)
+      for (int cc = 0; cc < 3; ++cc) {
+        F[9 * p + 3 * rr + cc] = f[6 + cc * 3 + rr];
+        C[9 * p + 3 * rr + cc] = f[15 + cc * 3 + rr];
+      }
+    J[p] = f[24];
+  }
+  return mpm_upload_soa(c, n, x.data(), v.data(), C.data(), F.data(), J.data(), mat.data());
+}
+
+mpm_status mpm_substep(mpm_ctx* c, int32_t nsteps) {
+  mpm_status st = check_ready(c);
+  if (st != MPM_OK) return st;
+  if (nsteps < 0) return fail(c, MPM_ERR_INVALID, "nsteps must be >= 0");
+  for (int32_t i = 0; i < nsteps; ++i) {
+    if (c->n > 0) {
+      if (c->params.sort_interval > 0 && c->since_sort >= c->params.sort_interval) {
+        st = run_sort(c);
+        if (st != MPM_OK) return st;
+      }
+      if (!c->pending) {
+        st = run_step(c, kStepP2GOnly);
+        if (st != MPM_OK) return st;
+      }
+      st = run_step(c, kStepFused);
+      if (st != MPM_OK) return st;
+    }
+    c->substeps += 1;
+    c->since_sort += 1;
+  }
+  return MPM_OK;
+}
+
+mpm_status mpm_sync(mpm_ctx* c) {
+  if (!c) return MPM_ERR_INVALID;
+  MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+  int flag = 0;
+  MPM_CUDA(c, cudaMemcpy(&flag, c->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag) {
+    MPM_CUDA(c, cudaMemset(c->status, 0, sizeof(int)));
+    if (flag & kStatusTimeout) return fail(c, MPM_ERR_TIMEOUT, "device wait timed out");
+    if (flag & kStatusNonFinite) return fail(c, MPM_ERR_STATE, "non-finite particle state");
+    return fail(c, MPM_ERR_STATE, "device index check failed");
+  }
+  return MPM_OK;
+}
+
+mpm_status mpm_download_soa(mpm_ctx* c, float* x, float* v, float* C, float* F, float* Jp, uint8_t* mat) {
+  if (!c) return MPM_ERR_INVALID;
+  const int64_t n = c->n;
+  if (n == 0) return MPM_OK;
+  mpm_status st = ensure_stage(c, 25 * sizeof(float) * (size_t)n + (size_t)n);
+  if (st != MPM_OK) return st;
+  MPM_CUDA(c, launch_interleave(c->sA, c->stride, c->idA, n, c->stage, c->liquid_layout, c->stream));
+  c->launches += 1;
+  float* xs = c->stage;
+  float* vs = xs + 3 * n;
+  float* Cs = vs + 3 * n;
+  float* Fs = Cs + 9 * n;
+  float* Js = Fs + 9 * n;
+  if (x) MPM_CUDA(c, cudaMemcpyAsync(x, xs, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+  if (v) MPM_CUDA(c, cudaMemcpyAsync(v, vs, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+  if (C) MPM_CUDA(c, cudaMemcpyAsync(C, Cs, sizeof(float) * 9 * n, cudaMemcpyDeviceToHost, c->stream));
+  if (F) MPM_CUDA(c, cudaMemcpyAsync(F, Fs, sizeof(float) * 9 * n, cudaMemcpyDeviceToHost, c->stream));
+  if (Jp) MPM_CUDA(c, cudaMemcpyAsync(Jp, Js, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+  if (mat) {
+    if (c->have_mat) {
+      uint8_t* ms = (uint8_t*)(Js + n);
+      MPM_CUDA(c, launch_scatter_u8(c->matA, c->idA, n, ms, c->stream));
+      c->launches += 1;
+      MPM_CUDA(c, cudaMemcpyAsync(mat, ms, n, cudaMemcpyDeviceToHost, c->stream));
+    } else {
+      std::memset(mat, 0, n);
+    }
+  }
+  MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+mpm_status mpm_download_aos(mpm_ctx* c, void* particles) {
+  if (!c) return MPM_ERR_INVALID;
+  const int64_t n = c->n;
+  if (n > 0 && !particles) return fail(c, MPM_ERR_INVALID, "particles is NULL");
+  std::vector<float> x(3 * n), v(3 * n), C(9 * n), F(9 * n), J(n);
+  std::vector<uint8_t> mat(n);
+  mpm_status st = mpm_download_soa(c, x.data(), v.data(), C.data(), F.data(), J.data(), mat.data());
+  if (st != MPM_OK) return st;
+  uint8_t* b = (uint8_t*)particles;
+  for (int64_t p = 0; p < n; ++p) {
+    uint8_t* r = b + 104 * p;
+    float f[25];
+    for (int d = 0; d < 3; ++d) {
+      f[d] = x[3 * p + d];
+      f[3 + d] = v[3 * p + d];
+    }
+    for (int rr = 0; rr < 3; ++rr)
+      for (int cc = 0; cc < 3; ++cc) {
+        f[6 + cc * 3 + rr] = F[9 * p + 3 * rr + cc];
+        f[15 + cc * 3 + rr] = C[9 * p + 3 * rr + cc];
+      }
+    f[24] = J[p];
+    std::memset(r, 0, 4);
+    r[0] = mat[p];
+    std::memcpy(r + 4, f, sizeof(f));
+  }
+  return MPM_OK;
+}
+
+mpm_status mpm_get_grid(mpm_ctx* c, int32_t which, float* out) {
+  if (!c || !out) return MPM_ERR_INVALID;
+  if (which != 0 && which != 1) return fail(c, MPM_ERR_INVALID, "which must be 0 (post-P2G) or 1 (post-op)");
+  if (c->prev < 0) return fail(c, MPM_ERR_INVALID, "no completed substep since the last upload");
+  const size_t bytes = sizeof(float4) * c->cells;
+  if (which == 0) {
+    MPM_CUDA(c, cudaMemcpyAsync(out, c->grid[c->prev], bytes, cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    mpm_status st = ensure_stage(c, bytes);
+    if (st != MPM_OK) return st;
+    MPM_CUDA(c, launch_grid_op(c->grid[c->prev], (float4*)c->stage, c->K, c->stream));
+    c->launches += 1;
+    MPM_CUDA(c, cudaMemcpyAsync(out, c->stage, bytes, cudaMemcpyDeviceToHost, c->stream));
+  }
+  MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+mpm_status mpm_sort(mpm_ctx* c) {
+  if (!c) return MPM_ERR_INVALID;
+  return run_sort(c);
+}
+
+int64_t mpm_particle_count(const mpm_ctx* c) { return c ? c->n : -1; }
+int64_t mpm_substep_count(const mpm_ctx* c) { return c ? c->substeps : -1; }
+int64_t mpm_launch_count(const mpm_ctx* c) { return c ? c->launches : -1; }
+
+mpm_status mpm_last_error(const mpm_ctx* c, char* buf, size_t len) {
+  if (!c || !buf || len == 0) return MPM_ERR_INVALID;
+  std::snprintf(buf, len, "%s", c->last_error.c_str());
+  return MPM_OK;
+}
+
+mpm_status mpm_set_tuning(mpm_ctx* c, int32_t steps_per_warp, int32_t tile_nodes, int32_t waves) {
+  if (!c) return MPM_ERR_INVALID;
+  if (steps_per_warp < 0 || steps_per_warp > 64) return fail(c, MPM_ERR_INVALID, "steps_per_warp out of range");
+  if (tile_nodes < 0 || tile_nodes > 13000) return fail(c, MPM_ERR_INVALID, "tile_nodes out of range (max 13000)");
+  if (waves < 0) return fail(c, MPM_ERR_INVALID, "waves must be >= 0");
+  if (steps_per_warp) c->steps_per_warp = steps_per_warp;
+  if (tile_nodes) c->tile_cap = tile_nodes;
+  c->waves = waves;
+  return MPM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,70 @@
+// Internal host/device interface between the C ABI (capi.cu) and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mpm_device.cuh"
+
+namespace mpm {
+
+// Arguments of the fused substep kernel.  One launch = G2P of substep n (from
+// grid_in, the P2G grid of substep n) + P2G of substep n+1 (into grid_out) +
+// clearing grid_zero (the grid substep n-1 read), so the three grid buffers rotate.
+struct StepArgs {
+  float* s;               // component-major particle state
+  int64_t stride;         // component stride (elements)
+  const uint8_t* mat;     // material index per particle (general layout), may be null
+  const uint32_t* id;     // original particle index (for the G2P guard)
+  int64_t n;
+  const float4* grid_in;  // P2G grid to apply (m v, m); null for a P2G-only launch
+  float4* grid_out;       // P2G accumulation target (already zero)
+  float4* grid_zero;      // buffer to clear for the launch after next
+  int64_t grid_cells;
+  int chunk;              // particles per CTA chunk (multiple of kThreads)
+  int tile_cap;           // capacity of the shared-memory velocity tile (nodes)
+  int64_t guard_limit;    // G2P only for id <= guard_limit when the guard is on
+  int check_finite;
+  int* status;
+  SimConsts K;
+};
+
+enum StepKind { kStepP2GOnly = 0, kStepFused = 1, kStepG2POnly = 2 };
+
+// Launches one substep kernel variant. liquid = liquid-only layout.
+cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guard, int grid_blocks,
+                        cudaStream_t st);
+// Max resident CTAs per SM for the variant at the given dynamic shared memory.
+int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem);
+
+// Cell sort (counting sort by the linear index of the base cell).
+struct SortArgs {
+  const float* sA;
+  float* sB;
+  int64_t stride;
+  int64_t n;
+  const uint8_t* matA;
+  uint8_t* matB;
+  const uint32_t* idA;
+  uint32_t* idB;
+  uint32_t* keys;
+  int* counts;   // grid_cells
+  int* block_sums;
+  int64_t cells;
+  int N;
+  float dx_inv;
+  int ncomp;            // components to move
+  const int* comp_list; // device list of component indices
+};
+cudaError_t launch_sort(const SortArgs& a, int num_sms, cudaStream_t st, int64_t* launches);
+
+// Host-interleaved <-> component-major conversion.
+cudaError_t launch_deinterleave(const float* stage, float* s, int64_t stride, int64_t n, int has_v,
+                                int has_C, int has_F, int has_Jp, cudaStream_t st);
+cudaError_t launch_interleave(const float* s, int64_t stride, const uint32_t* id, int64_t n, float* stage,
+                              int liquid_layout, cudaStream_t st);
+cudaError_t launch_iota(uint32_t* id, int64_t n, cudaStream_t st);
+cudaError_t launch_scatter_u8(const uint8_t* src, const uint32_t* id, int64_t n, uint8_t* dst, cudaStream_t st);
+// Post-op grid with the reference's mass slot (src/mpm.cu:86-88).
+cudaError_t launch_grid_op(const float4* in, float4* out, SimConsts K, cudaStream_t st);
+
+}  // namespace mpm

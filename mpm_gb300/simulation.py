@@ -1,0 +1,172 @@
+"""Python mirror of the reference's ``Simulation`` host class.
+
+``Simulation`` (include/mpm.cuh:44-106, src/mpm.cu:180-329) keeps the same method
+names — ``initCuda``, ``advance``, ``syncDevice``, ``getFullParticleCount`` — on
+top of the C ABI in include/mpm_gb300.h.  Errors are raised as
+:class:`mpm_gb300._lib.MpmError` with the library's message (the reference calls
+``exit()`` or does not check).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .materials import Material
+
+
+def _f32(a, shape):
+    if a is None:
+        return None
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(shape))
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Simulation:
+    """One simulation context on the current CUDA device.
+
+    Parameters mirror ``SimulationParameters`` (dt, N) plus the options the
+    reference hard-codes (gravity -9.81, the 0.05 boundary fraction) and the
+    sort interval of the cell-sorted layout."""
+
+    def __init__(self, dt=1e-4, N=60, gravity=-9.81, boundary_mode=0, boundary_cells=3, g2p_guard=False,
+                 sort_interval=16, check_finite=False, materials=None):
+        self.L = _lib.lib()
+        self.params = _lib.MpmParams(float(dt), int(N), float(gravity), int(boundary_mode), int(boundary_cells),
+                                     int(bool(g2p_guard)), int(sort_interval), int(bool(check_finite)))
+        ctx = ctypes.c_void_p()
+        code = self.L.mpm_create(ctypes.byref(self.params), ctypes.byref(ctx))
+        if code != 0:
+            raise _lib.MpmError(code, "mpm_create failed")
+        self.ctx = ctx
+        self.N = int(N)
+        self.n = 0
+        self.materials = []
+        if materials is not None:
+            self.set_materials(materials)
+
+    @classmethod
+    def from_config(cls, cfg: dict, **overrides):
+        p = dict(cfg["params"])
+        p.update(overrides)
+        sim = cls(**p)
+        sim.set_materials(cfg["materials"])
+        return sim
+
+    # -- setup -------------------------------------------------------------
+    def set_materials(self, materials):
+        arr = (_lib.MpmMaterial * len(materials))()
+        for i, m in enumerate(materials):
+            if not isinstance(m, Material):
+                raise TypeError("materials must be mpm_gb300.materials.Material")
+            arr[i] = _lib.MpmMaterial(int(m.kind), float(m.particle_volume), float(m.density), float(m.E),
+                                      float(m.nu), float(m.hardening), float(m.clamp_lo), float(m.clamp_hi),
+                                      float(m.bulk))
+        _lib.check(self.L.mpm_set_materials(self.ctx, arr, len(materials)), self.ctx)
+        self.materials = list(materials)
+
+    def set_params(self, **kw):
+        for k, v in kw.items():
+            setattr(self.params, k, v)
+        _lib.check(self.L.mpm_set_params(self.ctx, ctypes.byref(self.params)), self.ctx)
+
+    def set_tuning(self, steps_per_warp=0, tile_nodes=0, waves=0):
+        _lib.check(self.L.mpm_set_tuning(self.ctx, int(steps_per_warp), int(tile_nodes), int(waves)), self.ctx)
+
+    def upload(self, state: dict):
+        """particlesToDevice (src/mpm.cu:278-286): x, v, C, F, Jp, mat host arrays."""
+        n = int(np.asarray(state["x"]).shape[0])
+        x = _f32(state["x"], (n, 3))
+        v = _f32(state.get("v"), (n, 3))
+        C = _f32(state.get("C"), (n, 9))
+        F = _f32(state.get("F"), (n, 9))
+        J = _f32(state.get("Jp"), (n,))
+        mat = state.get("mat")
+        if mat is not None:
+            mat = np.ascontiguousarray(np.asarray(mat, dtype=np.uint8).reshape(n))
+        _lib.check(self.L.mpm_upload_soa(self.ctx, n, _ptr(x), _ptr(v), _ptr(C), _ptr(F), _ptr(J), _ptr(mat)),
+                   self.ctx)
+        self.n = n
+
+    initCuda = upload
+
+    def upload_aos(self, records: np.ndarray):
+        """Upload the reference's 104-byte MLS_APIC_Particle records."""
+        rec = np.ascontiguousarray(records)
+        n = rec.nbytes // 104
+        _lib.check(self.L.mpm_upload_aos(self.ctx, _ptr(rec), n), self.ctx)
+        self.n = n
+
+    # -- stepping ----------------------------------------------------------
+    def advance(self, nsteps: int = 1):
+        """Simulation::advance (src/mpm.cu:323-329), nsteps times, asynchronous."""
+        _lib.check(self.L.mpm_substep(self.ctx, int(nsteps)), self.ctx)
+
+    def sync(self):
+        _lib.check(self.L.mpm_sync(self.ctx), self.ctx)
+
+    def sort(self):
+        _lib.check(self.L.mpm_sort(self.ctx), self.ctx)
+
+    # -- readback ----------------------------------------------------------
+    def download(self, fields=("x", "v", "C", "F", "Jp", "mat")) -> dict:
+        n = self.n
+        out = {
+            "x": np.empty((n, 3), np.float32) if "x" in fields else None,
+            "v": np.empty((n, 3), np.float32) if "v" in fields else None,
+            "C": np.empty((n, 3, 3), np.float32) if "C" in fields else None,
+            "F": np.empty((n, 3, 3), np.float32) if "F" in fields else None,
+            "Jp": np.empty((n,), np.float32) if "Jp" in fields else None,
+            "mat": np.empty((n,), np.uint8) if "mat" in fields else None,
+        }
+        _lib.check(self.L.mpm_download_soa(self.ctx, _ptr(out["x"]), _ptr(out["v"]), _ptr(out["C"]),
+                                           _ptr(out["F"]), _ptr(out["Jp"]), _ptr(out["mat"])), self.ctx)
+        return {k: v for k, v in out.items() if v is not None}
+
+    def syncDevice(self) -> dict:
+        """Simulation::syncDevice (src/mpm.cu:209-211): blocking readback of all particles."""
+        self.sync()
+        return self.download()
+
+    def download_aos(self) -> np.ndarray:
+        out = np.zeros(self.n * 104, np.uint8)
+        _lib.check(self.L.mpm_download_aos(self.ctx, _ptr(out)), self.ctx)
+        return out
+
+    def get_grid(self, which: int = 0) -> np.ndarray:
+        """Grid of the last completed substep: 0 = after P2G (m v, m), 1 = after the grid op."""
+        out = np.empty((self.N, self.N, self.N, 4), np.float32)
+        _lib.check(self.L.mpm_get_grid(self.ctx, int(which), _ptr(out)), self.ctx)
+        return out
+
+    def getFullParticleCount(self) -> int:
+        return int(self.L.mpm_particle_count(self.ctx))
+
+    @property
+    def substeps(self) -> int:
+        return int(self.L.mpm_substep_count(self.ctx))
+
+    @property
+    def launches(self) -> int:
+        return int(self.L.mpm_launch_count(self.ctx))
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.mpm_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -1,0 +1,72 @@
+"""Build recipe for the oracle (test infrastructure).
+
+* ``libmpm_oracle.so`` — the C++ restatement of the reference substep (always).
+* ``_ref/libref_svd.so`` — the reference's own ``include/svd3_cuda.h`` compiled
+  for the host from where it lies in the reference checkout, through
+  ``ref_shim/`` (host definitions of the three CUDA rounding intrinsics it uses).
+  Built only when the reference checkout is present (this container); nothing
+  from the reference is copied into the repository.
+* ``_ref/libref_substep.so`` — the reference's own policy headers
+  (TransferScheme.h, MaterialModel.cuh, InterpolationKernel.cuh, types.h,
+  svd3_cuda.h) compiled for the host against the project-written Eigen subset in
+  ``ref_shim/``, driven by the loop skeleton in ``ref_substep.cpp``.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = os.environ.get("MPM_REFERENCE_ROOT", "/root/reference")
+
+
+def _run(cmd):
+    subprocess.run(cmd, check=True)
+
+
+def build_oracle(force: bool = False) -> str:
+    out = os.path.join(HERE, "libmpm_oracle.so")
+    src = os.path.join(HERE, "mpm_oracle.cpp")
+    hdr = os.path.join(HERE, "mpm_oracle.h")
+    if force or not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(src), os.path.getmtime(hdr)):
+        tmp = out + ".tmp"
+        _run(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
+              "-o", tmp, src])
+        os.replace(tmp, out)
+    return out
+
+
+def reference_available() -> bool:
+    return os.path.isfile(os.path.join(REF_ROOT, "include", "svd3_cuda.h"))
+
+
+def build_ref(force: bool = False) -> list:
+    """Compile the reference-derived host libraries into oracle/_ref (only when the
+    reference checkout exists). Returns the list of built paths."""
+    if not reference_available():
+        return []
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    inc = os.path.join(REF_ROOT, "include")
+    shim = os.path.join(HERE, "ref_shim")
+    built = []
+    for name, src in (("libref_svd.so", "ref_svd.cpp"), ("libref_substep.so", "ref_substep.cpp")):
+        srcp = os.path.join(HERE, src)
+        if not os.path.exists(srcp):
+            continue
+        out = os.path.join(outdir, name)
+        deps = [srcp] + [os.path.join(shim, f) for f in os.listdir(shim)]
+        if force or not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(d) for d in deps):
+            tmp = out + ".tmp"
+            # The shim directory comes first so its cuda.h / cuda_runtime.h / Eigen stand-ins
+            # are found before any system header of the same name.
+            _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w",
+                  "-I", shim, "-I", inc, "-o", tmp, srcp])
+            os.replace(tmp, out)
+        built.append(out)
+    return built
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    print(build_ref(force=True))

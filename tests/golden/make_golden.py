@@ -1,0 +1,79 @@
+"""Generate the golden fixtures under tests/golden from the reference checkout.
+
+Run here, where the reference is present (it is not on the GPU machines):
+    python tests/golden/make_golden.py
+Writes:
+  ref_linalg.json  — the matrices and tolerances of the reference's own tests
+                     (tests/test_linalg.cu: TestPolar.*, TestDevicePolar.Basic,
+                     TestDeterminant.Identity), read from the test source as text.
+  ref_svd.npz      — seeded 3x3 matrices and the outputs of the reference's own
+                     include/svd3_cuda.h, compiled for the host (oracle/_ref).
+  ref_substep.npz  — (when oracle/_ref/libref_substep.so is built) small seeded
+                     particle states advanced by the reference's own policy headers.
+"""
+import ctypes
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import build as obuild  # noqa: E402
+
+REF = obuild.REF_ROOT
+
+
+def linalg_vectors():
+    src = open(os.path.join(REF, "tests", "test_linalg.cu")).read()
+    mats = []
+    for m in re.finditer(r"M << ([^;]+);", src):
+        vals = [float(t) for t in m.group(1).split(",")]
+        mats.append(vals)
+    tols = sorted({float(t) for t in re.findall(r"ASSERT_LT\(\w+, ([0-9.e-]+)\)", src)})
+    return {"source": "tests/test_linalg.cu", "matrices": mats, "tolerances": tols,
+            "det_identity": 1.0}
+
+
+def svd_vectors():
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libref_svd.so"))
+    rng = np.random.default_rng(1234)
+    A = [rng.standard_normal((96, 3, 3)),
+         np.eye(3) + 0.05 * rng.standard_normal((96, 3, 3)),
+         np.eye(3)[None] * rng.uniform(0.5, 1.5, (32, 1, 1)),
+         rng.standard_normal((32, 3, 3)) * np.array([1, 1, 0])[None, :, None]]
+    A = np.concatenate(A, 0).astype(np.float32)
+    lin = linalg_vectors()
+    extra = np.array([np.array(m, np.float32).reshape(3, 3) for m in lin["matrices"]])
+    A = np.ascontiguousarray(np.concatenate([A, extra], 0))
+    n = A.shape[0]
+    U = np.zeros_like(A)
+    V = np.zeros_like(A)
+    s = np.zeros((n, 3), np.float32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    lib.ref_svd(ctypes.c_int64(n), P(A), P(U), P(s), P(V))
+    return {"A": A, "U": U, "s": s, "V": V}
+
+
+def main():
+    obuild.build_oracle()
+    built = obuild.build_ref()
+    if not built:
+        raise SystemExit("reference checkout not found; fixtures unchanged")
+    with open(os.path.join(HERE, "ref_linalg.json"), "w") as f:
+        json.dump(linalg_vectors(), f, indent=1)
+    np.savez_compressed(os.path.join(HERE, "ref_svd.npz"), **svd_vectors())
+    sub = os.path.join(ROOT, "oracle", "_ref", "libref_substep.so")
+    if os.path.exists(sub):
+        from tests.golden import ref_substep_vectors
+
+        np.savez_compressed(os.path.join(HERE, "ref_substep.npz"), **ref_substep_vectors.make(sub))
+    print("golden fixtures written")
+
+
+if __name__ == "__main__":
+    main()

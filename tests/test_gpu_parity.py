@@ -1,0 +1,240 @@
+"""GPU parity tests: the CUDA substep (through the C ABI) against the CPU oracle.
+
+Bars (written per test):
+  * one substep, FP32 oracle vs GPU: particle x, v, C, F, Jp and the grid after P2G
+    (mass and momentum) within 1e-5 relative (norm-wise, with the field scale of
+    tests/helpers.py as floor for fields that are zero up to rounding);
+  * the same against the FP64 oracle: within 1e-4 (FP32 rounding of the whole step);
+  * multi-substep runs: trajectories of total mass, momentum and kinetic energy.
+"""
+import numpy as np
+import pytest
+
+from helpers import compare_states, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(cfg, nsteps, want_grid=False, **over):
+    from mpm_gb300.simulation import Simulation
+
+    with Simulation.from_config(cfg, **over) as sim:
+        sim.upload(cfg["state"])
+        sim.advance(nsteps)
+        out = sim.syncDevice()
+        grids = (sim.get_grid(0), sim.get_grid(1)) if want_grid else (None, None)
+    return out, grids
+
+
+def run_oracle(oracle_lib, cfg, nsteps, dtype, params=None):
+    mats = [m.derived() for m in cfg["materials"]]
+    return oracle_lib.substep(cfg["state"], params or cfg["params"], mats, nsteps, dtype, want_grids=True)
+
+
+def configs():
+    from mpm_gb300 import scenes
+
+    return {
+        "elastic_10k_N16": lambda: scenes.config_elastic(),
+        "liquid_1M_N32": lambda: scenes.config_liquid(),
+        "snow_500k_N64": lambda: scenes.config_snow(),
+        "mixed_20k_N32": lambda: scenes.mixed_scene(),
+        "fixed_corotated_100k_N64": lambda: scenes.config_differentiable(),
+    }
+
+
+@pytest.mark.parametrize("name", list(configs().keys()))
+def test_one_substep_parity(gpu_lib, oracle_lib, name):
+    cfg = configs()[name]()
+    out, (g_p2g, g_op) = run_gpu(cfg, 1, want_grid=True)
+    o32, r_p2g, r_op = run_oracle(oracle_lib, cfg, 1, np.float32)
+    errs = compare_states(out, o32, cfg["params"], cfg["state"])
+    assert max(errs.values()) < 1e-5, errs
+    # grid after P2G: mass and momentum
+    assert rel_err(g_p2g[..., 3], r_p2g[..., 3]) < 1e-5
+    assert rel_err(g_p2g[..., :3], r_p2g[..., :3], 1e-12) < 1e-5
+    # grid after the op (velocities; mass slot 1 where m > 0)
+    assert rel_err(g_op[..., :3], r_op[..., :3], 1e-12) < 1e-5
+    assert np.array_equal(g_op[..., 3] == 1.0, r_op[..., 3] == 1.0)
+    # against FP64
+    o64, q_p2g, _ = run_oracle(oracle_lib, cfg, 1, np.float64)
+    errs64 = compare_states(out, o64, cfg["params"], cfg["state"])
+    assert max(errs64.values()) < 1e-4, errs64
+    assert rel_err(g_p2g[..., 3], q_p2g[..., 3]) < 1e-5
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_boundary_modes(gpu_lib, oracle_lib, mode):
+    from mpm_gb300 import scenes
+
+    cfg = scenes.config_snow(n=60_000, seed=3, N=32)
+    cfg["params"] = dict(cfg["params"], boundary_mode=mode, boundary_cells=3)
+    # push the snow against the floor and a wall so the walls act
+    cfg["state"]["x"][:, 1] -= 0.15
+    cfg["state"]["v"][:, 0] = -2.0
+    out, _ = run_gpu(cfg, 5)
+    o32, _, _ = run_oracle(oracle_lib, cfg, 5, np.float32)
+    errs = compare_states(out, o32, cfg["params"], cfg["state"])
+    assert max(errs.values()) < 2e-5, errs
+
+
+def test_g2p_guard_mode(gpu_lib, oracle_lib):
+    """src/mpm.cu:114 reproduced: particles with index > N^3 skip G2P but scatter."""
+    from mpm_gb300 import scenes
+
+    cfg = scenes.config_elastic(n=10_000, seed=4, N=16)
+    cfg["params"] = dict(cfg["params"], g2p_guard=1)
+    out, _ = run_gpu(cfg, 3, sort_interval=1)
+    o32, _, _ = run_oracle(oracle_lib, cfg, 3, np.float32)
+    errs = compare_states(out, o32, cfg["params"], cfg["state"])
+    assert max(errs.values()) < 1e-5, errs
+    lim = 16 ** 3
+    assert np.array_equal(out["x"][lim + 1:], cfg["state"]["x"][lim + 1:])
+
+
+@pytest.mark.parametrize("sort_interval", [0, 1, 3])
+def test_sort_does_not_change_results(gpu_lib, oracle_lib, sort_interval):
+    from mpm_gb300 import scenes
+
+    cfg = scenes.config_liquid(n=200_000, seed=5)
+    out, _ = run_gpu(cfg, 6, sort_interval=sort_interval)
+    o32, _, _ = run_oracle(oracle_lib, cfg, 6, np.float32)
+    errs = compare_states(out, o32, cfg["params"], cfg["state"])
+    assert max(errs.values()) < 2e-5, errs
+
+
+@pytest.mark.parametrize("tuning", [(1, 64, 0), (4, 4096, 1), (16, 8192, 0), (8, 27, 0)])
+def test_tuning_variants(gpu_lib, oracle_lib, tuning):
+    """Chunk sizes and tile capacities (including tiles too small to use) give the same result."""
+    from mpm_gb300 import scenes
+    from mpm_gb300.simulation import Simulation
+
+    cfg = scenes.config_snow(n=100_000, seed=6, N=64)
+    with Simulation.from_config(cfg) as sim:
+        sim.set_tuning(*tuning)
+        sim.upload(cfg["state"])
+        sim.advance(2)
+        out = sim.syncDevice()
+    o32, _, _ = run_oracle(oracle_lib, cfg, 2, np.float32)
+    errs = compare_states(out, o32, cfg["params"], cfg["state"])
+    assert max(errs.values()) < 1e-5, errs
+
+
+def test_multi_substep_trajectory(gpu_lib, oracle_lib):
+    """1000 substeps of the elastic cube: total mass exact, momentum and kinetic
+    energy trajectories within 1e-3 of the FP64 oracle's (sampled every 100)."""
+    from mpm_gb300 import scenes
+    from mpm_gb300.simulation import Simulation
+
+    cfg = scenes.config_elastic(n=10_000, seed=7)
+    mats = [m.derived() for m in cfg["materials"]]
+    m = float(mats[0]["particle_mass"])
+    state = cfg["state"]
+    with Simulation.from_config(cfg) as sim:
+        sim.upload(state)
+        ref = {k: np.array(v, np.float64) if k != "mat" else v for k, v in state.items()}
+        for block in range(10):
+            sim.advance(100)
+            out = sim.syncDevice()
+            ref, g, _ = oracle_lib.substep(ref, cfg["params"], mats, 100, np.float64, want_grids=True)
+            p_gpu = m * out["v"].astype(np.float64).sum(0)
+            p_ref = m * ref["v"].sum(0)
+            ke_gpu = 0.5 * m * (out["v"].astype(np.float64) ** 2).sum()
+            ke_ref = 0.5 * m * (ref["v"] ** 2).sum()
+            assert abs(g[..., 3].sum() - m * 10_000) < 1e-9 * m * 10_000
+            assert np.linalg.norm(p_gpu - p_ref) <= 1e-3 * np.linalg.norm(p_ref) + 1e-9
+            assert abs(ke_gpu - ke_ref) <= 1e-3 * ke_ref + 1e-12
+        errs = compare_states(out, ref, cfg["params"], ref)
+        assert errs["x"] < 1e-5, errs
+
+
+def test_single_particle_known_answer(gpu_lib):
+    """A particle at rest with F = I: after one substep v = dt g and C = 0."""
+    from mpm_gb300 import materials as M
+    from mpm_gb300.simulation import Simulation
+
+    st = {"x": np.array([[0.5, 0.5, 0.5]], np.float32)}
+    with Simulation(dt=1e-4, N=16, gravity=-9.8, materials=[M.elastic(1e-5)]) as sim:
+        sim.upload(st)
+        sim.advance(1)
+        out = sim.syncDevice()
+    g = np.float32(1e-4) * np.float32(-9.8)
+    assert abs(out["v"][0, 1] - g) < 1e-6 * abs(g)
+    assert abs(out["v"][0, 0]) < 1e-12 and abs(out["v"][0, 2]) < 1e-12
+    assert np.abs(out["C"]).max() < 1e-6
+
+
+def test_empty_and_outside_particles(gpu_lib, oracle_lib):
+    from mpm_gb300 import materials as M
+    from mpm_gb300.simulation import Simulation
+
+    with Simulation(dt=1e-4, N=16, materials=[M.elastic(1e-5)]) as sim:
+        sim.upload({"x": np.zeros((0, 3), np.float32)})
+        sim.advance(3)
+        sim.sync()
+        assert sim.getFullParticleCount() == 0
+        # particles fully outside the grid are frozen; one near the upper faces is clipped
+        x = np.array([[-0.5, 0.5, 0.5], [0.5, 1.7, 0.5], [0.98, 0.98, 0.98], [0.01, 0.02, 0.5], [0.5, 0.5, 0.5]],
+                     np.float32)
+        st = {"x": x, "v": np.tile(np.array([[0.1, -0.3, 0.2]], np.float32), (5, 1))}
+        sim.upload(st)
+        sim.advance(2)
+        out = sim.syncDevice()
+    full = {"x": x, "v": st["v"], "C": np.zeros((5, 3, 3), np.float32), "F": np.tile(np.eye(3), (5, 1, 1)),
+            "Jp": np.ones(5, np.float32), "mat": np.zeros(5, np.uint8)}
+    o32, _, _ = oracle_lib.substep(full, {"dt": 1e-4, "N": 16, "gravity": -9.81}, [M.elastic(1e-5).derived()], 2,
+                                   np.float32)
+    assert np.array_equal(out["x"][:2], x[:2])
+    assert np.allclose(out["x"], o32["x"], atol=1e-6)
+    assert np.allclose(out["v"], o32["v"], atol=1e-5)
+
+
+def test_aos_round_trip(gpu_lib):
+    from mpm_gb300 import aos, scenes
+    from mpm_gb300.simulation import Simulation
+
+    cfg = scenes.mixed_scene(n=3000, seed=8)
+    st = cfg["state"]
+    st["C"] = np.random.default_rng(0).standard_normal((3000, 3, 3)).astype(np.float32) * 0.01
+    rec = aos.pack(st)
+    with Simulation.from_config(cfg) as sim:
+        sim.upload_aos(rec)
+        back = sim.download_aos()
+        soa = sim.download()
+    assert np.array_equal(back, rec)
+    for k in ("x", "v", "C", "F", "Jp", "mat"):
+        assert np.array_equal(soa[k], st[k]), k
+
+
+def test_check_finite_flags_blow_up(gpu_lib):
+    """An unstable time step drives particles non-finite; the kernel records it in the
+    status word and mpm_sync reports MPM_ERR_STATE (no trap)."""
+    from mpm_gb300 import _lib, scenes
+    from mpm_gb300.simulation import Simulation
+
+    cfg = scenes.config_elastic(n=2000, seed=9)
+    cfg["materials"][0].E = 1e9
+    with Simulation.from_config(cfg, check_finite=True, dt=5e-3) as sim:
+        sim.upload(cfg["state"])
+        sim.advance(200)
+        with pytest.raises(_lib.MpmError) as ei:
+            sim.sync()
+        assert ei.value.code == 3
+        sim.sync()  # the status word is cleared once reported
+
+
+def test_api_errors(gpu_lib):
+    from mpm_gb300 import _lib
+    from mpm_gb300 import materials as M
+    from mpm_gb300.simulation import Simulation
+
+    with pytest.raises(_lib.MpmError):
+        Simulation(N=2)
+    with Simulation(N=16) as sim:
+        with pytest.raises(_lib.MpmError):
+            sim.advance(1)  # no materials yet
+        sim.set_materials([M.elastic(1e-5)])
+        with pytest.raises(_lib.MpmError):
+            sim.upload({"x": np.zeros((2, 3), np.float32), "mat": np.array([0, 3], np.uint8)})
+        with pytest.raises(_lib.MpmError):
+            sim.get_grid(0)  # no completed substep
