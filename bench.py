@@ -163,7 +163,7 @@ def cpu_baseline(cfg, budget_s=12.0, max_particles=None):
         n = max_particles
     threads = oracle.max_threads()
     t1 = oracle.time_f32(st, cfg["params"], mats, 1, threads)
-    steps = int(max(1, min(50, budget_s / max(t1, 1e-6))))
+    steps = int(max(1, min(500, budget_s / max(t1, 1e-6))))
     t = oracle.time_f32(st, cfg["params"], mats, steps, threads)
     return {"value": n * steps / t, "unit": "particle-substeps/s", "cores": threads, "kind": "port",
             "sample": f"{n} particles x {steps} substeps of the same scene (FP32 oracle, {threads} threads, "
@@ -230,9 +230,12 @@ def run_ours(args):
     cfg, workload = make_cfg(args.config)
     n = cfg["state"]["x"].shape[0]
     N = cfg["params"]["N"]
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the events and the L2 flush are ordered with the
+    # library's kernels on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sim = Simulation.from_config(cfg)
-    sim.L.mpm_set_stream(sim.ctx, stream.cuda_stream)
+    sim.set_stream(stream.cuda_stream)
     sim.upload(cfg["state"])
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 

@@ -4,9 +4,12 @@
 namespace mpm {
 
 // ---------------------------------------------------------------------------
-// Cell sort: counting sort of particles by the linear index of their base cell
-// (keys < N^3).  histogram (warp-aggregated atomics) -> exclusive scan -> scatter.
-// Order inside a cell is not stable; the substep does not depend on it.
+// Cell sort: counting sort of particles by a bricked key of their base cell:
+// bricks of 4x4x4 cells in row-major order, cells row-major inside a brick.  Any
+// run of consecutive sorted particles then covers a compact box of cells in all
+// three dimensions, which keeps the substep kernel's per-chunk grid tile small.
+// histogram (warp-aggregated atomics) -> exclusive scan -> scatter.  Order inside
+// a cell is not stable; the substep does not depend on it.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t cell_key(const float* s, int64_t st, int64_t p, float dx_inv, int N) {
   int b[3];
@@ -15,7 +18,9 @@ __device__ __forceinline__ uint32_t cell_key(const float* s, int64_t st, int64_t
     int v = QuadraticInterpolationKernel::base_cell(s[(kX + d) * st + p], dx_inv);
     b[d] = min(max(v, 0), N - 1);
   }
-  return (uint32_t)(((int64_t)b[0] * N + b[1]) * N + b[2]);
+  const uint32_t nb = (uint32_t)(N + 3) >> 2;
+  const uint32_t brick = ((uint32_t)(b[0] >> 2) * nb + (uint32_t)(b[1] >> 2)) * nb + (uint32_t)(b[2] >> 2);
+  return brick * 64u + (uint32_t)(((b[0] & 3) << 4) | ((b[1] & 3) << 2) | (b[2] & 3));
 }
 
 __global__ void sort_histogram(SortArgs a) {

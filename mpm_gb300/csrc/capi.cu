@@ -11,7 +11,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/mpm_gb300.h"
+#include "mpm_gb300.h"
 #include "mpm_internal.h"
 
 using namespace mpm;
@@ -42,6 +42,7 @@ struct mpm_ctx {
   // grid: three rotating buffers
   float4* grid[3] = {nullptr, nullptr, nullptr};
   int64_t cells = 0;
+  int64_t sort_keys = 0;  // key space of the bricked cell sort (>= cells)
   int cur = 0;            // slot holding the P2G grid of the next substep (when pending)
   int prev = -1;          // slot the last completed substep's G2P read
   bool pending = false;
@@ -55,12 +56,14 @@ struct mpm_ctx {
   float* stage = nullptr;
   size_t stage_bytes = 0;
   int* status = nullptr;
+  int* work = nullptr;  // two range counters, alternating between substep launches
+  int launch_parity = 0;
 
   int64_t substeps = 0;
   int64_t since_sort = 0;
   int64_t launches = 0;
-  int steps_per_warp = 8;
-  int tile_cap = 4096;
+  int steps_per_warp = 2;
+  int tile_cap = 256;  // nodes per warp tile
   int waves = 0;
   std::string last_error;
 };
@@ -200,19 +203,18 @@ StepArgs make_step_args(mpm_ctx* c) {
   return a;
 }
 
-// Chunk size: about steps_per_warp particles per lane, rounded so the chunks split
-// evenly over the resident CTAs.
+// Ranges of steps_per_warp steps (32 particles each), fewer for small particle
+// counts so every resident warp gets work; the kernel deals them out dynamically.
 void launch_shape(mpm_ctx* c, StepKind kind, bool guard, int& chunk, int& blocks) {
-  const size_t smem = (kind == kStepP2GOnly) ? 0 : (size_t)c->tile_cap * sizeof(float4);
+  const size_t smem = step_smem_bytes(kind, c->tile_cap);
   const int bps = step_blocks_per_sm(kind, c->liquid_layout, guard, smem);
-  const int64_t resident = (int64_t)c->num_sms * bps;
-  const int64_t target = (int64_t)kThreads * c->steps_per_warp;
-  int64_t waves = c->waves > 0 ? c->waves : std::max<int64_t>(1, (c->n + resident * target / 2) / (resident * target));
-  int64_t steps = (c->n + resident * waves * kThreads - 1) / (resident * waves * kThreads);
-  steps = std::max<int64_t>(1, std::min<int64_t>(steps, 64));
-  chunk = (int)(steps * kThreads);
-  const int64_t nchunks = (c->n + chunk - 1) / chunk;
-  blocks = (int)std::max<int64_t>(1, std::min<int64_t>(nchunks, resident));
+  const int64_t resident_warps = (int64_t)c->num_sms * bps * kStepWarps;
+  int64_t steps = c->steps_per_warp;
+  while (steps > 1 && c->n < resident_warps * 32 * steps * 2) steps /= 2;
+  chunk = (int)(steps * 32);
+  const int64_t nranges = (c->n + chunk - 1) / chunk;
+  blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nranges + kStepWarps - 1) / kStepWarps,
+                                                       (int64_t)c->num_sms * bps));
 }
 
 mpm_status run_step(mpm_ctx* c, StepKind kind) {
@@ -221,6 +223,9 @@ mpm_status run_step(mpm_ctx* c, StepKind kind) {
   int chunk, blocks;
   launch_shape(c, kind, guard, chunk, blocks);
   a.chunk = chunk;
+  a.work = c->work + (c->launch_parity & 1);
+  a.work_next = c->work + ((c->launch_parity + 1) & 1);
+  c->launch_parity ^= 1;
   const int r = c->cur;
   a.grid_in = (kind == kStepP2GOnly) ? nullptr : c->grid[r];
   a.grid_out = c->grid[(r + 1) % 3];
@@ -247,7 +252,7 @@ mpm_status run_sort(mpm_ctx* c) {
   s.keys = c->keys;
   s.counts = c->counts;
   s.block_sums = c->block_sums;
-  s.cells = c->cells;
+  s.cells = c->sort_keys;
   s.N = (int)c->params.N;
   s.dx_inv = c->K.dx_inv;
   // liquid layout: x, v, C, J (16 components); general: all 25
@@ -296,10 +301,15 @@ mpm_status mpm_create(const mpm_params* params, mpm_ctx** out) {
       return bail(MPM_ERR_CUDA);
   }
   const int per = kThreads * 8;
-  const int64_t nb = (c->cells + per - 1) / per;
-  if (cudaMalloc(&c->counts, sizeof(int) * c->cells) != cudaSuccess) return bail(MPM_ERR_NOMEM);
+  const int64_t nbr = (params->N + 3) / 4;
+  c->sort_keys = nbr * nbr * nbr * 64;
+  const int64_t nb = (c->sort_keys + per - 1) / per;
+  if (cudaMalloc(&c->counts, sizeof(int) * c->sort_keys) != cudaSuccess) return bail(MPM_ERR_NOMEM);
   if (cudaMalloc(&c->block_sums, sizeof(int) * std::max<int64_t>(nb, 1)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
   if (cudaMalloc(&c->status, sizeof(int)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
+  if (cudaMalloc(&c->work, 2 * sizeof(int)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
+  if (cudaMemsetAsync(c->work, 0, 2 * sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
+
   if (cudaMemsetAsync(c->status, 0, sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
   // component lists for the sort: liquid layout = x, v, C, J; general = all
   int comps[kNumComps];
@@ -328,6 +338,7 @@ mpm_status mpm_destroy(mpm_ctx* c) {
   cudaFree(c->comp_list);
   cudaFree(c->stage);
   cudaFree(c->status);
+  cudaFree(c->work);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return MPM_OK;
@@ -379,6 +390,8 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   if (mat)
     for (int64_t p = 0; p < n; ++p)
       if (mat[p] >= c->n_materials) return fail(c, MPM_ERR_INVALID, "material index out of range");
+  for (int64_t i = 0; i < 3 * n; ++i)
+    if (!std::isfinite(x[i])) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
   st = ensure_particles(c, n);
   if (st != MPM_OK) return st;
   c->n = n;
@@ -584,8 +597,8 @@ mpm_status mpm_last_error(const mpm_ctx* c, char* buf, size_t len) {
 
 mpm_status mpm_set_tuning(mpm_ctx* c, int32_t steps_per_warp, int32_t tile_nodes, int32_t waves) {
   if (!c) return MPM_ERR_INVALID;
-  if (steps_per_warp < 0 || steps_per_warp > 64) return fail(c, MPM_ERR_INVALID, "steps_per_warp out of range");
-  if (tile_nodes < 0 || tile_nodes > 13000) return fail(c, MPM_ERR_INVALID, "tile_nodes out of range (max 13000)");
+  if (steps_per_warp < 0 || steps_per_warp > 256) return fail(c, MPM_ERR_INVALID, "steps_per_warp out of range");
+  if (tile_nodes < 0 || tile_nodes > 288) return fail(c, MPM_ERR_INVALID, "tile_nodes out of range (max 288 per warp)");
   if (waves < 0) return fail(c, MPM_ERR_INVALID, "waves must be >= 0");
   if (steps_per_warp) c->steps_per_warp = steps_per_warp;
   if (tile_nodes) c->tile_cap = tile_nodes;

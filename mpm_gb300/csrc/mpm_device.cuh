@@ -16,8 +16,10 @@
 namespace mpm {
 
 constexpr int kMaxMaterials = 16;
-constexpr int kThreads = 256;  // CTA size of the particle kernels (8 warps)
+constexpr int kThreads = 256;  // CTA size of the auxiliary kernels (8 warps)
 constexpr int kWarps = kThreads / 32;
+constexpr int kStepThreads = 384;  // CTA size of the substep kernel (12 warps, <= 168 registers)
+constexpr int kStepWarps = kStepThreads / 32;
 constexpr unsigned kFull = 0xffffffffu;
 
 enum MatKind { kSnow = 0, kFixedCorotated = 1, kJelly = 2, kLiquid = 3 };
@@ -87,9 +89,10 @@ __device__ __forceinline__ bool outside_domain(int b0, int b1, int b2, int N) {
 __device__ __forceinline__ float3 grid_node_velocity(float4 g, int i, int j, int k, const SimConsts& K) {
   float3 v = make_float3(g.x, g.y, g.z);
   if (g.w > 0.f) {
-    v.x = g.x / g.w;
-    v.y = g.y / g.w;
-    v.z = g.z / g.w;
+    const float inv = 1.f / g.w;
+    v.x = g.x * inv;
+    v.y = g.y * inv;
+    v.z = g.z * inv;
     v.y += K.dtg;
     bool sticky, floor_;
     const int N = K.N;

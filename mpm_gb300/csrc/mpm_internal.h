@@ -20,11 +20,13 @@ struct StepArgs {
   float4* grid_out;       // P2G accumulation target (already zero)
   float4* grid_zero;      // buffer to clear for the launch after next
   int64_t grid_cells;
-  int chunk;              // particles per CTA chunk (multiple of kThreads)
+  int chunk;              // particles per range (multiple of 32); ranges go to warps dynamically
   int tile_cap;           // capacity of the shared-memory velocity tile (nodes)
   int64_t guard_limit;    // G2P only for id <= guard_limit when the guard is on
   int check_finite;
   int* status;
+  int* work;              // range counter of this launch, starts at 0
+  int* work_next;         // range counter of the next launch, cleared by this one
   SimConsts K;
 };
 
@@ -33,6 +35,8 @@ enum StepKind { kStepP2GOnly = 0, kStepFused = 1, kStepG2POnly = 2 };
 // Launches one substep kernel variant. liquid = liquid-only layout.
 cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guard, int grid_blocks,
                         cudaStream_t st);
+// Dynamic shared memory of a variant: velocity tile (G2P) + per-warp reduction buffers (P2G).
+size_t step_smem_bytes(StepKind kind, int tile_cap);
 // Max resident CTAs per SM for the variant at the given dynamic shared memory.
 int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem);
 
@@ -47,9 +51,9 @@ struct SortArgs {
   const uint32_t* idA;
   uint32_t* idB;
   uint32_t* keys;
-  int* counts;   // grid_cells
+  int* counts;   // one per sort key
   int* block_sums;
-  int64_t cells;
+  int64_t cells;  // sort key space (bricked cell index range)
   int N;
   float dx_inv;
   int ncomp;            // components to move

@@ -3,8 +3,8 @@
 // The reference runs four launches per substep (src/mpm.cu:323-329): cudaMemset of
 // the grid, particleToGrid (27 x 4 float atomics per particle), gridOpKernel, and
 // gridToParticle.  Here one launch does
-//     G2P of substep n  (gather from the P2G grid of substep n, grid op applied on
-//                        the fly while a block stages its grid tile in shared memory)
+//     G2P of substep n  (gather from the P2G grid of substep n; the grid op is applied
+//                        while a block stages its grid tile in shared memory)
 //   + constitutive update + advection, state written once
 //   + P2G of substep n+1 (scatter of the new state)
 //   + clearing of the grid buffer substep n-1 read,
@@ -15,18 +15,24 @@
 // particles; each warp walks its slice 32 particles at a time (lane = particle,
 // coalesced SoA loads/stores).  P2G contributions are accumulated in registers
 // (27 nodes x 4 values per lane) while the lane's particles stay in one cell; when a
-// lane's cell changes, the warp flushes whole cell groups with a shuffle
-// reduce-scatter (lane l ends with node l's total) and one vector atomic per node,
-// or, when a warp's particles scatter over many cells, each lane adds its 27 nodes
-// directly.  Dense scenes (100+ particles per cell) thus issue well under one
-// global atomic per particle instead of the reference's 108.
+// lane's cell changes, the warp flushes whole cell groups: members park their
+// accumulators in a per-warp shared-memory buffer, lane l sums node l over the
+// group and issues one vector atomic.  When a warp's particles scatter over many
+// cells, each lane adds its 27 nodes directly.  Dense scenes (100+ particles per
+// cell) thus issue well under one global atomic per particle instead of the
+// reference's 108.
+//
+// Code size matters: the hot loop holds one copy each of the gather, the
+// accumulate and the flush (the rare paths are out of line) so it stays resident
+// in the instruction cache at one 8-warp CTA per SM.
 #include <climits>
 
 #include "mpm_internal.h"
 
 namespace mpm {
 
-constexpr int kMaxGroups = 3;  // cell groups reduced with shuffles per flush before falling back
+constexpr int kRedStride = 33;     // float4 row stride of the per-warp transpose buffer
+constexpr int kRedFloat4 = 27 * kRedStride;
 
 __device__ __forceinline__ int pack_key(int b0, int b1, int b2) {
   return ((b0 + 4) << 20) | ((b1 + 4) << 10) | (b2 + 4);
@@ -37,10 +43,23 @@ __device__ __forceinline__ void unpack_key(int key, int& b0, int& b1, int& b2) {
   b2 = (key & 1023) - 4;
 }
 
-// p2g_node_contribution (include/TransferScheme.h:88-100) for all 27 nodes:
-//   acc[n] += w_n (m v + A dpos_n), acc[n].w += w_n m
-__device__ __forceinline__ void p2g_accumulate(float (&acc)[27][4], const float w[3][3], const float d[3][3],
-                                               const float Aff[3][3], const float mv[3], float m) {
+__device__ __forceinline__ void add_node(float4* grid, int N, int i, int j, int k, float4 val) {
+  if ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N)
+    atomicAdd(grid + ((int64_t)i * N + j) * N + k, val);
+}
+
+__device__ __forceinline__ void f4add(float4& a, const float4 b) {
+  a.x += b.x;
+  a.y += b.y;
+  a.z += b.z;
+  a.w += b.w;
+}
+
+// p2g_node_contribution (include/TransferScheme.h:88-100) for all 27 nodes, written
+// as column `lane` of the warp's transpose buffer: row n = node (a, b, c) holds
+//   (w_n (m v + A dpos_n), w_n m).
+__device__ __forceinline__ void p2g_write_column(float4* wbuf, int lane, const float w[3][3], const float d[3][3],
+                                                 const float Aff[3][3], const float mv[3], float m) {
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     float qa[3];
@@ -55,139 +74,76 @@ __device__ __forceinline__ void p2g_accumulate(float (&acc)[27][4], const float 
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const float wt = wab * w[2][c];
-        const int n = a * 9 + b * 3 + c;
-#pragma unroll
-        for (int r = 0; r < 3; ++r) acc[n][r] = fmaf(wt, fmaf(Aff[r][2], d[2][c], qab[r]), acc[n][r]);
-        acc[n][3] = fmaf(wt, m, acc[n][3]);
+        float4 val;
+        val.x = wt * fmaf(Aff[0][2], d[2][c], qab[0]);
+        val.y = wt * fmaf(Aff[1][2], d[2][c], qab[1]);
+        val.z = wt * fmaf(Aff[2][2], d[2][c], qab[2]);
+        val.w = wt * m;
+        wbuf[(a * 9 + b * 3 + c) * kRedStride + lane] = val;
       }
     }
   }
 }
 
-template <int H>
-__device__ __forceinline__ void reduce_half(float (&r)[16][4], int lane) {
-  const bool up = (lane & H) != 0;
+// Warp-collective scatter of one step's P2G contributions (particleToGrid's atomic
+// loop, src/mpm.cu:47-73).  Every lane with a contribution writes its 27 node values
+// as one column of the warp's buffer.  Lane l < 27 then walks the 32 columns in
+// order, summing node l over each run of consecutive lanes that share a base cell
+// (cell-sorted particles make a run per cell) and issuing one vector atomic per run;
+// columns of lanes without a contribution fall in runs with key -1, which are
+// dropped.  The run boundaries are warp-uniform, so the walk does not diverge.
+__device__ __forceinline__ void p2g_scatter_step(float4* wbuf, int lane, int key, const float w[3][3],
+                                                 const float d[3][3], const float Aff[3][3], const float mv[3],
+                                                 float m, float4* grid, int N) {
+  const unsigned has = __ballot_sync(kFull, key >= 0);
+  if (has == 0u) return;
+  const int prev = __shfl_up_sync(kFull, key, 1);
+  const unsigned starts = __ballot_sync(kFull, lane == 0 || key != prev);
+  if (key >= 0) p2g_write_column(wbuf, lane, w, d, Aff, mv, m);
+  __syncwarp();
+  const int oi = lane / 9, oj = (lane / 3) % 3, ok = lane % 3;
+  const float4* row = wbuf + (lane < 27 ? lane : 0) * kRedStride;
+  int run_key = __shfl_sync(kFull, key, 0);
+  float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-  for (int j = 0; j < H; ++j)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const float lo = r[j][c], hi = r[j + H][c];
-      const float send = up ? lo : hi;
-      const float keep = up ? hi : lo;
-      r[j][c] = keep + __shfl_xor_sync(kFull, send, H);
+  for (int j = 0; j < 32; ++j) {
+    if (j > 0 && ((starts >> j) & 1u)) {  // warp-uniform
+      if (run_key >= 0 && lane < 27) {
+        int b0, b1, b2;
+        unpack_key(run_key, b0, b1, b2);
+        add_node(grid, N, b0 + oi, b1 + oj, b2 + ok, sum);
+      }
+      sum = make_float4(0.f, 0.f, 0.f, 0.f);
+      run_key = __shfl_sync(kFull, key, j);
     }
-}
-
-__device__ __forceinline__ void add_node(float4* grid, int N, int i, int j, int k, float4 val) {
-  if ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N)
-    atomicAdd(grid + ((int64_t)i * N + j) * N + k, val);
-}
-
-// Warp-collective: sum the accumulators of the lanes with in == true (one cell group,
-// base cell `key`) and add the 27 node totals to the grid, one vector atomic per node.
-__device__ __forceinline__ void flush_group(const float (&acc)[27][4], bool in, int key, int lane, float4* grid,
-                                            int N) {
-  float r[16][4];
-  const bool up = (lane & 16) != 0;
-#pragma unroll
-  for (int j = 0; j < 16; ++j)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const float lo = acc[j][c];
-      const float hi = (j + 16 < 27) ? acc[(j + 16 < 27) ? j + 16 : 0][c] : 0.f;
-      float send = up ? lo : hi;
-      float keep = up ? hi : lo;
-      send = in ? send : 0.f;
-      keep = in ? keep : 0.f;
-      r[j][c] = keep + __shfl_xor_sync(kFull, send, 16);
-    }
-  reduce_half<8>(r, lane);
-  reduce_half<4>(r, lane);
-  reduce_half<2>(r, lane);
-  reduce_half<1>(r, lane);
-  if (lane < 27) {
+    f4add(sum, row[j]);
+  }
+  if (run_key >= 0 && lane < 27) {
     int b0, b1, b2;
-    unpack_key(key, b0, b1, b2);
-    add_node(grid, N, b0 + lane / 9, b1 + (lane / 3) % 3, b2 + lane % 3,
-             make_float4(r[0][0], r[0][1], r[0][2], r[0][3]));
+    unpack_key(run_key, b0, b1, b2);
+    add_node(grid, N, b0 + oi, b1 + oj, b2 + ok, sum);
   }
+  __syncwarp();
 }
 
-// One lane adds its own 27 accumulators (sparse fallback).
-__device__ __forceinline__ void flush_direct(const float (&acc)[27][4], int key, float4* grid, int N) {
-  int b0, b1, b2;
-  unpack_key(key, b0, b1, b2);
+// weights_per_direction for all three dimensions plus the node offsets
+// dpos = (base + a) dx - x (src/mpm.cu:50-60).
+__device__ __forceinline__ void stencil(const float x[3], const SimConsts& K, int b[3], float w[3][3], float d[3][3]) {
 #pragma unroll
-  for (int n = 0; n < 27; ++n)
-    add_node(grid, N, b0 + n / 9, b1 + (n / 3) % 3, b2 + n % 3, make_float4(acc[n][0], acc[n][1], acc[n][2], acc[n][3]));
-}
-
-__device__ __forceinline__ void zero_acc(float (&acc)[27][4]) {
-#pragma unroll
-  for (int n = 0; n < 27; ++n)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) acc[n][c] = 0.f;
-}
-
-// Warp-collective flush of every cell group whose `flag` is set in some member lane.
-__device__ __forceinline__ void flush_groups(float (&acc)[27][4], int& acc_key, bool flag, int lane, float4* grid,
-                                             int N) {
-  const unsigned need = __ballot_sync(kFull, flag);
-  const unsigned same = __match_any_sync(kFull, acc_key);
-  const bool gflag = (same & need) != 0u && acc_key >= 0;
-  const bool leader = gflag && lane == __ffs(same) - 1;
-  unsigned leaders = __ballot_sync(kFull, leader);
-  if (__popc(leaders) <= kMaxGroups) {
-    while (leaders) {
-      const int ll = __ffs(leaders) - 1;
-      leaders &= leaders - 1u;
-      const int K = __shfl_sync(kFull, acc_key, ll);
-      const bool in = acc_key == K;
-      flush_group(acc, in, K, lane, grid, N);
-      if (in) {
-        zero_acc(acc);
-        acc_key = -1;
-      }
-    }
-  } else if (gflag) {
-    flush_direct(acc, acc_key, grid, N);
-    zero_acc(acc);
-    acc_key = -1;
+  for (int dim = 0; dim < 3; ++dim) {
+    QuadraticInterpolationKernel::weights_per_direction(x[dim], K.dx_inv, b[dim], w[dim]);
+    d[dim][0] = fmaf((float)b[dim], K.dx, -x[dim]);
+    d[dim][1] = d[dim][0] + K.dx;
+    d[dim][2] = d[dim][1] + K.dx;
   }
-}
-
-// Velocity of grid node (i,j,k) for G2P, either from the block's tile or straight
-// from the P2G grid (grid op applied per fetch) when the tile did not fit.
-struct NodeFetch {
-  const float4* tile;
-  const float4* grid_in;
-  int t0, t1, t2, d1, d2;  // tile origin and extents (d0 implied)
-  int vol;                 // nodes in the tile
-  bool use_tile;
-};
-
-__device__ __forceinline__ float3 fetch_node(const NodeFetch& f, const SimConsts& K, int i, int j, int k) {
-  if (f.use_tile) {
-    const int idx = ((i - f.t0) * f.d1 + (j - f.t1)) * f.d2 + (k - f.t2);
-    // every gathered node lies in the chunk's tile by construction; the check keeps a
-    // node outside it (which would be a bug) on the global path instead of off the tile
-    if ((unsigned)idx < (unsigned)f.vol && (unsigned)(k - f.t2) < (unsigned)f.d2 &&
-        (unsigned)(j - f.t1) < (unsigned)f.d1) {
-      const float4 g = f.tile[idx];
-      return make_float3(g.x, g.y, g.z);
-    }
-  }
-  const float4 g = __ldg(f.grid_in + ((int64_t)i * K.N + j) * K.N + k);
-  return grid_node_velocity(g, i, j, k, K);
 }
 
 // gridToParticle gather (src/mpm.cu:136-167 + g2p_node_contribution), factorised per
-// dimension: v = sum w g, C = D sum w g dpos^T (D = 4/dx^2), with nodes outside the
-// grid skipped as the reference's clipped loop does.
-__device__ __forceinline__ void g2p_gather(const NodeFetch& f, const SimConsts& K, const int b[3], const float w[3][3],
-                                           const float d[3][3], float v[3], float C[3][3]) {
-  const int N = K.N;
-  const bool interior = b[0] >= 0 && b[0] + 2 < N && b[1] >= 0 && b[1] + 2 < N && b[2] >= 0 && b[2] + 2 < N;
+// dimension: v = sum w g, C = D sum w g dpos^T (D = 4/dx^2).  `node(a, b, c)`
+// returns the grid velocity of node base + (a, b, c), zero outside the grid.
+template <class NodeFn>
+__device__ __forceinline__ void g2p_gather(NodeFn node, const SimConsts& K, const float w[3][3], const float d[3][3],
+                                           float v[3], float C[3][3]) {
   float c0[3] = {0.f, 0.f, 0.f}, c1[3] = {0.f, 0.f, 0.f}, c2[3] = {0.f, 0.f, 0.f};
   v[0] = v[1] = v[2] = 0.f;
 #pragma unroll
@@ -198,10 +154,7 @@ __device__ __forceinline__ void g2p_gather(const NodeFetch& f, const SimConsts& 
       float S[3] = {0.f, 0.f, 0.f}, T[3] = {0.f, 0.f, 0.f};
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const int i = b[0] + a, j = b[1] + bb, k = b[2] + c;
-        float3 g = make_float3(0.f, 0.f, 0.f);
-        if (interior || ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N))
-          g = fetch_node(f, K, i, j, k);
+        const float4 g = node(a, bb, c);
         const float wz = w[2][c], wzd = w[2][c] * d[2][c];
         S[0] = fmaf(wz, g.x, S[0]);
         S[1] = fmaf(wz, g.y, S[1]);
@@ -235,127 +188,160 @@ __device__ __forceinline__ void g2p_gather(const NodeFetch& f, const SimConsts& 
   }
 }
 
-// weights_per_direction for all three dimensions plus the node offsets
-// dpos = (base + a) dx - x (src/mpm.cu:50-60).
-__device__ __forceinline__ void stencil(const float x[3], const SimConsts& K, int b[3], float w[3][3], float d[3][3]) {
+struct G2POut {
+  float v[3];
+  float C[3][3];
+};
+
+// Gather straight from the P2G grid (grid op per node) for chunks whose tile does
+// not fit in shared memory; out of line to keep the hot loop small.
+__device__ __noinline__ G2POut g2p_gather_global(const float4* grid_in, const SimConsts& K, float x0, float x1,
+                                                 float x2) {
+  const int N = K.N;
+  const float x[3] = {x0, x1, x2};
+  int b[3];
+  float w[3][3], d[3][3];
+  stencil(x, K, b, w, d);
+  const int b0 = b[0], b1 = b[1], b2 = b[2];
+  auto node = [&](int a, int bb, int c) -> float4 {
+    const int i = b0 + a, j = b1 + bb, k = b2 + c;
+    if ((unsigned)i >= (unsigned)N || (unsigned)j >= (unsigned)N || (unsigned)k >= (unsigned)N)
+      return make_float4(0.f, 0.f, 0.f, 0.f);
+    const float3 v = grid_node_velocity(__ldg(grid_in + ((int64_t)i * N + j) * N + k), i, j, k, K);
+    return make_float4(v.x, v.y, v.z, 0.f);
+  };
+  G2POut o;
+  g2p_gather(node, K, w, d, o.v, o.C);
+  return o;
+}
+
+// Per-warp grid tile: the nodes [lo, hi + 2]^3 around a box of base cells, with the
+// grid op applied (grid velocity), zero outside the grid.  lo/hi are warp-uniform.
+struct TileBox {
+  int t0, t1, t2, d1, d2;
+};
+
+__device__ __forceinline__ bool box_fits(const int lo[3], const int hi[3], int cap) {
+  int64_t vol = 1;
 #pragma unroll
-  for (int dim = 0; dim < 3; ++dim) {
-    QuadraticInterpolationKernel::weights_per_direction(x[dim], K.dx_inv, b[dim], w[dim]);
+  for (int dd = 0; dd < 3; ++dd) vol *= (hi[dd] >= lo[dd]) ? (int64_t)(hi[dd] + 3 - lo[dd]) : 0;
+  return vol <= cap;
+}
+
+__device__ __forceinline__ void warp_tile_build(float4* wtile, int lane, const int lo[3], const int hi[3],
+                                                const float4* grid_in, const SimConsts& K, TileBox& tb) {
+  int ext[3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) d[dim][a] = (float)(b[dim] + a) * K.dx - x[dim];
+  for (int dd = 0; dd < 3; ++dd) ext[dd] = (hi[dd] >= lo[dd]) ? hi[dd] + 3 - lo[dd] : 0;
+  const int vol = ext[0] * ext[1] * ext[2];
+  const int N = K.N;
+  tb.t0 = lo[0];
+  tb.t1 = lo[1];
+  tb.t2 = lo[2];
+  tb.d1 = max(ext[1], 1);
+  tb.d2 = max(ext[2], 1);
+  const int d12 = tb.d1 * tb.d2;
+  __syncwarp();  // every lane is done with the previous tile
+  for (int idx = lane; idx < vol; idx += 32) {
+    const int i = tb.t0 + idx / d12;
+    const int rem = idx - (idx / d12) * d12;
+    const int j = tb.t1 + rem / tb.d2;
+    const int k = tb.t2 + rem - (rem / tb.d2) * tb.d2;
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N) {
+      const float3 vv = grid_node_velocity(grid_in[((int64_t)i * N + j) * N + k], i, j, k, K);
+      out = make_float4(vv.x, vv.y, vv.z, 0.f);
+    }
+    wtile[idx] = out;
   }
+  __syncwarp();
 }
 
 template <bool LIQ, bool G2P, bool P2G, bool GUARD>
-__global__ void __launch_bounds__(kThreads, 1) step_kernel(const __grid_constant__ StepArgs A) {
-  extern __shared__ float4 tile[];
-  __shared__ int s_red[kWarps][6];
-  __shared__ int s_box[7];
-
+__global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_constant__ StepArgs A) {
+  extern __shared__ float4 smem[];
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
+  // per-warp regions: velocity tile (G2P), P2G transpose buffer
+  float4* wtile = smem + warp * A.tile_cap;
+  float4* wbuf = smem + (G2P ? kStepWarps * A.tile_cap : 0) + warp * kRedFloat4;
   const SimConsts& K = A.K;
   const int N = K.N;
   float* __restrict__ s = A.s;
   const int64_t st = A.stride;
-  const int64_t nchunks = (A.n + A.chunk - 1) / A.chunk;
 
-  for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-    const int64_t p0 = ch * A.chunk;
-    const int64_t p1 = min(p0 + (int64_t)A.chunk, A.n);
-    NodeFetch nf;
-    nf.tile = tile;
-    nf.grid_in = A.grid_in;
-    nf.use_tile = false;
-    nf.t0 = nf.t1 = nf.t2 = 0;
-    nf.d1 = nf.d2 = 1;
-    nf.vol = 0;
-    if (G2P) {
-      // ---- bounding box of the chunk's base cells -> shared-memory velocity tile
-      int lo0 = INT_MAX, lo1 = INT_MAX, lo2 = INT_MAX, hi0 = INT_MIN, hi1 = INT_MIN, hi2 = INT_MIN;
-      for (int64_t p = p0 + tid; p < p1; p += kThreads) {
-        if (GUARD && (int64_t)A.id[p] > A.guard_limit) continue;
-        const float x0 = s[(kX + 0) * st + p], x1 = s[(kX + 1) * st + p], x2 = s[(kX + 2) * st + p];
-        const int b0 = QuadraticInterpolationKernel::base_cell(x0, K.dx_inv);
-        const int b1 = QuadraticInterpolationKernel::base_cell(x1, K.dx_inv);
-        const int b2 = QuadraticInterpolationKernel::base_cell(x2, K.dx_inv);
-        if (outside_domain(b0, b1, b2, N)) continue;
-        lo0 = min(lo0, b0);
-        lo1 = min(lo1, b1);
-        lo2 = min(lo2, b2);
-        hi0 = max(hi0, b0);
-        hi1 = max(hi1, b1);
-        hi2 = max(hi2, b2);
-      }
-      lo0 = __reduce_min_sync(kFull, lo0);
-      lo1 = __reduce_min_sync(kFull, lo1);
-      lo2 = __reduce_min_sync(kFull, lo2);
-      hi0 = __reduce_max_sync(kFull, hi0);
-      hi1 = __reduce_max_sync(kFull, hi1);
-      hi2 = __reduce_max_sync(kFull, hi2);
-      if (lane == 0) {
-        s_red[warp][0] = lo0;
-        s_red[warp][1] = lo1;
-        s_red[warp][2] = lo2;
-        s_red[warp][3] = hi0;
-        s_red[warp][4] = hi1;
-        s_red[warp][5] = hi2;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        int l[3] = {INT_MAX, INT_MAX, INT_MAX}, h[3] = {INT_MIN, INT_MIN, INT_MIN};
-        for (int w = 0; w < kWarps; ++w)
-          for (int dd = 0; dd < 3; ++dd) {
-            l[dd] = min(l[dd], s_red[w][dd]);
-            h[dd] = max(h[dd], s_red[w][3 + dd]);
-          }
-        int64_t vol = 1;
-        for (int dd = 0; dd < 3; ++dd) {
-          l[dd] = max(l[dd], 0);
-          h[dd] = (h[dd] == INT_MIN) ? -1 : min(h[dd] + 2, N - 1);
-          const int ext = h[dd] >= l[dd] ? h[dd] - l[dd] + 1 : 0;
-          s_box[dd] = l[dd];
-          s_box[3 + dd] = ext;
-          vol *= ext;
-        }
-        s_box[6] = (vol <= (int64_t)A.tile_cap) ? (int)vol : -1;
-      }
-      __syncthreads();
-      const int vol = s_box[6];
-      nf.t0 = s_box[0];
-      nf.t1 = s_box[1];
-      nf.t2 = s_box[2];
-      nf.d1 = max(s_box[4], 1);
-      nf.d2 = max(s_box[5], 1);
-      nf.use_tile = vol >= 0;
-      nf.vol = vol;
-      if (nf.use_tile) {
-        const int d12 = nf.d1 * nf.d2;
-        for (int idx = tid; idx < vol; idx += kThreads) {
-          const int i = nf.t0 + idx / d12;
-          const int rem = idx - (idx / d12) * d12;
-          const int j = nf.t1 + rem / nf.d2;
-          const int k = nf.t2 + rem - (rem / nf.d2) * nf.d2;
-          const float4 g = A.grid_in[((int64_t)i * N + j) * N + k];
-          const float3 vv = grid_node_velocity(g, i, j, k, K);
-          tile[idx] = make_float4(vv.x, vv.y, vv.z, 0.f);
-        }
-      }
-      __syncthreads();
+  // Warps are the scheduling unit: each resident warp starts on one range of A.chunk
+  // consecutive (cell-sorted) particles and claims further ranges from a global
+  // counter while finishing the last step of its current one, so warps that run
+  // faster take more ranges; no CTA barriers.
+  if (blockIdx.x == 0 && tid == 0) *A.work_next = 0;
+  const int64_t nranges = (A.n + A.chunk - 1) / A.chunk;
+  const int64_t first_wave = (int64_t)gridDim.x * kStepWarps;
+  int64_t r = (int64_t)blockIdx.x * kStepWarps + warp;
+  while (r < nranges) {
+    int claim = 0;
+    const int64_t wbeg = r * A.chunk;
+    const int64_t wend = min(wbeg + (int64_t)A.chunk, A.n);
+    TileBox tb{0, 0, 0, 1, 1};
+    int64_t win_end = wbeg;  // end of the steps the current tile covers
+    bool tile_ok = false;
+
+    // ---- walk the range, one particle per lane; positions and Jp of the next step
+    // are loaded one step ahead
+    float nx0 = 0.f, nx1 = 0.f, nx2 = 0.f, nJ = 1.f;
+    if (wbeg + lane < wend) {
+      nx0 = s[(kX + 0) * st + wbeg + lane];
+      nx1 = s[(kX + 1) * st + wbeg + lane];
+      nx2 = s[(kX + 2) * st + wbeg + lane];
+      nJ = s[kJp * st + wbeg + lane];
     }
-
-    // ---- per-warp walk over the chunk slice, one particle per lane
-    const int seg = A.chunk / kWarps;
-    const int64_t wbeg = p0 + (int64_t)warp * seg;
-    const int64_t wend = min(wbeg + seg, p1);
-    float acc[27][4];
-    int acc_key = -1;
-    if (P2G) zero_acc(acc);
-
     for (int64_t pb = wbeg; pb < wend; pb += 32) {
+      if (G2P && pb >= win_end) {
+        // grow a window of steps from pb while the union of their base-cell boxes fits
+        // the warp's tile, then stage the tile once for the whole window
+        int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+        int64_t we = pb;
+        while (we < wend) {
+          const int64_t q = we + lane;
+          int slo[3] = {INT_MAX, INT_MAX, INT_MAX}, shi[3] = {INT_MIN, INT_MIN, INT_MIN};
+          if (q < wend && !(GUARD && (int64_t)A.id[q] > A.guard_limit)) {
+            int bb[3];
+#pragma unroll
+            for (int dd = 0; dd < 3; ++dd)
+              bb[dd] = QuadraticInterpolationKernel::base_cell(s[(kX + dd) * st + q], K.dx_inv);
+            if (!outside_domain(bb[0], bb[1], bb[2], N)) {
+#pragma unroll
+              for (int dd = 0; dd < 3; ++dd) slo[dd] = shi[dd] = bb[dd];
+            }
+          }
+          int nlo[3], nhi[3];
+#pragma unroll
+          for (int dd = 0; dd < 3; ++dd) {
+            nlo[dd] = min(lo[dd], __reduce_min_sync(kFull, slo[dd]));
+            nhi[dd] = max(hi[dd], __reduce_max_sync(kFull, shi[dd]));
+          }
+          if (!box_fits(nlo, nhi, A.tile_cap)) break;
+#pragma unroll
+          for (int dd = 0; dd < 3; ++dd) {
+            lo[dd] = nlo[dd];
+            hi[dd] = nhi[dd];
+          }
+          we += 32;
+        }
+        tile_ok = we > pb;
+        win_end = tile_ok ? we : pb + 32;  // a step that alone does not fit gathers from global
+        if (tile_ok) warp_tile_build(wtile, lane, lo, hi, A.grid_in, K, tb);
+      }
       const int64_t p = pb + lane;
       const bool valid = p < wend;
-      float x[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f}, Cm[3][3], F[3][3], Jp = 1.f;
+      if (pb + 32 >= wend && lane == 0) claim = atomicAdd(A.work, 1);
+      float x[3] = {nx0, nx1, nx2}, v[3] = {0.f, 0.f, 0.f}, Cm[3][3], F[3][3], Jp = nJ;
+      if (p + 32 < wend) {
+        nx0 = s[(kX + 0) * st + p + 32];
+        nx1 = s[(kX + 1) * st + p + 32];
+        nx2 = s[(kX + 2) * st + p + 32];
+        nJ = s[kJp * st + p + 32];
+      }
       int mi = 0;
       bool frozen = !G2P;
 #pragma unroll
@@ -366,9 +352,6 @@ __global__ void __launch_bounds__(kThreads, 1) step_kernel(const __grid_constant
           F[i][j] = (i == j) ? 1.f : 0.f;
         }
       if (valid) {
-#pragma unroll
-        for (int dd = 0; dd < 3; ++dd) x[dd] = s[(kX + dd) * st + p];
-        Jp = s[kJp * st + p];
         if (!LIQ) {
 #pragma unroll
           for (int i = 0; i < 9; ++i) F[i / 3][i % 3] = s[(kF + i) * st + p];
@@ -383,16 +366,35 @@ __global__ void __launch_bounds__(kThreads, 1) step_kernel(const __grid_constant
         }
       }
       const DevMaterial& M = K.mat[mi];
-
       // ---- G2P + constitutive update + advection (gridToParticle)
       bool have_uv = false;
       float Usv[3][3], Vsv[3][3];
+      bool g2p_on = false;
       if (G2P && valid && !frozen) {
         int b[3];
         float w[3][3], d[3][3];
         stencil(x, K, b, w, d);
-        if (!outside_domain(b[0], b[1], b[2], N)) {
-          g2p_gather(nf, K, b, w, d, v, Cm);
+        g2p_on = !outside_domain(b[0], b[1], b[2], N);
+        if (!g2p_on) {
+          frozen = true;  // completely outside: unchanged; P2G skips it too
+        } else if (tile_ok) {
+          const int t0 = ((b[0] - tb.t0) * tb.d1 + (b[1] - tb.t1)) * tb.d2 + (b[2] - tb.t2);
+          const int d12 = tb.d1 * tb.d2;
+          auto node = [&](int a, int bb, int c) -> float4 { return wtile[t0 + a * d12 + bb * tb.d2 + c]; };
+          g2p_gather(node, K, w, d, v, Cm);
+        } else {
+          // a step whose own box exceeds the tile (rare: a jump between brick rows)
+          const G2POut o = g2p_gather_global(A.grid_in, K, x[0], x[1], x[2]);
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            v[r] = o.v[r];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) Cm[r][c] = o.C[r][c];
+          }
+        }
+      }
+      if (g2p_on) {
+        {
           if (LIQ || M.kind == kLiquid) {
             // J <- J det(I + dt C), F = J^(1/3) I
             float G[3][3];
@@ -458,8 +460,6 @@ __global__ void __launch_bounds__(kThreads, 1) step_kernel(const __grid_constant
           s[kJp * st + p] = Jp;
           if (A.check_finite && !isfinite(x[0] + x[1] + x[2] + v[0] + v[1] + v[2]))
             atomicOr(A.status, kStatusNonFinite);
-        } else {
-          frozen = true;  // completely outside: unchanged; P2G skips it too
         }
       }
 
@@ -505,29 +505,17 @@ __global__ void __launch_bounds__(kThreads, 1) step_kernel(const __grid_constant
             for (int dd = 0; dd < 3; ++dd) mv[dd] = v[dd] * m;
           }
         }
-        bool todo = key >= 0;
-        if (todo && (acc_key < 0 || acc_key == key)) {
-          acc_key = key;
-          p2g_accumulate(acc, w, d, Aff, mv, m);
-          todo = false;
-        }
-        if (__any_sync(kFull, todo)) {
-          flush_groups(acc, acc_key, todo, lane, A.grid_out, N);
-          if (todo) {
-            acc_key = key;
-            p2g_accumulate(acc, w, d, Aff, mv, m);
-          }
-        }
+        p2g_scatter_step(wbuf, lane, key, w, d, Aff, mv, m, A.grid_out, N);
       }
     }
-    if (P2G) flush_groups(acc, acc_key, acc_key >= 0, lane, A.grid_out, N);
-    if (G2P) __syncthreads();  // the tile is rebuilt for the next chunk
+    r = first_wave + __shfl_sync(kFull, claim, 0);
   }
 
   // ---- clear the grid buffer the previous substep read (used by the launch after next)
   if (A.grid_zero) {
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int64_t i = (int64_t)blockIdx.x * kThreads + tid; i < A.grid_cells; i += (int64_t)gridDim.x * kThreads)
+    for (int64_t i = (int64_t)blockIdx.x * kStepThreads + tid; i < A.grid_cells;
+         i += (int64_t)gridDim.x * kStepThreads)
       A.grid_zero[i] = z;
   }
 }
@@ -552,21 +540,28 @@ static void* select_kernel(StepKind kind, bool liquid, bool guard) {
   return nullptr;
 }
 
+size_t step_smem_bytes(StepKind kind, int tile_cap) {
+  size_t b = 0;
+  if (kind != kStepP2GOnly) b += (size_t)kStepWarps * tile_cap * sizeof(float4);
+  if (kind != kStepG2POnly) b += (size_t)kStepWarps * kRedFloat4 * sizeof(float4);
+  return b;
+}
+
 cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guard, int grid_blocks, cudaStream_t st) {
   void* fn = select_kernel(kind, liquid, guard);
-  const size_t smem = (kind == kStepP2GOnly) ? 0 : (size_t)a.tile_cap * sizeof(float4);
+  const size_t smem = step_smem_bytes(kind, a.tile_cap);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   StepArgs copy = a;
   void* args[] = {&copy};
-  return cudaLaunchKernel(fn, dim3(grid_blocks), dim3(kThreads), args, smem, st);
+  return cudaLaunchKernel(fn, dim3(grid_blocks), dim3(kStepThreads), args, smem, st);
 }
 
 int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem) {
   void* fn = select_kernel(kind, liquid, guard);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem) != cudaSuccess || nb < 1) nb = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kStepThreads, smem) != cudaSuccess || nb < 1) nb = 1;
   return nb;
 }
 

@@ -74,6 +74,10 @@ class Simulation:
             setattr(self.params, k, v)
         _lib.check(self.L.mpm_set_params(self.ctx, ctypes.byref(self.params)), self.ctx)
 
+    def set_stream(self, handle):
+        """Enqueue all further work on the cudaStream_t `handle` (an int; 0 = the context's own)."""
+        _lib.check(self.L.mpm_set_stream(self.ctx, ctypes.c_void_p(int(handle)) if handle else None), self.ctx)
+
     def set_tuning(self, steps_per_warp=0, tile_nodes=0, waves=0):
         _lib.check(self.L.mpm_set_tuning(self.ctx, int(steps_per_warp), int(tile_nodes), int(waves)), self.ctx)
 
