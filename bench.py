@@ -47,7 +47,7 @@ GRID_BYTES_PER_NODE = 32.0  # one float4 read + one float4 written per grid node
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="liquid", choices=["liquid", "snow", "elastic"])
@@ -77,7 +77,8 @@ def dist_setup(args):
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
@@ -90,7 +91,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -102,7 +103,9 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
-    def stop(self):
+    def stop(self, t0=None, t1=None):
+        """Median SM clock and active throttle reasons over the samples taken between
+        wall-clock times t0 and t1 (all samples when not given)."""
         if not self.proc:
             return None
         self.proc.terminate()
@@ -116,14 +119,21 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
+                ts = time.mktime(time.strptime(parts[0].split(".")[0], "%Y/%m/%d %H:%M:%S")) + \
+                    float("0." + parts[0].split(".")[1]) if "." in parts[0] else 0.0
+            except Exception:
+                ts = None
+            if t0 is not None and ts is not None and not (t0 - 0.05 <= ts <= t1 + 0.05):
+                continue
+            try:
+                sm.append(float(parts[2]))
+                smax.append(float(parts[3]))
             except ValueError:
                 continue
-            for nm, val in zip(names, parts[5:9]):
+            for nm, val in zip(names, parts[6:10]):
                 if val.lower() == "active":
                     reasons.add(nm)
         if not sm:
@@ -254,6 +264,7 @@ def run_ours(args):
     sampler.start()
     time.sleep(0.3)
     launches0 = sim.launches
+    wall0_abs = time.time()
     wall0 = time.perf_counter()
     for k in range(args.steps):
         flush.fill_(float(k))
@@ -265,7 +276,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     launches = sim.launches - launches0
-    clocks = sampler.stop()
+    clocks = sampler.stop(wall0_abs, wall0_abs + wall)
     ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     sim.sync()
     dev_ms = sum(ms)

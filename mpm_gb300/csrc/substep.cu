@@ -101,27 +101,29 @@ __device__ __forceinline__ void p2g_scatter_step(float4* wbuf, int lane, int key
   const unsigned starts = __ballot_sync(kFull, lane == 0 || key != prev);
   if (key >= 0) p2g_write_column(wbuf, lane, w, d, Aff, mv, m);
   __syncwarp();
-  const int oi = lane / 9, oj = (lane / 3) % 3, ok = lane % 3;
+  // walk the runs (warp-uniform loop); lane l < 27 sums node l over the run's columns
   const float4* row = wbuf + (lane < 27 ? lane : 0) * kRedStride;
-  int run_key = __shfl_sync(kFull, key, 0);
-  float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-  for (int j = 0; j < 32; ++j) {
-    if (j > 0 && ((starts >> j) & 1u)) {  // warp-uniform
-      if (run_key >= 0 && lane < 27) {
-        int b0, b1, b2;
-        unpack_key(run_key, b0, b1, b2);
-        add_node(grid, N, b0 + oi, b1 + oj, b2 + ok, sum);
+  unsigned rs = starts;
+#pragma unroll 1
+  while (rs) {
+    const int j0 = __ffs(rs) - 1;
+    rs &= rs - 1u;
+    const int j1 = rs ? __ffs(rs) - 1 : 32;
+    const int run_key = __shfl_sync(kFull, key, j0);
+    if (run_key >= 0 && lane < 27) {
+      float4 s0 = make_float4(0.f, 0.f, 0.f, 0.f), s1 = s0;
+      int j = j0;
+#pragma unroll 1
+      for (; j + 1 < j1; j += 2) {
+        f4add(s0, row[j]);
+        f4add(s1, row[j + 1]);
       }
-      sum = make_float4(0.f, 0.f, 0.f, 0.f);
-      run_key = __shfl_sync(kFull, key, j);
+      if (j < j1) f4add(s0, row[j]);
+      f4add(s0, s1);
+      int b0, b1, b2;
+      unpack_key(run_key, b0, b1, b2);
+      add_node(grid, N, b0 + lane / 9, b1 + (lane / 3) % 3, b2 + lane % 3, s0);
     }
-    f4add(sum, row[j]);
-  }
-  if (run_key >= 0 && lane < 27) {
-    int b0, b1, b2;
-    unpack_key(run_key, b0, b1, b2);
-    add_node(grid, N, b0 + oi, b1 + oj, b2 + ok, sum);
   }
   __syncwarp();
 }
