@@ -147,6 +147,27 @@ int64_t mpm_launch_count(const mpm_ctx* ctx);
  * tile capacity), waves (chunks per SM). */
 mpm_status mpm_set_tuning(mpm_ctx* ctx, int32_t steps_per_warp, int32_t tile_nodes, int32_t waves);
 
+/* Substep entry point that allocates nothing.  It has no counterpart in the reference.
+ * For callers that cannot call cudaMalloc: code running while someone else captures a CUDA
+ * graph, plugins whose host owns all device memory, and callers that forbid allocation after
+ * start-up.  It runs `nsteps` substeps on the caller's device state in place, on `stream`
+ * (NULL: the legacy default stream), asynchronously:
+ *   - state: caller-owned device memory in the library's component-major layout, component k
+ *     of particle p at state[k * stride + p]: x 0-2, v 3-5, C 6-14 and F 15-23 (row-major),
+ *     Jp 24 (J for a single-liquid table, whose F components are not touched);
+ *   - mat: device array of material indices, or NULL for material 0;
+ *   - the scratch (three P2G grids and two counters) is a static device array of 1.5 MiB
+ *     that every GPU loading the library holds until exit, so N is limited to 32
+ *     (MPM_ERR_UNSUPPORTED above); g2p_guard and check_finite are not supported here.
+ * Particles are processed in the caller's order (no cell sort; sorted input runs faster).
+ * The first call on a device looks up the scratch's device address (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  All calls share the scratch, which keeps
+ * the last call's contents (each call clears what must start at zero): calls that overlap on
+ * the GPU, from any thread or stream, race and must be serialised by the caller. */
+mpm_status mpm_substep_noalloc(const mpm_params* params, const mpm_material* materials, int32_t n_materials,
+                               float* state, int64_t stride, const uint8_t* mat, int64_t n, int32_t nsteps,
+                               void* stream);
+
 #ifdef __cplusplus
 }
 #endif

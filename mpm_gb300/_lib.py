@@ -65,6 +65,8 @@ SIGNATURES = [
     ("mpm_last_error", I32, [P, ctypes.c_char_p, ctypes.c_size_t]),
     ("mpm_launch_count", I64, [P]),
     ("mpm_set_tuning", I32, [P, I32, I32, I32]),
+    ("mpm_substep_noalloc", I32, [ctypes.POINTER(MpmParams), ctypes.POINTER(MpmMaterial), I32, P, I64, P, I64, I32,
+                                  P]),
 ]
 
 _lib = None

@@ -111,36 +111,7 @@ bool valid_params(const mpm_params* p, std::string& why) {
   return true;
 }
 
-void derive_consts(mpm_ctx* c) {
-  SimConsts& K = c->K;
-  const mpm_params& p = c->params;
-  K.N = (int)p.N;
-  K.dt = p.dt;
-  // SimulationParameters: dx = 1.0/N (double, stored as float), dx_inv = 1.0/dx
-  // (include/TransferScheme.h:22-28); D_inv_const = I * 4.0 * dx_inv * dx_inv.
-  const float dx = (float)(1.0 / (double)p.N);
-  const float dxi = (float)(1.0 / (double)dx);
-  K.dx = dx;
-  K.dx_inv = dxi;
-  K.dinv = (4.0f * dxi) * dxi;
-  K.dtg = p.dt * p.gravity;
-  K.boundary_mode = p.boundary_mode;
-  K.boundary_cells = p.boundary_cells;
-  K.n_materials = c->n_materials;
-  for (int i = 0; i < c->n_materials; ++i) {
-    const mpm_material& m = c->mats[i];
-    DevMaterial& d = K.mat[i];
-    d.kind = m.kind;
-    d.vol = m.particle_volume;
-    d.mass = m.density * m.particle_volume;                       // MaterialModelBase
-    d.mu0 = m.E / (2.f * (1.f + m.nu));                            // MMFixedCorotated
-    d.lambda0 = m.E * m.nu / ((1.f + m.nu) * (1.f - 2.f * m.nu));
-    d.hardening = m.hardening;
-    d.clamp_lo = m.clamp_lo;
-    d.clamp_hi = m.clamp_hi;
-    d.bulk = m.bulk;
-  }
-}
+void derive_consts(mpm_ctx* c) { mpm::make_sim_consts(c->params, c->mats, c->n_materials, c->K); }
 
 // The compact liquid layout (x, v, C, J) is used when the table is a single liquid.
 bool all_liquid(const mpm_ctx* c) { return c->n_materials == 1 && c->mats[0].kind == MPM_MAT_LIQUID; }
@@ -203,18 +174,9 @@ StepArgs make_step_args(mpm_ctx* c) {
   return a;
 }
 
-// Ranges of steps_per_warp steps (32 particles each), fewer for small particle
-// counts so every resident warp gets work; the kernel deals them out dynamically.
 void launch_shape(mpm_ctx* c, StepKind kind, bool guard, int& chunk, int& blocks) {
-  const size_t smem = step_smem_bytes(kind, c->tile_cap);
-  const int bps = step_blocks_per_sm(kind, c->liquid_layout, guard, smem);
-  const int64_t resident_warps = (int64_t)c->num_sms * bps * kStepWarps;
-  int64_t steps = c->steps_per_warp;
-  while (steps > 1 && c->n < resident_warps * 32 * steps * 2) steps /= 2;
-  chunk = (int)(steps * 32);
-  const int64_t nranges = (c->n + chunk - 1) / chunk;
-  blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nranges + kStepWarps - 1) / kStepWarps,
-                                                       (int64_t)c->num_sms * bps));
+  mpm::step_launch_shape(c->num_sms, c->n, c->liquid_layout, guard, kind, c->steps_per_warp, c->tile_cap, chunk,
+                         blocks);
 }
 
 mpm_status run_step(mpm_ctx* c, StepKind kind) {
@@ -273,6 +235,55 @@ mpm_status check_ready(mpm_ctx* c) {
 }
 
 }  // namespace
+
+namespace mpm {
+
+// SimulationParameters (include/TransferScheme.h:6-29) and the material constants,
+// derived in float exactly as the reference constructors do.
+void make_sim_consts(const mpm_params& p, const mpm_material* mats, int n_materials, SimConsts& K) {
+  K.N = (int)p.N;
+  K.dt = p.dt;
+  // dx = 1.0/N (double, stored as float), dx_inv = 1.0/dx; D_inv_const = I * 4.0 * dx_inv * dx_inv
+  const float dx = (float)(1.0 / (double)p.N);
+  const float dxi = (float)(1.0 / (double)dx);
+  K.dx = dx;
+  K.dx_inv = dxi;
+  K.dinv = (4.0f * dxi) * dxi;
+  K.dtg = p.dt * p.gravity;
+  K.boundary_mode = p.boundary_mode;
+  K.boundary_cells = p.boundary_cells;
+  K.n_materials = n_materials;
+  for (int i = 0; i < n_materials; ++i) {
+    const mpm_material& m = mats[i];
+    DevMaterial& d = K.mat[i];
+    d.kind = m.kind;
+    d.vol = m.particle_volume;
+    d.mass = m.density * m.particle_volume;                       // MaterialModelBase
+    d.mu0 = m.E / (2.f * (1.f + m.nu));                            // MMFixedCorotated
+    d.lambda0 = m.E * m.nu / ((1.f + m.nu) * (1.f - 2.f * m.nu));
+    d.hardening = m.hardening;
+    d.clamp_lo = m.clamp_lo;
+    d.clamp_hi = m.clamp_hi;
+    d.bulk = m.bulk;
+  }
+}
+
+// Ranges of steps_per_warp steps (32 particles each), fewer for small particle
+// counts so every resident warp gets work; the kernel deals them out dynamically.
+void step_launch_shape(int num_sms, int64_t n, bool liquid, bool guard, StepKind kind, int steps_per_warp,
+                       int tile_cap, int& chunk, int& blocks) {
+  const size_t smem = step_smem_bytes(kind, tile_cap);
+  const int bps = step_blocks_per_sm(kind, liquid, guard, smem);
+  const int64_t resident_warps = (int64_t)num_sms * bps * kStepWarps;
+  int64_t steps = steps_per_warp;
+  while (steps > 1 && n < resident_warps * 32 * steps * 2) steps /= 2;
+  chunk = (int)(steps * 32);
+  const int64_t nranges = (n + chunk - 1) / chunk;
+  blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nranges + kStepWarps - 1) / kStepWarps,
+                                                       (int64_t)num_sms * bps));
+}
+
+}  // namespace mpm
 
 extern "C" {
 

@@ -40,6 +40,18 @@ size_t step_smem_bytes(StepKind kind, int tile_cap);
 // Max resident CTAs per SM for the variant at the given dynamic shared memory.
 int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem);
 
+}  // namespace mpm
+
+#include "mpm_gb300.h"
+
+namespace mpm {
+
+// Device constants from the C ABI parameters and material table.
+void make_sim_consts(const mpm_params& p, const mpm_material* mats, int n_materials, SimConsts& K);
+// Range size (chunk, particles) and grid size of a substep launch.
+void step_launch_shape(int num_sms, int64_t n, bool liquid, bool guard, StepKind kind, int steps_per_warp,
+                       int tile_cap, int& chunk, int& blocks);
+
 // Cell sort (counting sort by the linear index of the base cell).
 struct SortArgs {
   const float* sA;

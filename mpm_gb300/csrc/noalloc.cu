@@ -1,0 +1,111 @@
+// A substep entry point that allocates nothing.
+//
+// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is being
+// captured by someone else, plugins loaded into a host that owns all device memory
+// through its own pool, and embedded or real-time callers that forbid allocation after
+// start-up.  mpm_substep_noalloc serves them: the caller passes the particle state in
+// its own device memory, and the only scratch the substep needs (three rotating P2G
+// grids and two range counters) lives in the file-scope array below, which every GPU
+// that loads this library holds until the process exits.
+#include <mutex>
+
+#include "mpm_internal.h"
+
+namespace {
+
+constexpr int kNoAllocMaxN = 32;  // largest grid the static scratch holds
+constexpr int64_t kNoAllocCells = (int64_t)kNoAllocMaxN * kNoAllocMaxN * kNoAllocMaxN;
+// three grids of kNoAllocCells float4 nodes, then one float4 of counters
+// (work[0], work[1], status, unused): 3 x 32768 x 16 B + 16 B = 1.5 MiB + 16 B
+constexpr int64_t kScratchFloat4 = 3 * kNoAllocCells + 1;
+
+static __device__ __align__(256) float4 g_noalloc_scratch[kScratchFloat4];
+
+// Device address of g_noalloc_scratch per device.  In host code the symbol's name is
+// only a host-side stand-in, so the address comes from cudaGetSymbolAddress, taken
+// once per device with that device current.
+constexpr int kMaxDevices = 64;
+float4* g_scratch_addr[kMaxDevices] = {};
+std::mutex g_scratch_mutex;
+
+mpm_status scratch_for_current_device(float4** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return MPM_ERR_CUDA;
+  if (dev < 0 || dev >= kMaxDevices) return MPM_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_addr[dev]) {
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return MPM_ERR_CUDA;
+    g_scratch_addr[dev] = static_cast<float4*>(ptr);
+  }
+  *out = g_scratch_addr[dev];
+  return MPM_OK;
+}
+
+}  // namespace
+
+using namespace mpm;
+
+extern "C" mpm_status mpm_substep_noalloc(const mpm_params* params, const mpm_material* materials,
+                                          int32_t n_materials, float* state, int64_t stride, const uint8_t* mat,
+                                          int64_t n, int32_t nsteps, void* stream) {
+  if (!params || !materials || n_materials <= 0 || n_materials > MPM_MAX_MATERIALS) return MPM_ERR_INVALID;
+  if (params->N < 4 || params->N > (uint32_t)kNoAllocMaxN) return MPM_ERR_UNSUPPORTED;  // beyond the scratch
+  if (!(params->dt > 0.f) || params->boundary_mode < 0 || params->boundary_mode > 2) return MPM_ERR_INVALID;
+  if (params->boundary_cells < 0 || (uint32_t)params->boundary_cells * 2 > params->N) return MPM_ERR_INVALID;
+  if (params->g2p_guard || params->check_finite) return MPM_ERR_UNSUPPORTED;
+  if (n < 0 || nsteps < 0 || (n > 0 && (!state || stride < n))) return MPM_ERR_INVALID;
+  for (int i = 0; i < n_materials; ++i)
+    if (materials[i].kind < 0 || materials[i].kind > MPM_MAT_LIQUID || !(materials[i].particle_volume > 0.f) ||
+        !(materials[i].density > 0.f))
+      return MPM_ERR_INVALID;
+  if (n == 0 || nsteps == 0) return MPM_OK;
+
+  float4* scratch = nullptr;
+  mpm_status st = scratch_for_current_device(&scratch);
+  if (st != MPM_OK) return st;
+  int dev = 0, num_sms = 1;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return MPM_ERR_CUDA;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+  const int64_t cells = (int64_t)params->N * params->N * params->N;
+  float4* grid[3] = {scratch, scratch + kNoAllocCells, scratch + 2 * kNoAllocCells};
+  int* counters = reinterpret_cast<int*>(scratch + 3 * kNoAllocCells);
+  // the array keeps the previous call's contents: clear the first P2G target and the
+  // counters (the other grids are cleared by the launches before they are written)
+  if (cudaMemsetAsync(grid[1], 0, sizeof(float4) * cells, s) != cudaSuccess) return MPM_ERR_CUDA;
+  if (cudaMemsetAsync(counters, 0, 4 * sizeof(int), s) != cudaSuccess) return MPM_ERR_CUDA;
+
+  StepArgs a{};
+  a.s = state;
+  a.stride = stride;
+  a.mat = mat;
+  a.id = nullptr;
+  a.n = n;
+  a.grid_cells = cells;
+  a.tile_cap = 256;
+  a.guard_limit = 0;
+  a.check_finite = 0;
+  a.status = counters + 2;
+  make_sim_consts(*params, materials, n_materials, a.K);
+  const bool liquid = n_materials == 1 && materials[0].kind == MPM_MAT_LIQUID;
+
+  int cur = 0, parity = 0;
+  for (int32_t i = -1; i < nsteps; ++i) {
+    const StepKind kind = (i < 0) ? kStepP2GOnly : kStepFused;
+    int chunk = 0, blocks = 0;
+    step_launch_shape(num_sms, n, liquid, false, kind, 2, a.tile_cap, chunk, blocks);
+    a.chunk = chunk;
+    a.grid_in = (kind == kStepP2GOnly) ? nullptr : grid[cur];
+    a.grid_out = grid[(cur + 1) % 3];
+    a.grid_zero = grid[(cur + 2) % 3];
+    a.work = counters + parity;
+    a.work_next = counters + (parity ^ 1);
+    parity ^= 1;
+    if (launch_step(a, kind, liquid, false, blocks, s) != cudaSuccess) return MPM_ERR_CUDA;
+    cur = (cur + 1) % 3;
+  }
+  return MPM_OK;
+}
