@@ -147,6 +147,38 @@ int64_t mpm_launch_count(const mpm_ctx* ctx);
  * tile capacity), waves (chunks per SM). */
 mpm_status mpm_set_tuning(mpm_ctx* ctx, int32_t steps_per_warp, int32_t tile_nodes, int32_t waves);
 
+/* ---------------------------------------------------------------------------
+ * Batched scenes.  The reference runs one scene per Simulation; a batch advances many
+ * independent scenes (own N, dt, gravity, boundary, material and particle count) with
+ * one fused launch per substep for all of them, optionally as a replayed CUDA graph.
+ * Particle arrays of a batch are the scenes' particles concatenated in scene order
+ * (same per-particle interleaved host layout as mpm_upload_soa).
+ * ------------------------------------------------------------------------- */
+typedef struct mpm_scene {
+  mpm_params params;     /* dt, N, gravity, boundary of this scene (g2p_guard unsupported) */
+  mpm_material material; /* the scene's material (particle_volume is per scene) */
+  int64_t count;         /* particles of this scene */
+} mpm_scene;
+
+typedef struct mpm_batch mpm_batch;
+
+mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t sort_interval, mpm_batch** out);
+mpm_status mpm_batch_destroy(mpm_batch* batch);
+/* A non-default cudaStream_t for all further work (graphs are re-captured). */
+mpm_status mpm_batch_set_stream(mpm_batch* batch, void* cuda_stream);
+mpm_status mpm_batch_upload_soa(mpm_batch* batch, const float* x, const float* v, const float* C, const float* F,
+                                const float* Jp);
+/* nsteps substeps of every scene, one launch each (plus the periodic cell sort). */
+mpm_status mpm_batch_substep(mpm_batch* batch, int32_t nsteps);
+/* The same as one CUDA graph (captured on first use per phase, then replayed); the
+ * particles are cell-sorted once at the start of each replayed run. */
+mpm_status mpm_batch_substep_graph(mpm_batch* batch, int32_t nsteps);
+mpm_status mpm_batch_sync(mpm_batch* batch);
+mpm_status mpm_batch_download_soa(mpm_batch* batch, float* x, float* v, float* C, float* F, float* Jp);
+int64_t mpm_batch_particle_count(const mpm_batch* batch);
+int64_t mpm_batch_launch_count(const mpm_batch* batch);
+mpm_status mpm_batch_last_error(const mpm_batch* batch, char* buf, size_t len);
+
 /* Substep entry point that allocates nothing.  It has no counterpart in the reference.
  * For callers that cannot call cudaMalloc: code running while someone else captures a CUDA
  * graph, plugins whose host owns all device memory, and callers that forbid allocation after

@@ -43,6 +43,10 @@ class MpmMaterial(ctypes.Structure):
     ]
 
 
+class MpmScene(ctypes.Structure):
+    _fields_ = [("params", MpmParams), ("material", MpmMaterial), ("count", ctypes.c_int64)]
+
+
 # (name, restype, argtypes) for every entry point of include/mpm_gb300.h
 P = ctypes.c_void_p
 I32, I64 = ctypes.c_int32, ctypes.c_int64
@@ -65,6 +69,17 @@ SIGNATURES = [
     ("mpm_last_error", I32, [P, ctypes.c_char_p, ctypes.c_size_t]),
     ("mpm_launch_count", I64, [P]),
     ("mpm_set_tuning", I32, [P, I32, I32, I32]),
+    ("mpm_batch_create", I32, [ctypes.POINTER(MpmScene), I32, I32, ctypes.POINTER(P)]),
+    ("mpm_batch_destroy", I32, [P]),
+    ("mpm_batch_set_stream", I32, [P, P]),
+    ("mpm_batch_upload_soa", I32, [P, P, P, P, P, P]),
+    ("mpm_batch_substep", I32, [P, I32]),
+    ("mpm_batch_substep_graph", I32, [P, I32]),
+    ("mpm_batch_sync", I32, [P]),
+    ("mpm_batch_download_soa", I32, [P, P, P, P, P, P]),
+    ("mpm_batch_particle_count", I64, [P]),
+    ("mpm_batch_launch_count", I64, [P]),
+    ("mpm_batch_last_error", I32, [P, ctypes.c_char_p, ctypes.c_size_t]),
     ("mpm_substep_noalloc", I32, [ctypes.POINTER(MpmParams), ctypes.POINTER(MpmMaterial), I32, P, I64, P, I64, I32,
                                   P]),
 ]

@@ -23,12 +23,31 @@ __device__ __forceinline__ uint32_t cell_key(const float* s, int64_t st, int64_t
   return brick * 64u + (uint32_t)(((b[0] & 3) << 4) | ((b[1] & 3) << 2) | (b[2] & 3));
 }
 
+// Scene of particle p in a batch (binary search over the scene offsets).
+__device__ __forceinline__ int scene_of(const int64_t* start, int nscenes, int64_t p) {
+  int lo = 0, hi = nscenes - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= p) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ uint32_t sort_key(const SortArgs& a, int64_t p) {
+  if (a.nscenes > 0) {
+    const int sc = scene_of(a.scene_start, a.nscenes, p);
+    const GridConsts& g = a.scenes[sc].g;
+    return a.scene_key_base[sc] + cell_key(a.sA, a.stride, p, g.dx_inv, g.N);
+  }
+  return cell_key(a.sA, a.stride, p, a.dx_inv, a.N);
+}
+
 __global__ void sort_histogram(SortArgs a) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < a.n; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = base + threadIdx.x;
     const bool valid = p < a.n;
-    uint32_t key = valid ? cell_key(a.sA, a.stride, p, a.dx_inv, a.N) : 0xffffffffu;
+    uint32_t key = valid ? sort_key(a, p) : 0xffffffffu;
     if (valid) a.keys[p] = key;
     const unsigned same = __match_any_sync(kFull, key);
     if (valid && lane == __ffs(same) - 1) atomicAdd(a.counts + key, __popc(same));
@@ -234,7 +253,7 @@ cudaError_t launch_scatter_u8(const uint8_t* src, const uint32_t* id, int64_t n,
 // gridOpKernel (src/mpm.cu:76-107) over the whole grid, for readback: nodes with
 // mass > 0 get the operated velocity and mass slot 1 (the reference divides all four
 // components by the mass); others keep their raw value.
-__global__ void grid_op_kernel(const float4* in, float4* out, SimConsts K) {
+__global__ void grid_op_kernel(const float4* in, float4* out, GridConsts K) {
   const int N = K.N;
   const int64_t cells = (int64_t)N * N * N;
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x) {
@@ -247,7 +266,7 @@ __global__ void grid_op_kernel(const float4* in, float4* out, SimConsts K) {
   }
 }
 
-cudaError_t launch_grid_op(const float4* in, float4* out, SimConsts K, cudaStream_t st) {
+cudaError_t launch_grid_op(const float4* in, float4* out, GridConsts K, cudaStream_t st) {
   const int64_t cells = (int64_t)K.N * K.N * K.N;
   grid_op_kernel<<<grid_for(cells), 256, 0, st>>>(in, out, K);
   return cudaGetLastError();

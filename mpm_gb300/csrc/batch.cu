@@ -1,0 +1,444 @@
+// Batched scenes: many independent MLS-MPM scenes (own N, dt, material, particle
+// count) advanced together, one launch per substep for the whole batch.
+//
+// The reference simulates one scene per Simulation (include/mpm.cuh:44-106); a batch is
+// the GB300 form of running many of them: all particles sit in one component-major
+// SoA (scene after scene, each scene cell-sorted inside its segment), all grids in one
+// pool, and the fused substep kernel walks a table of particle ranges that never cross
+// a scene boundary.  Grids are cleared sparsely (the box each scene's P2G touched),
+// not as dense N^3 blocks.  A run of substeps can be captured once as a CUDA graph and
+// replayed.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "mpm_internal.h"
+
+using namespace mpm;
+
+struct mpm_batch {
+  int nscenes = 0;
+  std::vector<mpm_scene> scenes;
+  std::vector<int64_t> start;  // nscenes + 1
+  SimConsts K{};
+  int sort_interval = 16;
+  int steps_per_warp = 2;
+  int tile_cap = 256;
+  int blocks_p2g = 1, blocks_fused = 1;  // launch grids, fixed at creation (outside any capture)
+
+  int device = 0, num_sms = 1;
+  cudaStream_t stream = nullptr, own_stream = nullptr;
+
+  int64_t n = 0, stride = 0;
+  float* sA = nullptr;
+  float* sB = nullptr;
+  uint8_t* matA = nullptr;
+  uint8_t* matB = nullptr;
+  uint32_t* idA = nullptr;
+  uint32_t* idB = nullptr;
+  uint32_t* keys = nullptr;
+
+  int64_t cells = 0;  // total grid nodes of all scenes
+  float4* grid[3] = {nullptr, nullptr, nullptr};
+  SceneDev* d_scenes = nullptr;
+  int64_t* d_start = nullptr;
+  uint32_t* d_key_base = nullptr;
+  int64_t key_space = 0;
+  int* counts = nullptr;
+  int* block_sums = nullptr;
+  int* comp_list = nullptr;
+  int4* d_ranges = nullptr;
+  int nranges = 0;
+  int* boxes = nullptr;
+  int* work = nullptr;
+  int* status = nullptr;
+  float* stage = nullptr;
+
+  int cur = 0;
+  bool pending = false;
+  int64_t launch_index = 0;  // fused/P2G launches since upload (selects the box slots)
+  int parity = 0;
+  int64_t since_sort = 0;
+  int64_t launches = 0;
+  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (nsteps, launch_index % 6) -> graph
+  std::string last_error;
+};
+
+namespace {
+
+mpm_status bfail(mpm_batch* b, mpm_status code, const std::string& msg) {
+  if (b) b->last_error = msg;
+  return code;
+}
+
+#define BCUDA(b, call)                                                                          \
+  do {                                                                                          \
+    cudaError_t _e = (call);                                                                    \
+    if (_e != cudaSuccess)                                                                      \
+      return bfail((b), _e == cudaErrorMemoryAllocation ? MPM_ERR_NOMEM : MPM_ERR_CUDA,         \
+                   std::string(#call) + ": " + cudaGetErrorString(_e));                         \
+  } while (0)
+
+void free_graphs(mpm_batch* b) {
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+}
+
+mpm_status launch(mpm_batch* b, StepKind kind) {
+  StepArgs a{};
+  a.s = b->sA;
+  a.stride = b->stride;
+  a.mat = nullptr;  // the material comes from the scene table
+  a.id = b->idA;
+  a.n = b->n;
+  a.tile_cap = b->tile_cap;
+  a.status = b->status;
+  a.K = b->K;
+  a.nscenes = b->nscenes;
+  a.ranges = b->d_ranges;
+  a.nranges = b->nranges;
+  a.scenes = b->d_scenes;
+  a.boxes = b->boxes;
+  const int64_t L = b->launch_index;
+  a.box_record = (int)(L % kBoxSlots);
+  a.box_clear = (int)((L + kBoxSlots - 2) % kBoxSlots);
+  a.box_reset = (int)((L + 1) % kBoxSlots);
+  const int r = b->cur;
+  a.grid_in = (kind == kStepP2GOnly) ? nullptr : b->grid[r];
+  a.grid_out = b->grid[(r + 1) % 3];
+  a.grid_zero = b->grid[(r + 2) % 3];
+  a.work = b->work + b->parity;
+  a.work_next = b->work + (b->parity ^ 1);
+  a.chunk = 32 * b->steps_per_warp;
+  const int blocks = (kind == kStepP2GOnly) ? b->blocks_p2g : b->blocks_fused;
+  BCUDA(b, launch_step(a, kind, false, false, blocks, b->stream));
+  b->parity ^= 1;
+  b->cur = (r + 1) % 3;
+  b->launch_index += 1;
+  b->pending = true;
+  b->launches += 1;
+  return MPM_OK;
+}
+
+mpm_status sort(mpm_batch* b) {
+  SortArgs s{};
+  s.sA = b->sA;
+  s.sB = b->sB;
+  s.stride = b->stride;
+  s.n = b->n;
+  s.matA = nullptr;  // per-scene materials: nothing per particle to move
+  s.matB = b->matB;
+  s.idA = b->idA;
+  s.idB = b->idB;
+  s.keys = b->keys;
+  s.counts = b->counts;
+  s.block_sums = b->block_sums;
+  s.cells = b->key_space;
+  s.ncomp = kNumComps;
+  s.comp_list = b->comp_list;
+  s.nscenes = b->nscenes;
+  s.scene_start = b->d_start;
+  s.scene_key_base = b->d_key_base;
+  s.scenes = b->d_scenes;
+  BCUDA(b, launch_sort(s, b->num_sms, b->stream, &b->launches));
+  std::swap(b->sA, b->sB);
+  std::swap(b->matA, b->matB);
+  std::swap(b->idA, b->idB);
+  b->since_sort = 0;
+  return MPM_OK;
+}
+
+mpm_status advance(mpm_batch* b, int32_t nsteps) {
+  for (int32_t i = 0; i < nsteps; ++i) {
+    if (b->sort_interval > 0 && b->since_sort >= b->sort_interval) {
+      mpm_status st = sort(b);
+      if (st != MPM_OK) return st;
+    }
+    if (!b->pending) {
+      mpm_status st = launch(b, kStepP2GOnly);
+      if (st != MPM_OK) return st;
+    }
+    mpm_status st = launch(b, kStepFused);
+    if (st != MPM_OK) return st;
+    b->since_sort += 1;
+  }
+  return MPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t sort_interval, mpm_batch** out) {
+  if (!out || !scenes || nscenes <= 0 || sort_interval < 0) return MPM_ERR_INVALID;
+  *out = nullptr;
+  for (int i = 0; i < nscenes; ++i) {
+    const mpm_params& p = scenes[i].params;
+    if (p.N < 4 || p.N > 1000 || !(p.dt > 0.f) || p.boundary_mode < 0 || p.boundary_mode > 2 ||
+        p.boundary_cells < 0 || (uint32_t)p.boundary_cells * 2 > p.N || scenes[i].count < 0)
+      return MPM_ERR_INVALID;
+    if (p.g2p_guard) return MPM_ERR_UNSUPPORTED;
+    const mpm_material& m = scenes[i].material;
+    if (m.kind < 0 || m.kind > MPM_MAT_LIQUID || !(m.particle_volume > 0.f) || !(m.density > 0.f))
+      return MPM_ERR_INVALID;
+  }
+
+  mpm_batch* b = new mpm_batch();
+  auto bail = [&](mpm_status s) {
+    mpm_batch_destroy(b);
+    return s;
+  };
+  b->nscenes = nscenes;
+  b->scenes.assign(scenes, scenes + nscenes);
+  make_sim_consts(scenes[0].params, &scenes[0].material, 1, b->K);
+  b->sort_interval = sort_interval;
+  if (cudaGetDevice(&b->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(MPM_ERR_CUDA);
+  b->stream = b->own_stream;
+
+  // particle segments, grid pool, sort key bases, range table
+  b->start.resize(nscenes + 1);
+  std::vector<SceneDev> sd(nscenes);
+  std::vector<uint32_t> key_base(nscenes);
+  std::vector<int4> ranges;
+  const int chunk = 32 * b->steps_per_warp;
+  int64_t off = 0, cells = 0, keys = 0;
+  for (int i = 0; i < nscenes; ++i) {
+    b->start[i] = off;
+    make_grid_consts(scenes[i].params, sd[i].g);
+    make_dev_material(scenes[i].material, sd[i].m);
+    sd[i].grid_offset = cells;
+    const int64_t N = scenes[i].params.N;
+    cells += N * N * N;
+    const int64_t nb = (N + 3) / 4;
+    key_base[i] = (uint32_t)keys;
+    keys += nb * nb * nb * 64;
+    for (int64_t p = 0; p < scenes[i].count; p += chunk)
+      ranges.push_back(make_int4(i, (int)(off + p), (int)(off + std::min<int64_t>(p + chunk, scenes[i].count)), 0));
+    off += scenes[i].count;
+  }
+  b->start[nscenes] = off;
+  if (off > (int64_t)INT_MAX || keys > (int64_t)UINT32_MAX) return bail(MPM_ERR_UNSUPPORTED);
+  b->n = off;
+  b->stride = std::max<int64_t>(64, (off + 63) / 64 * 64);
+  b->cells = cells;
+  b->key_space = keys;
+  b->nranges = (int)ranges.size();
+  for (int k = 0; k < 2; ++k) {
+    const StepKind kind = k ? kStepFused : kStepP2GOnly;
+    const int bps = step_blocks_per_sm(kind, false, false, step_smem_bytes(kind, b->tile_cap), true);
+    const int blocks = std::max(1, std::min((b->nranges + kStepWarps - 1) / kStepWarps, b->num_sms * bps));
+    (k ? b->blocks_fused : b->blocks_p2g) = blocks;
+  }
+
+  const size_t fb = sizeof(float) * (size_t)kNumComps * b->stride;
+  if (cudaMalloc(&b->sA, fb) || cudaMalloc(&b->sB, fb) || cudaMalloc(&b->matA, b->stride) ||
+      cudaMalloc(&b->matB, b->stride) || cudaMalloc(&b->idA, 4 * b->stride) || cudaMalloc(&b->idB, 4 * b->stride) ||
+      cudaMalloc(&b->keys, 4 * b->stride) || cudaMalloc(&b->stage, fb))
+    return bail(MPM_ERR_NOMEM);
+  for (auto& g : b->grid) {
+    if (cudaMalloc(&g, sizeof(float4) * std::max<int64_t>(cells, 1))) return bail(MPM_ERR_NOMEM);
+    if (cudaMemsetAsync(g, 0, sizeof(float4) * cells, b->stream)) return bail(MPM_ERR_CUDA);
+  }
+  const int64_t nbs = (keys + kThreads * 8 - 1) / (kThreads * 8);
+  if (cudaMalloc(&b->counts, 4 * keys) || cudaMalloc(&b->block_sums, 4 * std::max<int64_t>(nbs, 1)) ||
+      cudaMalloc(&b->d_scenes, sizeof(SceneDev) * nscenes) || cudaMalloc(&b->d_start, 8 * (nscenes + 1)) ||
+      cudaMalloc(&b->d_key_base, 4 * nscenes) || cudaMalloc(&b->d_ranges, sizeof(int4) * std::max(b->nranges, 1)) ||
+      cudaMalloc(&b->boxes, sizeof(int) * 6 * kBoxSlots * nscenes) || cudaMalloc(&b->work, 2 * sizeof(int)) ||
+      cudaMalloc(&b->status, sizeof(int)) || cudaMalloc(&b->comp_list, sizeof(int) * kNumComps))
+    return bail(MPM_ERR_NOMEM);
+  std::vector<int> boxes(6 * kBoxSlots * nscenes);
+  for (size_t i = 0; i < boxes.size(); ++i) boxes[i] = (i % 6 < 3) ? INT_MAX : INT_MIN;
+  int comps[kNumComps];
+  for (int i = 0; i < kNumComps; ++i) comps[i] = i;
+  if (cudaMemcpy(b->d_scenes, sd.data(), sizeof(SceneDev) * nscenes, cudaMemcpyHostToDevice) ||
+      cudaMemcpy(b->d_start, b->start.data(), 8 * (nscenes + 1), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(b->d_key_base, key_base.data(), 4 * nscenes, cudaMemcpyHostToDevice) ||
+      (b->nranges && cudaMemcpy(b->d_ranges, ranges.data(), sizeof(int4) * b->nranges, cudaMemcpyHostToDevice)) ||
+      cudaMemcpy(b->boxes, boxes.data(), sizeof(int) * boxes.size(), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(b->comp_list, comps, sizeof(comps), cudaMemcpyHostToDevice) ||
+      cudaMemset(b->work, 0, 2 * sizeof(int)) || cudaMemset(b->status, 0, sizeof(int)) ||
+      cudaStreamSynchronize(b->stream))
+    return bail(MPM_ERR_CUDA);
+  *out = b;
+  return MPM_OK;
+}
+
+mpm_status mpm_batch_destroy(mpm_batch* b) {
+  if (!b) return MPM_ERR_INVALID;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  free_graphs(b);
+  for (void* p : {(void*)b->sA, (void*)b->sB, (void*)b->matA, (void*)b->matB, (void*)b->idA, (void*)b->idB,
+                  (void*)b->keys, (void*)b->stage, (void*)b->grid[0], (void*)b->grid[1], (void*)b->grid[2],
+                  (void*)b->counts, (void*)b->block_sums, (void*)b->d_scenes, (void*)b->d_start, (void*)b->d_key_base,
+                  (void*)b->d_ranges, (void*)b->boxes, (void*)b->work, (void*)b->status, (void*)b->comp_list})
+    cudaFree(p);
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  delete b;
+  return MPM_OK;
+}
+
+mpm_status mpm_batch_set_stream(mpm_batch* b, void* stream) {
+  if (!b) return MPM_ERR_INVALID;
+  if (!stream) return bfail(b, MPM_ERR_INVALID, "a batch needs a non-default stream (graph capture)");
+  b->stream = (cudaStream_t)stream;
+  free_graphs(b);
+  return MPM_OK;
+}
+
+mpm_status mpm_batch_upload_soa(mpm_batch* b, const float* x, const float* v, const float* C, const float* F,
+                                const float* Jp) {
+  if (!b) return MPM_ERR_INVALID;
+  const int64_t n = b->n;
+  if (n > 0 && !x) return bfail(b, MPM_ERR_INVALID, "x is required");
+  for (int64_t i = 0; i < 3 * n; ++i)
+    if (!std::isfinite(x[i])) return bfail(b, MPM_ERR_INVALID, "non-finite particle position");
+  b->pending = false;
+  b->launch_index = 0;
+  b->since_sort = b->sort_interval;
+  if (n == 0) return MPM_OK;
+  float* xs = b->stage;
+  float* vs = xs + 3 * n;
+  float* Cs = vs + 3 * n;
+  float* Fs = Cs + 9 * n;
+  float* Js = Fs + 9 * n;
+  BCUDA(b, cudaMemcpyAsync(xs, x, 12 * n, cudaMemcpyHostToDevice, b->stream));
+  if (v) BCUDA(b, cudaMemcpyAsync(vs, v, 12 * n, cudaMemcpyHostToDevice, b->stream));
+  if (C) BCUDA(b, cudaMemcpyAsync(Cs, C, 36 * n, cudaMemcpyHostToDevice, b->stream));
+  if (F) BCUDA(b, cudaMemcpyAsync(Fs, F, 36 * n, cudaMemcpyHostToDevice, b->stream));
+  if (Jp) BCUDA(b, cudaMemcpyAsync(Js, Jp, 4 * n, cudaMemcpyHostToDevice, b->stream));
+  BCUDA(b, launch_deinterleave(b->stage, b->sA, b->stride, n, v != nullptr, C != nullptr, F != nullptr,
+                               Jp != nullptr, b->stream));
+  BCUDA(b, launch_iota(b->idA, n, b->stream));
+  // fresh grids and box slots
+  for (auto& g : b->grid) BCUDA(b, cudaMemsetAsync(g, 0, sizeof(float4) * b->cells, b->stream));
+  std::vector<int> boxes(6 * kBoxSlots * b->nscenes);
+  for (size_t i = 0; i < boxes.size(); ++i) boxes[i] = (i % 6 < 3) ? INT_MAX : INT_MIN;
+  BCUDA(b, cudaMemcpyAsync(b->boxes, boxes.data(), sizeof(int) * boxes.size(), cudaMemcpyHostToDevice, b->stream));
+  b->launches += 2;
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  return MPM_OK;
+}
+
+mpm_status mpm_batch_substep(mpm_batch* b, int32_t nsteps) {
+  if (!b || nsteps < 0) return MPM_ERR_INVALID;
+  if (b->n == 0) return MPM_OK;
+  return advance(b, nsteps);
+}
+
+mpm_status mpm_batch_substep_graph(mpm_batch* b, int32_t nsteps) {
+  if (!b || nsteps < 0) return MPM_ERR_INVALID;
+  if (b->n == 0 || nsteps == 0) return MPM_OK;
+  if (!b->pending) {  // the first P2G of a run stays outside the graph
+    mpm_status st = launch(b, kStepP2GOnly);
+    if (st != MPM_OK) return st;
+  }
+  // A captured run is: one cell sort (when sorting is on), then nsteps fused launches.
+  // The graph bakes in the particle-buffer roles and the grid, counter and box-slot
+  // indices (launch index mod 6), so one graph is kept per (nsteps, phase, buffer role).
+  const bool sorting = b->sort_interval > 0;
+  const int role = (b->sA < b->sB) ? 0 : 1;
+  const int key_phase = (int)(b->launch_index % 6) * 2 + role;
+  const std::pair<int, int> key(nsteps, key_phase);
+  auto it = b->graphs.find(key);
+  if (it == b->graphs.end()) {
+    const int cur = b->cur, parity = b->parity;
+    const int64_t li = b->launch_index, ss = b->since_sort, lc = b->launches;
+    float* sA = b->sA;
+    float* sB = b->sB;
+    uint8_t* mA = b->matA;
+    uint8_t* mB = b->matB;
+    uint32_t* iA = b->idA;
+    uint32_t* iB = b->idB;
+    BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    mpm_status st = sorting ? sort(b) : MPM_OK;
+    for (int32_t i = 0; i < nsteps && st == MPM_OK; ++i) st = launch(b, kStepFused);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    // capturing recorded the work without running it: restore the host-side state
+    b->cur = cur;
+    b->parity = parity;
+    b->launch_index = li;
+    b->since_sort = ss;
+    b->launches = lc;
+    b->sA = sA;
+    b->sB = sB;
+    b->matA = mA;
+    b->matB = mB;
+    b->idA = iA;
+    b->idB = iB;
+    if (st != MPM_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (e != cudaSuccess) return bfail(b, MPM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    cudaGraphExec_t ge = nullptr;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bfail(b, MPM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    it = b->graphs.emplace(key, ge).first;
+  }
+  BCUDA(b, cudaGraphLaunch(it->second, b->stream));
+  // advance the host-side state exactly as the recorded work does
+  if (sorting) {
+    std::swap(b->sA, b->sB);
+    std::swap(b->matA, b->matB);
+    std::swap(b->idA, b->idB);
+    b->launches += 5;
+  }
+  b->cur = (int)((b->cur + nsteps) % 3);
+  b->parity ^= (nsteps & 1);
+  b->launch_index += nsteps;
+  b->since_sort = nsteps;
+  b->launches += nsteps;
+  return MPM_OK;
+}
+
+mpm_status mpm_batch_sync(mpm_batch* b) {
+  if (!b) return MPM_ERR_INVALID;
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  int flag = 0;
+  BCUDA(b, cudaMemcpy(&flag, b->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag) {
+    BCUDA(b, cudaMemset(b->status, 0, sizeof(int)));
+    return bfail(b, MPM_ERR_STATE, "non-finite particle state");
+  }
+  return MPM_OK;
+}
+
+mpm_status mpm_batch_download_soa(mpm_batch* b, float* x, float* v, float* C, float* F, float* Jp) {
+  if (!b) return MPM_ERR_INVALID;
+  const int64_t n = b->n;
+  if (n == 0) return MPM_OK;
+  BCUDA(b, launch_interleave(b->sA, b->stride, b->idA, n, b->stage, 0, b->stream));
+  b->launches += 1;
+  float* xs = b->stage;
+  float* vs = xs + 3 * n;
+  float* Cs = vs + 3 * n;
+  float* Fs = Cs + 9 * n;
+  float* Js = Fs + 9 * n;
+  if (x) BCUDA(b, cudaMemcpyAsync(x, xs, 12 * n, cudaMemcpyDeviceToHost, b->stream));
+  if (v) BCUDA(b, cudaMemcpyAsync(v, vs, 12 * n, cudaMemcpyDeviceToHost, b->stream));
+  if (C) BCUDA(b, cudaMemcpyAsync(C, Cs, 36 * n, cudaMemcpyDeviceToHost, b->stream));
+  if (F) BCUDA(b, cudaMemcpyAsync(F, Fs, 36 * n, cudaMemcpyDeviceToHost, b->stream));
+  if (Jp) BCUDA(b, cudaMemcpyAsync(Jp, Js, 4 * n, cudaMemcpyDeviceToHost, b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  return MPM_OK;
+}
+
+int64_t mpm_batch_particle_count(const mpm_batch* b) { return b ? b->n : -1; }
+int64_t mpm_batch_launch_count(const mpm_batch* b) { return b ? b->launches : -1; }
+
+mpm_status mpm_batch_last_error(const mpm_batch* b, char* buf, size_t len) {
+  if (!b || !buf || len == 0) return MPM_ERR_INVALID;
+  std::snprintf(buf, len, "%s", b->last_error.c_str());
+  return MPM_OK;
+}
+
+}  // extern "C"

@@ -216,7 +216,7 @@ mpm_status run_sort(mpm_ctx* c) {
   s.block_sums = c->block_sums;
   s.cells = c->sort_keys;
   s.N = (int)c->params.N;
-  s.dx_inv = c->K.dx_inv;
+  s.dx_inv = c->K.g.dx_inv;
   // liquid layout: x, v, C, J (16 components); general: all 25
   s.ncomp = c->liquid_layout ? kLiquidComps : kNumComps;
   s.comp_list = c->liquid_layout ? c->comp_list : c->comp_list + kLiquidComps;
@@ -240,7 +240,7 @@ namespace mpm {
 
 // SimulationParameters (include/TransferScheme.h:6-29) and the material constants,
 // derived in float exactly as the reference constructors do.
-void make_sim_consts(const mpm_params& p, const mpm_material* mats, int n_materials, SimConsts& K) {
+void make_grid_consts(const mpm_params& p, GridConsts& K) {
   K.N = (int)p.N;
   K.dt = p.dt;
   // dx = 1.0/N (double, stored as float), dx_inv = 1.0/dx; D_inv_const = I * 4.0 * dx_inv * dx_inv
@@ -252,10 +252,16 @@ void make_sim_consts(const mpm_params& p, const mpm_material* mats, int n_materi
   K.dtg = p.dt * p.gravity;
   K.boundary_mode = p.boundary_mode;
   K.boundary_cells = p.boundary_cells;
+}
+
+void make_sim_consts(const mpm_params& p, const mpm_material* mats, int n_materials, SimConsts& K) {
+  make_grid_consts(p, K.g);
   K.n_materials = n_materials;
-  for (int i = 0; i < n_materials; ++i) {
-    const mpm_material& m = mats[i];
-    DevMaterial& d = K.mat[i];
+  for (int i = 0; i < n_materials; ++i) make_dev_material(mats[i], K.mat[i]);
+}
+
+void make_dev_material(const mpm_material& m, DevMaterial& d) {
+  {
     d.kind = m.kind;
     d.vol = m.particle_volume;
     d.mass = m.density * m.particle_volume;                       // MaterialModelBase
@@ -583,7 +589,7 @@ mpm_status mpm_get_grid(mpm_ctx* c, int32_t which, float* out) {
   } else {
     mpm_status st = ensure_stage(c, bytes);
     if (st != MPM_OK) return st;
-    MPM_CUDA(c, launch_grid_op(c->grid[c->prev], (float4*)c->stage, c->K, c->stream));
+    MPM_CUDA(c, launch_grid_op(c->grid[c->prev], (float4*)c->stage, c->K.g, c->stream));
     c->launches += 1;
     MPM_CUDA(c, cudaMemcpyAsync(out, c->stage, bytes, cudaMemcpyDeviceToHost, c->stream));
   }

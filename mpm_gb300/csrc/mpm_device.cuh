@@ -35,11 +35,17 @@ struct DevMaterial {
   float vol, mass, mu0, lambda0, hardening, clamp_lo, clamp_hi, bulk;
 };
 
-// SimulationParameters (include/TransferScheme.h:6-29) plus the grid-op constants.
-struct SimConsts {
+// SimulationParameters (include/TransferScheme.h:6-29) plus the grid-op constants
+// of one grid (one scene).
+struct GridConsts {
   float dt, dx, dx_inv, dinv, dtg;  // dinv = D_inv_const diagonal = 4 dx_inv^2; dtg = dt * gravity
   int N;
   int boundary_mode, boundary_cells;
+};
+
+// Grid constants plus the material table.
+struct SimConsts {
+  GridConsts g;
   int n_materials;
   DevMaterial mat[kMaxMaterials];
 };
@@ -86,7 +92,7 @@ __device__ __forceinline__ bool outside_domain(int b0, int b1, int b2, int N) {
 // Grid operation (gridOpKernel, src/mpm.cu:76-107) for one node, returning the
 // velocity G2P reads (cell.head<3>()).  Nodes with mass <= 0 keep their raw value.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float3 grid_node_velocity(float4 g, int i, int j, int k, const SimConsts& K) {
+__device__ __forceinline__ float3 grid_node_velocity(float4 g, int i, int j, int k, const GridConsts& K) {
   float3 v = make_float3(g.x, g.y, g.z);
   if (g.w > 0.f) {
     const float inv = 1.f / g.w;

@@ -7,6 +7,16 @@
 
 namespace mpm {
 
+// One scene of a batch: its grid constants and where its grid starts in the pooled
+// grid buffers.
+struct SceneDev {
+  GridConsts g;
+  DevMaterial m;  // every particle of a scene has the scene's material
+  int64_t grid_offset;
+};
+
+constexpr int kBoxSlots = 6;  // per-scene P2G box slots (record / clear / reset rotate)
+
 // Arguments of the fused substep kernel.  One launch = G2P of substep n (from
 // grid_in, the P2G grid of substep n) + P2G of substep n+1 (into grid_out) +
 // clearing grid_zero (the grid substep n-1 read), so the three grid buffers rotate.
@@ -27,6 +37,13 @@ struct StepArgs {
   int* status;
   int* work;              // range counter of this launch, starts at 0
   int* work_next;         // range counter of the next launch, cleared by this one
+  // batch mode (nscenes > 0): ranges never straddle scenes; grids are cleared sparsely
+  int nscenes;
+  const int4* ranges;     // (scene, begin, end, 0)
+  int nranges;
+  const SceneDev* scenes;
+  int* boxes;             // [scene][kBoxSlots][6]: lo xyz, hi xyz of P2G base cells
+  int box_record, box_clear, box_reset;
   SimConsts K;
 };
 
@@ -38,7 +55,7 @@ cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guar
 // Dynamic shared memory of a variant: velocity tile (G2P) + per-warp reduction buffers (P2G).
 size_t step_smem_bytes(StepKind kind, int tile_cap);
 // Max resident CTAs per SM for the variant at the given dynamic shared memory.
-int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem);
+int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem, bool batch = false);
 
 }  // namespace mpm
 
@@ -47,6 +64,8 @@ int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem);
 namespace mpm {
 
 // Device constants from the C ABI parameters and material table.
+void make_grid_consts(const mpm_params& p, GridConsts& K);
+void make_dev_material(const mpm_material& m, DevMaterial& d);
 void make_sim_consts(const mpm_params& p, const mpm_material* mats, int n_materials, SimConsts& K);
 // Range size (chunk, particles) and grid size of a substep launch.
 void step_launch_shape(int num_sms, int64_t n, bool liquid, bool guard, StepKind kind, int steps_per_warp,
@@ -70,6 +89,11 @@ struct SortArgs {
   float dx_inv;
   int ncomp;            // components to move
   const int* comp_list; // device list of component indices
+  // batch mode (nscenes > 0): keys are scene_key_base[scene] + the bricked key in the scene's grid
+  int nscenes;
+  const int64_t* scene_start;      // nscenes + 1 particle offsets
+  const uint32_t* scene_key_base;  // nscenes
+  const SceneDev* scenes;
 };
 cudaError_t launch_sort(const SortArgs& a, int num_sms, cudaStream_t st, int64_t* launches);
 
@@ -81,6 +105,6 @@ cudaError_t launch_interleave(const float* s, int64_t stride, const uint32_t* id
 cudaError_t launch_iota(uint32_t* id, int64_t n, cudaStream_t st);
 cudaError_t launch_scatter_u8(const uint8_t* src, const uint32_t* id, int64_t n, uint8_t* dst, cudaStream_t st);
 // Post-op grid with the reference's mass slot (src/mpm.cu:86-88).
-cudaError_t launch_grid_op(const float4* in, float4* out, SimConsts K, cudaStream_t st);
+cudaError_t launch_grid_op(const float4* in, float4* out, GridConsts K, cudaStream_t st);
 
 }  // namespace mpm

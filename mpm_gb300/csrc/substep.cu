@@ -130,7 +130,7 @@ __device__ __forceinline__ void p2g_scatter_step(float4* wbuf, int lane, int key
 
 // weights_per_direction for all three dimensions plus the node offsets
 // dpos = (base + a) dx - x (src/mpm.cu:50-60).
-__device__ __forceinline__ void stencil(const float x[3], const SimConsts& K, int b[3], float w[3][3], float d[3][3]) {
+__device__ __forceinline__ void stencil(const float x[3], const GridConsts& K, int b[3], float w[3][3], float d[3][3]) {
 #pragma unroll
   for (int dim = 0; dim < 3; ++dim) {
     QuadraticInterpolationKernel::weights_per_direction(x[dim], K.dx_inv, b[dim], w[dim]);
@@ -144,7 +144,7 @@ __device__ __forceinline__ void stencil(const float x[3], const SimConsts& K, in
 // dimension: v = sum w g, C = D sum w g dpos^T (D = 4/dx^2).  `node(a, b, c)`
 // returns the grid velocity of node base + (a, b, c), zero outside the grid.
 template <class NodeFn>
-__device__ __forceinline__ void g2p_gather(NodeFn node, const SimConsts& K, const float w[3][3], const float d[3][3],
+__device__ __forceinline__ void g2p_gather(NodeFn node, const GridConsts& K, const float w[3][3], const float d[3][3],
                                            float v[3], float C[3][3]) {
   float c0[3] = {0.f, 0.f, 0.f}, c1[3] = {0.f, 0.f, 0.f}, c2[3] = {0.f, 0.f, 0.f};
   v[0] = v[1] = v[2] = 0.f;
@@ -197,7 +197,7 @@ struct G2POut {
 
 // Gather straight from the P2G grid (grid op per node) for chunks whose tile does
 // not fit in shared memory; out of line to keep the hot loop small.
-__device__ __noinline__ G2POut g2p_gather_global(const float4* grid_in, const SimConsts& K, float x0, float x1,
+__device__ __noinline__ G2POut g2p_gather_global(const float4* grid_in, const GridConsts& K, float x0, float x1,
                                                  float x2) {
   const int N = K.N;
   const float x[3] = {x0, x1, x2};
@@ -231,7 +231,7 @@ __device__ __forceinline__ bool box_fits(const int lo[3], const int hi[3], int c
 }
 
 __device__ __forceinline__ void warp_tile_build(float4* wtile, int lane, const int lo[3], const int hi[3],
-                                                const float4* grid_in, const SimConsts& K, TileBox& tb) {
+                                                const float4* grid_in, const GridConsts& K, TileBox& tb) {
   int ext[3];
 #pragma unroll
   for (int dd = 0; dd < 3; ++dd) ext[dd] = (hi[dd] >= lo[dd]) ? hi[dd] + 3 - lo[dd] : 0;
@@ -259,7 +259,7 @@ __device__ __forceinline__ void warp_tile_build(float4* wtile, int lane, const i
   __syncwarp();
 }
 
-template <bool LIQ, bool G2P, bool P2G, bool GUARD>
+template <bool LIQ, bool G2P, bool P2G, bool GUARD, bool BATCH>
 __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_constant__ StepArgs A) {
   extern __shared__ float4 smem[];
   const int tid = threadIdx.x;
@@ -267,8 +267,10 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
   // per-warp regions: velocity tile (G2P), P2G transpose buffer
   float4* wtile = smem + warp * A.tile_cap;
   float4* wbuf = smem + (G2P ? kStepWarps * A.tile_cap : 0) + warp * kRedFloat4;
-  const SimConsts& K = A.K;
-  const int N = K.N;
+  GridConsts K = A.K.g;
+  int N = K.N;
+  const float4* gin = A.grid_in;
+  float4* gout = A.grid_out;
   float* __restrict__ s = A.s;
   const int64_t st = A.stride;
 
@@ -277,13 +279,50 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
   // counter while finishing the last step of its current one, so warps that run
   // faster take more ranges; no CTA barriers.
   if (blockIdx.x == 0 && tid == 0) *A.work_next = 0;
-  const int64_t nranges = (A.n + A.chunk - 1) / A.chunk;
+  if (BATCH) {
+    // clear, per scene, the grid region the launch two substeps back accumulated (the
+    // buffer this launch leaves for the next one to fill), then free its box slot
+    for (int sc = blockIdx.x; sc < A.nscenes; sc += gridDim.x) {
+      const int* bx = A.boxes + ((int64_t)sc * kBoxSlots + A.box_clear) * 6;
+      const SceneDev& sd = A.scenes[sc];
+      const int Ns = sd.g.N;
+      const int l0 = max(bx[0], 0), l1 = max(bx[1], 0), l2 = max(bx[2], 0);
+      const int h0 = min(bx[3] + 2, Ns - 1), h1 = min(bx[4] + 2, Ns - 1), h2 = min(bx[5] + 2, Ns - 1);
+      if (h0 >= l0 && h1 >= l1 && h2 >= l2 && A.grid_zero) {
+        const int e1 = h1 - l1 + 1, e2 = h2 - l2 + 1;
+        const int64_t vol = (int64_t)(h0 - l0 + 1) * e1 * e2;
+        float4* gz = A.grid_zero + sd.grid_offset;
+        for (int64_t q = tid; q < vol; q += kStepThreads) {
+          const int i = l0 + (int)(q / ((int64_t)e1 * e2));
+          const int rem = (int)(q % ((int64_t)e1 * e2));
+          gz[((int64_t)i * Ns + (l1 + rem / e2)) * Ns + (l2 + rem % e2)] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      }
+      if (tid < 6) A.boxes[((int64_t)sc * kBoxSlots + A.box_reset) * 6 + tid] = (tid < 3) ? INT_MAX : INT_MIN;
+    }
+  }
+  const int64_t nranges = BATCH ? A.nranges : (A.n + A.chunk - 1) / A.chunk;
   const int64_t first_wave = (int64_t)gridDim.x * kStepWarps;
   int64_t r = (int64_t)blockIdx.x * kStepWarps + warp;
   while (r < nranges) {
     int claim = 0;
-    const int64_t wbeg = r * A.chunk;
-    const int64_t wend = min(wbeg + (int64_t)A.chunk, A.n);
+    int64_t wbeg, wend;
+    int scene = 0;
+    if (BATCH) {
+      const int4 rg = A.ranges[r];
+      scene = rg.x;
+      wbeg = rg.y;
+      wend = rg.z;
+      const SceneDev& sd = A.scenes[scene];
+      K = sd.g;
+      N = K.N;
+      gin = A.grid_in ? A.grid_in + sd.grid_offset : nullptr;
+      gout = A.grid_out + sd.grid_offset;
+    } else {
+      wbeg = r * A.chunk;
+      wend = min(wbeg + (int64_t)A.chunk, A.n);
+    }
+    int plo[3] = {INT_MAX, INT_MAX, INT_MAX}, phi[3] = {INT_MIN, INT_MIN, INT_MIN};  // P2G box (batch)
     TileBox tb{0, 0, 0, 1, 1};
     int64_t win_end = wbeg;  // end of the steps the current tile covers
     bool tile_ok = false;
@@ -332,7 +371,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
         }
         tile_ok = we > pb;
         win_end = tile_ok ? we : pb + 32;  // a step that alone does not fit gathers from global
-        if (tile_ok) warp_tile_build(wtile, lane, lo, hi, A.grid_in, K, tb);
+        if (tile_ok) warp_tile_build(wtile, lane, lo, hi, gin, K, tb);
       }
       const int64_t p = pb + lane;
       const bool valid = p < wend;
@@ -367,7 +406,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
           for (int i = 0; i < 9; ++i) Cm[i / 3][i % 3] = s[(kC + i) * st + p];
         }
       }
-      const DevMaterial& M = K.mat[mi];
+      const DevMaterial& M = BATCH ? A.scenes[scene].m : A.K.mat[mi];
       // ---- G2P + constitutive update + advection (gridToParticle)
       bool have_uv = false;
       float Usv[3][3], Vsv[3][3];
@@ -386,7 +425,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
           g2p_gather(node, K, w, d, v, Cm);
         } else {
           // a step whose own box exceeds the tile (rare: a jump between brick rows)
-          const G2POut o = g2p_gather_global(A.grid_in, K, x[0], x[1], x[2]);
+          const G2POut o = g2p_gather_global(gin, K, x[0], x[1], x[2]);
 #pragma unroll
           for (int r = 0; r < 3; ++r) {
             v[r] = o.v[r];
@@ -474,6 +513,13 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
           stencil(x, K, b, w, d);
           if (!outside_domain(b[0], b[1], b[2], N)) {
             key = pack_key(b[0], b[1], b[2]);
+            if (BATCH) {
+#pragma unroll
+              for (int dd = 0; dd < 3; ++dd) {
+                plo[dd] = min(plo[dd], b[dd]);
+                phi[dd] = max(phi[dd], b[dd]);
+              }
+            }
             m = M.mass;
             float PF[3][3];
             if (LIQ || M.kind == kLiquid) {
@@ -507,14 +553,27 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
             for (int dd = 0; dd < 3; ++dd) mv[dd] = v[dd] * m;
           }
         }
-        p2g_scatter_step(wbuf, lane, key, w, d, Aff, mv, m, A.grid_out, N);
+        p2g_scatter_step(wbuf, lane, key, w, d, Aff, mv, m, gout, N);
+      }
+    }
+    if (BATCH && P2G) {
+      // record the range's P2G box in its scene's slot (cleared two launches later)
+      int* bx = A.boxes + ((int64_t)scene * kBoxSlots + A.box_record) * 6;
+#pragma unroll
+      for (int dd = 0; dd < 3; ++dd) {
+        const int l = __reduce_min_sync(kFull, plo[dd]);
+        const int h = __reduce_max_sync(kFull, phi[dd]);
+        if (lane == 0 && h >= l) {
+          atomicMin(bx + dd, l);
+          atomicMax(bx + 3 + dd, h);
+        }
       }
     }
     r = first_wave + __shfl_sync(kFull, claim, 0);
   }
 
   // ---- clear the grid buffer the previous substep read (used by the launch after next)
-  if (A.grid_zero) {
+  if (!BATCH && A.grid_zero) {
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int64_t i = (int64_t)blockIdx.x * kStepThreads + tid; i < A.grid_cells;
          i += (int64_t)gridDim.x * kStepThreads)
@@ -522,17 +581,21 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
   }
 }
 
-template <bool LIQ, bool G2P, bool P2G, bool GUARD>
+template <bool LIQ, bool G2P, bool P2G, bool GUARD, bool BATCH>
 static void* kernel_ptr() {
-  return (void*)step_kernel<LIQ, G2P, P2G, GUARD>;
+  return (void*)step_kernel<LIQ, G2P, P2G, GUARD, BATCH>;
 }
 
-static void* select_kernel(StepKind kind, bool liquid, bool guard) {
-#define MPM_SEL(L, G)                                                   \
-  if (liquid == L && guard == G) {                                      \
-    if (kind == kStepP2GOnly) return kernel_ptr<L, false, true, G>();   \
-    if (kind == kStepFused) return kernel_ptr<L, true, true, G>();      \
-    return kernel_ptr<L, true, false, G>();                             \
+static void* select_kernel(StepKind kind, bool liquid, bool guard, bool batch) {
+  if (batch) {  // batches use the general layout, no guard
+    if (kind == kStepP2GOnly) return kernel_ptr<false, false, true, false, true>();
+    return kernel_ptr<false, true, true, false, true>();
+  }
+#define MPM_SEL(L, G)                                                        \
+  if (liquid == L && guard == G) {                                           \
+    if (kind == kStepP2GOnly) return kernel_ptr<L, false, true, G, false>(); \
+    if (kind == kStepFused) return kernel_ptr<L, true, true, G, false>();    \
+    return kernel_ptr<L, true, false, G, false>();                           \
   }
   MPM_SEL(true, false)
   MPM_SEL(true, true)
@@ -550,7 +613,7 @@ size_t step_smem_bytes(StepKind kind, int tile_cap) {
 }
 
 cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guard, int grid_blocks, cudaStream_t st) {
-  void* fn = select_kernel(kind, liquid, guard);
+  void* fn = select_kernel(kind, liquid, guard, a.nscenes > 0);
   const size_t smem = step_smem_bytes(kind, a.tile_cap);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -559,8 +622,8 @@ cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guar
   return cudaLaunchKernel(fn, dim3(grid_blocks), dim3(kStepThreads), args, smem, st);
 }
 
-int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem) {
-  void* fn = select_kernel(kind, liquid, guard);
+int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem, bool batch) {
+  void* fn = select_kernel(kind, liquid, guard, batch);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kStepThreads, smem) != cudaSuccess || nb < 1) nb = 1;

@@ -148,3 +148,38 @@ CONFIGS = {
     "snow": config_snow,
     "differentiable": config_differentiable,
 }
+
+
+def config_batched(nscenes=256, seed=0, count_range=(2_000, 200_000), grids=(16, 32, 64)):
+    """Batched: independent scenes with log-uniform particle counts, N from {16,32,64},
+    material from {elastic, liquid, snow} (the parameters of the plain scenes), a box
+    or a sphere with a seeded random centre and size inside [0.1,0.9]^3; dt 1e-4."""
+    rng = np.random.default_rng(seed)
+    scenes = []
+    lo, hi = np.log(count_range[0]), np.log(count_range[1])
+    for i in range(nscenes):
+        n = int(round(np.exp(rng.uniform(lo, hi))))
+        N = int(rng.choice(grids))
+        kind = int(rng.integers(0, 3))
+        st = _empty_state(n)
+        if rng.random() < 0.5:
+            side = rng.uniform(0.1, 0.35, 3)
+            c = rng.uniform(0.1 + side / 2, 0.9 - side / 2)
+            st["x"] = sample_box(rng, n, c - side / 2, c + side / 2)
+            vol_region = float(np.prod(side))
+        else:
+            r = rng.uniform(0.05, 0.18)
+            c = rng.uniform(0.1 + r, 0.9 - r, 3)
+            st["x"] = sample_sphere(rng, n, c, r)
+            vol_region = 4.0 / 3.0 * math.pi * r ** 3
+        vol = vol_region / n
+        if kind == 0:
+            mat = M.elastic(vol, density=1000.0, E=1e4, nu=0.3)
+        elif kind == 1:
+            mat = M.liquid(vol, density=1000.0, bulk=4e4)
+        else:
+            mat = M.snow(vol, density=700.0, E=1.4e5, nu=0.2, hardening=10.0)
+            st["v"][:, 1] = -1.0
+        scenes.append({"name": f"scene{i}", "state": st, "material": mat,
+                       "params": {"dt": 1e-4, "N": N, "gravity": GRAVITY, "boundary_mode": 0, "boundary_cells": 3}})
+    return scenes
