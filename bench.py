@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="liquid", choices=["liquid", "snow", "elastic", "batched"])
+    ap.add_argument("--config", default="liquid", choices=["liquid", "snow", "elastic", "batched", "differentiable"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -431,12 +431,58 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+def run_differentiable(args):
+    """Config 5: 100k fixed-corotated particles, N=64, 256 substeps, checkpoint every 16;
+    forward (checkpointed) and backward (recompute + adjoint kernels) wall times."""
+    from mpm_gb300 import build
+
+    build.build()
+    import torch
+
+    from mpm_gb300 import scenes
+    from mpm_gb300.autograd import DiffSim
+
+    cfg = scenes.config_differentiable()
+    st = cfg["state"]
+    n = st["x"].shape[0]
+    nsteps = 256
+    sim = DiffSim(cfg["params"], cfg["materials"][0], n, nsteps, 16)
+    target = np.array([0.6, 0.3, 0.5])
+    fw, bw = [], []
+    for k in range(max(args.warmup, 1) + max(1, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        xo, _ = sim.forward(st, nsteps)
+        t1 = time.perf_counter()
+        com = xo.astype(np.float64).mean(0)
+        gx = np.tile(2.0 * (com - target) / n, (n, 1))
+        t2 = time.perf_counter()
+        sim.backward(gx)
+        t3 = time.perf_counter()
+        if k >= max(args.warmup, 1):
+            fw.append(t1 - t0)
+            bw.append(t3 - t2)
+    sim.close()
+    f, b = statistics.median(fw), statistics.median(bw)
+    torch.cuda.synchronize()
+    line = {"metric": "particle-substeps/s", "value": n * nsteps / f, "unit": "particle-substeps/s", "n_gpus": 1,
+            "steps": len(fw), "warmup": args.warmup, "ms_per_step": 1e3 * f / nsteps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "differentiable_100k_N64_256", "particles": n, "N": 64, "substeps": nsteps,
+                       "checkpoint_every": 16},
+            "forward_s": f, "backward_s": b, "bwd_fwd_ratio": b / f,
+            "timing": "wall clock around the blocking mpm_diff_forward / mpm_diff_backward calls (host copies of the "
+                      "initial state and of the gradients included)"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.config == "batched":
         run_batched(args)
+    elif args.config == "differentiable":
+        run_differentiable(args)
     else:
         run_ours(args)
 

@@ -179,6 +179,27 @@ int64_t mpm_batch_particle_count(const mpm_batch* batch);
 int64_t mpm_batch_launch_count(const mpm_batch* batch);
 mpm_status mpm_batch_last_error(const mpm_batch* batch, char* buf, size_t len);
 
+/* ---------------------------------------------------------------------------
+ * Differentiable substeps (no counterpart in the reference, which has no gradients).
+ * A fixed-corotated scene (MMFixedCorotated, include/MaterialModel.cuh:40-62) is run
+ * forward with a checkpoint every `checkpoint_every` substeps; the backward pass
+ * recomputes each segment and runs hand-written adjoint kernels in reverse.  Host
+ * arrays use the interleaved layout of mpm_upload_soa.
+ * ------------------------------------------------------------------------- */
+typedef struct mpm_diff mpm_diff;
+mpm_status mpm_diff_create(const mpm_params* params, const mpm_material* material, int64_t n, int32_t max_steps,
+                           int32_t checkpoint_every, mpm_diff** out);
+mpm_status mpm_diff_destroy(mpm_diff* diff);
+/* Change E / nu (the material must stay fixed-corotated). */
+mpm_status mpm_diff_set_material(mpm_diff* diff, const mpm_material* material);
+/* nsteps substeps from the initial state; writes the final x and v (either may be NULL). */
+mpm_status mpm_diff_forward(mpm_diff* diff, const float* x0, const float* v0, const float* C0, const float* F0,
+                            const float* Jp0, int32_t nsteps, float* x_out, float* v_out);
+/* Adjoint of the last forward run: from dL/dx, dL/dv of the final state to dL/d of the
+ * initial x, v, C, F and dL/dmu0, dL/dlambda0 (gmu_glambda[2]); outputs may be NULL. */
+mpm_status mpm_diff_backward(mpm_diff* diff, const float* gx_final, const float* gv_final, float* gx0, float* gv0,
+                             float* gC0, float* gF0, double* gmu_glambda);
+
 /* Substep entry point that allocates nothing.  It has no counterpart in the reference.
  * For callers that cannot call cudaMalloc: code running while someone else captures a CUDA
  * graph, plugins whose host owns all device memory, and callers that forbid allocation after

@@ -80,6 +80,12 @@ SIGNATURES = [
     ("mpm_batch_particle_count", I64, [P]),
     ("mpm_batch_launch_count", I64, [P]),
     ("mpm_batch_last_error", I32, [P, ctypes.c_char_p, ctypes.c_size_t]),
+    ("mpm_diff_create", I32, [ctypes.POINTER(MpmParams), ctypes.POINTER(MpmMaterial), I64, I32, I32,
+                              ctypes.POINTER(P)]),
+    ("mpm_diff_destroy", I32, [P]),
+    ("mpm_diff_set_material", I32, [P, ctypes.POINTER(MpmMaterial)]),
+    ("mpm_diff_forward", I32, [P, P, P, P, P, P, I32, P, P]),
+    ("mpm_diff_backward", I32, [P, P, P, P, P, P, P, P]),
     ("mpm_substep_noalloc", I32, [ctypes.POINTER(MpmParams), ctypes.POINTER(MpmMaterial), I32, P, I64, P, I64, I32,
                                   P]),
 ]

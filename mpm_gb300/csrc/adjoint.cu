@@ -1,0 +1,676 @@
+// Differentiable substep: checkpointed forward and hand-written adjoint kernels.
+//
+// The reference has no gradients.  This file differentiates the substep of
+// src/mpm.cu:14-178 for the fixed-corotated material (MMFixedCorotated,
+// include/MaterialModel.cuh:40-62: P F^T = 2 mu (F - R) F^T + lambda (Jp - 1) Jp I,
+// no plasticity, Jp constant).  One substep n maps state_n = (x, v, C, F) to state_{n+1};
+// its adjoint runs three kernels:
+//   adj_g2p    per particle: back through advection, the F update and the G2P gather;
+//              gathers the grid velocity and SCATTERS the grid-velocity adjoint (the
+//              G2P adjoint is a cell-sorted scatter, reduced per warp like P2G);
+//   adj_gridop per node: back through the grid operation (division by the mass,
+//              gravity, walls) to adjoints of the P2G momentum and mass;
+//   adj_p2g    per particle: GATHERS the momentum/mass adjoints (the P2G adjoint is a
+//              gather) and goes back through the affine term, the stress (with the
+//              polar decomposition's adjoint) and the weights; accumulates dL/dmu and
+//              dL/dlambda.
+// The forward run stores the state every `checkpoint_every` substeps; the backward
+// pass recomputes each segment forward (keeping every state and P2G grid of the
+// segment) and then runs the adjoint substeps in reverse.
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "mpm_internal.h"
+#include "warp_ops.cuh"
+
+namespace mpm {
+
+struct AdjArgs {
+  const float* s;      // state_n, component-major (stride)
+  const float* s1;     // state_{n+1}
+  float* a;            // adjoint state: in = adjoint of state_{n+1}, out = of state_n
+  int64_t stride, n;
+  const float4* grid;  // P2G grid of substep n: (m v, m)
+  const float4* vgrid; // grid velocity of substep n (grid op applied)
+  float4* gadj;        // grid adjoint: velocity adjoint (adj_g2p), then (m v, m) adjoints
+  double* pgrad;       // [dL/dmu, dL/dlambda]
+  GridConsts K;
+  DevMaterial M;
+};
+
+constexpr int kAdjThreads = 256;
+constexpr int kAdjWarps = kAdjThreads / 32;
+
+// d w_a / d f for the quadratic B-spline (include/InterpolationKernel.cuh:64-66)
+__device__ __forceinline__ void weight_derivs(float x, float dx_inv, float dw[3]) {
+  const float xg = QuadraticInterpolationKernel::grid_coord(x, dx_inv);
+  const int b = (int)__fsub_rn(xg, 0.5f);
+  const float f = xg - (float)b;
+  dw[0] = -(1.5f - f) * dx_inv;
+  dw[1] = -2.f * (f - 1.f) * dx_inv;
+  dw[2] = (f - 0.5f) * dx_inv;
+}
+
+__device__ __forceinline__ float ld(const float* s, int64_t st, int comp, int64_t p) { return s[comp * st + p]; }
+
+__global__ void adj_velocity_kernel(const float4* grid, float4* vgrid, GridConsts K) {
+  const int N = K.N;
+  const int64_t cells = (int64_t)N * N * N;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c / ((int64_t)N * N)), j = (int)((c / N) % N), k = (int)(c % N);
+    const float3 v = grid_node_velocity(grid[c], i, j, k, K);
+    vgrid[c] = make_float4(v.x, v.y, v.z, 0.f);
+  }
+}
+
+// Back through x' = x + dt v', F' = (I + dt C') F and the G2P gather (src/mpm.cu:136-176).
+__global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(const AdjArgs A) {
+  extern __shared__ float4 smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float4* wbuf = smem + warp * kRedFloat4;
+  const GridConsts& K = A.K;
+  const int N = K.N;
+  const int64_t st = A.stride;
+  const int64_t nsteps = (A.n + 31) / 32;
+  for (int64_t ws = (int64_t)blockIdx.x * kAdjWarps + warp; ws < nsteps; ws += (int64_t)gridDim.x * kAdjWarps) {
+    const int64_t p = ws * 32 + lane;
+    const bool valid = p < A.n;
+    int key = -1;
+    float w[3][3], d[3][3], vt[3], Ct[3][3];
+    if (valid) {
+      float x[3], F[3][3], C1[3][3], ax[3], av[3], aC[3][3], aF[3][3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        x[q] = ld(A.s, st, kX + q, p);
+        ax[q] = ld(A.a, st, kX + q, p);
+        av[q] = ld(A.a, st, kV + q, p);
+      }
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        F[q / 3][q % 3] = ld(A.s, st, kF + q, p);
+        C1[q / 3][q % 3] = ld(A.s1, st, kC + q, p);
+        aC[q / 3][q % 3] = ld(A.a, st, kC + q, p);
+        aF[q / 3][q % 3] = ld(A.a, st, kF + q, p);
+      }
+      int b[3];
+      stencil(x, K, b, w, d);
+      if (!outside_domain(b[0], b[1], b[2], N)) {
+        key = pack_key(b[0], b[1], b[2]);
+        // v' total adjoint, C' total adjoint
+#pragma unroll
+        for (int q = 0; q < 3; ++q) vt[q] = av[q] + K.dt * ax[q];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            Ct[r][c] = aC[r][c] + K.dt * (aF[r][0] * F[c][0] + aF[r][1] * F[c][1] + aF[r][2] * F[c][2]);
+        // F adjoint: (I + dt C')^T F'adj
+        float Fa[3][3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            Fa[r][c] = aF[r][c] + K.dt * (C1[0][r] * aF[0][c] + C1[1][r] * aF[1][c] + C1[2][r] * aF[2][c]);
+        // gather grid velocity; x adjoint through the weights and dpos; node velocity adjoints
+        float dwd[3][3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) weight_derivs(x[q], K.dx_inv, dwd[q]);
+        float gx[3] = {ax[0], ax[1], ax[2]};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const int i = b[0] + a, j = b[1] + bb, k = b[2] + c;
+              float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+              if ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N)
+                g = __ldg(A.vgrid + ((int64_t)i * N + j) * N + k);
+              const float wt = w[0][a] * w[1][bb] * w[2][c];
+              const float dd[3] = {d[0][a], d[1][bb], d[2][c]};
+              const float vi[3] = {g.x, g.y, g.z};
+              float Cd[3], CTv[3];
+#pragma unroll
+              for (int r = 0; r < 3; ++r) {
+                Cd[r] = Ct[r][0] * dd[0] + Ct[r][1] * dd[1] + Ct[r][2] * dd[2];
+                CTv[r] = Ct[0][r] * vi[0] + Ct[1][r] * vi[1] + Ct[2][r] * vi[2];
+              }
+              // w-adjoint = v'adj . v_i + D v_i . (C'adj d)
+              const float wbar = vt[0] * vi[0] + vt[1] * vi[1] + vt[2] * vi[2] +
+                                 K.dinv * (vi[0] * Cd[0] + vi[1] * Cd[1] + vi[2] * Cd[2]);
+              const float gw[3] = {dwd[0][a] * w[1][bb] * w[2][c], w[0][a] * dwd[1][bb] * w[2][c],
+                                   w[0][a] * w[1][bb] * dwd[2][c]};
+#pragma unroll
+              for (int r = 0; r < 3; ++r) gx[r] += wbar * gw[r] - K.dinv * wt * CTv[r];
+              // velocity adjoint of node i
+              wbuf[(a * 9 + bb * 3 + c) * kRedStride + lane] =
+                  make_float4(wt * (vt[0] + K.dinv * Cd[0]), wt * (vt[1] + K.dinv * Cd[1]),
+                              wt * (vt[2] + K.dinv * Cd[2]), 0.f);
+            }
+#pragma unroll
+        for (int q = 0; q < 3; ++q) A.a[(kX + q) * st + p] = gx[q];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) A.a[(kF + q) * st + p] = Fa[q / 3][q % 3];
+      }
+    }
+    if (__ballot_sync(kFull, key >= 0)) warp_scatter_runs(wbuf, lane, key, A.gadj, N);
+  }
+}
+
+// Back through gridOpKernel (src/mpm.cu:76-107): velocity adjoint -> (m v, m) adjoints.
+__global__ void adj_gridop_kernel(const float4* grid, float4* gadj, GridConsts K) {
+  const int N = K.N;
+  const int64_t cells = (int64_t)N * N * N;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x) {
+    const float4 g = grid[c];
+    float4 ga = gadj[c];
+    if (g.w > 0.f) {
+      const int i = (int)(c / ((int64_t)N * N)), j = (int)((c / N) % N), k = (int)(c % N);
+      bool sticky, floor_;
+      if (K.boundary_mode == kBoundaryRefFraction) {
+        const float bnd = 0.05f, fN = (float)N;
+        const float x = (float)i / fN, y = (float)j / fN, z = (float)k / fN;
+        sticky = x < bnd || x > 1.f - bnd || y > 1.f - bnd || z < bnd || z > 1.f - bnd;
+        floor_ = y < bnd;
+      } else if (K.boundary_mode == kBoundaryStickyCells) {
+        const int bc = K.boundary_cells;
+        sticky = i < bc || i >= N - bc || j < bc || j >= N - bc || k < bc || k >= N - bc;
+        floor_ = false;
+      } else {
+        const int bc = K.boundary_cells;
+        sticky = i < bc || i >= N - bc || j >= N - bc || k < bc || k >= N - bc;
+        floor_ = j < bc;
+      }
+      const float inv = 1.f / g.w;
+      if (sticky) ga = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (floor_ && !(g.y * inv + K.dtg > 0.f)) ga.y = 0.f;
+      // v = m v / m (+ gravity): d/d(mv) = 1/m, d/dm = -(m v)/m^2
+      const float mb = -(ga.x * g.x + ga.y * g.y + ga.z * g.z) * inv * inv;
+      gadj[c] = make_float4(ga.x * inv, ga.y * inv, ga.z * inv, mb);
+    } else {
+      gadj[c] = make_float4(ga.x, ga.y, ga.z, 0.f);  // raw value passed through (v = m v)
+    }
+  }
+}
+
+__device__ __forceinline__ void cross_mat(const float y[3], float Y[3][3]) {
+  Y[0][0] = 0.f;
+  Y[0][1] = -y[2];
+  Y[0][2] = y[1];
+  Y[1][0] = y[2];
+  Y[1][1] = 0.f;
+  Y[1][2] = -y[0];
+  Y[2][0] = -y[1];
+  Y[2][1] = y[0];
+  Y[2][2] = 0.f;
+}
+
+// Back through the P2G scatter (src/mpm.cu:14-74, TransferScheme.h:66-100) and
+// MMFixedCorotated::computePF, with the polar decomposition's adjoint:
+//   F = R S, dR = R [w]x with (tr(S) I - S) w = axial(R^T dF - dF^T R), so for a
+//   rotation adjoint Rbar: Fbar = R [y]x, y = (tr(S) I - S)^-1 k, k = axial part of R^T Rbar.
+__global__ void __launch_bounds__(kAdjThreads) adj_p2g_kernel(const AdjArgs A) {
+  const GridConsts& K = A.K;
+  const DevMaterial& M = A.M;
+  const int N = K.N;
+  const int64_t st = A.stride;
+  double mubar = 0.0, lambar = 0.0;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < A.n; p += (int64_t)gridDim.x * blockDim.x) {
+    float x[3], v[3], C[3][3], F[3][3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      x[q] = ld(A.s, st, kX + q, p);
+      v[q] = ld(A.s, st, kV + q, p);
+    }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      C[q / 3][q % 3] = ld(A.s, st, kC + q, p);
+      F[q / 3][q % 3] = ld(A.s, st, kF + q, p);
+    }
+    const float Jp = ld(A.s, st, kJp, p);
+    int b[3];
+    float w[3][3], d[3][3];
+    stencil(x, K, b, w, d);
+    if (outside_domain(b[0], b[1], b[2], N)) continue;  // frozen: adjoint passes through
+    float R[3][3], S[3][3];
+    polar_decomposition(F, R, S);
+    float PF[3][3];
+    compute_PF(M, F, R, Jp, PF);
+    const float m = M.mass;
+    const float sc = ((-K.dinv) * K.dt) * M.vol;
+    float Aff[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Aff[r][c] = sc * PF[r][c] + m * C[r][c];
+    float dwd[3][3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) weight_derivs(x[q], K.dx_inv, dwd[q]);
+    float vb[3] = {0.f, 0.f, 0.f}, Ab[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    float xb[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int i = b[0] + a, j = b[1] + bb, k = b[2] + c;
+          if ((unsigned)i >= (unsigned)N || (unsigned)j >= (unsigned)N || (unsigned)k >= (unsigned)N) continue;
+          const float4 g = __ldg(A.gadj + ((int64_t)i * N + j) * N + k);
+          const float gm[3] = {g.x, g.y, g.z};
+          const float wt = w[0][a] * w[1][bb] * w[2][c];
+          const float dd[3] = {d[0][a], d[1][bb], d[2][c]};
+          float contrib[3], ATg[3];
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            contrib[r] = m * v[r] + Aff[r][0] * dd[0] + Aff[r][1] * dd[1] + Aff[r][2] * dd[2];
+            ATg[r] = Aff[0][r] * gm[0] + Aff[1][r] * gm[1] + Aff[2][r] * gm[2];
+            vb[r] += wt * m * gm[r];
+          }
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) Ab[r][cc] += wt * gm[r] * dd[cc];
+          const float wbar = gm[0] * contrib[0] + gm[1] * contrib[1] + gm[2] * contrib[2] + g.w * m;
+          const float gw[3] = {dwd[0][a] * w[1][bb] * w[2][c], w[0][a] * dwd[1][bb] * w[2][c],
+                               w[0][a] * w[1][bb] * dwd[2][c]};
+#pragma unroll
+          for (int r = 0; r < 3; ++r) xb[r] += wbar * gw[r] - wt * ATg[r];
+        }
+    // affine = sc PF + m C
+    float PFb[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) PFb[r][c] = sc * Ab[r][c];
+    float mu = M.mu0;
+    // dL/dmu = <PFb, 2 (F - R) F^T>, dL/dlambda = tr(PFb) (Jp - 1) Jp
+    float G[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        G[r][c] = (F[r][0] - R[r][0]) * F[c][0] + (F[r][1] - R[r][1]) * F[c][1] + (F[r][2] - R[r][2]) * F[c][2];
+    float dmu = 0.f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) dmu += 2.f * PFb[r][c] * G[r][c];
+    mubar += dmu;
+    lambar += (double)(PFb[0][0] + PFb[1][1] + PFb[2][2]) * ((Jp - 1.f) * Jp);
+    // F adjoint of G(F) = (F - R) F^T with Gbar = 2 mu PFb
+    float Gb[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Gb[r][c] = 2.f * mu * PFb[r][c];
+    float Fb[3][3], Rb[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float gf = 0.f, gtf = 0.f, gtr = 0.f;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          gf += Gb[r][q] * F[q][c];
+          gtf += Gb[q][r] * F[q][c];
+          gtr += Gb[q][r] * R[q][c];
+        }
+        Fb[r][c] = gf + gtf - gtr;
+        Rb[r][c] = -gf;
+      }
+    // polar adjoint
+    float Kr[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Kr[r][c] = R[0][r] * Rb[0][c] + R[1][r] * Rb[1][c] + R[2][r] * Rb[2][c];
+    const float kv[3] = {Kr[2][1] - Kr[1][2], Kr[0][2] - Kr[2][0], Kr[1][0] - Kr[0][1]};
+    float Sp[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Sp[r][c] = R[0][r] * F[0][c] + R[1][r] * F[1][c] + R[2][r] * F[2][c];
+    const float tr = Sp[0][0] + Sp[1][1] + Sp[2][2];
+    float T[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) T[r][c] = (r == c ? tr : 0.f) - 0.5f * (Sp[r][c] + Sp[c][r]);
+    // y = T^-1 k by the adjugate
+    const float det = det3(T);
+    float y[3] = {0.f, 0.f, 0.f};
+    if (fabsf(det) > 1e-30f) {
+      float adj[3][3];
+      adj[0][0] = T[1][1] * T[2][2] - T[1][2] * T[2][1];
+      adj[0][1] = T[0][2] * T[2][1] - T[0][1] * T[2][2];
+      adj[0][2] = T[0][1] * T[1][2] - T[0][2] * T[1][1];
+      adj[1][0] = T[1][2] * T[2][0] - T[1][0] * T[2][2];
+      adj[1][1] = T[0][0] * T[2][2] - T[0][2] * T[2][0];
+      adj[1][2] = T[0][2] * T[1][0] - T[0][0] * T[1][2];
+      adj[2][0] = T[1][0] * T[2][1] - T[1][1] * T[2][0];
+      adj[2][1] = T[0][1] * T[2][0] - T[0][0] * T[2][1];
+      adj[2][2] = T[0][0] * T[1][1] - T[0][1] * T[1][0];
+      const float id = 1.f / det;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) y[r] = id * (adj[r][0] * kv[0] + adj[r][1] * kv[1] + adj[r][2] * kv[2]);
+    }
+    float Y[3][3];
+    cross_mat(y, Y);
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Fb[r][c] += R[r][0] * Y[0][c] + R[r][1] * Y[1][c] + R[r][2] * Y[2][c];
+    // write the adjoint of state_n (x and F add to the adj_g2p parts)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      A.a[(kX + q) * st + p] += xb[q];
+      A.a[(kV + q) * st + p] = vb[q];
+    }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      A.a[(kC + q) * st + p] = m * Ab[q / 3][q % 3];
+      A.a[(kF + q) * st + p] += Fb[q / 3][q % 3];
+    }
+  }
+  // block reduction of the parameter gradients
+  __shared__ double red[2][kAdjWarps];
+  for (int o = 16; o; o >>= 1) {
+    mubar += __shfl_xor_sync(kFull, mubar, o);
+    lambar += __shfl_xor_sync(kFull, lambar, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][warp] = mubar;
+    red[1][warp] = lambar;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a0 = 0.0, a1 = 0.0;
+    for (int q = 0; q < kAdjWarps; ++q) {
+      a0 += red[0][q];
+      a1 += red[1][q];
+    }
+    atomicAdd(A.pgrad, a0);
+    atomicAdd(A.pgrad + 1, a1);
+  }
+}
+
+}  // namespace mpm
+
+using namespace mpm;
+
+struct mpm_diff {
+  mpm_params params{};
+  mpm_material material{};
+  SimConsts K{};
+  int64_t n = 0, stride = 0;
+  int ckpt_every = 16, max_steps = 0, nsteps = 0;
+  int num_sms = 1;
+  cudaStream_t stream = nullptr;
+  float* ckpt = nullptr;       // (max_steps / ckpt_every + 1) states
+  float* seg = nullptr;        // (ckpt_every + 1) states
+  float4* seg_grid = nullptr;  // ckpt_every P2G grids
+  float4* grid3 = nullptr;     // 3 rotating grids for the forward run
+  float4* vgrid = nullptr;
+  float4* gadj = nullptr;
+  float* adj = nullptr;
+  double* pgrad = nullptr;
+  float* stage = nullptr;
+  uint32_t* id = nullptr;
+  int* work = nullptr;
+  int* status = nullptr;
+  int parity = 0;
+  int64_t cells = 0;
+  std::string last_error;
+};
+
+namespace {
+
+size_t state_floats(const mpm_diff* d) { return (size_t)kNumComps * d->stride; }
+
+mpm_status dlaunch(mpm_diff* d, StepKind kind, float* state, const float4* gin, float4* gout) {
+  StepArgs a{};
+  a.s = state;
+  a.stride = d->stride;
+  a.mat = nullptr;
+  a.id = d->id;
+  a.n = d->n;
+  a.grid_in = gin;
+  a.grid_out = gout;
+  a.grid_zero = nullptr;
+  a.grid_cells = d->cells;
+  a.tile_cap = 256;
+  a.status = d->status;
+  a.work = d->work + d->parity;
+  a.work_next = d->work + (d->parity ^ 1);
+  a.K = d->K;
+  int chunk = 0, blocks = 0;
+  step_launch_shape(d->num_sms, d->n, false, false, kind, 2, 256, chunk, blocks);
+  a.chunk = chunk;
+  if (launch_step(a, kind, false, false, blocks, d->stream) != cudaSuccess) return MPM_ERR_CUDA;
+  d->parity ^= 1;
+  return MPM_OK;
+}
+
+mpm_status forward_substep(mpm_diff* d, float* state, float4* grid) {
+  // P2G of state into `grid`, then G2P from it (in place): state_n -> state_{n+1}
+  if (cudaMemsetAsync(grid, 0, sizeof(float4) * d->cells, d->stream) != cudaSuccess) return MPM_ERR_CUDA;
+  mpm_status st = dlaunch(d, kStepP2GOnly, state, nullptr, grid);
+  if (st != MPM_OK) return st;
+  return dlaunch(d, kStepG2POnly, state, grid, nullptr);
+}
+
+int adj_blocks(const mpm_diff* d) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((d->n + kAdjThreads - 1) / kAdjThreads, (int64_t)d->num_sms * 2));
+}
+
+}  // namespace
+
+extern "C" {
+
+mpm_status mpm_diff_create(const mpm_params* params, const mpm_material* material, int64_t n, int32_t max_steps,
+                           int32_t checkpoint_every, mpm_diff** out) {
+  if (!params || !material || !out || n <= 0 || max_steps <= 0 || checkpoint_every <= 0) return MPM_ERR_INVALID;
+  if (material->kind != MPM_MAT_FIXED_COROTATED) return MPM_ERR_UNSUPPORTED;
+  if (params->N < 4 || params->N > 1000 || !(params->dt > 0.f) || params->g2p_guard) return MPM_ERR_INVALID;
+  *out = nullptr;
+  mpm_diff* d = new mpm_diff();
+  d->params = *params;
+  d->material = *material;
+  make_sim_consts(*params, material, 1, d->K);
+  d->n = n;
+  d->stride = (n + 63) / 64 * 64;
+  d->ckpt_every = checkpoint_every;
+  d->max_steps = max_steps;
+  d->cells = (int64_t)params->N * params->N * params->N;
+  int dev = 0;
+  const size_t sf = state_floats(d) * sizeof(float);
+  const int nck = max_steps / checkpoint_every + 2;
+  if (cudaGetDevice(&dev) || cudaDeviceGetAttribute(&d->num_sms, cudaDevAttrMultiProcessorCount, dev) ||
+      cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) || cudaMalloc(&d->ckpt, sf * nck) ||
+      cudaMalloc(&d->seg, sf * (checkpoint_every + 1)) ||
+      cudaMalloc(&d->seg_grid, sizeof(float4) * d->cells * checkpoint_every) ||
+      cudaMalloc(&d->grid3, sizeof(float4) * d->cells * 3) || cudaMalloc(&d->vgrid, sizeof(float4) * d->cells) ||
+      cudaMalloc(&d->gadj, sizeof(float4) * d->cells) || cudaMalloc(&d->adj, sf) ||
+      cudaMalloc(&d->pgrad, 2 * sizeof(double)) || cudaMalloc(&d->stage, sf) ||
+      cudaMalloc(&d->id, sizeof(uint32_t) * d->stride) || cudaMalloc(&d->work, 2 * sizeof(int)) ||
+      cudaMalloc(&d->status, sizeof(int)) || cudaMemset(d->work, 0, 2 * sizeof(int)) ||
+      cudaMemset(d->status, 0, sizeof(int)) || cudaMemset(d->ckpt, 0, sf * nck) || cudaMemset(d->seg, 0, sf) ||
+      cudaMemset(d->adj, 0, sf)) {
+    mpm_diff_destroy(d);
+    return MPM_ERR_NOMEM;
+  }
+  if (launch_iota(d->id, n, d->stream) != cudaSuccess) {
+    mpm_diff_destroy(d);
+    return MPM_ERR_CUDA;
+  }
+  *out = d;
+  return MPM_OK;
+}
+
+mpm_status mpm_diff_destroy(mpm_diff* d) {
+  if (!d) return MPM_ERR_INVALID;
+  if (d->stream) cudaStreamSynchronize(d->stream);
+  for (void* p : {(void*)d->ckpt, (void*)d->seg, (void*)d->seg_grid, (void*)d->grid3, (void*)d->vgrid,
+                  (void*)d->gadj, (void*)d->adj, (void*)d->pgrad, (void*)d->stage, (void*)d->id, (void*)d->work,
+                  (void*)d->status})
+    cudaFree(p);
+  if (d->stream) cudaStreamDestroy(d->stream);
+  delete d;
+  return MPM_OK;
+}
+
+mpm_status mpm_diff_set_material(mpm_diff* d, const mpm_material* material) {
+  if (!d || !material) return MPM_ERR_INVALID;
+  if (material->kind != MPM_MAT_FIXED_COROTATED) return MPM_ERR_UNSUPPORTED;
+  d->material = *material;
+  make_sim_consts(d->params, material, 1, d->K);
+  return MPM_OK;
+}
+
+// Forward run of nsteps substeps from the host state (interleaved x[3n], v[3n], C[9n],
+// F[9n], Jp[n]); keeps a checkpoint every checkpoint_every substeps.  The final state
+// goes to the host arrays given (any may be NULL).
+mpm_status mpm_diff_forward(mpm_diff* d, const float* x0, const float* v0, const float* C0, const float* F0,
+                            const float* Jp0, int32_t nsteps, float* x_out, float* v_out) {
+  if (!d || !x0 || nsteps <= 0 || nsteps > d->max_steps) return MPM_ERR_INVALID;
+  const int64_t n = d->n;
+  float* xs = d->stage;
+  float* vs = xs + 3 * n;
+  float* Cs = vs + 3 * n;
+  float* Fs = Cs + 9 * n;
+  float* Js = Fs + 9 * n;
+  cudaStream_t s = d->stream;
+  if (cudaMemcpyAsync(xs, x0, 12 * n, cudaMemcpyHostToDevice, s) ||
+      (v0 && cudaMemcpyAsync(vs, v0, 12 * n, cudaMemcpyHostToDevice, s)) ||
+      (C0 && cudaMemcpyAsync(Cs, C0, 36 * n, cudaMemcpyHostToDevice, s)) ||
+      (F0 && cudaMemcpyAsync(Fs, F0, 36 * n, cudaMemcpyHostToDevice, s)) ||
+      (Jp0 && cudaMemcpyAsync(Js, Jp0, 4 * n, cudaMemcpyHostToDevice, s)))
+    return MPM_ERR_CUDA;
+  if (launch_deinterleave(d->stage, d->ckpt, d->stride, n, v0 != nullptr, C0 != nullptr, F0 != nullptr,
+                          Jp0 != nullptr, s) != cudaSuccess)
+    return MPM_ERR_CUDA;
+  // work copy of the state; fused launches with three rotating grids, checkpoints copied out
+  const size_t sb = state_floats(d) * sizeof(float);
+  float* work = d->seg;
+  if (cudaMemcpyAsync(work, d->ckpt, sb, cudaMemcpyDeviceToDevice, s)) return MPM_ERR_CUDA;
+  if (cudaMemsetAsync(d->grid3, 0, sizeof(float4) * d->cells * 3, s)) return MPM_ERR_CUDA;
+  float4* g[3] = {d->grid3, d->grid3 + d->cells, d->grid3 + 2 * d->cells};
+  int cur = 0;
+  mpm_status st = dlaunch(d, kStepP2GOnly, work, nullptr, g[1]);
+  if (st != MPM_OK) return st;
+  cur = 1;
+  for (int32_t i = 0; i < nsteps; ++i) {
+    StepArgs dummy{};
+    (void)dummy;
+    // fused: G2P of substep i from g[cur], P2G of i+1 into g[cur+1], clear g[cur+2]
+    StepArgs a{};
+    a.s = work;
+    a.stride = d->stride;
+    a.id = d->id;
+    a.n = n;
+    a.grid_in = g[cur];
+    a.grid_out = g[(cur + 1) % 3];
+    a.grid_zero = g[(cur + 2) % 3];
+    a.grid_cells = d->cells;
+    a.tile_cap = 256;
+    a.status = d->status;
+    a.work = d->work + d->parity;
+    a.work_next = d->work + (d->parity ^ 1);
+    a.K = d->K;
+    int chunk = 0, blocks = 0;
+    step_launch_shape(d->num_sms, n, false, false, kStepFused, 2, 256, chunk, blocks);
+    a.chunk = chunk;
+    if (launch_step(a, kStepFused, false, false, blocks, s) != cudaSuccess) return MPM_ERR_CUDA;
+    d->parity ^= 1;
+    cur = (cur + 1) % 3;
+    if ((i + 1) % d->ckpt_every == 0 && i + 1 < nsteps)
+      if (cudaMemcpyAsync(d->ckpt + state_floats(d) * ((i + 1) / d->ckpt_every), work, sb, cudaMemcpyDeviceToDevice,
+                          s))
+        return MPM_ERR_CUDA;
+  }
+  d->nsteps = nsteps;
+  if (x_out || v_out) {
+    if (launch_interleave(work, d->stride, d->id, n, d->stage, 0, s) != cudaSuccess) return MPM_ERR_CUDA;
+    if (x_out && cudaMemcpyAsync(x_out, d->stage, 12 * n, cudaMemcpyDeviceToHost, s)) return MPM_ERR_CUDA;
+    if (v_out && cudaMemcpyAsync(v_out, d->stage + 3 * n, 12 * n, cudaMemcpyDeviceToHost, s)) return MPM_ERR_CUDA;
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) return MPM_ERR_CUDA;
+  return MPM_OK;
+}
+
+// Backward pass of the last forward run.  Inputs: dL/dx and dL/dv of the final state
+// (host, interleaved; either may be NULL for zero).  Outputs (host, any may be NULL):
+// dL/d of the initial x, v, C, F and dL/dmu0, dL/dlambda0 of the material.
+mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv_final, float* gx0, float* gv0,
+                             float* gC0, float* gF0, double* gmu_glambda) {
+  if (!d || d->nsteps <= 0) return MPM_ERR_INVALID;
+  const int64_t n = d->n;
+  cudaStream_t s = d->stream;
+  const size_t sf = state_floats(d);
+  const size_t sb = sf * sizeof(float);
+  float* xs = d->stage;
+  float* vs = xs + 3 * n;
+  if (cudaMemsetAsync(d->stage, 0, sb, s) || cudaMemsetAsync(d->pgrad, 0, 2 * sizeof(double), s) ||
+      (gx_final && cudaMemcpyAsync(xs, gx_final, 12 * n, cudaMemcpyHostToDevice, s)) ||
+      (gv_final && cudaMemcpyAsync(vs, gv_final, 12 * n, cudaMemcpyHostToDevice, s)))
+    return MPM_ERR_CUDA;
+  // adjoint state = (gx, gv, 0, 0, 0); the stage holds interleaved x, v, C, F, Jp slots
+  if (launch_deinterleave(d->stage, d->adj, d->stride, n, 1, 1, 1, 1, s) != cudaSuccess) return MPM_ERR_CUDA;
+  const int nseg = (d->nsteps + d->ckpt_every - 1) / d->ckpt_every;
+  AdjArgs A{};
+  A.stride = d->stride;
+  A.n = n;
+  A.a = d->adj;
+  A.gadj = d->gadj;
+  A.vgrid = d->vgrid;
+  A.pgrad = d->pgrad;
+  A.K = d->K.g;
+  A.M = d->K.mat[0];
+  const int blocks = adj_blocks(d);
+  const size_t smem = (size_t)kAdjWarps * kRedFloat4 * sizeof(float4);
+  if (cudaFuncSetAttribute(adj_g2p_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))
+    return MPM_ERR_CUDA;
+  const int gblocks = (int)std::min<int64_t>((d->cells + 255) / 256, 4096);
+  for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+    const int s0 = sgi * d->ckpt_every;
+    const int len = std::min(d->ckpt_every, d->nsteps - s0);
+    // recompute the segment, keeping every state and P2G grid
+    if (cudaMemcpyAsync(d->seg, d->ckpt + sf * sgi, sb, cudaMemcpyDeviceToDevice, s)) return MPM_ERR_CUDA;
+    for (int j = 0; j < len; ++j) {
+      if (cudaMemcpyAsync(d->seg + sf * (j + 1), d->seg + sf * j, sb, cudaMemcpyDeviceToDevice, s))
+        return MPM_ERR_CUDA;
+      mpm_status st = forward_substep(d, d->seg + sf * (j + 1), d->seg_grid + d->cells * j);
+      if (st != MPM_OK) return st;
+    }
+    // adjoint substeps in reverse
+    for (int j = len - 1; j >= 0; --j) {
+      A.s = d->seg + sf * j;
+      A.s1 = d->seg + sf * (j + 1);
+      A.grid = d->seg_grid + d->cells * j;
+      adj_velocity_kernel<<<gblocks, 256, 0, s>>>(A.grid, d->vgrid, A.K);
+      if (cudaMemsetAsync(d->gadj, 0, sizeof(float4) * d->cells, s)) return MPM_ERR_CUDA;
+      adj_g2p_kernel<<<blocks, kAdjThreads, smem, s>>>(A);
+      adj_gridop_kernel<<<gblocks, 256, 0, s>>>(A.grid, d->gadj, A.K);
+      adj_p2g_kernel<<<blocks, kAdjThreads, 0, s>>>(A);
+      if (cudaGetLastError() != cudaSuccess) return MPM_ERR_CUDA;
+    }
+  }
+  // out: adjoint of the initial state, host interleaved
+  if (launch_interleave(d->adj, d->stride, d->id, n, d->stage, 0, s) != cudaSuccess) return MPM_ERR_CUDA;
+  float* Cs = vs + 3 * n;
+  float* Fs = Cs + 9 * n;
+  if ((gx0 && cudaMemcpyAsync(gx0, xs, 12 * n, cudaMemcpyDeviceToHost, s)) ||
+      (gv0 && cudaMemcpyAsync(gv0, vs, 12 * n, cudaMemcpyDeviceToHost, s)) ||
+      (gC0 && cudaMemcpyAsync(gC0, Cs, 36 * n, cudaMemcpyDeviceToHost, s)) ||
+      (gF0 && cudaMemcpyAsync(gF0, Fs, 36 * n, cudaMemcpyDeviceToHost, s)) ||
+      (gmu_glambda && cudaMemcpyAsync(gmu_glambda, d->pgrad, 2 * sizeof(double), cudaMemcpyDeviceToHost, s)))
+    return MPM_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return MPM_ERR_CUDA;
+  return MPM_OK;
+}
+
+}  // extern "C"
