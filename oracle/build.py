@@ -55,13 +55,13 @@ def build_ref(force: bool = False) -> list:
         if not os.path.exists(srcp):
             continue
         out = os.path.join(outdir, name)
-        deps = [srcp] + [os.path.join(shim, f) for f in os.listdir(shim)]
+        deps = [srcp] + [os.path.join(d, f) for d, _, fs in os.walk(shim) for f in fs]
         if force or not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(d) for d in deps):
             tmp = out + ".tmp"
             # The shim directory comes first so its cuda.h / cuda_runtime.h / Eigen stand-ins
             # are found before any system header of the same name.
             _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w",
-                  "-I", shim, "-I", inc, "-o", tmp, srcp])
+                  "-I", shim, "-I", inc, "-I", os.path.join(REF_ROOT, "src"), "-o", tmp, srcp])
             os.replace(tmp, out)
         built.append(out)
     return built

@@ -69,7 +69,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "ref_svd.npz"), **svd_vectors())
     sub = os.path.join(ROOT, "oracle", "_ref", "libref_substep.so")
     if os.path.exists(sub):
-        from tests.golden import ref_substep_vectors
+        sys.path.insert(0, HERE)
+        import ref_substep_vectors
 
         np.savez_compressed(os.path.join(HERE, "ref_substep.npz"), **ref_substep_vectors.make(sub))
     print("golden fixtures written")

@@ -1,4 +1,6 @@
 """Shared comparison helpers for the parity tests."""
+import os
+
 import numpy as np
 
 FIELDS = ("x", "v", "C", "F", "Jp")
@@ -25,3 +27,25 @@ def field_scales(state, params):
 def compare_states(a, b, params, ref_state=None):
     sc = field_scales(ref_state if ref_state is not None else b, params)
     return {k: rel_err(a[k], b[k], sc[k]) for k in FIELDS}
+
+
+GOLDEN_SUBSTEP = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_substep.npz")
+
+
+def golden_substep_cases():
+    """The reference-policy substep vectors (tests/golden/ref_substep.npz) as
+    (name, cfg, nsteps, expected_state, expected_grid_after_p2g); cfg is in the form
+    ``Simulation.from_config`` and the oracle take."""
+    from mpm_gb300.materials import Material
+
+    d = np.load(GOLDEN_SUBSTEP)
+    cases = []
+    for name in (str(c) for c in d["cases"]):
+        dt, N, nsteps = d[name + "_params"]
+        state = {k: d[f"{name}_{k}_in"] for k in FIELDS}
+        state["mat"] = d[name + "_mat"]
+        expect = {k: d[f"{name}_{k}_out"] for k in FIELDS}
+        mats = [Material(int(r[0]), *(float(q) for q in r[1:])) for r in d[name + "_materials"]]
+        cfg = {"params": {"dt": float(dt), "N": int(N), "g2p_guard": 1}, "materials": mats, "state": state}
+        cases.append((name, cfg, int(nsteps), expect, d[name + "_grid"]))
+    return cases

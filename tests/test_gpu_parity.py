@@ -245,3 +245,23 @@ def test_api_errors(gpu_lib):
             sim.upload({"x": np.zeros((2, 3), np.float32), "mat": np.array([0, 3], np.uint8)})
         with pytest.raises(_lib.MpmError):
             sim.get_grid(0)  # no completed substep
+
+
+def _golden_ids():
+    from helpers import golden_substep_cases
+
+    return [c[0] for c in golden_substep_cases()]
+
+
+@pytest.mark.parametrize("case", _golden_ids())
+def test_matches_reference_policy_vectors(gpu_lib, case):
+    """The CUDA substep against the reference's own policy code run on the host
+    (tests/golden/ref_substep.npz, MMSnow elastic / snow / two-material scenes):
+    every particle field and the grid after the last P2G within 1e-5 relative."""
+    from helpers import golden_substep_cases
+
+    name, cfg, nsteps, expect, grid = next(c for c in golden_substep_cases() if c[0] == case)
+    out, (g_p2g, _) = run_gpu(cfg, nsteps, want_grid=True)
+    errs = compare_states(out, expect, cfg["params"], cfg["state"])
+    assert max(errs.values()) < 1e-5, errs
+    assert rel_err(g_p2g, grid) < 1e-5

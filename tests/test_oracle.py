@@ -199,3 +199,25 @@ def test_g2p_guard_freezes_high_indices(oracle_lib):
     lim = 8 ** 3
     assert np.array_equal(out["x"][lim + 1:], cfg["state"]["x"][lim + 1:].astype(np.float64))
     assert not np.array_equal(out["x"][:lim + 1], cfg["state"]["x"][:lim + 1].astype(np.float64))
+
+
+def _golden_ids():
+    from helpers import golden_substep_cases
+
+    return [c[0] for c in golden_substep_cases()]
+
+
+@pytest.mark.parametrize("case", _golden_ids())
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_substep_matches_reference_policies(oracle_lib, case, dtype):
+    """The oracle against the reference's own TransferScheme / MaterialModel (MMSnow) /
+    InterpolationKernel / linalg code, compiled for the host (tests/golden/ref_substep.npz):
+    every particle field and the grid after P2G within 1e-5 relative after 1-4 substeps."""
+    from helpers import golden_substep_cases
+
+    name, cfg, nsteps, expect, grid = next(c for c in golden_substep_cases() if c[0] == case)
+    mats = [m.derived() for m in cfg["materials"]]
+    out, g_p2g, _ = oracle_lib.substep(cfg["state"], cfg["params"], mats, nsteps, dtype, want_grids=True)
+    errs = compare_states(out, expect, cfg["params"], cfg["state"])
+    assert max(errs.values()) < 1e-5, errs
+    assert np.linalg.norm(g_p2g - grid) < 1e-5 * np.linalg.norm(grid)
