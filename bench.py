@@ -364,14 +364,24 @@ def run_batched(args):
     against looping plain launches scene by scene (one context per scene)."""
     import torch
 
+    world, rank, local = dist_setup(args)
+    if world > 1:
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
     from mpm_gb300 import build
 
-    build.build()
+    if rank == 0 or world == 1:
+        build.build()
+    if world > 1:
+        torch.distributed.barrier()
     from mpm_gb300 import scenes
     from mpm_gb300.batch import Batch
     from mpm_gb300.simulation import Simulation
 
-    scs = scenes.config_batched(nscenes=256, seed=0)
+    all_scenes = scenes.config_batched(nscenes=256, seed=0)
+    n_all = sum(s["state"]["x"].shape[0] for s in all_scenes)
+    # scenes are independent: rank r takes scenes r, r + world, ... (no collective on the data path)
+    scs = all_scenes[rank::world]
     n = sum(s["state"]["x"].shape[0] for s in scs)
     sub = 50
     stream = torch.cuda.Stream()
@@ -382,6 +392,9 @@ def run_batched(args):
     for _ in range(max(args.warmup, 3)):
         b.advance(sub, graph=True)
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
     steps = max(1, min(args.steps, 20))
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     l0 = b.launches
@@ -391,10 +404,15 @@ def run_batched(args):
         e.record(stream)
     torch.cuda.synchronize()
     batched_ms = sum(a.elapsed_time(e) for a, e in ev)
+    local_rate = n * sub * steps / (batched_ms * 1e-3)
+    if world > 1:
+        t = torch.tensor([batched_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        batched_ms = float(t.item())
     launches = b.launches - l0
     b.sync()
     b.close()
-    value = n * sub * steps / (batched_ms * 1e-3)
+    value = n_all * sub * steps / (batched_ms * 1e-3)
 
     # looped plain launches: one context per scene, substep by substep over the scenes
     sims = []
@@ -420,14 +438,20 @@ def run_batched(args):
     looped = n * loop_sub / (max(loop_ms * 1e-3, loop_wall))
     for sim in sims:
         sim.close()
-    line = {"metric": "particle-substeps/s", "value": value, "unit": "particle-substeps/s", "n_gpus": 1,
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return
+    line = {"metric": "particle-substeps/s", "value": value, "unit": "particle-substeps/s", "n_gpus": world,
             "steps": steps, "warmup": args.warmup, "ms_per_step": batched_ms / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batched_256_scenes", "particles": n, "scenes": 256,
+            "config": {"workload": "batched_256_scenes", "particles": n_all, "scenes": 256,
+                       "parallelism": f"scenes split over {world} ranks" if world > 1 else "single",
                        "substeps_per_step": sub, "graph": True, "l2": "inputs larger than L2 (state ~1 GB)"},
             "looped_plain": {"value": looped, "unit": "particle-substeps/s",
-                             "how": "256 contexts, mpm_substep(1) per scene per substep, 10 substeps"},
-            "batched_vs_looped": value / looped, "gpu_launches": launches}
+                             "how": "one context per scene of rank 0, mpm_substep(1) per scene per substep, 10 substeps"},
+            "batched_vs_looped": local_rate / looped, "gpu_launches": launches}
     print(json.dumps(line), flush=True)
 
 

@@ -143,9 +143,10 @@ mpm_status mpm_last_error(const mpm_ctx* ctx, char* buf, size_t len);
 int64_t mpm_launch_count(const mpm_ctx* ctx);
 
 /* Tuning knobs of the fused substep kernel (0 = keep the current value):
- * steps_per_warp (particles per lane per chunk), tile_nodes (shared-memory grid
- * tile capacity), waves (chunks per SM). */
-mpm_status mpm_set_tuning(mpm_ctx* ctx, int32_t steps_per_warp, int32_t tile_nodes, int32_t waves);
+ * steps_per_warp: 32-particle steps in each range a warp claims (1..256, default 2);
+ * tile_nodes: capacity of a warp's shared-memory grid-velocity tile (1..288, default 256);
+ * reserved: must be >= 0; ignored (the launch is sized by occupancy). */
+mpm_status mpm_set_tuning(mpm_ctx* ctx, int32_t steps_per_warp, int32_t tile_nodes, int32_t reserved);
 
 /* ---------------------------------------------------------------------------
  * Batched scenes.  The reference runs one scene per Simulation; a batch advances many

@@ -64,7 +64,6 @@ struct mpm_ctx {
   int64_t launches = 0;
   int steps_per_warp = 2;
   int tile_cap = 256;  // nodes per warp tile
-  int waves = 0;
   std::string last_error;
 };
 
@@ -612,14 +611,13 @@ mpm_status mpm_last_error(const mpm_ctx* c, char* buf, size_t len) {
   return MPM_OK;
 }
 
-mpm_status mpm_set_tuning(mpm_ctx* c, int32_t steps_per_warp, int32_t tile_nodes, int32_t waves) {
+mpm_status mpm_set_tuning(mpm_ctx* c, int32_t steps_per_warp, int32_t tile_nodes, int32_t reserved) {
   if (!c) return MPM_ERR_INVALID;
   if (steps_per_warp < 0 || steps_per_warp > 256) return fail(c, MPM_ERR_INVALID, "steps_per_warp out of range");
   if (tile_nodes < 0 || tile_nodes > 288) return fail(c, MPM_ERR_INVALID, "tile_nodes out of range (max 288 per warp)");
-  if (waves < 0) return fail(c, MPM_ERR_INVALID, "waves must be >= 0");
+  if (reserved < 0) return fail(c, MPM_ERR_INVALID, "reserved must be >= 0");
   if (steps_per_warp) c->steps_per_warp = steps_per_warp;
   if (tile_nodes) c->tile_cap = tile_nodes;
-  c->waves = waves;
   return MPM_OK;
 }
 

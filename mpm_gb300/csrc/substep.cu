@@ -11,20 +11,20 @@
 // so particle state is read once and written once per substep and the three grid
 // buffers rotate.  A P2G-only variant starts a run from uploaded state.
 //
-// Work decomposition: a CTA of 8 warps takes a contiguous chunk of cell-sorted
-// particles; each warp walks its slice 32 particles at a time (lane = particle,
-// coalesced SoA loads/stores).  P2G contributions are accumulated in registers
-// (27 nodes x 4 values per lane) while the lane's particles stay in one cell; when a
-// lane's cell changes, the warp flushes whole cell groups: members park their
-// accumulators in a per-warp shared-memory buffer, lane l sums node l over the
-// group and issues one vector atomic.  When a warp's particles scatter over many
-// cells, each lane adds its 27 nodes directly.  Dense scenes (100+ particles per
-// cell) thus issue well under one global atomic per particle instead of the
-// reference's 108.
+// Work decomposition: warps are the scheduling unit.  Each warp of a 12-warp CTA
+// takes a range of cell-sorted particles (steps_per_warp x 32) and walks it 32
+// particles at a time (lane = particle, coalesced component-major loads/stores);
+// further ranges are claimed from a global counter, so faster warps take more.
+// G2P reads a per-warp shared-memory tile of grid velocities staged once for a
+// window of steps whose base cells fit the tile.  P2G is a warp transpose-reduce:
+// every lane writes its 27 node contributions as a column of a per-warp buffer, and
+// lane l < 27 sums node l over each run of same-cell lanes and issues one vector
+// atomic per run.  Dense scenes (100+ particles per cell) thus issue about one
+// global atomic per node and step instead of the reference's 108 per particle.
 //
-// Code size matters: the hot loop holds one copy each of the gather, the
-// accumulate and the flush (the rare paths are out of line) so it stays resident
-// in the instruction cache at one 8-warp CTA per SM.
+// Code size matters: the hot loop holds one copy each of the gather, the column
+// write and the run walk (the rare paths are out of line) so it stays resident in
+// the instruction cache.
 #include <climits>
 
 #include "mpm_internal.h"
