@@ -272,7 +272,7 @@ def run_ours(args):
         starts[k].record(stream)
         sim.advance(1)
         ends[k].record(stream)
-        pure.append(sim.launches - l0 == 1)
+        pure.append(sim.launches - l0 == 2)  # velocity pass + fused kernel, no sort
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     launches = sim.launches - launches0
@@ -295,7 +295,7 @@ def run_ours(args):
     achieved = bytes_per_launch / (kernel_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": profile_traffic(workload), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": "mpm::step_kernel (fused G2P + P2G)", "kernel_ms": kernel_ms,
+                "kernel": "mpm::grid_velocity_kernel + mpm::scene_step_kernel (one substep)", "kernel_ms": kernel_ms,
                 "bytes_per_launch": bytes_per_launch}
 
     e2e = None

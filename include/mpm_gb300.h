@@ -142,11 +142,11 @@ mpm_status mpm_last_error(const mpm_ctx* ctx, char* buf, size_t len);
 /* Kernel launches issued by this context since creation (for accounting). */
 int64_t mpm_launch_count(const mpm_ctx* ctx);
 
-/* Tuning knobs of the fused substep kernel (0 = keep the current value):
- * steps_per_warp: 32-particle steps in each range a warp claims (1..256, default 2);
- * tile_nodes: capacity of a warp's shared-memory grid-velocity tile (1..288, default 256);
- * reserved: must be >= 0; ignored (the launch is sized by occupancy). */
-mpm_status mpm_set_tuning(mpm_ctx* ctx, int32_t steps_per_warp, int32_t tile_nodes, int32_t reserved);
+/* Tuning knob of the fused substep kernel: steps_per_warp, the 32-particle steps in
+ * each range a warp claims (1..256, default 2; 0 keeps the current value).
+ * reserved1, reserved2: must be >= 0; ignored (the grid tile is a fixed TMA box and
+ * the launch is sized by occupancy). */
+mpm_status mpm_set_tuning(mpm_ctx* ctx, int32_t steps_per_warp, int32_t reserved1, int32_t reserved2);
 
 /* ---------------------------------------------------------------------------
  * Batched scenes.  The reference runs one scene per Simulation; a batch advances many
@@ -210,8 +210,9 @@ mpm_status mpm_diff_backward(mpm_diff* diff, const float* gx_final, const float*
  *     of particle p at state[k * stride + p]: x 0-2, v 3-5, C 6-14 and F 15-23 (row-major),
  *     Jp 24 (J for a single-liquid table, whose F components are not touched);
  *   - mat: device array of material indices, or NULL for material 0;
- *   - the scratch (three P2G grids and two counters) is a static device array of 1.5 MiB
- *     that every GPU loading the library holds until exit, so N is limited to 32
+ *   - the scratch (three P2G grids, the padded velocity grid and two counters) is a static
+ *     device array of 2.3 MiB that every GPU loading the library holds until exit, so N is
+ *     limited to 32
  *     (MPM_ERR_UNSUPPORTED above); g2p_guard and check_finite are not supported here.
  * Particles are processed in the caller's order (no cell sort; sorted input runs faster).
  * The first call on a device looks up the scratch's device address (cudaGetSymbolAddress), so

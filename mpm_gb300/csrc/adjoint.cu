@@ -414,7 +414,9 @@ struct mpm_diff {
   float* seg = nullptr;        // (ckpt_every + 1) states
   float4* seg_grid = nullptr;  // ckpt_every P2G grids
   float4* grid3 = nullptr;     // 3 rotating grids for the forward run
-  float4* vgrid = nullptr;
+  float4* vgrid = nullptr;      // grid velocities of the adjoint kernels
+  float4* step_vgrid = nullptr; // padded velocity grid of the forward substep kernels
+  VelocityGrid vel;
   float4* gadj = nullptr;
   float* adj = nullptr;
   double* pgrad = nullptr;
@@ -442,13 +444,13 @@ mpm_status dlaunch(mpm_diff* d, StepKind kind, float* state, const float4* gin, 
   a.grid_out = gout;
   a.grid_zero = nullptr;
   a.grid_cells = d->cells;
-  a.tile_cap = 256;
+  set_vgrid(a, d->vel);
   a.status = d->status;
   a.work = d->work + d->parity;
   a.work_next = d->work + (d->parity ^ 1);
   a.K = d->K;
   int chunk = 0, blocks = 0;
-  step_launch_shape(d->num_sms, d->n, false, false, kind, 2, 256, chunk, blocks);
+  step_launch_shape(d->num_sms, d->n, false, false, kind, 2, chunk, blocks);
   a.chunk = chunk;
   if (launch_step(a, kind, false, false, blocks, d->stream) != cudaSuccess) return MPM_ERR_CUDA;
   d->parity ^= 1;
@@ -499,9 +501,14 @@ mpm_status mpm_diff_create(const mpm_params* params, const mpm_material* materia
       cudaMalloc(&d->id, sizeof(uint32_t) * d->stride) || cudaMalloc(&d->work, 2 * sizeof(int)) ||
       cudaMalloc(&d->status, sizeof(int)) || cudaMemset(d->work, 0, 2 * sizeof(int)) ||
       cudaMemset(d->status, 0, sizeof(int)) || cudaMemset(d->ckpt, 0, sf * nck) || cudaMemset(d->seg, 0, sf) ||
-      cudaMemset(d->adj, 0, sf)) {
+      cudaMemset(d->adj, 0, sf) ||
+      cudaMalloc(&d->step_vgrid, sizeof(float4) * vgrid_nodes((int)params->N))) {
     mpm_diff_destroy(d);
     return MPM_ERR_NOMEM;
+  }
+  if (vgrid_bind(d->vel, d->step_vgrid, (int)params->N) != cudaSuccess) {
+    mpm_diff_destroy(d);
+    return MPM_ERR_CUDA;
   }
   if (launch_iota(d->id, n, d->stream) != cudaSuccess) {
     mpm_diff_destroy(d);
@@ -515,7 +522,7 @@ mpm_status mpm_diff_destroy(mpm_diff* d) {
   if (!d) return MPM_ERR_INVALID;
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (void* p : {(void*)d->ckpt, (void*)d->seg, (void*)d->seg_grid, (void*)d->grid3, (void*)d->vgrid,
-                  (void*)d->gadj, (void*)d->adj, (void*)d->pgrad, (void*)d->stage, (void*)d->id, (void*)d->work,
+                  (void*)d->step_vgrid, (void*)d->gadj, (void*)d->adj, (void*)d->pgrad, (void*)d->stage, (void*)d->id, (void*)d->work,
                   (void*)d->status})
     cudaFree(p);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -576,13 +583,13 @@ mpm_status mpm_diff_forward(mpm_diff* d, const float* x0, const float* v0, const
     a.grid_out = g[(cur + 1) % 3];
     a.grid_zero = g[(cur + 2) % 3];
     a.grid_cells = d->cells;
-    a.tile_cap = 256;
+    set_vgrid(a, d->vel);
     a.status = d->status;
     a.work = d->work + d->parity;
     a.work_next = d->work + (d->parity ^ 1);
     a.K = d->K;
     int chunk = 0, blocks = 0;
-    step_launch_shape(d->num_sms, n, false, false, kStepFused, 2, 256, chunk, blocks);
+    step_launch_shape(d->num_sms, n, false, false, kStepFused, 2, chunk, blocks);
     a.chunk = chunk;
     if (launch_step(a, kStepFused, false, false, blocks, s) != cudaSuccess) return MPM_ERR_CUDA;
     d->parity ^= 1;

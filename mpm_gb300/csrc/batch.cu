@@ -115,12 +115,11 @@ mpm_status launch(mpm_batch* b, StepKind kind) {
   a.work_next = b->work + (b->parity ^ 1);
   a.chunk = 32 * b->steps_per_warp;
   const int blocks = (kind == kStepP2GOnly) ? b->blocks_p2g : b->blocks_fused;
-  BCUDA(b, launch_step(a, kind, false, false, blocks, b->stream));
+  BCUDA(b, launch_step(a, kind, false, false, blocks, b->stream, &b->launches));
   b->parity ^= 1;
   b->cur = (r + 1) % 3;
   b->launch_index += 1;
   b->pending = true;
-  b->launches += 1;
   return MPM_OK;
 }
 
@@ -232,7 +231,7 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
   b->nranges = (int)ranges.size();
   for (int k = 0; k < 2; ++k) {
     const StepKind kind = k ? kStepFused : kStepP2GOnly;
-    const int bps = step_blocks_per_sm(kind, false, false, step_smem_bytes(kind, b->tile_cap), true);
+    const int bps = step_blocks_per_sm(kind, false, false, step_smem_bytes(kind, b->tile_cap, true), true);
     const int blocks = std::max(1, std::min((b->nranges + kStepWarps - 1) / kStepWarps, b->num_sms * bps));
     (k ? b->blocks_fused : b->blocks_p2g) = blocks;
   }

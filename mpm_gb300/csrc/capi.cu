@@ -39,8 +39,10 @@ struct mpm_ctx {
   uint32_t* keys = nullptr;
   bool have_mat = false;
 
-  // grid: three rotating buffers
+  // grid: three rotating P2G buffers and the padded velocity grid G2P reads
   float4* grid[3] = {nullptr, nullptr, nullptr};
+  float4* vgrid_mem = nullptr;
+  VelocityGrid vel;
   int64_t cells = 0;
   int64_t sort_keys = 0;  // key space of the bricked cell sort (>= cells)
   int cur = 0;            // slot holding the P2G grid of the next substep (when pending)
@@ -63,7 +65,6 @@ struct mpm_ctx {
   int64_t since_sort = 0;
   int64_t launches = 0;
   int steps_per_warp = 2;
-  int tile_cap = 256;  // nodes per warp tile
   std::string last_error;
 };
 
@@ -165,7 +166,7 @@ StepArgs make_step_args(mpm_ctx* c) {
   a.id = c->idA;
   a.n = c->n;
   a.grid_cells = c->cells;
-  a.tile_cap = c->tile_cap;
+  set_vgrid(a, c->vel);
   a.guard_limit = (int64_t)c->params.N * c->params.N * c->params.N;
   a.check_finite = c->params.check_finite;
   a.status = c->status;
@@ -174,8 +175,7 @@ StepArgs make_step_args(mpm_ctx* c) {
 }
 
 void launch_shape(mpm_ctx* c, StepKind kind, bool guard, int& chunk, int& blocks) {
-  mpm::step_launch_shape(c->num_sms, c->n, c->liquid_layout, guard, kind, c->steps_per_warp, c->tile_cap, chunk,
-                         blocks);
+  mpm::step_launch_shape(c->num_sms, c->n, c->liquid_layout, guard, kind, c->steps_per_warp, chunk, blocks);
 }
 
 mpm_status run_step(mpm_ctx* c, StepKind kind) {
@@ -191,8 +191,7 @@ mpm_status run_step(mpm_ctx* c, StepKind kind) {
   a.grid_in = (kind == kStepP2GOnly) ? nullptr : c->grid[r];
   a.grid_out = c->grid[(r + 1) % 3];
   a.grid_zero = c->grid[(r + 2) % 3];
-  MPM_CUDA(c, launch_step(a, kind, c->liquid_layout, guard, blocks, c->stream));
-  c->launches += 1;
+  MPM_CUDA(c, launch_step(a, kind, c->liquid_layout, guard, blocks, c->stream, &c->launches));
   if (kind == kStepFused) c->prev = r;
   c->cur = (r + 1) % 3;
   c->pending = true;
@@ -276,8 +275,8 @@ void make_dev_material(const mpm_material& m, DevMaterial& d) {
 // Ranges of steps_per_warp steps (32 particles each), fewer for small particle
 // counts so every resident warp gets work; the kernel deals them out dynamically.
 void step_launch_shape(int num_sms, int64_t n, bool liquid, bool guard, StepKind kind, int steps_per_warp,
-                       int tile_cap, int& chunk, int& blocks) {
-  const size_t smem = step_smem_bytes(kind, tile_cap);
+                       int& chunk, int& blocks) {
+  const size_t smem = step_smem_bytes(kind, 0, false);
   const int bps = step_blocks_per_sm(kind, liquid, guard, smem);
   const int64_t resident_warps = (int64_t)num_sms * bps * kStepWarps;
   int64_t steps = steps_per_warp;
@@ -316,6 +315,9 @@ mpm_status mpm_create(const mpm_params* params, mpm_ctx** out) {
     if (cudaMemsetAsync(c->grid[i], 0, sizeof(float4) * c->cells, c->stream) != cudaSuccess)
       return bail(MPM_ERR_CUDA);
   }
+  if (cudaMalloc(&c->vgrid_mem, sizeof(float4) * vgrid_nodes((int)params->N)) != cudaSuccess)
+    return bail(MPM_ERR_NOMEM);
+  if (vgrid_bind(c->vel, c->vgrid_mem, (int)params->N) != cudaSuccess) return bail(MPM_ERR_CUDA);
   const int per = kThreads * 8;
   const int64_t nbr = (params->N + 3) / 4;
   c->sort_keys = nbr * nbr * nbr * 64;
@@ -349,6 +351,7 @@ mpm_status mpm_destroy(mpm_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_particles(c);
   for (auto& g : c->grid) cudaFree(g);
+  cudaFree(c->vgrid_mem);
   cudaFree(c->counts);
   cudaFree(c->block_sums);
   cudaFree(c->comp_list);
@@ -611,13 +614,11 @@ mpm_status mpm_last_error(const mpm_ctx* c, char* buf, size_t len) {
   return MPM_OK;
 }
 
-mpm_status mpm_set_tuning(mpm_ctx* c, int32_t steps_per_warp, int32_t tile_nodes, int32_t reserved) {
+mpm_status mpm_set_tuning(mpm_ctx* c, int32_t steps_per_warp, int32_t reserved1, int32_t reserved2) {
   if (!c) return MPM_ERR_INVALID;
   if (steps_per_warp < 0 || steps_per_warp > 256) return fail(c, MPM_ERR_INVALID, "steps_per_warp out of range");
-  if (tile_nodes < 0 || tile_nodes > 288) return fail(c, MPM_ERR_INVALID, "tile_nodes out of range (max 288 per warp)");
-  if (reserved < 0) return fail(c, MPM_ERR_INVALID, "reserved must be >= 0");
+  if (reserved1 < 0 || reserved2 < 0) return fail(c, MPM_ERR_INVALID, "reserved arguments must be >= 0");
   if (steps_per_warp) c->steps_per_warp = steps_per_warp;
-  if (tile_nodes) c->tile_cap = tile_nodes;
   return MPM_OK;
 }
 

@@ -52,9 +52,8 @@ struct SimConsts {
 
 // Particle state, component-major SoA: component k of particle p at s[k * stride + p].
 // Components: x 0-2, v 3-5, C 6-14 (row-major), F 15-23 (row-major), Jp 24.
-// The liquid-only layout uses x, v, C and keeps J in component 15.
+// The liquid-only layout touches x, v, C and J (component 24) only: 16 components.
 enum Comp { kX = 0, kV = 3, kC = 6, kF = 15, kJp = 24, kNumComps = 25 };
-constexpr int kLiquidJ = 15;
 constexpr int kLiquidComps = 16;
 
 // ---------------------------------------------------------------------------

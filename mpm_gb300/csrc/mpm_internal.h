@@ -1,5 +1,6 @@
 // Internal host/device interface between the C ABI (capi.cu) and the kernels.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -44,16 +45,37 @@ struct StepArgs {
   const SceneDev* scenes;
   int* boxes;             // [scene][kBoxSlots][6]: lo xyz, hi xyz of P2G base cells
   int box_record, box_clear, box_reset;
+  // single-scene G2P: the padded velocity grid the launch's first kernel writes from
+  // grid_in, and its TMA tensor map
+  float4* vgrid;
+  CUtensorMap vmap;
   SimConsts K;
 };
 
+// Velocity grid of a single-scene substep: the grid operation applied to a P2G grid,
+// padded by 3 nodes below and 2 above in each dimension ((N + 5)^3 float4 nodes, zero
+// in the padding), so the G2P stencil of every particle that is not completely
+// outside the domain reads inside it; plus the TMA tensor map of its tiles.
+struct VelocityGrid {
+  CUtensorMap map;
+  float4* ptr = nullptr;
+  int N = 0;
+};
+int64_t vgrid_nodes(int N);
+// Describes caller-owned memory of vgrid_nodes(N) float4 (16-byte aligned) as a velocity grid.
+cudaError_t vgrid_bind(VelocityGrid& v, float4* ptr, int N);
+// Points a launch's arguments at a velocity grid.
+void set_vgrid(StepArgs& a, const VelocityGrid& v);
+
 enum StepKind { kStepP2GOnly = 0, kStepFused = 1, kStepG2POnly = 2 };
 
-// Launches one substep kernel variant. liquid = liquid-only layout.
+// Launches one substep (a.nscenes > 0: a batch). liquid = liquid-only layout.  A
+// single-scene launch with G2P is two kernels: the velocity pass (grid_in -> a.vgrid)
+// and the substep kernel.  *launches (may be null) counts the kernels.
 cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guard, int grid_blocks,
-                        cudaStream_t st);
-// Dynamic shared memory of a variant: velocity tile (G2P) + per-warp reduction buffers (P2G).
-size_t step_smem_bytes(StepKind kind, int tile_cap);
+                        cudaStream_t st, int64_t* launches = nullptr);
+// Dynamic shared memory of a variant: G2P tiles + per-warp P2G reduction buffers.
+size_t step_smem_bytes(StepKind kind, int tile_cap, bool batch);
 // Max resident CTAs per SM for the variant at the given dynamic shared memory.
 int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem, bool batch = false);
 
@@ -69,7 +91,7 @@ void make_dev_material(const mpm_material& m, DevMaterial& d);
 void make_sim_consts(const mpm_params& p, const mpm_material* mats, int n_materials, SimConsts& K);
 // Range size (chunk, particles) and grid size of a substep launch.
 void step_launch_shape(int num_sms, int64_t n, bool liquid, bool guard, StepKind kind, int steps_per_warp,
-                       int tile_cap, int& chunk, int& blocks);
+                       int& chunk, int& blocks);
 
 // Cell sort (counting sort by the linear index of the base cell).
 struct SortArgs {

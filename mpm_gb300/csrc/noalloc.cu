@@ -5,8 +5,8 @@
 // through its own pool, and embedded or real-time callers that forbid allocation after
 // start-up.  mpm_substep_noalloc serves them: the caller passes the particle state in
 // its own device memory, and the only scratch the substep needs (three rotating P2G
-// grids and two range counters) lives in the file-scope array below, which every GPU
-// that loads this library holds until the process exits.
+// grids, the padded velocity grid and two range counters) lives in the file-scope array
+// below, which every GPU that loads this library holds until the process exits.
 #include <mutex>
 
 #include "mpm_internal.h"
@@ -15,9 +15,12 @@ namespace {
 
 constexpr int kNoAllocMaxN = 32;  // largest grid the static scratch holds
 constexpr int64_t kNoAllocCells = (int64_t)kNoAllocMaxN * kNoAllocMaxN * kNoAllocMaxN;
-// three grids of kNoAllocCells float4 nodes, then one float4 of counters
-// (work[0], work[1], status, unused): 3 x 32768 x 16 B + 16 B = 1.5 MiB + 16 B
-constexpr int64_t kScratchFloat4 = 3 * kNoAllocCells + 1;
+// the velocity grid is padded to (N + 5)^3 nodes
+constexpr int64_t kNoAllocVelNodes = (int64_t)(kNoAllocMaxN + 5) * (kNoAllocMaxN + 5) * (kNoAllocMaxN + 5);
+// three grids of kNoAllocCells float4 nodes, the velocity grid, then one float4 of
+// counters (work[0], work[1], status, unused):
+// (3 x 32768 + 50653 + 1) x 16 B = 2.27 MiB
+constexpr int64_t kScratchFloat4 = 3 * kNoAllocCells + kNoAllocVelNodes + 1;
 
 static __device__ __align__(256) float4 g_noalloc_scratch[kScratchFloat4];
 
@@ -72,7 +75,9 @@ extern "C" mpm_status mpm_substep_noalloc(const mpm_params* params, const mpm_ma
 
   const int64_t cells = (int64_t)params->N * params->N * params->N;
   float4* grid[3] = {scratch, scratch + kNoAllocCells, scratch + 2 * kNoAllocCells};
-  int* counters = reinterpret_cast<int*>(scratch + 3 * kNoAllocCells);
+  VelocityGrid vel;
+  if (vgrid_bind(vel, scratch + 3 * kNoAllocCells, (int)params->N) != cudaSuccess) return MPM_ERR_CUDA;
+  int* counters = reinterpret_cast<int*>(scratch + 3 * kNoAllocCells + kNoAllocVelNodes);
   // the array keeps the previous call's contents: clear the first P2G target and the
   // counters (the other grids are cleared by the launches before they are written)
   if (cudaMemsetAsync(grid[1], 0, sizeof(float4) * cells, s) != cudaSuccess) return MPM_ERR_CUDA;
@@ -85,7 +90,7 @@ extern "C" mpm_status mpm_substep_noalloc(const mpm_params* params, const mpm_ma
   a.id = nullptr;
   a.n = n;
   a.grid_cells = cells;
-  a.tile_cap = 256;
+  set_vgrid(a, vel);
   a.guard_limit = 0;
   a.check_finite = 0;
   a.status = counters + 2;
@@ -96,7 +101,7 @@ extern "C" mpm_status mpm_substep_noalloc(const mpm_params* params, const mpm_ma
   for (int32_t i = -1; i < nsteps; ++i) {
     const StepKind kind = (i < 0) ? kStepP2GOnly : kStepFused;
     int chunk = 0, blocks = 0;
-    step_launch_shape(num_sms, n, liquid, false, kind, 2, a.tile_cap, chunk, blocks);
+    step_launch_shape(num_sms, n, liquid, false, kind, 2, chunk, blocks);
     a.chunk = chunk;
     a.grid_in = (kind == kStepP2GOnly) ? nullptr : grid[cur];
     a.grid_out = grid[(cur + 1) % 3];

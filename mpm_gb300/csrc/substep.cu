@@ -1,34 +1,47 @@
-// Fused MLS-MPM substep kernel for sm_103a.
+// Fused MLS-MPM substep kernels for sm_103a.
 //
 // The reference runs four launches per substep (src/mpm.cu:323-329): cudaMemset of
 // the grid, particleToGrid (27 x 4 float atomics per particle), gridOpKernel, and
-// gridToParticle.  Here one launch does
-//     G2P of substep n  (gather from the P2G grid of substep n; the grid op is applied
-//                        while a block stages its grid tile in shared memory)
-//   + constitutive update + advection, state written once
-//   + P2G of substep n+1 (scatter of the new state)
-//   + clearing of the grid buffer substep n-1 read,
-// so particle state is read once and written once per substep and the three grid
-// buffers rotate.  A P2G-only variant starts a run from uploaded state.
+// gridToParticle.  Here a substep is
+//   a velocity pass: the grid operation applied once per node of the P2G grid of
+//                    substep n, written to a zero-padded velocity grid, and
+//   one fused launch: G2P of substep n from the velocity grid
+//                     + constitutive update + advection, state written once
+//                     + P2G of substep n+1 (scatter of the new state)
+//                     + clearing of the grid buffer substep n-1 read,
+// so particle state is read once and written once per substep and the three P2G
+// grid buffers rotate.  A P2G-only variant starts a run from uploaded state.
 //
 // Work decomposition: warps are the scheduling unit.  Each warp of a 12-warp CTA
 // takes a range of cell-sorted particles (steps_per_warp x 32) and walks it 32
 // particles at a time (lane = particle, coalesced component-major loads/stores);
 // further ranges are claimed from a global counter, so faster warps take more.
-// G2P reads a per-warp shared-memory tile of grid velocities staged once for a
-// window of steps whose base cells fit the tile.  P2G is a warp transpose-reduce:
-// every lane writes its 27 node contributions as a column of a per-warp buffer, and
-// lane l < 27 sums node l over each run of same-cell lanes and issues one vector
-// atomic per run.  Dense scenes (100+ particles per cell) thus issue about one
-// global atomic per node and step instead of the reference's 108 per particle.
 //
-// Code size matters: the hot loop holds one copy each of the gather, the column
-// write and the run walk (the rare paths are out of line) so it stays resident in
-// the instruction cache.
+// G2P reads a per-step tile of the velocity grid in shared memory: a fixed box of
+// 4 x 4 x 6 nodes that one TMA copy (cp.async.bulk.tensor, completion on an mbarrier)
+// loads.  The copy for step k+1 is issued during step k, from positions loaded one
+// step ahead, into the other of two buffers, so its latency hides behind the
+// update and P2G of step k.  The box covers every step whose base cells span at most
+// 2 x 2 x 4 cells (one cell in dense scenes, or two neighbours in the bricked sort
+// order); other steps gather straight from the velocity grid.
+//
+// P2G is a warp transpose-reduce: every lane writes its 27 node contributions as a
+// column of a per-warp buffer, and lane l < 27 sums node l over each run of same-cell
+// lanes and issues one vector atomic per run.  Dense scenes (100+ particles per cell)
+// thus issue about one global atomic per node and step instead of the reference's 108
+// per particle.
+//
+// Batches of scenes (batch.cu) use batch_step_kernel below: per-range scene constants,
+// a shared-memory tile staged with the grid op applied, sparse grid clearing.
+#include <cudaTypedefs.h>
+
+#include <algorithm>
 #include <climits>
+#include <mutex>
 
 #include "mpm_internal.h"
-#include "warp_ops.cuh"
+#include "particle_ops.cuh"
+#include "tma.cuh"
 
 namespace mpm {
 
@@ -42,6 +55,258 @@ __device__ __forceinline__ void p2g_scatter_step(float4* wbuf, int lane, int key
   if (key >= 0) p2g_write_column(wbuf, lane, w, d, Aff, mv, m);
   warp_scatter_runs(wbuf, lane, key, grid, N);
 }
+
+// ===========================================================================
+// Single scene
+// ===========================================================================
+
+// Velocity grid padding (nodes below / above the grid in each dimension) and the TMA
+// tile box (x = slowest grid index i, z = fastest index k).
+constexpr int kPadLo = 3, kPadHi = 2;
+constexpr int kTileX = 4, kTileY = 4, kTileZ = 6;
+constexpr int kTileNodes = kTileX * kTileY * kTileZ;
+constexpr uint32_t kTileBytes = kTileNodes * sizeof(float4);
+enum TileState { kTileNone = 0, kTileSmem = 1, kTileGlobal = 2 };
+
+// gridOpKernel (src/mpm.cu:76-107) for every node, into the padded velocity grid;
+// padding nodes get zeros.
+__global__ void grid_velocity_kernel(const float4* __restrict__ grid, float4* __restrict__ vgrid, GridConsts K) {
+  const int N = K.N, P = N + kPadLo + kPadHi;
+  const int64_t PP = (int64_t)P * P, tot = PP * P;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+    const int pi = (int)(q / PP);
+    const int rem = (int)(q - (int64_t)pi * PP);
+    const int pj = rem / P;
+    const int i = pi - kPadLo, j = pj - kPadLo, k = rem - pj * P - kPadLo;
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N) {
+      const float3 v = grid_node_velocity(grid[((int64_t)i * N + j) * N + k], i, j, k, K);
+      out = make_float4(v.x, v.y, v.z, 0.f);
+    }
+    vgrid[q] = out;
+  }
+}
+
+// G2P gather straight from the velocity grid, for steps whose box exceeds the tile;
+// out of line to keep the hot loop small.
+static __device__ __noinline__ G2POut g2p_gather_vgrid(const float4* vgrid, GridConsts K, float x0, float x1,
+                                                       float x2) {
+  const float x[3] = {x0, x1, x2};
+  int b[3];
+  float w[3][3], d[3][3];
+  stencil(x, K, b, w, d);
+  const int P = K.N + kPadLo + kPadHi;
+  const float4* vb = vgrid + ((int64_t)(b[0] + kPadLo) * P + (b[1] + kPadLo)) * P + (b[2] + kPadLo);
+  auto node = [&](int a, int bb, int c) -> float4 { return __ldg(vb + ((int64_t)a * P + bb) * P + c); };
+  G2POut o;
+  g2p_gather(node, K, w, d, o.v, o.C);
+  return o;
+}
+
+// Positions, J and the G2P-guard state of one step's particle (lane).
+template <bool GUARD>
+__device__ __forceinline__ void load_step_head(const StepArgs& A, const float* s, int64_t st, int64_t p, bool valid,
+                                               float x[3], float& J, bool& frz) {
+  if (valid) {
+    x[0] = s[(kX + 0) * st + p];
+    x[1] = s[(kX + 1) * st + p];
+    x[2] = s[(kX + 2) * st + p];
+    J = s[kJp * st + p];
+    if (GUARD) frz = (int64_t)A.id[p] > A.guard_limit;
+  }
+}
+
+// Box of the base cells of a step's G2P particles (warp-collective).  When it fits the
+// tile, lane 0 starts the TMA copy of the tile into `tile`, completing on `bar`.
+__device__ __forceinline__ int plan_tile(const float x[3], bool active, const GridConsts& K, int lane,
+                                         const CUtensorMap* map, float4* tile, uint64_t* bar, int lo[3]) {
+  int b[3], hi[3];
+#pragma unroll
+  for (int dd = 0; dd < 3; ++dd) b[dd] = QuadraticInterpolationKernel::base_cell(x[dd], K.dx_inv);
+  active = active && !outside_domain(b[0], b[1], b[2], K.N);
+#pragma unroll
+  for (int dd = 0; dd < 3; ++dd) {
+    lo[dd] = __reduce_min_sync(kFull, active ? b[dd] : INT_MAX);
+    hi[dd] = __reduce_max_sync(kFull, active ? b[dd] : INT_MIN);
+  }
+  if (hi[0] < lo[0]) return kTileNone;
+  if (hi[0] - lo[0] > kTileX - 3 || hi[1] - lo[1] > kTileY - 3 || hi[2] - lo[2] > kTileZ - 3) return kTileGlobal;
+  if (lane == 0) {
+    // x coordinate in floats: 4 (lo + pad) is a multiple of 4 floats = 16 bytes
+    mbar_arrive_expect_tx(bar, kTileBytes);
+    tma_load_3d(tile, map, 4 * (lo[2] + kPadLo), lo[1] + kPadLo, lo[0] + kPadLo, bar);
+  }
+  return kTileSmem;
+}
+
+__device__ __forceinline__ float4* align_smem128(float4* p) {
+  const uint32_t a = smem_addr(p);
+  return reinterpret_cast<float4*>(reinterpret_cast<char*>(p) + ((128u - (a & 127u)) & 127u));
+}
+
+template <bool LIQ, bool G2P, bool P2G, bool GUARD>
+__global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __grid_constant__ StepArgs A) {
+  extern __shared__ float4 smem_dyn[];
+  float4* smem = align_smem128(smem_dyn);
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  // per-warp regions: two TMA tiles (G2P), the P2G transpose buffer, two mbarriers
+  float4* tiles = smem + warp * (2 * kTileNodes);
+  float4* wbuf = smem + (G2P ? kStepWarps * 2 * kTileNodes : 0) + warp * kRedFloat4;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (G2P ? kStepWarps * 2 * kTileNodes : 0) +
+                                               (P2G ? kStepWarps * kRedFloat4 : 0)) +
+                   2 * warp;
+  const GridConsts K = A.K.g;
+  const int N = K.N;
+  float* __restrict__ s = A.s;
+  const int64_t st = A.stride, n = A.n, chunk = A.chunk;
+
+  if (blockIdx.x == 0 && tid == 0) *A.work_next = 0;
+  if (G2P) {
+    if (lane == 0) {
+      mbar_init(bars, 1);
+      mbar_init(bars + 1, 1);
+      fence_barrier_init();
+    }
+    __syncwarp();
+  }
+  const int64_t nranges = (n + chunk - 1) / chunk;
+  const int64_t first_wave = (int64_t)gridDim.x * kStepWarps;
+  const int64_t r0 = (int64_t)blockIdx.x * kStepWarps + warp;
+  if (r0 < nranges) {
+    // Warp-uniform range bookkeeping: the current range ends at `re`; `rn` is the next
+    // range, claimed one range ahead so the step after a range's last is known early.
+    int claim = 0;
+    if (lane == 0) claim = atomicAdd(A.work, 1);
+    int64_t rn = first_wave + __shfl_sync(kFull, claim, 0);
+    if (lane == 0) claim = atomicAdd(A.work, 1);
+    int64_t pb = r0 * chunk;
+    int64_t re = min(pb + chunk, n);
+    float cx[3] = {0.f, 0.f, 0.f}, cJ = 1.f;
+    bool cfz = false;
+    load_step_head<GUARD>(A, s, st, pb + lane, pb + lane < re, cx, cJ, cfz);
+    int tstate = kTileNone, tlo[3] = {0, 0, 0}, buf = 0;
+    uint32_t parity = 0u;  // bit b: phase parity of bars[b]
+    if (G2P) tstate = plan_tile(cx, pb + lane < re && !cfz, K, lane, &A.vmap, tiles, bars, tlo);
+
+    while (true) {
+      const bool last = pb + 32 >= re;
+      const bool more = !last || rn < nranges;
+      const int64_t pn = last ? rn * chunk : pb + 32;
+      const int64_t pe = last ? min(pn + chunk, n) : re;
+      // the next step's positions, one step ahead
+      float nx[3] = {0.f, 0.f, 0.f}, nJ = 1.f;
+      bool nfz = false;
+      const bool nvalid = more && pn + lane < pe;
+      load_step_head<GUARD>(A, s, st, pn + lane, nvalid, nx, nJ, nfz);
+
+      const int64_t p = pb + lane;
+      const bool valid = p < re;
+      float x[3] = {cx[0], cx[1], cx[2]}, v[3] = {0.f, 0.f, 0.f}, Cm[3][3], F[3][3], Jp = cJ;
+      int mi = 0;
+      bool frozen = !G2P || cfz;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          Cm[i][j] = 0.f;
+          F[i][j] = (i == j) ? 1.f : 0.f;
+        }
+      if (valid) {
+        if (!LIQ) {
+#pragma unroll
+          for (int i = 0; i < 9; ++i) F[i / 3][i % 3] = s[(kF + i) * st + p];
+          if (A.mat) mi = A.mat[p];
+        }
+        if (frozen && P2G) {
+#pragma unroll
+          for (int dd = 0; dd < 3; ++dd) v[dd] = s[(kV + dd) * st + p];
+#pragma unroll
+          for (int i = 0; i < 9; ++i) Cm[i / 3][i % 3] = s[(kC + i) * st + p];
+        }
+      }
+      const DevMaterial& M = A.K.mat[mi];
+      bool have_uv = false;
+      float Usv[3][3], Vsv[3][3];
+      bool g2p_on = false;
+      // ---- G2P (gridToParticle, src/mpm.cu:109-167)
+      if (G2P) {
+        int b[3] = {0, 0, 0};
+        float w[3][3], d[3][3];
+        if (valid && !frozen) {
+          stencil(x, K, b, w, d);
+          g2p_on = !outside_domain(b[0], b[1], b[2], N);
+          if (!g2p_on) frozen = true;  // completely outside: unchanged; P2G skips it too
+        }
+        if (tstate == kTileSmem) {
+          if (!mbar_wait(bars + buf, (parity >> buf) & 1u) && lane == 0) atomicOr(A.status, kStatusTimeout);
+          parity ^= 1u << buf;
+          if (g2p_on) {
+            const float4* t = tiles + buf * kTileNodes +
+                              ((b[0] - tlo[0]) * kTileY + (b[1] - tlo[1])) * kTileZ + (b[2] - tlo[2]);
+            auto node = [&](int a, int bb, int c) -> float4 { return t[(a * kTileY + bb) * kTileZ + c]; };
+            g2p_gather(node, K, w, d, v, Cm);
+          }
+        } else if (tstate == kTileGlobal && g2p_on) {
+          const G2POut o = g2p_gather_vgrid(A.vgrid, K, x[0], x[1], x[2]);
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            v[r] = o.v[r];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) Cm[r][c] = o.C[r][c];
+          }
+        }
+        // The next step's tile goes to the other buffer, whose last reader was the
+        // previous step (every lane has passed that step's P2G warp syncs).
+        if (more)
+          tstate = plan_tile(nx, nvalid && !nfz, K, lane, &A.vmap, tiles + (buf ^ 1) * kTileNodes, bars + (buf ^ 1),
+                             tlo);
+      }
+      if (g2p_on) {
+        particle_update<LIQ>(M, K, x, v, Cm, F, Jp, have_uv, Usv, Vsv);
+        store_particle<LIQ>(s, st, p, x, v, Cm, F, Jp);
+        if (A.check_finite && !isfinite(x[0] + x[1] + x[2] + v[0] + v[1] + v[2])) atomicOr(A.status, kStatusNonFinite);
+      }
+      // ---- P2G of the next substep (particleToGrid)
+      if (P2G) {
+        int key = -1;
+        float w[3][3], d[3][3], Aff[3][3], mv[3], m = 0.f;
+        if (valid) {
+          int b[3];
+          stencil(x, K, b, w, d);
+          if (!outside_domain(b[0], b[1], b[2], N)) {
+            key = pack_key(b[0], b[1], b[2]);
+            p2g_prepare<LIQ>(M, K, F, Jp, Cm, v, have_uv, Usv, Vsv, Aff, mv, m);
+          }
+        }
+        p2g_scatter_step(wbuf, lane, key, w, d, Aff, mv, m, A.grid_out, N);
+      }
+      if (!more) break;
+      if (last) {
+        re = pe;
+        rn = first_wave + __shfl_sync(kFull, claim, 0);
+        if (lane == 0) claim = atomicAdd(A.work, 1);
+      }
+      pb = pn;
+#pragma unroll
+      for (int dd = 0; dd < 3; ++dd) cx[dd] = nx[dd];
+      cJ = nJ;
+      cfz = nfz;
+      buf ^= 1;
+    }
+  }
+
+  // ---- clear the grid buffer the previous substep read (used by the launch after next)
+  if (A.grid_zero) {
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t i = (int64_t)blockIdx.x * kStepThreads + tid; i < A.grid_cells; i += (int64_t)gridDim.x * kStepThreads)
+      A.grid_zero[i] = z;
+  }
+}
+
+// ===========================================================================
+// Batch of scenes
+// ===========================================================================
 
 // Per-warp grid tile: the nodes [lo, hi + 2]^3 around a box of base cells, with the
 // grid op applied (grid velocity), zero outside the grid.  lo/hi are warp-uniform.
@@ -85,76 +350,60 @@ __device__ __forceinline__ void warp_tile_build(float4* wtile, int lane, const i
   __syncwarp();
 }
 
-template <bool LIQ, bool G2P, bool P2G, bool GUARD, bool BATCH>
-__global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_constant__ StepArgs A) {
+// Batched substep: ranges of the range table never cross a scene, so a warp loads its
+// scene's constants once per range.  The G2P tile of a window of steps is staged with
+// the grid op applied; each scene's P2G box is recorded so the grid it accumulated is
+// cleared sparsely two launches later.
+template <bool G2P, bool P2G>
+__global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __grid_constant__ StepArgs A) {
   extern __shared__ float4 smem[];
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
-  // per-warp regions: velocity tile (G2P), P2G transpose buffer
   float4* wtile = smem + warp * A.tile_cap;
   float4* wbuf = smem + (G2P ? kStepWarps * A.tile_cap : 0) + warp * kRedFloat4;
-  GridConsts K = A.K.g;
-  int N = K.N;
-  const float4* gin = A.grid_in;
-  float4* gout = A.grid_out;
   float* __restrict__ s = A.s;
   const int64_t st = A.stride;
 
-  // Warps are the scheduling unit: each resident warp starts on one range of A.chunk
-  // consecutive (cell-sorted) particles and claims further ranges from a global
-  // counter while finishing the last step of its current one, so warps that run
-  // faster take more ranges; no CTA barriers.
   if (blockIdx.x == 0 && tid == 0) *A.work_next = 0;
-  if (BATCH) {
-    // clear, per scene, the grid region the launch two substeps back accumulated (the
-    // buffer this launch leaves for the next one to fill), then free its box slot
-    for (int sc = blockIdx.x; sc < A.nscenes; sc += gridDim.x) {
-      const int* bx = A.boxes + ((int64_t)sc * kBoxSlots + A.box_clear) * 6;
-      const SceneDev& sd = A.scenes[sc];
-      const int Ns = sd.g.N;
-      const int l0 = max(bx[0], 0), l1 = max(bx[1], 0), l2 = max(bx[2], 0);
-      const int h0 = min(bx[3] + 2, Ns - 1), h1 = min(bx[4] + 2, Ns - 1), h2 = min(bx[5] + 2, Ns - 1);
-      if (h0 >= l0 && h1 >= l1 && h2 >= l2 && A.grid_zero) {
-        const int e1 = h1 - l1 + 1, e2 = h2 - l2 + 1;
-        const int64_t vol = (int64_t)(h0 - l0 + 1) * e1 * e2;
-        float4* gz = A.grid_zero + sd.grid_offset;
-        for (int64_t q = tid; q < vol; q += kStepThreads) {
-          const int i = l0 + (int)(q / ((int64_t)e1 * e2));
-          const int rem = (int)(q % ((int64_t)e1 * e2));
-          gz[((int64_t)i * Ns + (l1 + rem / e2)) * Ns + (l2 + rem % e2)] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
+  // clear, per scene, the grid region the launch two substeps back accumulated (the
+  // buffer this launch leaves for the next one to fill), then free its box slot
+  for (int sc = blockIdx.x; sc < A.nscenes; sc += gridDim.x) {
+    const int* bx = A.boxes + ((int64_t)sc * kBoxSlots + A.box_clear) * 6;
+    const SceneDev& sd = A.scenes[sc];
+    const int Ns = sd.g.N;
+    const int l0 = max(bx[0], 0), l1 = max(bx[1], 0), l2 = max(bx[2], 0);
+    const int h0 = min(bx[3] + 2, Ns - 1), h1 = min(bx[4] + 2, Ns - 1), h2 = min(bx[5] + 2, Ns - 1);
+    if (h0 >= l0 && h1 >= l1 && h2 >= l2 && A.grid_zero) {
+      const int e1 = h1 - l1 + 1, e2 = h2 - l2 + 1;
+      const int64_t vol = (int64_t)(h0 - l0 + 1) * e1 * e2;
+      float4* gz = A.grid_zero + sd.grid_offset;
+      for (int64_t q = tid; q < vol; q += kStepThreads) {
+        const int i = l0 + (int)(q / ((int64_t)e1 * e2));
+        const int rem = (int)(q % ((int64_t)e1 * e2));
+        gz[((int64_t)i * Ns + (l1 + rem / e2)) * Ns + (l2 + rem % e2)] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      if (tid < 6) A.boxes[((int64_t)sc * kBoxSlots + A.box_reset) * 6 + tid] = (tid < 3) ? INT_MAX : INT_MIN;
     }
+    if (tid < 6) A.boxes[((int64_t)sc * kBoxSlots + A.box_reset) * 6 + tid] = (tid < 3) ? INT_MAX : INT_MIN;
   }
-  const int64_t nranges = BATCH ? A.nranges : (A.n + A.chunk - 1) / A.chunk;
+  const int64_t nranges = A.nranges;
   const int64_t first_wave = (int64_t)gridDim.x * kStepWarps;
   int64_t r = (int64_t)blockIdx.x * kStepWarps + warp;
   while (r < nranges) {
     int claim = 0;
-    int64_t wbeg, wend;
-    int scene = 0;
-    if (BATCH) {
-      const int4 rg = A.ranges[r];
-      scene = rg.x;
-      wbeg = rg.y;
-      wend = rg.z;
-      const SceneDev& sd = A.scenes[scene];
-      K = sd.g;
-      N = K.N;
-      gin = A.grid_in ? A.grid_in + sd.grid_offset : nullptr;
-      gout = A.grid_out + sd.grid_offset;
-    } else {
-      wbeg = r * A.chunk;
-      wend = min(wbeg + (int64_t)A.chunk, A.n);
-    }
-    int plo[3] = {INT_MAX, INT_MAX, INT_MAX}, phi[3] = {INT_MIN, INT_MIN, INT_MIN};  // P2G box (batch)
+    const int4 rg = A.ranges[r];
+    const int scene = rg.x;
+    const int64_t wbeg = rg.y, wend = rg.z;
+    const SceneDev& sd = A.scenes[scene];
+    const GridConsts K = sd.g;
+    const int N = K.N;
+    const DevMaterial& M = sd.m;
+    const float4* gin = A.grid_in ? A.grid_in + sd.grid_offset : nullptr;
+    float4* gout = A.grid_out + sd.grid_offset;
+    int plo[3] = {INT_MAX, INT_MAX, INT_MAX}, phi[3] = {INT_MIN, INT_MIN, INT_MIN};
     TileBox tb{0, 0, 0, 1, 1};
-    int64_t win_end = wbeg;  // end of the steps the current tile covers
+    int64_t win_end = wbeg;
     bool tile_ok = false;
 
-    // ---- walk the range, one particle per lane; positions and Jp of the next step
-    // are loaded one step ahead
     float nx0 = 0.f, nx1 = 0.f, nx2 = 0.f, nJ = 1.f;
     if (wbeg + lane < wend) {
       nx0 = s[(kX + 0) * st + wbeg + lane];
@@ -171,7 +420,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
         while (we < wend) {
           const int64_t q = we + lane;
           int slo[3] = {INT_MAX, INT_MAX, INT_MAX}, shi[3] = {INT_MIN, INT_MIN, INT_MIN};
-          if (q < wend && !(GUARD && (int64_t)A.id[q] > A.guard_limit)) {
+          if (q < wend) {
             int bb[3];
 #pragma unroll
             for (int dd = 0; dd < 3; ++dd)
@@ -209,7 +458,6 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
         nx2 = s[(kX + 2) * st + p + 32];
         nJ = s[kJp * st + p + 32];
       }
-      int mi = 0;
       bool frozen = !G2P;
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -219,12 +467,8 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
           F[i][j] = (i == j) ? 1.f : 0.f;
         }
       if (valid) {
-        if (!LIQ) {
 #pragma unroll
-          for (int i = 0; i < 9; ++i) F[i / 3][i % 3] = s[(kF + i) * st + p];
-          if (A.mat) mi = A.mat[p];
-        }
-        if (GUARD && (int64_t)A.id[p] > A.guard_limit) frozen = true;
+        for (int i = 0; i < 9; ++i) F[i / 3][i % 3] = s[(kF + i) * st + p];
         if (frozen && P2G) {
 #pragma unroll
           for (int dd = 0; dd < 3; ++dd) v[dd] = s[(kV + dd) * st + p];
@@ -232,8 +476,6 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
           for (int i = 0; i < 9; ++i) Cm[i / 3][i % 3] = s[(kC + i) * st + p];
         }
       }
-      const DevMaterial& M = BATCH ? A.scenes[scene].m : A.K.mat[mi];
-      // ---- G2P + constitutive update + advection (gridToParticle)
       bool have_uv = false;
       float Usv[3][3], Vsv[3][3];
       bool g2p_on = false;
@@ -243,94 +485,27 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
         stencil(x, K, b, w, d);
         g2p_on = !outside_domain(b[0], b[1], b[2], N);
         if (!g2p_on) {
-          frozen = true;  // completely outside: unchanged; P2G skips it too
+          frozen = true;
         } else if (tile_ok) {
           const int t0 = ((b[0] - tb.t0) * tb.d1 + (b[1] - tb.t1)) * tb.d2 + (b[2] - tb.t2);
           const int d12 = tb.d1 * tb.d2;
           auto node = [&](int a, int bb, int c) -> float4 { return wtile[t0 + a * d12 + bb * tb.d2 + c]; };
           g2p_gather(node, K, w, d, v, Cm);
         } else {
-          // a step whose own box exceeds the tile (rare: a jump between brick rows)
           const G2POut o = g2p_gather_global(gin, K, x[0], x[1], x[2]);
 #pragma unroll
-          for (int r = 0; r < 3; ++r) {
-            v[r] = o.v[r];
+          for (int r2 = 0; r2 < 3; ++r2) {
+            v[r2] = o.v[r2];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) Cm[r][c] = o.C[r][c];
+            for (int c = 0; c < 3; ++c) Cm[r2][c] = o.C[r2][c];
           }
         }
       }
       if (g2p_on) {
-        {
-          if (LIQ || M.kind == kLiquid) {
-            // J <- J det(I + dt C), F = J^(1/3) I
-            float G[3][3];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-              for (int j = 0; j < 3; ++j) G[i][j] = (i == j ? 1.f : 0.f) + K.dt * Cm[i][j];
-            Jp = Jp * det3(G);
-            if (!LIQ) {
-              const float cr = cbrtf(Jp);
-#pragma unroll
-              for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) F[i][j] = (i == j) ? cr : 0.f;
-            }
-          } else {
-            // g2p_finish_particle: F <- (I + dt C) F   (include/TransferScheme.h:134-142)
-            float Fn[3][3];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-              for (int j = 0; j < 3; ++j)
-                Fn[i][j] = F[i][j] + K.dt * (Cm[i][0] * F[0][j] + Cm[i][1] * F[1][j] + Cm[i][2] * F[2][j]);
-            if (M.kind == kSnow) {
-              // MMSnow::endOfStepMutation (include/MaterialModel.cuh:95-115)
-              float sg[3];
-              svd3(Fn, Usv, sg, Vsv);
-#pragma unroll
-              for (int i = 0; i < 3; ++i) sg[i] = clampf(sg[i], M.clamp_lo, M.clamp_hi);
-              const float oldJ = det3(Fn);
-#pragma unroll
-              for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j)
-                  Fn[i][j] = Usv[i][0] * sg[0] * Vsv[j][0] + Usv[i][1] * sg[1] * Vsv[j][1] + Usv[i][2] * sg[2] * Vsv[j][2];
-              const float Fdet = det3(Fn);
-              Jp = clampf(Jp * oldJ / Fdet, 0.6f, 20.0f);
-              have_uv = true;
-            } else if (M.kind == kJelly) {
-              // MMJelly::endOfStepMutation (include/MaterialModel.cuh:142-148)
-              const float oldJ = det3_colwise(Fn);
-              Jp = clampf(Jp * oldJ / det3_colwise(Fn), 0.6f, 20.0f);
-            }
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-              for (int j = 0; j < 3; ++j) F[i][j] = Fn[i][j];
-          }
-#pragma unroll
-          for (int dd = 0; dd < 3; ++dd) x[dd] = x[dd] + K.dt * v[dd];
-          // ---- write back (particles[pi] = particle, src/mpm.cu:177)
-#pragma unroll
-          for (int dd = 0; dd < 3; ++dd) {
-            s[(kX + dd) * st + p] = x[dd];
-            s[(kV + dd) * st + p] = v[dd];
-          }
-#pragma unroll
-          for (int i = 0; i < 9; ++i) s[(kC + i) * st + p] = Cm[i / 3][i % 3];
-          if (!LIQ) {
-#pragma unroll
-            for (int i = 0; i < 9; ++i) s[(kF + i) * st + p] = F[i / 3][i % 3];
-          }
-          s[kJp * st + p] = Jp;
-          if (A.check_finite && !isfinite(x[0] + x[1] + x[2] + v[0] + v[1] + v[2]))
-            atomicOr(A.status, kStatusNonFinite);
-        }
+        particle_update<false>(M, K, x, v, Cm, F, Jp, have_uv, Usv, Vsv);
+        store_particle<false>(s, st, p, x, v, Cm, F, Jp);
+        if (A.check_finite && !isfinite(x[0] + x[1] + x[2] + v[0] + v[1] + v[2])) atomicOr(A.status, kStatusNonFinite);
       }
-
-      // ---- P2G of the next substep (particleToGrid)
       if (P2G) {
         int key = -1;
         float w[3][3], d[3][3], Aff[3][3], mv[3], m = 0.f;
@@ -339,50 +514,18 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
           stencil(x, K, b, w, d);
           if (!outside_domain(b[0], b[1], b[2], N)) {
             key = pack_key(b[0], b[1], b[2]);
-            if (BATCH) {
 #pragma unroll
-              for (int dd = 0; dd < 3; ++dd) {
-                plo[dd] = min(plo[dd], b[dd]);
-                phi[dd] = max(phi[dd], b[dd]);
-              }
+            for (int dd = 0; dd < 3; ++dd) {
+              plo[dd] = min(plo[dd], b[dd]);
+              phi[dd] = max(phi[dd], b[dd]);
             }
-            m = M.mass;
-            float PF[3][3];
-            if (LIQ || M.kind == kLiquid) {
-              const float pr = M.bulk * (Jp - 1.f) * Jp;
-#pragma unroll
-              for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) PF[i][j] = (i == j) ? pr : 0.f;
-            } else {
-              float R[3][3];
-              if (have_uv) {
-                // F = U clamp(Sigma) V^T with clamp(Sigma) >= 0, so its polar rotation is U V^T
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                  for (int j = 0; j < 3; ++j)
-                    R[i][j] = Usv[i][0] * Vsv[j][0] + Usv[i][1] * Vsv[j][1] + Usv[i][2] * Vsv[j][2];
-              } else {
-                float Sdummy[3][3];
-                polar_decomposition(F, R, Sdummy);
-              }
-              compute_PF(M, F, R, Jp, PF);
-            }
-            // p2g_prepare_particle: affine = -D dt vol PF + m C (include/TransferScheme.h:78-85)
-            const float sc = ((-K.dinv) * K.dt) * M.vol;
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-              for (int j = 0; j < 3; ++j) Aff[i][j] = fmaf(sc, PF[i][j], m * Cm[i][j]);
-#pragma unroll
-            for (int dd = 0; dd < 3; ++dd) mv[dd] = v[dd] * m;
+            p2g_prepare<false>(M, K, F, Jp, Cm, v, have_uv, Usv, Vsv, Aff, mv, m);
           }
         }
         p2g_scatter_step(wbuf, lane, key, w, d, Aff, mv, m, gout, N);
       }
     }
-    if (BATCH && P2G) {
+    if (P2G) {
       // record the range's P2G box in its scene's slot (cleared two launches later)
       int* bx = A.boxes + ((int64_t)scene * kBoxSlots + A.box_record) * 6;
 #pragma unroll
@@ -397,31 +540,73 @@ __global__ void __launch_bounds__(kStepThreads, 1) step_kernel(const __grid_cons
     }
     r = first_wave + __shfl_sync(kFull, claim, 0);
   }
-
-  // ---- clear the grid buffer the previous substep read (used by the launch after next)
-  if (!BATCH && A.grid_zero) {
-    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int64_t i = (int64_t)blockIdx.x * kStepThreads + tid; i < A.grid_cells;
-         i += (int64_t)gridDim.x * kStepThreads)
-      A.grid_zero[i] = z;
-  }
 }
 
-template <bool LIQ, bool G2P, bool P2G, bool GUARD, bool BATCH>
-static void* kernel_ptr() {
-  return (void*)step_kernel<LIQ, G2P, P2G, GUARD, BATCH>;
+// ===========================================================================
+// Host side
+// ===========================================================================
+
+int64_t vgrid_nodes(int N) {
+  const int64_t P = (int64_t)N + kPadLo + kPadHi;
+  return P * P * P;
+}
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+}  // namespace
+
+cudaError_t vgrid_bind(VelocityGrid& v, float4* ptr, int N) {
+  if (!ptr || N < 1 || (reinterpret_cast<uintptr_t>(ptr) & 15u)) return cudaErrorInvalidValue;
+  PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  if (!encode) return cudaErrorNotSupported;
+  // the grid as float32 [P][P][4 P]: one node is 4 consecutive floats
+  const cuuint64_t P = (cuuint64_t)N + kPadLo + kPadHi;
+  const cuuint64_t dims[3] = {4 * P, P, P};
+  const cuuint64_t strides[2] = {16 * P, 16 * P * P};  // bytes, dimensions 1 and 2
+  const cuuint32_t box[3] = {4 * kTileZ, kTileY, kTileX};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = encode(&v.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, ptr, dims, strides, box, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+  v.ptr = ptr;
+  v.N = N;
+  return cudaSuccess;
+}
+
+void set_vgrid(StepArgs& a, const VelocityGrid& v) {
+  a.vgrid = v.ptr;
+  a.vmap = v.map;
+}
+
+template <bool LIQ, bool G2P, bool P2G, bool GUARD>
+static void* scene_kernel() {
+  return (void*)scene_step_kernel<LIQ, G2P, P2G, GUARD>;
 }
 
 static void* select_kernel(StepKind kind, bool liquid, bool guard, bool batch) {
   if (batch) {  // batches use the general layout, no guard
-    if (kind == kStepP2GOnly) return kernel_ptr<false, false, true, false, true>();
-    return kernel_ptr<false, true, true, false, true>();
+    if (kind == kStepP2GOnly) return (void*)batch_step_kernel<false, true>;
+    return (void*)batch_step_kernel<true, true>;
   }
-#define MPM_SEL(L, G)                                                        \
-  if (liquid == L && guard == G) {                                           \
-    if (kind == kStepP2GOnly) return kernel_ptr<L, false, true, G, false>(); \
-    if (kind == kStepFused) return kernel_ptr<L, true, true, G, false>();    \
-    return kernel_ptr<L, true, false, G, false>();                           \
+#define MPM_SEL(L, G)                                                    \
+  if (liquid == L && guard == G) {                                       \
+    if (kind == kStepP2GOnly) return scene_kernel<L, false, true, G>();  \
+    if (kind == kStepFused) return scene_kernel<L, true, true, G>();     \
+    return scene_kernel<L, true, false, G>();                            \
   }
   MPM_SEL(true, false)
   MPM_SEL(true, true)
@@ -431,21 +616,37 @@ static void* select_kernel(StepKind kind, bool liquid, bool guard, bool batch) {
   return nullptr;
 }
 
-size_t step_smem_bytes(StepKind kind, int tile_cap) {
+size_t step_smem_bytes(StepKind kind, int tile_cap, bool batch) {
   size_t b = 0;
-  if (kind != kStepP2GOnly) b += (size_t)kStepWarps * tile_cap * sizeof(float4);
+  if (batch) {
+    if (kind != kStepP2GOnly) b += (size_t)kStepWarps * tile_cap * sizeof(float4);
+    if (kind != kStepG2POnly) b += (size_t)kStepWarps * kRedFloat4 * sizeof(float4);
+    return b;
+  }
+  if (kind != kStepP2GOnly) b += (size_t)kStepWarps * 2 * (kTileBytes + sizeof(uint64_t));
   if (kind != kStepG2POnly) b += (size_t)kStepWarps * kRedFloat4 * sizeof(float4);
-  return b;
+  return b + 128;  // alignment of the TMA tiles
 }
 
-cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guard, int grid_blocks, cudaStream_t st) {
-  void* fn = select_kernel(kind, liquid, guard, a.nscenes > 0);
-  const size_t smem = step_smem_bytes(kind, a.tile_cap);
+cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guard, int grid_blocks, cudaStream_t st,
+                        int64_t* launches) {
+  const bool batch = a.nscenes > 0;
+  void* fn = select_kernel(kind, liquid, guard, batch);
+  const size_t smem = step_smem_bytes(kind, a.tile_cap, batch);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  if (!batch && kind != kStepP2GOnly) {
+    if (!a.vgrid || !a.grid_in) return cudaErrorInvalidValue;
+    const int64_t tot = vgrid_nodes(a.K.g.N);
+    const int vb = (int)std::min<int64_t>((tot + kThreads - 1) / kThreads, 4096);
+    grid_velocity_kernel<<<vb, kThreads, 0, st>>>(a.grid_in, a.vgrid, a.K.g);
+    if (launches) *launches += 1;
+  }
   StepArgs copy = a;
   void* args[] = {&copy};
-  return cudaLaunchKernel(fn, dim3(grid_blocks), dim3(kStepThreads), args, smem, st);
+  e = cudaLaunchKernel(fn, dim3(grid_blocks), dim3(kStepThreads), args, smem, st);
+  if (launches) *launches += 1;
+  return e;
 }
 
 int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem, bool batch) {

@@ -78,10 +78,9 @@ class Simulation:
         """Enqueue all further work on the cudaStream_t `handle` (an int; 0 = the context's own)."""
         _lib.check(self.L.mpm_set_stream(self.ctx, ctypes.c_void_p(int(handle)) if handle else None), self.ctx)
 
-    def set_tuning(self, steps_per_warp=0, tile_nodes=0):
-        """Fused-kernel knobs (0 keeps the current value): 32-particle steps per claimed
-        range, and the per-warp grid tile capacity in nodes (at most 288)."""
-        _lib.check(self.L.mpm_set_tuning(self.ctx, int(steps_per_warp), int(tile_nodes), 0), self.ctx)
+    def set_tuning(self, steps_per_warp=0):
+        """Fused-kernel knob: 32-particle steps per range a warp claims (0 keeps the current value)."""
+        _lib.check(self.L.mpm_set_tuning(self.ctx, int(steps_per_warp), 0, 0), self.ctx)
 
     def upload(self, state: dict):
         """particlesToDevice (src/mpm.cu:278-286): x, v, C, F, Jp, mat host arrays."""
