@@ -70,7 +70,11 @@ enum TileState { kTileNone = 0, kTileSmem = 1, kTileGlobal = 2 };
 
 // gridOpKernel (src/mpm.cu:76-107) for every node, into the padded velocity grid;
 // padding nodes get zeros.
+// The substep kernel is launched as its programmatic dependent: it may start (claim
+// ranges, load its first positions) while this pass runs, and waits for the pass
+// with griddepcontrol.wait before it reads the velocity grid.
 __global__ void grid_velocity_kernel(const float4* __restrict__ grid, float4* __restrict__ vgrid, GridConsts K) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   const int N = K.N, P = N + kPadLo + kPadHi;
   const int64_t PP = (int64_t)P * P, tot = PP * P;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
@@ -103,15 +107,24 @@ static __device__ __noinline__ G2POut g2p_gather_vgrid(const float4* vgrid, Grid
   return o;
 }
 
+// A load kept where it is written (volatile asm is not moved past the other volatile
+// asm of the step, such as the mbarrier wait), so the next step's positions are
+// requested at the top of the step and arrive while this step computes.
+__device__ __forceinline__ float ld_pin(const float* p) {
+  float v;
+  asm volatile("ld.global.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+
 // Positions, J and the G2P-guard state of one step's particle (lane).
 template <bool GUARD>
 __device__ __forceinline__ void load_step_head(const StepArgs& A, const float* s, int64_t st, int64_t p, bool valid,
                                                float x[3], float& J, bool& frz) {
   if (valid) {
-    x[0] = s[(kX + 0) * st + p];
-    x[1] = s[(kX + 1) * st + p];
-    x[2] = s[(kX + 2) * st + p];
-    J = s[kJp * st + p];
+    x[0] = ld_pin(s + (kX + 0) * st + p);
+    x[1] = ld_pin(s + (kX + 1) * st + p);
+    x[2] = ld_pin(s + (kX + 2) * st + p);
+    J = ld_pin(s + kJp * st + p);
     if (GUARD) frz = (int64_t)A.id[p] > A.guard_limit;
   }
 }
@@ -187,6 +200,8 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
     load_step_head<GUARD>(A, s, st, pb + lane, pb + lane < re, cx, cJ, cfz);
     int tstate = kTileNone, tlo[3] = {0, 0, 0}, buf = 0;
     uint32_t parity = 0u;  // bit b: phase parity of bars[b]
+    // the velocity pass (this launch's programmatic prerequisite) has completed past here
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     if (G2P) tstate = plan_tile(cx, pb + lane < re && !cfz, K, lane, &A.vmap, tiles, bars, tlo);
 
     while (true) {
@@ -644,7 +659,18 @@ cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guar
   }
   StepArgs copy = a;
   void* args[] = {&copy};
-  e = cudaLaunchKernel(fn, dim3(grid_blocks), dim3(kStepThreads), args, smem, st);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid_blocks);
+  cfg.blockDim = dim3(kStepThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  // programmatic dependent launch after the velocity pass (see grid_velocity_kernel)
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = (!batch && kind != kStepP2GOnly) ? 1 : 0;
+  e = cudaLaunchKernelExC(&cfg, fn, args);
   if (launches) *launches += 1;
   return e;
 }

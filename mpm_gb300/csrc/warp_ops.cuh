@@ -78,15 +78,20 @@ __device__ __forceinline__ void warp_scatter_runs(float4* wbuf, int lane, int ke
     const int j1 = rs ? __ffs(rs) - 1 : 32;
     const int run_key = __shfl_sync(kFull, key, j0);
     if (run_key >= 0 && lane < 27) {
-      float4 s0 = make_float4(0.f, 0.f, 0.f, 0.f), s1 = s0;
+      float4 s0 = make_float4(0.f, 0.f, 0.f, 0.f), s1 = s0, s2 = s0, s3 = s0;
       int j = j0;
 #pragma unroll 1
-      for (; j + 1 < j1; j += 2) {
+      for (; j + 3 < j1; j += 4) {
         f4add(s0, row[j]);
         f4add(s1, row[j + 1]);
+        f4add(s2, row[j + 2]);
+        f4add(s3, row[j + 3]);
       }
-      if (j < j1) f4add(s0, row[j]);
+#pragma unroll 1
+      for (; j < j1; ++j) f4add(s0, row[j]);
       f4add(s0, s1);
+      f4add(s2, s3);
+      f4add(s0, s2);
       int b0, b1, b2;
       unpack_key(run_key, b0, b1, b2);
       add_node(grid, N, b0 + lane / 9, b1 + (lane / 3) % 3, b2 + lane % 3, s0);
