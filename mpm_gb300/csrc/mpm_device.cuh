@@ -79,6 +79,19 @@ struct QuadraticInterpolationKernel {
     w[1] = 0.75f - b * b;
     w[2] = 0.5f * (c * c);
   }
+  // The same weights plus f = x / dx - range_begin, the particle's offset from its base
+  // node in cells (in [0.5, 1.5)); node a of the stencil is at dpos = (a - f) dx.
+  __device__ __forceinline__ static void weights_and_offset(float x, float dx_inv, int& range_begin, float w[3],
+                                                            float& f) {
+    const float xg = grid_coord(x, dx_inv);
+    range_begin = (int)__fsub_rn(xg, 0.5f);
+    const float fx = xg - (float)range_begin;
+    const float a = 1.5f - fx, b = fx - 1.f, c = fx - 0.5f;
+    w[0] = 0.5f * (a * a);
+    w[1] = 0.75f - b * b;
+    w[2] = 0.5f * (c * c);
+    f = fx;
+  }
   // D^-1 = 4 / dx^2 I for the quadratic kernel (computed on the host as (4 dx_inv) dx_inv)
 };
 

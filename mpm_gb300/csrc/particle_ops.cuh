@@ -82,15 +82,12 @@ __device__ __forceinline__ void store_particle(float* s, int64_t st, int64_t p, 
   s[kJp * st + p] = Jp;
 }
 
-// p2g_prepare_particle (include/TransferScheme.h:64-86): affine = -D dt vol PF + m C
-// and the momentum m v; PF from MaterialModel::computePF.
+// MaterialModel::computePF (include/MaterialModel.cuh:56-61, 85-93): P F^T of the
+// particle.  For snow after plasticity the polar rotation of the clamped F is U V^T
+// (have_uv): F = U clamp(Sigma) V^T with clamp(Sigma) >= 0.
 template <bool LIQ>
-__device__ __forceinline__ void p2g_prepare(const DevMaterial& M, const GridConsts& K, const float F[3][3], float Jp,
-                                            const float Cm[3][3], const float v[3], bool have_uv,
-                                            const float Usv[3][3], const float Vsv[3][3], float Aff[3][3],
-                                            float mv[3], float& m) {
-  m = M.mass;
-  float PF[3][3];
+__device__ __forceinline__ void material_PF(const DevMaterial& M, const float F[3][3], float Jp, bool have_uv,
+                                            const float Usv[3][3], const float Vsv[3][3], float PF[3][3]) {
   if (LIQ || M.kind == kLiquid) {
     const float pr = M.bulk * (Jp - 1.f) * Jp;
 #pragma unroll
@@ -100,7 +97,6 @@ __device__ __forceinline__ void p2g_prepare(const DevMaterial& M, const GridCons
   } else {
     float R[3][3];
     if (have_uv) {
-      // F = U clamp(Sigma) V^T with clamp(Sigma) >= 0, so its polar rotation is U V^T
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -112,13 +108,27 @@ __device__ __forceinline__ void p2g_prepare(const DevMaterial& M, const GridCons
     }
     compute_PF(M, F, R, Jp, PF);
   }
-  const float sc = ((-K.dinv) * K.dt) * M.vol;
+}
+
+// p2g_prepare_particle (include/TransferScheme.h:64-86): affine = -D dt vol PF + m C,
+// here in the node-offset form of p2g_write_column_f: E_k = dx affine[:, k] (dx folded
+// into the affine's two scale factors) and q0 = m v - sum_k E_k f_k.
+template <bool LIQ>
+__device__ __forceinline__ void p2g_prepare_f(const DevMaterial& M, const GridConsts& K, const float F[3][3], float Jp,
+                                              const float Cm[3][3], const float v[3], bool have_uv,
+                                              const float Usv[3][3], const float Vsv[3][3], const float f[3],
+                                              float E[3][3], float q0[3], float& m) {
+  m = M.mass;
+  float PF[3][3];
+  material_PF<LIQ>(M, F, Jp, have_uv, Usv, Vsv, PF);
+  const float scx = (((-K.dinv) * K.dt) * M.vol) * K.dx;
+  const float mdx = m * K.dx;
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+  for (int k = 0; k < 3; ++k)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) Aff[i][j] = fmaf(sc, PF[i][j], m * Cm[i][j]);
+    for (int r = 0; r < 3; ++r) E[k][r] = fmaf(scx, PF[r][k], mdx * Cm[r][k]);
 #pragma unroll
-  for (int dd = 0; dd < 3; ++dd) mv[dd] = v[dd] * m;
+  for (int r = 0; r < 3; ++r) q0[r] = fmaf(-E[2][r], f[2], fmaf(-E[1][r], f[1], fmaf(-E[0][r], f[0], m * v[r])));
 }
 
 }  // namespace mpm

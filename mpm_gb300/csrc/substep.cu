@@ -48,12 +48,14 @@ namespace mpm {
 // One step's P2G scatter (particleToGrid's atomic loop, src/mpm.cu:47-73): each lane
 // with a contribution writes its 27 node values as a column, then the warp reduces
 // runs of same-cell lanes.
+// UNIT_MASS: every particle of the warp has mass `run_mass` (a single-material table).
+template <bool UNIT_MASS>
 __device__ __forceinline__ void p2g_scatter_step(float4* wbuf, int lane, int key, const float w[3][3],
-                                                 const float d[3][3], const float Aff[3][3], const float mv[3],
-                                                 float m, float4* grid, int N) {
+                                                 const float q0[3], const float E[3][3], float m, float run_mass,
+                                                 float4* grid, int N) {
   if (__ballot_sync(kFull, key >= 0) == 0u) return;
-  if (key >= 0) p2g_write_column(wbuf, lane, w, d, Aff, mv, m);
-  warp_scatter_runs(wbuf, lane, key, grid, N);
+  if (key >= 0) p2g_write_column_f<UNIT_MASS>(wbuf, lane, w, q0, E, m);
+  warp_scatter_runs(wbuf, lane, key, grid, N, UNIT_MASS ? run_mass : 1.f);
 }
 
 // ===========================================================================
@@ -97,13 +99,13 @@ static __device__ __noinline__ G2POut g2p_gather_vgrid(const float4* vgrid, Grid
                                                        float x2) {
   const float x[3] = {x0, x1, x2};
   int b[3];
-  float w[3][3], d[3][3];
-  stencil(x, K, b, w, d);
+  float w[3][3], f[3];
+  stencil_f(x, K, b, w, f);
   const int P = K.N + kPadLo + kPadHi;
   const float4* vb = vgrid + ((int64_t)(b[0] + kPadLo) * P + (b[1] + kPadLo)) * P + (b[2] + kPadLo);
   auto node = [&](int a, int bb, int c) -> float4 { return __ldg(vb + ((int64_t)a * P + bb) * P + c); };
   G2POut o;
-  g2p_gather(node, K, w, d, o.v, o.C);
+  g2p_gather_f(node, K.dinv * K.dx, w, f, o.v, o.C);
   return o;
 }
 
@@ -171,6 +173,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
                    2 * warp;
   const GridConsts K = A.K.g;
   const int N = K.N;
+  const float ddx = K.dinv * K.dx;  // D dx of the node-offset gather
   float* __restrict__ s = A.s;
   const int64_t st = A.stride, n = A.n, chunk = A.chunk;
 
@@ -247,9 +250,9 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
       // ---- G2P (gridToParticle, src/mpm.cu:109-167)
       if (G2P) {
         int b[3] = {0, 0, 0};
-        float w[3][3], d[3][3];
+        float w[3][3], f[3];
         if (valid && !frozen) {
-          stencil(x, K, b, w, d);
+          stencil_f(x, K, b, w, f);
           g2p_on = !outside_domain(b[0], b[1], b[2], N);
           if (!g2p_on) frozen = true;  // completely outside: unchanged; P2G skips it too
         }
@@ -260,7 +263,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
             const float4* t = tiles + buf * kTileNodes +
                               ((b[0] - tlo[0]) * kTileY + (b[1] - tlo[1])) * kTileZ + (b[2] - tlo[2]);
             auto node = [&](int a, int bb, int c) -> float4 { return t[(a * kTileY + bb) * kTileZ + c]; };
-            g2p_gather(node, K, w, d, v, Cm);
+            g2p_gather_f(node, ddx, w, f, v, Cm);
           }
         } else if (tstate == kTileGlobal && g2p_on) {
           const G2POut o = g2p_gather_vgrid(A.vgrid, K, x[0], x[1], x[2]);
@@ -285,16 +288,16 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
       // ---- P2G of the next substep (particleToGrid)
       if (P2G) {
         int key = -1;
-        float w[3][3], d[3][3], Aff[3][3], mv[3], m = 0.f;
+        float w[3][3], f[3], E[3][3], q0[3], m = 0.f;
         if (valid) {
           int b[3];
-          stencil(x, K, b, w, d);
+          stencil_f(x, K, b, w, f);
           if (!outside_domain(b[0], b[1], b[2], N)) {
             key = pack_key(b[0], b[1], b[2]);
-            p2g_prepare<LIQ>(M, K, F, Jp, Cm, v, have_uv, Usv, Vsv, Aff, mv, m);
+            p2g_prepare_f<LIQ>(M, K, F, Jp, Cm, v, have_uv, Usv, Vsv, f, E, q0, m);
           }
         }
-        p2g_scatter_step(wbuf, lane, key, w, d, Aff, mv, m, A.grid_out, N);
+        p2g_scatter_step<LIQ>(wbuf, lane, key, w, q0, E, m, A.K.mat[0].mass, A.grid_out, N);
       }
       if (!more) break;
       if (last) {
@@ -496,8 +499,8 @@ __global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __gri
       bool g2p_on = false;
       if (G2P && valid && !frozen) {
         int b[3];
-        float w[3][3], d[3][3];
-        stencil(x, K, b, w, d);
+        float w[3][3], f[3];
+        stencil_f(x, K, b, w, f);
         g2p_on = !outside_domain(b[0], b[1], b[2], N);
         if (!g2p_on) {
           frozen = true;
@@ -505,7 +508,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __gri
           const int t0 = ((b[0] - tb.t0) * tb.d1 + (b[1] - tb.t1)) * tb.d2 + (b[2] - tb.t2);
           const int d12 = tb.d1 * tb.d2;
           auto node = [&](int a, int bb, int c) -> float4 { return wtile[t0 + a * d12 + bb * tb.d2 + c]; };
-          g2p_gather(node, K, w, d, v, Cm);
+          g2p_gather_f(node, K.dinv * K.dx, w, f, v, Cm);
         } else {
           const G2POut o = g2p_gather_global(gin, K, x[0], x[1], x[2]);
 #pragma unroll
@@ -523,10 +526,10 @@ __global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __gri
       }
       if (P2G) {
         int key = -1;
-        float w[3][3], d[3][3], Aff[3][3], mv[3], m = 0.f;
+        float w[3][3], f[3], E[3][3], q0[3], m = 0.f;
         if (valid) {
           int b[3];
-          stencil(x, K, b, w, d);
+          stencil_f(x, K, b, w, f);
           if (!outside_domain(b[0], b[1], b[2], N)) {
             key = pack_key(b[0], b[1], b[2]);
 #pragma unroll
@@ -534,10 +537,10 @@ __global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __gri
               plo[dd] = min(plo[dd], b[dd]);
               phi[dd] = max(phi[dd], b[dd]);
             }
-            p2g_prepare<false>(M, K, F, Jp, Cm, v, have_uv, Usv, Vsv, Aff, mv, m);
+            p2g_prepare_f<false>(M, K, F, Jp, Cm, v, have_uv, Usv, Vsv, f, E, q0, m);
           }
         }
-        p2g_scatter_step(wbuf, lane, key, w, d, Aff, mv, m, gout, N);
+        p2g_scatter_step<false>(wbuf, lane, key, w, q0, E, m, 1.f, gout, N);
       }
     }
     if (P2G) {

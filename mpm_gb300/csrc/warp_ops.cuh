@@ -28,43 +28,15 @@ __device__ __forceinline__ void f4add(float4& a, const float4 b) {
   a.w += b.w;
 }
 
-// p2g_node_contribution (include/TransferScheme.h:88-100) for all 27 nodes, written
-// as column `lane` of the warp's transpose buffer: row n = node (a, b, c) holds
-//   (w_n (m v + A dpos_n), w_n m).
-__device__ __forceinline__ void p2g_write_column(float4* wbuf, int lane, const float w[3][3], const float d[3][3],
-                                                 const float Aff[3][3], const float mv[3], float m) {
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    float qa[3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) qa[r] = fmaf(Aff[r][0], d[0][a], mv[r]);
-#pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      float qab[3];
-#pragma unroll
-      for (int r = 0; r < 3; ++r) qab[r] = fmaf(Aff[r][1], d[1][b], qa[r]);
-      const float wab = w[0][a] * w[1][b];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float wt = wab * w[2][c];
-        float4 val;
-        val.x = wt * fmaf(Aff[0][2], d[2][c], qab[0]);
-        val.y = wt * fmaf(Aff[1][2], d[2][c], qab[1]);
-        val.z = wt * fmaf(Aff[2][2], d[2][c], qab[2]);
-        val.w = wt * m;
-        wbuf[(a * 9 + b * 3 + c) * kRedStride + lane] = val;
-      }
-    }
-  }
-}
-
 // Warp-collective scatter of 27 node values per lane (column `lane` of the warp's
 // buffer, written by the caller; key = packed base cell, -1 for no contribution).
 // Lane l < 27 walks the 32 columns in order, summing node l over each run of
 // consecutive lanes that share a base cell (cell-sorted particles make a run per
 // cell) and issuing one vector atomic per run; runs with key -1 are dropped.  The run
 // boundaries are warp-uniform, so the walk does not diverge.
-__device__ __forceinline__ void warp_scatter_runs(float4* wbuf, int lane, int key, float4* grid, int N) {
+// `mass_scale` multiplies the summed .w (columns written with unit mass hold weights).
+__device__ __forceinline__ void warp_scatter_runs(float4* wbuf, int lane, int key, float4* grid, int N,
+                                                  float mass_scale = 1.f) {
   const int prev = __shfl_up_sync(kFull, key, 1);
   const unsigned starts = __ballot_sync(kFull, lane == 0 || key != prev);
   __syncwarp();
@@ -92,6 +64,7 @@ __device__ __forceinline__ void warp_scatter_runs(float4* wbuf, int lane, int ke
       f4add(s0, s1);
       f4add(s2, s3);
       f4add(s0, s2);
+      s0.w *= mass_scale;
       int b0, b1, b2;
       unpack_key(run_key, b0, b1, b2);
       add_node(grid, N, b0 + lane / 9, b1 + (lane / 3) % 3, b2 + lane % 3, s0);
@@ -112,53 +85,98 @@ __device__ __forceinline__ void stencil(const float x[3], const GridConsts& K, i
   }
 }
 
-// gridToParticle gather (src/mpm.cu:136-167 + g2p_node_contribution), factorised per
-// dimension: v = sum w g, C = D sum w g dpos^T (D = 4/dx^2).  `node(a, b, c)`
-// returns the grid velocity of node base + (a, b, c), zero outside the grid.
+// Weights and base cells like stencil(), with the offsets f = x / dx - base instead of
+// the node distances: the distance of node a is dpos = (a - f) dx.
+__device__ __forceinline__ void stencil_f(const float x[3], const GridConsts& K, int b[3], float w[3][3], float f[3]) {
+#pragma unroll
+  for (int dim = 0; dim < 3; ++dim)
+    QuadraticInterpolationKernel::weights_and_offset(x[dim], K.dx_inv, b[dim], w[dim], f[dim]);
+}
+
+// gridToParticle gather (src/mpm.cu:136-167 + g2p_node_contribution) with integer node
+// offsets o in {0, 1, 2}^3: dpos = (o - f) dx, so
+//   v = sum w g,   C = D sum w g dpos^T = D dx (sum w g o^T - v f^T)   (ddx = D dx),
+// factorised per dimension; the o = 0 terms of the first moments vanish.
 template <class NodeFn>
-__device__ __forceinline__ void g2p_gather(NodeFn node, const GridConsts& K, const float w[3][3], const float d[3][3],
-                                           float v[3], float C[3][3]) {
-  float c0[3] = {0.f, 0.f, 0.f}, c1[3] = {0.f, 0.f, 0.f}, c2[3] = {0.f, 0.f, 0.f};
-  v[0] = v[1] = v[2] = 0.f;
+__device__ __forceinline__ void g2p_gather_f(NodeFn node, float ddx, const float w[3][3], const float f[3], float v[3],
+                                             float C[3][3]) {
+  float mx[3], my[3], mz[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    float U[3] = {0.f, 0.f, 0.f}, Vv[3] = {0.f, 0.f, 0.f}, W[3] = {0.f, 0.f, 0.f};
+    float U[3], Vy[3], Wz[3];
 #pragma unroll
     for (int bb = 0; bb < 3; ++bb) {
-      float S[3] = {0.f, 0.f, 0.f}, T[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float4 g = node(a, bb, c);
-        const float wz = w[2][c], wzd = w[2][c] * d[2][c];
-        S[0] = fmaf(wz, g.x, S[0]);
-        S[1] = fmaf(wz, g.y, S[1]);
-        S[2] = fmaf(wz, g.z, S[2]);
-        T[0] = fmaf(wzd, g.x, T[0]);
-        T[1] = fmaf(wzd, g.y, T[1]);
-        T[2] = fmaf(wzd, g.z, T[2]);
-      }
-      const float wy = w[1][bb], wyd = w[1][bb] * d[1][bb];
+      const float4 g0 = node(a, bb, 0), g1 = node(a, bb, 1), g2 = node(a, bb, 2);
+      const float w0 = w[2][0], w1 = w[2][1], w2 = w[2][2], w2x2 = 2.f * w[2][2];
+      float S[3], T[3];
+      S[0] = fmaf(w2, g2.x, fmaf(w1, g1.x, w0 * g0.x));
+      S[1] = fmaf(w2, g2.y, fmaf(w1, g1.y, w0 * g0.y));
+      S[2] = fmaf(w2, g2.z, fmaf(w1, g1.z, w0 * g0.z));
+      T[0] = fmaf(w2x2, g2.x, w1 * g1.x);
+      T[1] = fmaf(w2x2, g2.y, w1 * g1.y);
+      T[2] = fmaf(w2x2, g2.z, w1 * g1.z);
+      const float wy = w[1][bb];
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
-        U[r] = fmaf(wy, S[r], U[r]);
-        Vv[r] = fmaf(wyd, S[r], Vv[r]);
-        W[r] = fmaf(wy, T[r], W[r]);
+        U[r] = bb ? fmaf(wy, S[r], U[r]) : wy * S[r];
+        Wz[r] = bb ? fmaf(wy, T[r], Wz[r]) : wy * T[r];
+        if (bb == 1) Vy[r] = wy * S[r];
+        if (bb == 2) Vy[r] = fmaf(2.f * wy, S[r], Vy[r]);
       }
     }
-    const float wx = w[0][a], wxd = w[0][a] * d[0][a];
+    const float wx = w[0][a];
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      v[r] = fmaf(wx, U[r], v[r]);
-      c0[r] = fmaf(wxd, U[r], c0[r]);
-      c1[r] = fmaf(wx, Vv[r], c1[r]);
-      c2[r] = fmaf(wx, W[r], c2[r]);
+      v[r] = a ? fmaf(wx, U[r], v[r]) : wx * U[r];
+      my[r] = a ? fmaf(wx, Vy[r], my[r]) : wx * Vy[r];
+      mz[r] = a ? fmaf(wx, Wz[r], mz[r]) : wx * Wz[r];
+      if (a == 1) mx[r] = wx * U[r];
+      if (a == 2) mx[r] = fmaf(2.f * wx, U[r], mx[r]);
     }
   }
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
-    C[r][0] = K.dinv * c0[r];
-    C[r][1] = K.dinv * c1[r];
-    C[r][2] = K.dinv * c2[r];
+    C[r][0] = ddx * fmaf(-v[r], f[0], mx[r]);
+    C[r][1] = ddx * fmaf(-v[r], f[1], my[r]);
+    C[r][2] = ddx * fmaf(-v[r], f[2], mz[r]);
+  }
+}
+
+// p2g_node_contribution (include/TransferScheme.h:88-100) for all 27 nodes with integer
+// node offsets: node o = (a, b, c) receives w_o (m v + A dpos_o) = w_o (q0 + a E0 + b E1 + c E2)
+// with E_k = dx A[:, k] (E[k][r]) and q0 = m v - sum_k E_k f_k.  Written as column `lane`
+// of the warp's transpose buffer: row a*9 + b*3 + c holds (w_o (...), w_o m), or w_o in
+// .w when UNIT_MASS (the walk scales the summed weight by the particles' common mass).
+template <bool UNIT_MASS>
+__device__ __forceinline__ void p2g_write_column_f(float4* wbuf, int lane, const float w[3][3], const float q0[3],
+                                                   const float E[3][3], float m) {
+  float qa[3] = {q0[0], q0[1], q0[2]};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (a) {
+#pragma unroll
+      for (int r = 0; r < 3; ++r) qa[r] += E[0][r];
+    }
+    float qab[3] = {qa[0], qa[1], qa[2]};
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      if (b) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) qab[r] += E[1][r];
+      }
+      const float wab = w[0][a] * w[1][b];
+      float q[3] = {qab[0], qab[1], qab[2]};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (c) {
+#pragma unroll
+          for (int r = 0; r < 3; ++r) q[r] += E[2][r];
+        }
+        const float wt = wab * w[2][c];
+        wbuf[(a * 9 + b * 3 + c) * kRedStride + lane] =
+            make_float4(wt * q[0], wt * q[1], wt * q[2], UNIT_MASS ? wt : wt * m);
+      }
+    }
   }
 }
 
@@ -174,8 +192,8 @@ static __device__ __noinline__ G2POut g2p_gather_global(const float4* grid_in, c
   const int N = K.N;
   const float x[3] = {x0, x1, x2};
   int b[3];
-  float w[3][3], d[3][3];
-  stencil(x, K, b, w, d);
+  float w[3][3], f[3];
+  stencil_f(x, K, b, w, f);
   const int b0 = b[0], b1 = b[1], b2 = b[2];
   auto node = [&](int a, int bb, int c) -> float4 {
     const int i = b0 + a, j = b1 + bb, k = b2 + c;
@@ -185,9 +203,8 @@ static __device__ __noinline__ G2POut g2p_gather_global(const float4* grid_in, c
     return make_float4(v.x, v.y, v.z, 0.f);
   };
   G2POut o;
-  g2p_gather(node, K, w, d, o.v, o.C);
+  g2p_gather_f(node, K.dinv * K.dx, w, f, o.v, o.C);
   return o;
 }
-
 
 }  // namespace mpm
