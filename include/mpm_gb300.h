@@ -142,8 +142,9 @@ mpm_status mpm_last_error(const mpm_ctx* ctx, char* buf, size_t len);
 /* Kernel launches issued by this context since creation (for accounting). */
 int64_t mpm_launch_count(const mpm_ctx* ctx);
 
-/* Tuning knob of the fused substep kernel: steps_per_warp, the 32-particle steps in
- * each range a warp claims (1..256, default 2; 0 keeps the current value).
+/* Tuning knob of the fused substep kernel: steps_per_warp, the largest number of
+ * 32-particle steps in each range a warp claims (1..256, default 2; 0 keeps the current
+ * value); it is halved while each warp would get fewer than 6 ranges.
  * reserved1, reserved2: must be >= 0; ignored (the grid tile is a fixed TMA box and
  * the launch is sized by occupancy). */
 mpm_status mpm_set_tuning(mpm_ctx* ctx, int32_t steps_per_warp, int32_t reserved1, int32_t reserved2);

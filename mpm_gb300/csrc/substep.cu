@@ -14,8 +14,10 @@
 //
 // Work decomposition: warps are the scheduling unit.  Each warp of a 12-warp CTA
 // takes a range of cell-sorted particles (steps_per_warp x 32) and walks it 32
-// particles at a time (lane = particle, coalesced component-major loads/stores);
-// further ranges are claimed from a global counter, so faster warps take more.
+// particles at a time (lane = particle, coalesced component-major loads/stores).  A
+// CTA owns every G-th range (G = grid size); its warps take them in turn from a
+// shared-memory counter, so faster warps take more without global atomics (one
+// global counter serialised 15k claims per launch at a single L2 slice).
 //
 // G2P reads a per-step tile of the velocity grid in shared memory: a fixed box of
 // 4 x 4 x 6 nodes that one TMA copy (cp.async.bulk.tensor, completion on an mbarrier)
@@ -162,6 +164,7 @@ __device__ __forceinline__ float4* align_smem128(float4* p) {
 template <bool LIQ, bool G2P, bool P2G, bool GUARD>
 __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __grid_constant__ StepArgs A) {
   extern __shared__ float4 smem_dyn[];
+  __shared__ int cta_next;  // next CTA-local range index to hand out
   float4* smem = align_smem128(smem_dyn);
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
@@ -171,13 +174,15 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (G2P ? kStepWarps * 2 * kTileNodes : 0) +
                                                (P2G ? kStepWarps * kRedFloat4 : 0)) +
                    2 * warp;
-  const GridConsts K = A.K.g;
+  const GridConsts& K = A.K.g;  // read from the parameter space, not copied to registers
   const int N = K.N;
   const float ddx = K.dinv * K.dx;  // D dx of the node-offset gather
   float* __restrict__ s = A.s;
-  const int64_t st = A.stride, n = A.n, chunk = A.chunk;
+  const int64_t st = A.stride;
+  const int64_t n = A.n, chunk = A.chunk;
 
-  if (blockIdx.x == 0 && tid == 0) *A.work_next = 0;
+  if (tid == 0) cta_next = kStepWarps;
+  __syncthreads();
   if (G2P) {
     if (lane == 0) {
       mbar_init(bars, 1);
@@ -186,16 +191,19 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
     }
     __syncwarp();
   }
+  // Ranges of `chunk` particles: CTA c owns ranges c, c + G, c + 2G, ... (G = grid
+  // size), interleaved through the sorted particles; its warps take them in turn from a
+  // shared-memory counter, so the warps of a CTA balance each other without global
+  // atomics.  Warp-uniform bookkeeping: the current range ends at `re`; `rn` is the next
+  // range, claimed one range ahead so the step after a range's last is known early.
   const int64_t nranges = (n + chunk - 1) / chunk;
-  const int64_t first_wave = (int64_t)gridDim.x * kStepWarps;
-  const int64_t r0 = (int64_t)blockIdx.x * kStepWarps + warp;
+  const int G = (int)gridDim.x;
+  const int64_t r0 = (int64_t)blockIdx.x + warp * G;
   if (r0 < nranges) {
-    // Warp-uniform range bookkeeping: the current range ends at `re`; `rn` is the next
-    // range, claimed one range ahead so the step after a range's last is known early.
     int claim = 0;
-    if (lane == 0) claim = atomicAdd(A.work, 1);
-    int64_t rn = first_wave + __shfl_sync(kFull, claim, 0);
-    if (lane == 0) claim = atomicAdd(A.work, 1);
+    if (lane == 0) claim = atomicAdd(&cta_next, 1);
+    int64_t rn = (int64_t)blockIdx.x + __shfl_sync(kFull, claim, 0) * G;
+    if (lane == 0) claim = atomicAdd(&cta_next, 1);
     int64_t pb = r0 * chunk;
     int64_t re = min(pb + chunk, n);
     float cx[3] = {0.f, 0.f, 0.f}, cJ = 1.f;
@@ -302,8 +310,8 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
       if (!more) break;
       if (last) {
         re = pe;
-        rn = first_wave + __shfl_sync(kFull, claim, 0);
-        if (lane == 0) claim = atomicAdd(A.work, 1);
+        rn = (int64_t)blockIdx.x + __shfl_sync(kFull, claim, 0) * G;
+        if (lane == 0) claim = atomicAdd(&cta_next, 1);
       }
       pb = pn;
 #pragma unroll
