@@ -127,8 +127,22 @@ __global__ void scan_add(int* counts, int64_t m, const int* block_sums) {
     if (off + i < m) counts[off + i] += add;
 }
 
+// Component k of the layout's c-th moved component: the liquid layout moves x, v, C
+// (components 0-14) and J (component 24); the general layout moves all 25.
+template <bool LIQ>
+__device__ __forceinline__ int moved_comp(int c) {
+  return LIQ ? (c < kLiquidComps - 1 ? c : kJp) : c;
+}
+
+// Scatter every particle to its sorted slot.  All components of a particle are
+// loaded before any is stored, so a thread keeps 16 or 25 loads in flight.
+template <bool LIQ>
 __global__ void sort_scatter(SortArgs a) {
+  constexpr int NC = LIQ ? kLiquidComps : kNumComps;
   const int lane = threadIdx.x & 31;
+  const float* __restrict__ sA = a.sA;
+  float* __restrict__ sB = a.sB;
+  const int64_t st = a.stride;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < a.n; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = base + threadIdx.x;
     const bool valid = p < a.n;
@@ -140,12 +154,58 @@ __global__ void sort_scatter(SortArgs a) {
     start = __shfl_sync(kFull, start, leader);
     if (!valid) continue;
     const int64_t q = (int64_t)start + __popc(same & ((1u << lane) - 1u));
-    for (int c = 0; c < a.ncomp; ++c) {
-      const int k = a.comp_list[c];
-      a.sB[k * a.stride + q] = a.sA[k * a.stride + p];
-    }
+    float vals[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) vals[c] = __ldg(sA + moved_comp<LIQ>(c) * st + p);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) sB[moved_comp<LIQ>(c) * st + q] = vals[c];
     if (a.matA) a.matB[q] = a.matA[p];
     a.idB[q] = a.idA[p];
+  }
+}
+
+// Exclusive scan of a small key space by one CTA of kScanThreads threads, tile by tile
+// (one launch instead of the three of the blocked scan).
+constexpr int kScanThreads = 1024;
+constexpr int64_t kSmallScan = 65536;
+
+__global__ void __launch_bounds__(kScanThreads) scan_small(int* counts, int64_t m) {
+  __shared__ int warp_tot[kScanThreads / 32];
+  __shared__ int carry;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t tile = 0; tile < m; tile += (int64_t)kScanThreads * kScanItems) {
+    const int64_t off = tile + (int64_t)threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int sum = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+      v[i] = (off + i < m) ? counts[off + i] : 0;
+      sum += v[i];
+    }
+    int inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(kFull, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_tot[warp] = inc;
+    __syncthreads();
+    int wpre = 0, tot = 0;
+    for (int w = 0; w < kScanThreads / 32; ++w) {
+      if (w < warp) wpre += warp_tot[w];
+      tot += warp_tot[w];
+    }
+    int run = carry + wpre + inc - sum;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+      if (off + i < m) counts[off + i] = run;
+      run += v[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
   }
 }
 
@@ -155,13 +215,22 @@ cudaError_t launch_sort(const SortArgs& a, int num_sms, cudaStream_t st, int64_t
   if (e != cudaSuccess) return e;
   int blocks = (int)std::min<int64_t>((a.n + kThreads - 1) / kThreads, (int64_t)num_sms * 8);
   sort_histogram<<<blocks, kThreads, 0, st>>>(a);
-  const int per = kThreads * kScanItems;
-  const int nb = (int)((a.cells + per - 1) / per);
-  scan_blocks<<<nb, kThreads, 0, st>>>(a.counts, a.cells, a.block_sums);
-  scan_block_sums<<<1, kThreads, 0, st>>>(a.block_sums, nb);
-  scan_add<<<nb, kThreads, 0, st>>>(a.counts, a.cells, a.block_sums);
-  sort_scatter<<<blocks, kThreads, 0, st>>>(a);
-  if (launches) *launches += 5;
+  int n_launch = 3;
+  if (a.cells <= kSmallScan) {
+    scan_small<<<1, kScanThreads, 0, st>>>(a.counts, a.cells);
+  } else {
+    const int per = kThreads * kScanItems;
+    const int nb = (int)((a.cells + per - 1) / per);
+    scan_blocks<<<nb, kThreads, 0, st>>>(a.counts, a.cells, a.block_sums);
+    scan_block_sums<<<1, kThreads, 0, st>>>(a.block_sums, nb);
+    scan_add<<<nb, kThreads, 0, st>>>(a.counts, a.cells, a.block_sums);
+    n_launch = 5;
+  }
+  if (a.ncomp == kLiquidComps)
+    sort_scatter<true><<<blocks, kThreads, 0, st>>>(a);
+  else
+    sort_scatter<false><<<blocks, kThreads, 0, st>>>(a);
+  if (launches) *launches += n_launch;
   return cudaGetLastError();
 }
 

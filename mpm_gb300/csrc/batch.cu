@@ -50,7 +50,6 @@ struct mpm_batch {
   int64_t key_space = 0;
   int* counts = nullptr;
   int* block_sums = nullptr;
-  int* comp_list = nullptr;
   int4* d_ranges = nullptr;
   int nranges = 0;
   int* boxes = nullptr;
@@ -138,7 +137,6 @@ mpm_status sort(mpm_batch* b) {
   s.block_sums = b->block_sums;
   s.cells = b->key_space;
   s.ncomp = kNumComps;
-  s.comp_list = b->comp_list;
   s.nscenes = b->nscenes;
   s.scene_start = b->d_start;
   s.scene_key_base = b->d_key_base;
@@ -250,18 +248,15 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
       cudaMalloc(&b->d_scenes, sizeof(SceneDev) * nscenes) || cudaMalloc(&b->d_start, 8 * (nscenes + 1)) ||
       cudaMalloc(&b->d_key_base, 4 * nscenes) || cudaMalloc(&b->d_ranges, sizeof(int4) * std::max(b->nranges, 1)) ||
       cudaMalloc(&b->boxes, sizeof(int) * 6 * kBoxSlots * nscenes) || cudaMalloc(&b->work, 2 * sizeof(int)) ||
-      cudaMalloc(&b->status, sizeof(int)) || cudaMalloc(&b->comp_list, sizeof(int) * kNumComps))
+      cudaMalloc(&b->status, sizeof(int)))
     return bail(MPM_ERR_NOMEM);
   std::vector<int> boxes(6 * kBoxSlots * nscenes);
   for (size_t i = 0; i < boxes.size(); ++i) boxes[i] = (i % 6 < 3) ? INT_MAX : INT_MIN;
-  int comps[kNumComps];
-  for (int i = 0; i < kNumComps; ++i) comps[i] = i;
   if (cudaMemcpy(b->d_scenes, sd.data(), sizeof(SceneDev) * nscenes, cudaMemcpyHostToDevice) ||
       cudaMemcpy(b->d_start, b->start.data(), 8 * (nscenes + 1), cudaMemcpyHostToDevice) ||
       cudaMemcpy(b->d_key_base, key_base.data(), 4 * nscenes, cudaMemcpyHostToDevice) ||
       (b->nranges && cudaMemcpy(b->d_ranges, ranges.data(), sizeof(int4) * b->nranges, cudaMemcpyHostToDevice)) ||
       cudaMemcpy(b->boxes, boxes.data(), sizeof(int) * boxes.size(), cudaMemcpyHostToDevice) ||
-      cudaMemcpy(b->comp_list, comps, sizeof(comps), cudaMemcpyHostToDevice) ||
       cudaMemset(b->work, 0, 2 * sizeof(int)) || cudaMemset(b->status, 0, sizeof(int)) ||
       cudaStreamSynchronize(b->stream))
     return bail(MPM_ERR_CUDA);
@@ -276,7 +271,7 @@ mpm_status mpm_batch_destroy(mpm_batch* b) {
   for (void* p : {(void*)b->sA, (void*)b->sB, (void*)b->matA, (void*)b->matB, (void*)b->idA, (void*)b->idB,
                   (void*)b->keys, (void*)b->stage, (void*)b->grid[0], (void*)b->grid[1], (void*)b->grid[2],
                   (void*)b->counts, (void*)b->block_sums, (void*)b->d_scenes, (void*)b->d_start, (void*)b->d_key_base,
-                  (void*)b->d_ranges, (void*)b->boxes, (void*)b->work, (void*)b->status, (void*)b->comp_list})
+                  (void*)b->d_ranges, (void*)b->boxes, (void*)b->work, (void*)b->status})
     cudaFree(p);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;

@@ -52,7 +52,6 @@ struct mpm_ctx {
   // sort scratch
   int* counts = nullptr;
   int* block_sums = nullptr;
-  int* comp_list = nullptr;
 
   // staging
   float* stage = nullptr;
@@ -217,7 +216,6 @@ mpm_status run_sort(mpm_ctx* c) {
   s.dx_inv = c->K.g.dx_inv;
   // liquid layout: x, v, C, J (16 components); general: all 25
   s.ncomp = c->liquid_layout ? kLiquidComps : kNumComps;
-  s.comp_list = c->liquid_layout ? c->comp_list : c->comp_list + kLiquidComps;
   MPM_CUDA(c, launch_sort(s, c->num_sms, c->stream, &c->launches));
   std::swap(c->sA, c->sB);
   std::swap(c->matA, c->matB);
@@ -331,17 +329,6 @@ mpm_status mpm_create(const mpm_params* params, mpm_ctx** out) {
   if (cudaMemsetAsync(c->work, 0, 2 * sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
 
   if (cudaMemsetAsync(c->status, 0, sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
-  // component lists for the sort: liquid layout = x, v, C, J; general = all
-  int comps[kNumComps];
-  for (int i = 0; i < kNumComps; ++i) comps[i] = i;
-  int liq[kLiquidComps];
-  for (int i = 0; i < 15; ++i) liq[i] = i;
-  liq[15] = kJp;
-  if (cudaMalloc(&c->comp_list, sizeof(int) * 2 * kNumComps) != cudaSuccess) return bail(MPM_ERR_NOMEM);
-  (void)comps;
-  if (cudaMemcpy(c->comp_list, liq, sizeof(liq), cudaMemcpyHostToDevice) != cudaSuccess) return bail(MPM_ERR_CUDA);
-  if (cudaMemcpy(c->comp_list + kLiquidComps, comps, sizeof(comps), cudaMemcpyHostToDevice) != cudaSuccess)
-    return bail(MPM_ERR_CUDA);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
   (void)st;
   *out = c;
@@ -356,7 +343,6 @@ mpm_status mpm_destroy(mpm_ctx* c) {
   cudaFree(c->vgrid_mem);
   cudaFree(c->counts);
   cudaFree(c->block_sums);
-  cudaFree(c->comp_list);
   cudaFree(c->stage);
   cudaFree(c->status);
   cudaFree(c->work);

@@ -109,8 +109,7 @@ struct SortArgs {
   int64_t cells;  // sort key space (bricked cell index range)
   int N;
   float dx_inv;
-  int ncomp;            // components to move
-  const int* comp_list; // device list of component indices
+  int ncomp;            // kLiquidComps (x, v, C, J) or kNumComps (all)
   // batch mode (nscenes > 0): keys are scene_key_base[scene] + the bricked key in the scene's grid
   int nscenes;
   const int64_t* scene_start;      // nscenes + 1 particle offsets
