@@ -152,12 +152,12 @@ def measured_peaks():
 
 
 def profile_traffic(workload):
-    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", f"fused_step_{workload}.json")
+    """DRAM bytes of one substep (velocity pass + fused kernel) from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", f"scene_step_{workload}.json")
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return d.get("dram_bytes_per_launch")
+        return d.get("dram_bytes_per_substep")
     return None
 
 

@@ -164,25 +164,29 @@ __global__ void sort_scatter(SortArgs a) {
   }
 }
 
-// Exclusive scan of a small key space by one CTA of kScanThreads threads, tile by tile
-// (one launch instead of the three of the blocked scan).
+// Exclusive scan of a small key space (a multiple of 4 counts) by one CTA: each of
+// kScanThreads threads scans kScanRun consecutive counts in registers (int4 loads),
+// then the CTA scans the threads' totals; tiles of kScanThreads x kScanRun counts
+// carry their total into the next.  One launch instead of the three of the blocked
+// scan, used up to one tile (kSmallScan keys, N <= 32): beyond that the single SM's
+// bandwidth makes it slower than the blocked scan.
 constexpr int kScanThreads = 1024;
-constexpr int64_t kSmallScan = 65536;
+constexpr int kScanRun = 32;
+constexpr int64_t kSmallScan = (int64_t)kScanThreads * kScanRun;  // one tile: one SM's bandwidth suffices
 
 __global__ void __launch_bounds__(kScanThreads) scan_small(int* counts, int64_t m) {
   __shared__ int warp_tot[kScanThreads / 32];
   __shared__ int carry;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  for (int64_t tile = 0; tile < m; tile += (int64_t)kScanThreads * kScanItems) {
-    const int64_t off = tile + (int64_t)threadIdx.x * kScanItems;
-    int v[kScanItems];
+  for (int64_t tile = 0; tile < m; tile += (int64_t)kScanThreads * kScanRun) {
+    const int64_t off = tile + (int64_t)threadIdx.x * kScanRun;
+    int4 v[kScanRun / 4];
     int sum = 0;
 #pragma unroll
-    for (int i = 0; i < kScanItems; ++i) {
-      v[i] = (off + i < m) ? counts[off + i] : 0;
-      sum += v[i];
+    for (int i = 0; i < kScanRun / 4; ++i) {
+      v[i] = (off + 4 * i < m) ? reinterpret_cast<const int4*>(counts + off)[i] : make_int4(0, 0, 0, 0);
+      sum += v[i].x + v[i].y + v[i].z + v[i].w;
     }
     int inc = sum;
 #pragma unroll
@@ -190,22 +194,35 @@ __global__ void __launch_bounds__(kScanThreads) scan_small(int* counts, int64_t 
       const int t = __shfl_up_sync(kFull, inc, o);
       if (lane >= o) inc += t;
     }
+    __syncthreads();  // warp_tot and carry of the previous tile are consumed
     if (lane == 31) warp_tot[warp] = inc;
     __syncthreads();
-    int wpre = 0, tot = 0;
-    for (int w = 0; w < kScanThreads / 32; ++w) {
-      if (w < warp) wpre += warp_tot[w];
-      tot += warp_tot[w];
-    }
-    int run = carry + wpre + inc - sum;
+    int wpre = 0;
+    if (lane < kScanThreads / 32) wpre = warp_tot[lane];
+    int wscan = wpre;
 #pragma unroll
-    for (int i = 0; i < kScanItems; ++i) {
-      if (off + i < m) counts[off + i] = run;
-      run += v[i];
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(kFull, wscan, o);
+      if (lane >= o) wscan += t;
+    }
+    const int before_warp = __shfl_sync(kFull, wscan - wpre, warp);  // exclusive prefix of this warp
+    const int tile_total = __shfl_sync(kFull, wscan, kScanThreads / 32 - 1);
+    int run = carry + before_warp + inc - sum;
+#pragma unroll
+    for (int i = 0; i < kScanRun / 4; ++i) {
+      int4 o;
+      o.x = run;
+      run += v[i].x;
+      o.y = run;
+      run += v[i].y;
+      o.z = run;
+      run += v[i].z;
+      o.w = run;
+      run += v[i].w;
+      if (off + 4 * i < m) reinterpret_cast<int4*>(counts + off)[i] = o;
     }
     __syncthreads();
-    if (threadIdx.x == 0) carry += tot;
-    __syncthreads();
+    if (threadIdx.x == 0) carry += tile_total;
   }
 }
 
@@ -216,7 +233,7 @@ cudaError_t launch_sort(const SortArgs& a, int num_sms, cudaStream_t st, int64_t
   int blocks = (int)std::min<int64_t>((a.n + kThreads - 1) / kThreads, (int64_t)num_sms * 8);
   sort_histogram<<<blocks, kThreads, 0, st>>>(a);
   int n_launch = 3;
-  if (a.cells <= kSmallScan) {
+  if (a.cells <= kSmallScan && a.cells % 4 == 0) {
     scan_small<<<1, kScanThreads, 0, st>>>(a.counts, a.cells);
   } else {
     const int per = kThreads * kScanItems;

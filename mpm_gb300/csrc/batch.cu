@@ -27,7 +27,6 @@ struct mpm_batch {
   SimConsts K{};
   int sort_interval = 16;
   int steps_per_warp = 2;
-  int tile_cap = 256;
   int blocks_p2g = 1, blocks_fused = 1;  // launch grids, fixed at creation (outside any capture)
 
   int device = 0, num_sms = 1;
@@ -44,6 +43,8 @@ struct mpm_batch {
 
   int64_t cells = 0;  // total grid nodes of all scenes
   float4* grid[3] = {nullptr, nullptr, nullptr};
+  float4* vgrid = nullptr;  // padded velocity grids of all scenes
+  int64_t vcells = 0;
   SceneDev* d_scenes = nullptr;
   int64_t* d_start = nullptr;
   uint32_t* d_key_base = nullptr;
@@ -63,7 +64,11 @@ struct mpm_batch {
   int parity = 0;
   int64_t since_sort = 0;
   int64_t launches = 0;
-  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (nsteps, launch_index % 6) -> graph
+  struct Graph {
+    cudaGraphExec_t exec;
+    int64_t launches;  // kernels one replay runs
+  };
+  std::map<std::pair<int, int>, Graph> graphs;  // (nsteps, launch_index % 6) -> graph
   std::string last_error;
 };
 
@@ -83,7 +88,7 @@ mpm_status bfail(mpm_batch* b, mpm_status code, const std::string& msg) {
   } while (0)
 
 void free_graphs(mpm_batch* b) {
-  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second.exec);
   b->graphs.clear();
 }
 
@@ -94,7 +99,6 @@ mpm_status launch(mpm_batch* b, StepKind kind) {
   a.mat = nullptr;  // the material comes from the scene table
   a.id = b->idA;
   a.n = b->n;
-  a.tile_cap = b->tile_cap;
   a.status = b->status;
   a.K = b->K;
   a.nscenes = b->nscenes;
@@ -108,6 +112,13 @@ mpm_status launch(mpm_batch* b, StepKind kind) {
   a.box_reset = (int)((L + 1) % kBoxSlots);
   const int r = b->cur;
   a.grid_in = (kind == kStepP2GOnly) ? nullptr : b->grid[r];
+  a.vgrid = b->vgrid;
+  if (kind != kStepP2GOnly) {
+    // velocity pass over the boxes the previous launch's P2G recorded
+    BCUDA(b, launch_batch_velocity(b->grid[r], b->vgrid, b->d_scenes, b->nscenes, b->boxes,
+                                   (int)((L + kBoxSlots - 1) % kBoxSlots), b->stream));
+    b->launches += 1;
+  }
   a.grid_out = b->grid[(r + 1) % 3];
   a.grid_zero = b->grid[(r + 2) % 3];
   a.work = b->work + b->parity;
@@ -205,14 +216,16 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
   std::vector<uint32_t> key_base(nscenes);
   std::vector<int4> ranges;
   const int chunk = 32 * b->steps_per_warp;
-  int64_t off = 0, cells = 0, keys = 0;
+  int64_t off = 0, cells = 0, keys = 0, vcells = 0;
   for (int i = 0; i < nscenes; ++i) {
     b->start[i] = off;
     make_grid_consts(scenes[i].params, sd[i].g);
     make_dev_material(scenes[i].material, sd[i].m);
     sd[i].grid_offset = cells;
+    sd[i].vgrid_offset = vcells;
     const int64_t N = scenes[i].params.N;
     cells += N * N * N;
+    vcells += vgrid_nodes((int)N);
     const int64_t nb = (N + 3) / 4;
     key_base[i] = (uint32_t)keys;
     keys += nb * nb * nb * 64;
@@ -225,11 +238,12 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
   b->n = off;
   b->stride = std::max<int64_t>(64, (off + 63) / 64 * 64);
   b->cells = cells;
+  b->vcells = vcells;
   b->key_space = keys;
   b->nranges = (int)ranges.size();
   for (int k = 0; k < 2; ++k) {
     const StepKind kind = k ? kStepFused : kStepP2GOnly;
-    const int bps = step_blocks_per_sm(kind, false, false, step_smem_bytes(kind, b->tile_cap, true), true);
+    const int bps = step_blocks_per_sm(kind, false, false, step_smem_bytes(kind, 0, true), true);
     const int blocks = std::max(1, std::min((b->nranges + kStepWarps - 1) / kStepWarps, b->num_sms * bps));
     (k ? b->blocks_fused : b->blocks_p2g) = blocks;
   }
@@ -243,6 +257,8 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
     if (cudaMalloc(&g, sizeof(float4) * std::max<int64_t>(cells, 1))) return bail(MPM_ERR_NOMEM);
     if (cudaMemsetAsync(g, 0, sizeof(float4) * cells, b->stream)) return bail(MPM_ERR_CUDA);
   }
+  if (cudaMalloc(&b->vgrid, sizeof(float4) * std::max<int64_t>(vcells, 1))) return bail(MPM_ERR_NOMEM);
+  if (cudaMemsetAsync(b->vgrid, 0, sizeof(float4) * vcells, b->stream)) return bail(MPM_ERR_CUDA);
   const int64_t nbs = (keys + kThreads * 8 - 1) / (kThreads * 8);
   if (cudaMalloc(&b->counts, 4 * keys) || cudaMalloc(&b->block_sums, 4 * std::max<int64_t>(nbs, 1)) ||
       cudaMalloc(&b->d_scenes, sizeof(SceneDev) * nscenes) || cudaMalloc(&b->d_start, 8 * (nscenes + 1)) ||
@@ -269,7 +285,7 @@ mpm_status mpm_batch_destroy(mpm_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   free_graphs(b);
   for (void* p : {(void*)b->sA, (void*)b->sB, (void*)b->matA, (void*)b->matB, (void*)b->idA, (void*)b->idB,
-                  (void*)b->keys, (void*)b->stage, (void*)b->grid[0], (void*)b->grid[1], (void*)b->grid[2],
+                  (void*)b->keys, (void*)b->stage, (void*)b->grid[0], (void*)b->grid[1], (void*)b->grid[2], (void*)b->vgrid,
                   (void*)b->counts, (void*)b->block_sums, (void*)b->d_scenes, (void*)b->d_start, (void*)b->d_key_base,
                   (void*)b->d_ranges, (void*)b->boxes, (void*)b->work, (void*)b->status})
     cudaFree(p);
@@ -355,6 +371,7 @@ mpm_status mpm_batch_substep_graph(mpm_batch* b, int32_t nsteps) {
     for (int32_t i = 0; i < nsteps && st == MPM_OK; ++i) st = launch(b, kStepFused);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    const int64_t captured = b->launches - lc;
     // capturing recorded the work without running it: restore the host-side state
     b->cur = cur;
     b->parity = parity;
@@ -376,21 +393,20 @@ mpm_status mpm_batch_substep_graph(mpm_batch* b, int32_t nsteps) {
     e = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return bfail(b, MPM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    it = b->graphs.emplace(key, ge).first;
+    it = b->graphs.emplace(key, mpm_batch::Graph{ge, captured}).first;
   }
-  BCUDA(b, cudaGraphLaunch(it->second, b->stream));
+  BCUDA(b, cudaGraphLaunch(it->second.exec, b->stream));
+  b->launches += it->second.launches;
   // advance the host-side state exactly as the recorded work does
   if (sorting) {
     std::swap(b->sA, b->sB);
     std::swap(b->matA, b->matB);
     std::swap(b->idA, b->idB);
-    b->launches += 5;
   }
   b->cur = (int)((b->cur + nsteps) % 3);
   b->parity ^= (nsteps & 1);
   b->launch_index += nsteps;
   b->since_sort = nsteps;
-  b->launches += nsteps;
   return MPM_OK;
 }
 

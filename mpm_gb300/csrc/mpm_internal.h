@@ -13,7 +13,8 @@ namespace mpm {
 struct SceneDev {
   GridConsts g;
   DevMaterial m;  // every particle of a scene has the scene's material
-  int64_t grid_offset;
+  int64_t grid_offset;   // of the scene's grid in the pooled P2G grids
+  int64_t vgrid_offset;  // of the scene's padded velocity grid ((N + 5)^3 nodes) in the pool
 };
 
 constexpr int kBoxSlots = 6;  // per-scene P2G box slots (record / clear / reset rotate)
@@ -66,6 +67,10 @@ int64_t vgrid_nodes(int N);
 cudaError_t vgrid_bind(VelocityGrid& v, float4* ptr, int N);
 // Points a launch's arguments at a velocity grid.
 void set_vgrid(StepArgs& a, const VelocityGrid& v);
+// Velocity pass of a batch: for every scene, the grid op over the nodes of the P2G box
+// recorded in box slot `slot` (plus the stencil's 2 nodes), into the padded velocity grids.
+cudaError_t launch_batch_velocity(const float4* grid, float4* vgrid, const SceneDev* scenes, int nscenes,
+                                  const int* boxes, int slot, cudaStream_t st);
 
 enum StepKind { kStepP2GOnly = 0, kStepFused = 1, kStepG2POnly = 2 };
 

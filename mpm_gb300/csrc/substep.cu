@@ -34,7 +34,7 @@
 // per particle.
 //
 // Batches of scenes (batch.cu) use batch_step_kernel below: per-range scene constants,
-// a shared-memory tile staged with the grid op applied, sparse grid clearing.
+// a velocity pass over each scene's recorded P2G box, sparse grid clearing.
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -334,63 +334,67 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
 // Batch of scenes
 // ===========================================================================
 
-// Per-warp grid tile: the nodes [lo, hi + 2]^3 around a box of base cells, with the
-// grid op applied (grid velocity), zero outside the grid.  lo/hi are warp-uniform.
-struct TileBox {
-  int t0, t1, t2, d1, d2;
-};
-
-__device__ __forceinline__ bool box_fits(const int lo[3], const int hi[3], int cap) {
-  int64_t vol = 1;
-#pragma unroll
-  for (int dd = 0; dd < 3; ++dd) vol *= (hi[dd] >= lo[dd]) ? (int64_t)(hi[dd] + 3 - lo[dd]) : 0;
-  return vol <= cap;
-}
-
-__device__ __forceinline__ void warp_tile_build(float4* wtile, int lane, const int lo[3], const int hi[3],
-                                                const float4* grid_in, const GridConsts& K, TileBox& tb) {
-  int ext[3];
-#pragma unroll
-  for (int dd = 0; dd < 3; ++dd) ext[dd] = (hi[dd] >= lo[dd]) ? hi[dd] + 3 - lo[dd] : 0;
-  const int vol = ext[0] * ext[1] * ext[2];
-  const int N = K.N;
-  tb.t0 = lo[0];
-  tb.t1 = lo[1];
-  tb.t2 = lo[2];
-  tb.d1 = max(ext[1], 1);
-  tb.d2 = max(ext[2], 1);
-  const int d12 = tb.d1 * tb.d2;
-  __syncwarp();  // every lane is done with the previous tile
-  for (int idx = lane; idx < vol; idx += 32) {
-    const int i = tb.t0 + idx / d12;
-    const int rem = idx - (idx / d12) * d12;
-    const int j = tb.t1 + rem / tb.d2;
-    const int k = tb.t2 + rem - (rem / tb.d2) * tb.d2;
+// Velocity pass of a batch (blockIdx.y = scene): the grid op over the nodes of the
+// scene's last recorded P2G box, [lo, hi + 2] in each dimension (the stencils of the
+// particles whose P2G recorded it), zero where the node is outside the grid.
+__global__ void batch_velocity_kernel(const float4* __restrict__ grid, float4* __restrict__ vgrid,
+                                      const SceneDev* __restrict__ scenes, const int* __restrict__ boxes, int slot) {
+  const int sc = blockIdx.y;
+  const SceneDev& sd = scenes[sc];
+  const int N = sd.g.N, P = N + kPadLo + kPadHi;
+  const int* bx = boxes + ((int64_t)sc * kBoxSlots + slot) * 6;
+  const int l0 = max(bx[0], -kPadLo), l1 = max(bx[1], -kPadLo), l2 = max(bx[2], -kPadLo);
+  const int h0 = min(bx[3] + 2, N + kPadHi - 1), h1 = min(bx[4] + 2, N + kPadHi - 1),
+            h2 = min(bx[5] + 2, N + kPadHi - 1);
+  if (h0 < l0 || h1 < l1 || h2 < l2) return;
+  const int e1 = h1 - l1 + 1, e2 = h2 - l2 + 1;
+  const int64_t e12 = (int64_t)e1 * e2, vol = (int64_t)(h0 - l0 + 1) * e12;
+  const float4* g = grid + sd.grid_offset;
+  float4* vg = vgrid + sd.vgrid_offset;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < vol; q += (int64_t)gridDim.x * blockDim.x) {
+    const int di = (int)(q / e12);
+    const int rem = (int)(q - (int64_t)di * e12);
+    const int i = l0 + di, j = l1 + rem / e2, k = l2 + rem % e2;
     float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
     if ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N) {
-      const float3 vv = grid_node_velocity(grid_in[((int64_t)i * N + j) * N + k], i, j, k, K);
-      out = make_float4(vv.x, vv.y, vv.z, 0.f);
+      const float3 v = grid_node_velocity(g[((int64_t)i * N + j) * N + k], i, j, k, sd.g);
+      out = make_float4(v.x, v.y, v.z, 0.f);
     }
-    wtile[idx] = out;
+    vg[((int64_t)(i + kPadLo) * P + (j + kPadLo)) * P + (k + kPadLo)] = out;
   }
-  __syncwarp();
+}
+
+// G2P gather from a padded velocity grid through L1 (`base`: the node of the
+// particle's base cell), for the batch kernel; out of line to keep its loop small.
+static __device__ __noinline__ G2POut g2p_gather_padded(const float4* base, int P, float ddx, float dx_inv, float x0,
+                                                        float x1, float x2) {
+  const float x[3] = {x0, x1, x2};
+  float w[3][3], f[3];
+  int b[3];
+#pragma unroll
+  for (int dim = 0; dim < 3; ++dim)
+    QuadraticInterpolationKernel::weights_and_offset(x[dim], dx_inv, b[dim], w[dim], f[dim]);
+  auto node = [&](int a, int bb, int c) -> float4 { return __ldg(base + ((int64_t)a * P + bb) * P + c); };
+  G2POut o;
+  g2p_gather_f(node, ddx, w, f, o.v, o.C);
+  return o;
 }
 
 // Batched substep: ranges of the range table never cross a scene, so a warp loads its
-// scene's constants once per range.  The G2P tile of a window of steps is staged with
-// the grid op applied; each scene's P2G box is recorded so the grid it accumulated is
-// cleared sparsely two launches later.
+// scene's constants once per range.  G2P gathers the scene's velocity grid (written by
+// batch_velocity_kernel) through L1; each scene's P2G box is recorded so the grid it
+// accumulated is cleared sparsely two launches later and the next velocity pass covers it.
 template <bool G2P, bool P2G>
 __global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __grid_constant__ StepArgs A) {
   extern __shared__ float4 smem[];
+  __shared__ int cta_next;  // next CTA-local range index (ranges c, c + G, ... of CTA c)
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
-  float4* wtile = smem + warp * A.tile_cap;
-  float4* wbuf = smem + (G2P ? kStepWarps * A.tile_cap : 0) + warp * kRedFloat4;
+  float4* wbuf = smem + warp * kRedFloat4;
   float* __restrict__ s = A.s;
   const int64_t st = A.stride;
 
-  if (blockIdx.x == 0 && tid == 0) *A.work_next = 0;
+  if (tid == 0) cta_next = kStepWarps;
   // clear, per scene, the grid region the launch two substeps back accumulated (the
   // buffer this launch leaves for the next one to fill), then free its box slot
   for (int sc = blockIdx.x; sc < A.nscenes; sc += gridDim.x) {
@@ -411,9 +415,10 @@ __global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __gri
     }
     if (tid < 6) A.boxes[((int64_t)sc * kBoxSlots + A.box_reset) * 6 + tid] = (tid < 3) ? INT_MAX : INT_MIN;
   }
+  __syncthreads();
   const int64_t nranges = A.nranges;
-  const int64_t first_wave = (int64_t)gridDim.x * kStepWarps;
-  int64_t r = (int64_t)blockIdx.x * kStepWarps + warp;
+  const int G = (int)gridDim.x;
+  int64_t r = (int64_t)blockIdx.x + warp * G;
   while (r < nranges) {
     int claim = 0;
     const int4 rg = A.ranges[r];
@@ -423,12 +428,11 @@ __global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __gri
     const GridConsts K = sd.g;
     const int N = K.N;
     const DevMaterial& M = sd.m;
-    const float4* gin = A.grid_in ? A.grid_in + sd.grid_offset : nullptr;
     float4* gout = A.grid_out + sd.grid_offset;
+    const float4* vg = A.vgrid + sd.vgrid_offset;
+    const int P = N + kPadLo + kPadHi;
+    const float ddx = K.dinv * K.dx;
     int plo[3] = {INT_MAX, INT_MAX, INT_MAX}, phi[3] = {INT_MIN, INT_MIN, INT_MIN};
-    TileBox tb{0, 0, 0, 1, 1};
-    int64_t win_end = wbeg;
-    bool tile_ok = false;
 
     float nx0 = 0.f, nx1 = 0.f, nx2 = 0.f, nJ = 1.f;
     if (wbeg + lane < wend) {
@@ -438,45 +442,9 @@ __global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __gri
       nJ = s[kJp * st + wbeg + lane];
     }
     for (int64_t pb = wbeg; pb < wend; pb += 32) {
-      if (G2P && pb >= win_end) {
-        // grow a window of steps from pb while the union of their base-cell boxes fits
-        // the warp's tile, then stage the tile once for the whole window
-        int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
-        int64_t we = pb;
-        while (we < wend) {
-          const int64_t q = we + lane;
-          int slo[3] = {INT_MAX, INT_MAX, INT_MAX}, shi[3] = {INT_MIN, INT_MIN, INT_MIN};
-          if (q < wend) {
-            int bb[3];
-#pragma unroll
-            for (int dd = 0; dd < 3; ++dd)
-              bb[dd] = QuadraticInterpolationKernel::base_cell(s[(kX + dd) * st + q], K.dx_inv);
-            if (!outside_domain(bb[0], bb[1], bb[2], N)) {
-#pragma unroll
-              for (int dd = 0; dd < 3; ++dd) slo[dd] = shi[dd] = bb[dd];
-            }
-          }
-          int nlo[3], nhi[3];
-#pragma unroll
-          for (int dd = 0; dd < 3; ++dd) {
-            nlo[dd] = min(lo[dd], __reduce_min_sync(kFull, slo[dd]));
-            nhi[dd] = max(hi[dd], __reduce_max_sync(kFull, shi[dd]));
-          }
-          if (!box_fits(nlo, nhi, A.tile_cap)) break;
-#pragma unroll
-          for (int dd = 0; dd < 3; ++dd) {
-            lo[dd] = nlo[dd];
-            hi[dd] = nhi[dd];
-          }
-          we += 32;
-        }
-        tile_ok = we > pb;
-        win_end = tile_ok ? we : pb + 32;  // a step that alone does not fit gathers from global
-        if (tile_ok) warp_tile_build(wtile, lane, lo, hi, gin, K, tb);
-      }
       const int64_t p = pb + lane;
       const bool valid = p < wend;
-      if (pb + 32 >= wend && lane == 0) claim = atomicAdd(A.work, 1);
+      if (pb + 32 >= wend && lane == 0) claim = atomicAdd(&cta_next, 1);
       float x[3] = {nx0, nx1, nx2}, v[3] = {0.f, 0.f, 0.f}, Cm[3][3], F[3][3], Jp = nJ;
       if (p + 32 < wend) {
         nx0 = s[(kX + 0) * st + p + 32];
@@ -507,18 +475,15 @@ __global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __gri
       bool g2p_on = false;
       if (G2P && valid && !frozen) {
         int b[3];
-        float w[3][3], f[3];
-        stencil_f(x, K, b, w, f);
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd) b[dd] = QuadraticInterpolationKernel::base_cell(x[dd], K.dx_inv);
         g2p_on = !outside_domain(b[0], b[1], b[2], N);
         if (!g2p_on) {
           frozen = true;
-        } else if (tile_ok) {
-          const int t0 = ((b[0] - tb.t0) * tb.d1 + (b[1] - tb.t1)) * tb.d2 + (b[2] - tb.t2);
-          const int d12 = tb.d1 * tb.d2;
-          auto node = [&](int a, int bb, int c) -> float4 { return wtile[t0 + a * d12 + bb * tb.d2 + c]; };
-          g2p_gather_f(node, K.dinv * K.dx, w, f, v, Cm);
         } else {
-          const G2POut o = g2p_gather_global(gin, K, x[0], x[1], x[2]);
+          const G2POut o = g2p_gather_padded(
+              vg + ((int64_t)(b[0] + kPadLo) * P + (b[1] + kPadLo)) * P + (b[2] + kPadLo), P, ddx, K.dx_inv, x[0], x[1],
+              x[2]);
 #pragma unroll
           for (int r2 = 0; r2 < 3; ++r2) {
             v[r2] = o.v[r2];
@@ -564,7 +529,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __gri
         }
       }
     }
-    r = first_wave + __shfl_sync(kFull, claim, 0);
+    r = (int64_t)blockIdx.x + (int64_t)__shfl_sync(kFull, claim, 0) * G;
   }
 }
 
@@ -618,6 +583,13 @@ void set_vgrid(StepArgs& a, const VelocityGrid& v) {
   a.vmap = v.map;
 }
 
+cudaError_t launch_batch_velocity(const float4* grid, float4* vgrid, const SceneDev* scenes, int nscenes,
+                                  const int* boxes, int slot, cudaStream_t st) {
+  if (nscenes <= 0) return cudaSuccess;
+  batch_velocity_kernel<<<dim3(16, nscenes), kThreads, 0, st>>>(grid, vgrid, scenes, boxes, slot);
+  return cudaGetLastError();
+}
+
 template <bool LIQ, bool G2P, bool P2G, bool GUARD>
 static void* scene_kernel() {
   return (void*)scene_step_kernel<LIQ, G2P, P2G, GUARD>;
@@ -644,11 +616,7 @@ static void* select_kernel(StepKind kind, bool liquid, bool guard, bool batch) {
 
 size_t step_smem_bytes(StepKind kind, int tile_cap, bool batch) {
   size_t b = 0;
-  if (batch) {
-    if (kind != kStepP2GOnly) b += (size_t)kStepWarps * tile_cap * sizeof(float4);
-    if (kind != kStepG2POnly) b += (size_t)kStepWarps * kRedFloat4 * sizeof(float4);
-    return b;
-  }
+  if (batch) return (kind != kStepG2POnly) ? (size_t)kStepWarps * kRedFloat4 * sizeof(float4) : 16;
   if (kind != kStepP2GOnly) b += (size_t)kStepWarps * 2 * (kTileBytes + sizeof(uint64_t));
   if (kind != kStepG2POnly) b += (size_t)kStepWarps * kRedFloat4 * sizeof(float4);
   return b + 128;  // alignment of the TMA tiles

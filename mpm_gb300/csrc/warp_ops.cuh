@@ -185,26 +185,4 @@ struct G2POut {
   float C[3][3];
 };
 
-// Gather straight from the P2G grid (grid op per node) for chunks whose tile does
-// not fit in shared memory; out of line to keep the hot loop small.
-static __device__ __noinline__ G2POut g2p_gather_global(const float4* grid_in, const GridConsts& K, float x0, float x1,
-                                                 float x2) {
-  const int N = K.N;
-  const float x[3] = {x0, x1, x2};
-  int b[3];
-  float w[3][3], f[3];
-  stencil_f(x, K, b, w, f);
-  const int b0 = b[0], b1 = b[1], b2 = b[2];
-  auto node = [&](int a, int bb, int c) -> float4 {
-    const int i = b0 + a, j = b1 + bb, k = b2 + c;
-    if ((unsigned)i >= (unsigned)N || (unsigned)j >= (unsigned)N || (unsigned)k >= (unsigned)N)
-      return make_float4(0.f, 0.f, 0.f, 0.f);
-    const float3 v = grid_node_velocity(__ldg(grid_in + ((int64_t)i * N + j) * N + k), i, j, k, K);
-    return make_float4(v.x, v.y, v.z, 0.f);
-  };
-  G2POut o;
-  g2p_gather_f(node, K.dinv * K.dx, w, f, o.v, o.C);
-  return o;
-}
-
 }  // namespace mpm
