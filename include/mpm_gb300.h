@@ -137,6 +137,13 @@ mpm_status mpm_sort(mpm_ctx* ctx);
 int64_t mpm_particle_count(const mpm_ctx* ctx);
 /* Number of substeps advanced since the last upload. */
 int64_t mpm_substep_count(const mpm_ctx* ctx);
+/* Self-check of failure detection (no counterpart in the reference): one warp waits on
+ * an mbarrier that nothing completes, gives up after `polls` polls (1..2^20; each poll
+ * may suspend for a hardware-defined interval, microseconds at most) and sets the status
+ * word, exactly as the substep kernel does when a tile copy never lands.  Returns
+ * MPM_ERR_TIMEOUT (the expected outcome) through mpm_sync; the context stays usable. */
+mpm_status mpm_check_wait_timeout(mpm_ctx* ctx, int32_t polls);
+
 /* Copy the last error message (NUL-terminated, truncated to len). */
 mpm_status mpm_last_error(const mpm_ctx* ctx, char* buf, size_t len);
 /* Kernel launches issued by this context since creation (for accounting). */

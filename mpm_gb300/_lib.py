@@ -64,6 +64,7 @@ SIGNATURES = [
     ("mpm_download_aos", I32, [P, P]),
     ("mpm_get_grid", I32, [P, I32, P]),
     ("mpm_sort", I32, [P]),
+    ("mpm_check_wait_timeout", I32, [P, I32]),
     ("mpm_particle_count", I64, [P]),
     ("mpm_substep_count", I64, [P]),
     ("mpm_last_error", I32, [P, ctypes.c_char_p, ctypes.c_size_t]),

@@ -55,13 +55,16 @@ __device__ __forceinline__ void weight_derivs(float x, float dx_inv, float dw[3]
 
 __device__ __forceinline__ float ld(const float* s, int64_t st, int comp, int64_t p) { return s[comp * st + p]; }
 
-__global__ void adj_velocity_kernel(const float4* grid, float4* vgrid, GridConsts K) {
+// Grid velocities of substep n for the adjoint kernels; also clears the grid adjoint
+// that adj_g2p accumulates into.
+__global__ void adj_velocity_kernel(const float4* grid, float4* vgrid, float4* gadj, GridConsts K) {
   const int N = K.N;
   const int64_t cells = (int64_t)N * N * N;
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(c / ((int64_t)N * N)), j = (int)((c / N) % N), k = (int)(c % N);
     const float3 v = grid_node_velocity(grid[c], i, j, k, K);
     vgrid[c] = make_float4(v.x, v.y, v.z, 0.f);
+    gadj[c] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 
@@ -433,16 +436,18 @@ namespace {
 
 size_t state_floats(const mpm_diff* d) { return (size_t)kNumComps * d->stride; }
 
-mpm_status dlaunch(mpm_diff* d, StepKind kind, float* state, const float4* gin, float4* gout) {
+mpm_status dlaunch(mpm_diff* d, StepKind kind, float* state, const float4* gin, float4* gout,
+                   float4* gzero = nullptr, float* state_out = nullptr) {
   StepArgs a{};
   a.s = state;
+  a.s_out = state_out;
   a.stride = d->stride;
   a.mat = nullptr;
   a.id = d->id;
   a.n = d->n;
   a.grid_in = gin;
   a.grid_out = gout;
-  a.grid_zero = nullptr;
+  a.grid_zero = gzero;
   a.grid_cells = d->cells;
   set_vgrid(a, d->vel);
   a.status = d->status;
@@ -457,12 +462,12 @@ mpm_status dlaunch(mpm_diff* d, StepKind kind, float* state, const float4* gin, 
   return MPM_OK;
 }
 
-mpm_status forward_substep(mpm_diff* d, float* state, float4* grid) {
-  // P2G of state into `grid`, then G2P from it (in place): state_n -> state_{n+1}
-  if (cudaMemsetAsync(grid, 0, sizeof(float4) * d->cells, d->stream) != cudaSuccess) return MPM_ERR_CUDA;
-  mpm_status st = dlaunch(d, kStepP2GOnly, state, nullptr, grid);
+// One recomputed substep: P2G of `state` into `grid` (cleared beforehand), which also
+// clears `next_grid` for the following substep, then G2P from it into `state_out`.
+mpm_status forward_substep(mpm_diff* d, float* state, float* state_out, float4* grid, float4* next_grid) {
+  mpm_status st = dlaunch(d, kStepP2GOnly, state, nullptr, grid, next_grid);
   if (st != MPM_OK) return st;
-  return dlaunch(d, kStepG2POnly, state, grid, nullptr);
+  return dlaunch(d, kStepG2POnly, state, grid, nullptr, nullptr, state_out);
 }
 
 int adj_blocks(const mpm_diff* d) {
@@ -646,11 +651,12 @@ mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv
     const int s0 = sgi * d->ckpt_every;
     const int len = std::min(d->ckpt_every, d->nsteps - s0);
     // recompute the segment, keeping every state and P2G grid
-    if (cudaMemcpyAsync(d->seg, d->ckpt + sf * sgi, sb, cudaMemcpyDeviceToDevice, s)) return MPM_ERR_CUDA;
+    if (cudaMemcpyAsync(d->seg, d->ckpt + sf * sgi, sb, cudaMemcpyDeviceToDevice, s) ||
+        cudaMemsetAsync(d->seg_grid, 0, sizeof(float4) * d->cells, s))
+      return MPM_ERR_CUDA;
     for (int j = 0; j < len; ++j) {
-      if (cudaMemcpyAsync(d->seg + sf * (j + 1), d->seg + sf * j, sb, cudaMemcpyDeviceToDevice, s))
-        return MPM_ERR_CUDA;
-      mpm_status st = forward_substep(d, d->seg + sf * (j + 1), d->seg_grid + d->cells * j);
+      mpm_status st = forward_substep(d, d->seg + sf * j, d->seg + sf * (j + 1), d->seg_grid + d->cells * j,
+                                      j + 1 < len ? d->seg_grid + d->cells * (j + 1) : nullptr);
       if (st != MPM_OK) return st;
     }
     // adjoint substeps in reverse
@@ -658,8 +664,7 @@ mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv
       A.s = d->seg + sf * j;
       A.s1 = d->seg + sf * (j + 1);
       A.grid = d->seg_grid + d->cells * j;
-      adj_velocity_kernel<<<gblocks, 256, 0, s>>>(A.grid, d->vgrid, A.K);
-      if (cudaMemsetAsync(d->gadj, 0, sizeof(float4) * d->cells, s)) return MPM_ERR_CUDA;
+      adj_velocity_kernel<<<gblocks, 256, 0, s>>>(A.grid, d->vgrid, d->gadj, A.K);
       adj_g2p_kernel<<<blocks, kAdjThreads, smem, s>>>(A);
       adj_gridop_kernel<<<gblocks, 256, 0, s>>>(A.grid, d->gadj, A.K);
       adj_p2g_kernel<<<blocks, kAdjThreads, 0, s>>>(A);

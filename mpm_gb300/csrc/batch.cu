@@ -243,7 +243,7 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
   b->nranges = (int)ranges.size();
   for (int k = 0; k < 2; ++k) {
     const StepKind kind = k ? kStepFused : kStepP2GOnly;
-    const int bps = step_blocks_per_sm(kind, false, false, step_smem_bytes(kind, 0, true), true);
+    const int bps = step_blocks_per_sm(kind, false, false, step_smem_bytes(kind, true), true);
     const int blocks = std::max(1, std::min((b->nranges + kStepWarps - 1) / kStepWarps, b->num_sms * bps));
     (k ? b->blocks_fused : b->blocks_p2g) = blocks;
   }

@@ -276,7 +276,7 @@ void make_dev_material(const mpm_material& m, DevMaterial& d) {
 // faster with 1-step than with 2-step ranges).
 void step_launch_shape(int num_sms, int64_t n, bool liquid, bool guard, StepKind kind, int steps_per_warp,
                        int& chunk, int& blocks) {
-  const size_t smem = step_smem_bytes(kind, 0, false);
+  const size_t smem = step_smem_bytes(kind, false);
   const int bps = step_blocks_per_sm(kind, liquid, guard, smem);
   const int64_t resident_warps = (int64_t)num_sms * bps * kStepWarps;
   int64_t steps = steps_per_warp;
@@ -585,6 +585,13 @@ mpm_status mpm_get_grid(mpm_ctx* c, int32_t which, float* out) {
   }
   MPM_CUDA(c, cudaStreamSynchronize(c->stream));
   return MPM_OK;
+}
+
+mpm_status mpm_check_wait_timeout(mpm_ctx* c, int32_t polls) {
+  if (!c || polls < 1 || polls > (1 << 20)) return MPM_ERR_INVALID;
+  MPM_CUDA(c, launch_wait_timeout_probe(c->status, polls, c->stream));
+  c->launches += 1;
+  return mpm_sync(c);
 }
 
 mpm_status mpm_sort(mpm_ctx* c) {

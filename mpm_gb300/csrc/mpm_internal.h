@@ -24,6 +24,7 @@ constexpr int kBoxSlots = 6;  // per-scene P2G box slots (record / clear / reset
 // clearing grid_zero (the grid substep n-1 read), so the three grid buffers rotate.
 struct StepArgs {
   float* s;               // component-major particle state
+  float* s_out;           // G2P-only launches: where the updated state goes (null: in place)
   int64_t stride;         // component stride (elements)
   const uint8_t* mat;     // material index per particle (general layout), may be null
   const uint32_t* id;     // original particle index (for the G2P guard)
@@ -33,7 +34,6 @@ struct StepArgs {
   float4* grid_zero;      // buffer to clear for the launch after next
   int64_t grid_cells;
   int chunk;              // particles per range (multiple of 32); ranges go to warps dynamically
-  int tile_cap;           // capacity of the shared-memory velocity tile (nodes)
   int64_t guard_limit;    // G2P only for id <= guard_limit when the guard is on
   int check_finite;
   int* status;
@@ -67,6 +67,8 @@ int64_t vgrid_nodes(int N);
 cudaError_t vgrid_bind(VelocityGrid& v, float4* ptr, int N);
 // Points a launch's arguments at a velocity grid.
 void set_vgrid(StepArgs& a, const VelocityGrid& v);
+// One warp waiting `polls` times on an mbarrier nothing arrives on; sets kStatusTimeout.
+cudaError_t launch_wait_timeout_probe(int* status, int polls, cudaStream_t st);
 // Velocity pass of a batch: for every scene, the grid op over the nodes of the P2G box
 // recorded in box slot `slot` (plus the stencil's 2 nodes), into the padded velocity grids.
 cudaError_t launch_batch_velocity(const float4* grid, float4* vgrid, const SceneDev* scenes, int nscenes,
@@ -80,7 +82,7 @@ enum StepKind { kStepP2GOnly = 0, kStepFused = 1, kStepG2POnly = 2 };
 cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guard, int grid_blocks,
                         cudaStream_t st, int64_t* launches = nullptr);
 // Dynamic shared memory of a variant: G2P tiles + per-warp P2G reduction buffers.
-size_t step_smem_bytes(StepKind kind, int tile_cap, bool batch);
+size_t step_smem_bytes(StepKind kind, bool batch);
 // Max resident CTAs per SM for the variant at the given dynamic shared memory.
 int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem, bool batch = false);
 

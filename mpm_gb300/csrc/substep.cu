@@ -178,6 +178,8 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
   const int N = K.N;
   const float ddx = K.dinv * K.dx;  // D dx of the node-offset gather
   float* __restrict__ s = A.s;
+  // a G2P-only launch may write the new state out of place (the adjoint's recompute)
+  float* const s_w = (!P2G && A.s_out) ? A.s_out : s;
   const int64_t st = A.stride;
   const int64_t n = A.n, chunk = A.chunk;
 
@@ -290,7 +292,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
       }
       if (g2p_on) {
         particle_update<LIQ>(M, K, x, v, Cm, F, Jp, have_uv, Usv, Vsv);
-        store_particle<LIQ>(s, st, p, x, v, Cm, F, Jp);
+        store_particle<LIQ>(s_w, st, p, x, v, Cm, F, Jp);
         if (A.check_finite && !isfinite(x[0] + x[1] + x[2] + v[0] + v[1] + v[2])) atomicOr(A.status, kStatusNonFinite);
       }
       // ---- P2G of the next substep (particleToGrid)
@@ -590,6 +592,24 @@ cudaError_t launch_batch_velocity(const float4* grid, float4* vgrid, const Scene
   return cudaGetLastError();
 }
 
+// Self-check of the bounded-wait path: one warp waits on an mbarrier that nothing
+// arrives on, gives up after `polls` polls and reports kStatusTimeout, as the substep
+// kernel does when a tile copy never completes.
+__global__ void wait_timeout_probe(int* status, int polls) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  __syncwarp();
+  if (!mbar_wait(&bar, 0u, polls) && threadIdx.x == 0) atomicOr(status, kStatusTimeout);
+}
+
+cudaError_t launch_wait_timeout_probe(int* status, int polls, cudaStream_t st) {
+  wait_timeout_probe<<<1, 32, 0, st>>>(status, polls);
+  return cudaGetLastError();
+}
+
 template <bool LIQ, bool G2P, bool P2G, bool GUARD>
 static void* scene_kernel() {
   return (void*)scene_step_kernel<LIQ, G2P, P2G, GUARD>;
@@ -614,7 +634,7 @@ static void* select_kernel(StepKind kind, bool liquid, bool guard, bool batch) {
   return nullptr;
 }
 
-size_t step_smem_bytes(StepKind kind, int tile_cap, bool batch) {
+size_t step_smem_bytes(StepKind kind, bool batch) {
   size_t b = 0;
   if (batch) return (kind != kStepG2POnly) ? (size_t)kStepWarps * kRedFloat4 * sizeof(float4) : 16;
   if (kind != kStepP2GOnly) b += (size_t)kStepWarps * 2 * (kTileBytes + sizeof(uint64_t));
@@ -626,7 +646,7 @@ cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guar
                         int64_t* launches) {
   const bool batch = a.nscenes > 0;
   void* fn = select_kernel(kind, liquid, guard, batch);
-  const size_t smem = step_smem_bytes(kind, a.tile_cap, batch);
+  const size_t smem = step_smem_bytes(kind, batch);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if (!batch && kind != kStepP2GOnly) {

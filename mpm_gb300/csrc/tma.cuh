@@ -43,8 +43,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait for the phase with the given parity; false if it never completed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int i = 0; i < kMaxBarrierPolls; ++i)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int max_polls = kMaxBarrierPolls) {
+  for (int i = 0; i < max_polls; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
