@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="liquid", choices=["liquid", "snow", "elastic", "batched", "differentiable"])
+    ap.add_argument("--config", default="liquid",
+                    choices=["liquid", "snow", "elastic", "batched", "differentiable", "seeding"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -499,6 +500,83 @@ def run_differentiable(args):
     print(json.dumps(line), flush=True)
 
 
+def run_seeding(args):
+    """Scene objects: GPU rejection sampling of a closed triangle mesh (an icosphere of
+    20 x 4^4 triangles, size 0.5) at 2e7 candidates per unit volume, through
+    mpm_add_object (seeding plus the append into the context); the oracle's restatement
+    seeds a bounded sample of the same object on one host thread."""
+    from mpm_gb300 import build
+
+    build.build()
+    import torch
+
+    import oracle
+    from mpm_gb300 import _lib
+    from mpm_gb300 import materials as M
+    from mpm_gb300.scene_file import SceneObject
+    from mpm_gb300.simulation import Simulation
+
+    V, F = _icosphere(4)
+    dens = 20_000_000
+    obj = SceneObject(shape=_lib.SHAPE_MESH, size=0.5, position=(0.25, 0.25, 0.25), vertices=V, triangles=F)
+    times, count = [], 0
+    for k in range(max(args.warmup, 1) + max(1, min(args.steps, 10))):
+        sim = Simulation(dt=1e-4, N=64, materials=[M.elastic(1.0 / dens)])
+        obj.seed = k
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        count = sim.add_object(obj)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        sim.close()
+        if k >= max(args.warmup, 1):
+            times.append(t1 - t0)
+    dt_s = statistics.median(times)
+    cand = int(dens * 0.5 ** 3)
+    # oracle: one host thread on a bounded sample (same object, smaller density)
+    sdens = 400_000
+    t0 = time.perf_counter()
+    xs = oracle.seed_object(_lib.SHAPE_MESH, 0.5, (0.25, 0.25, 0.25), seed=0, density=sdens, vertices=V, triangles=F)
+    cpu_s = time.perf_counter() - t0
+    line = {"metric": "seeded particles/s", "value": count / dt_s, "unit": "particles/s", "n_gpus": 1,
+            "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * dt_s, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 tests, f32 positions", "data": "synthetic",
+            "config": {"workload": "seed_icosphere_5120tri_2e7", "candidates": cand, "particles": count,
+                       "triangles": int(F.shape[0])},
+            "cpu_baseline": {"value": len(xs) / cpu_s, "unit": "particles/s", "cores": 1, "kind": "port",
+                             "sample": f"{len(xs)} particles of the same object at density {sdens} (oracle, "
+                                       f"all triangles per candidate, {cpu_s:.1f} s)"},
+            "timing": "wall clock around mpm_add_object (GPU seeding, count readback, append)"}
+    print(json.dumps(line), flush=True)
+
+
+def _icosphere(subdivisions):
+    t = (1.0 + 5 ** 0.5) / 2.0
+    V = [[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+         [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]]
+    F = [[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2], [10, 7, 6],
+         [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5], [2, 4, 11], [6, 2, 10],
+         [8, 6, 7], [9, 8, 1]]
+    V = [np.asarray(v, np.float64) / np.linalg.norm(v) for v in V]
+    for _ in range(subdivisions):
+        mid = {}
+
+        def midpoint(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                m = (V[a] + V[b]) / 2.0
+                V.append(m / np.linalg.norm(m))
+                mid[key] = len(V) - 1
+            return mid[key]
+
+        nf = []
+        for a, b, c in F:
+            ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+            nf += [[a, ab, ca], [b, bc, ab], [c, ca, bc], [ab, bc, ca]]
+        F = nf
+    return np.asarray(V, np.float32), np.asarray(F, np.int32)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -507,6 +585,8 @@ def main():
         run_batched(args)
     elif args.config == "differentiable":
         run_differentiable(args)
+    elif args.config == "seeding":
+        run_seeding(args)
     else:
         run_ours(args)
 

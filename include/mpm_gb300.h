@@ -137,6 +137,53 @@ mpm_status mpm_sort(mpm_ctx* ctx);
 int64_t mpm_particle_count(const mpm_ctx* ctx);
 /* Number of substeps advanced since the last upload. */
 int64_t mpm_substep_count(const mpm_ctx* ctx);
+/* ---------------------------------------------------------------------------
+ * Scene objects: Simulation::addObject (src/mpm.cu:237-251) with the particle seeding of
+ * Simulation::addParticles (src/mpm.cu:346-394).  An object is a shape scaled so that the
+ * longest edge of its bounding box is `size`, with the box's lowest corner at `position`
+ * (Simulation::loadMesh, src/mpm.cu:330-344).  Its particles are seeded on the GPU by
+ * rejection sampling: u32(density x bounding-box volume) candidates uniform in the box,
+ * kept when inside the shape, density = u32(1 / particle_volume) of the object's material.
+ * The reference draws candidates with rand() and tests meshes with libigl's winding
+ * number; here candidate i comes from a SplitMix64 hash of (seed, i), so seeding is
+ * reproducible, and closed meshes are tested by +x ray parity.  Seeded particles start
+ * with the object's velocity, C = 0, F = I and Jp = 1.
+ * An object is active for lifetime_begin <= t < lifetime_end (SimObject::isActive,
+ * include/mpm.cuh:36-38): mpm_add_object appends it at once when active at the current
+ * t, and mpm_substep appends and removes objects at substep boundaries.  Downloads list
+ * uploaded particles first, then active objects in activation order.
+ * ------------------------------------------------------------------------- */
+enum { MPM_SHAPE_BOX = 0, MPM_SHAPE_SPHERE = 1, MPM_SHAPE_MESH = 2 };
+
+typedef struct mpm_object {
+  int32_t shape;             /* MPM_SHAPE_* */
+  int32_t material;          /* index into the context's material table */
+  float size;                /* longest edge of the bounding box */
+  float position[3];         /* lowest corner of the bounding box */
+  float velocity[3];         /* initial velocity of every particle */
+  float box_extent[3];       /* BOX: edge lengths relative to each other ({1,1,1}: a cube) */
+  double lifetime_begin;     /* active from this time on (0: from the start) */
+  double lifetime_end;       /* inactive from this time on (e.g. 1e300: never) */
+  uint64_t seed;             /* seeding stream */
+  const float* vertices;     /* MESH: 3 floats per vertex, any scale (host memory) */
+  int64_t n_vertices;
+  const int32_t* triangles;  /* MESH: 3 vertex indices per triangle of a closed mesh */
+  int64_t n_triangles;
+} mpm_object;
+
+/* Seed an object's particles on the GPU and add it to the scene; *n_particles (may be
+ * NULL) receives its particle count.  Removes nothing: objects live until the context is
+ * destroyed or particles are uploaded again (an upload forgets all objects). */
+mpm_status mpm_add_object(mpm_ctx* ctx, const mpm_object* object, int64_t* n_particles);
+/* Simulated time: dt summed over the substeps run since the last upload (or creation). */
+double mpm_time(const mpm_ctx* ctx);
+/* Objects added (active or not). */
+int32_t mpm_object_count(const mpm_ctx* ctx);
+/* Seeding alone, for tools and tests: the object's particle positions at `density`
+ * candidates per unit volume, 3 floats per particle in candidate order, into host x
+ * (room for `capacity` particles); *n receives the count, which may exceed capacity. */
+mpm_status mpm_seed_object(const mpm_object* object, uint32_t density, float* x, int64_t capacity, int64_t* n);
+
 /* Self-check of failure detection (no counterpart in the reference): one warp waits on
  * an mbarrier that nothing completes, gives up after `polls` polls (1..2^20; each poll
  * may suspend for a hardware-defined interval, microseconds at most) and sets the status

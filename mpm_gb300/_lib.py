@@ -47,6 +47,27 @@ class MpmScene(ctypes.Structure):
     _fields_ = [("params", MpmParams), ("material", MpmMaterial), ("count", ctypes.c_int64)]
 
 
+SHAPE_BOX, SHAPE_SPHERE, SHAPE_MESH = 0, 1, 2
+
+
+class MpmObject(ctypes.Structure):
+    _fields_ = [
+        ("shape", ctypes.c_int32),
+        ("material", ctypes.c_int32),
+        ("size", ctypes.c_float),
+        ("position", ctypes.c_float * 3),
+        ("velocity", ctypes.c_float * 3),
+        ("box_extent", ctypes.c_float * 3),
+        ("lifetime_begin", ctypes.c_double),
+        ("lifetime_end", ctypes.c_double),
+        ("seed", ctypes.c_uint64),
+        ("vertices", ctypes.c_void_p),
+        ("n_vertices", ctypes.c_int64),
+        ("triangles", ctypes.c_void_p),
+        ("n_triangles", ctypes.c_int64),
+    ]
+
+
 # (name, restype, argtypes) for every entry point of include/mpm_gb300.h
 P = ctypes.c_void_p
 I32, I64 = ctypes.c_int32, ctypes.c_int64
@@ -65,6 +86,10 @@ SIGNATURES = [
     ("mpm_get_grid", I32, [P, I32, P]),
     ("mpm_sort", I32, [P]),
     ("mpm_check_wait_timeout", I32, [P, I32]),
+    ("mpm_add_object", I32, [P, ctypes.POINTER(MpmObject), ctypes.POINTER(I64)]),
+    ("mpm_time", ctypes.c_double, [P]),
+    ("mpm_object_count", I32, [P]),
+    ("mpm_seed_object", I32, [ctypes.POINTER(MpmObject), ctypes.c_uint32, P, I64, ctypes.POINTER(I64)]),
     ("mpm_particle_count", I64, [P]),
     ("mpm_substep_count", I64, [P]),
     ("mpm_last_error", I32, [P, ctypes.c_char_p, ctypes.c_size_t]),

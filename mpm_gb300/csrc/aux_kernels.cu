@@ -352,6 +352,91 @@ __global__ void grid_op_kernel(const float4* in, float4* out, GridConsts K) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Scene objects joining or leaving a context: appending seeded particles and removing
+// the particles of a retired object (an id range) by compaction.
+// ---------------------------------------------------------------------------
+__global__ void append_object_kernel(float* s, int64_t st, int64_t n0, int64_t k, const float* xs, float vx, float vy,
+                                     float vz, int liquid, uint8_t* mat, uint8_t mat_index, uint32_t* id,
+                                     uint32_t id0) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < k; p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = n0 + p;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) s[(kX + d) * st + q] = xs[3 * p + d];
+    s[(kV + 0) * st + q] = vx;
+    s[(kV + 1) * st + q] = vy;
+    s[(kV + 2) * st + q] = vz;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) s[(kC + i) * st + q] = 0.f;
+    if (!liquid) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) s[(kF + i) * st + q] = (i % 4 == 0) ? 1.f : 0.f;
+    }
+    s[kJp * st + q] = 1.f;
+    if (mat) mat[q] = mat_index;
+    id[q] = id0 + (uint32_t)p;
+  }
+}
+
+__global__ void keep_flags_kernel(const uint32_t* id, int64_t n, uint32_t lo, uint32_t hi, int* flags) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p <= n; p += (int64_t)gridDim.x * blockDim.x)
+    flags[p] = (p < n && (id[p] < lo || id[p] >= hi)) ? 1 : 0;
+}
+
+template <bool LIQ>
+__global__ void compact_kernel(const float* __restrict__ sA, float* __restrict__ sB, int64_t st, int64_t n,
+                               const int* __restrict__ pos, const uint32_t* idA, uint32_t* idB, const uint8_t* matA,
+                               uint8_t* matB, uint32_t lo, uint32_t hi) {
+  constexpr int NC = LIQ ? kLiquidComps : kNumComps;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t i = idA[p];
+    if (i >= lo && i < hi) continue;
+    const int64_t q = pos[p];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) sB[moved_comp<LIQ>(c) * st + q] = sA[moved_comp<LIQ>(c) * st + p];
+    idB[q] = i >= hi ? i - (hi - lo) : i;
+    if (matA) matB[q] = matA[p];
+  }
+}
+
+cudaError_t launch_append_object(float* s, int64_t st, int64_t n0, int64_t k, const float* xs, const float v[3],
+                                 bool liquid, uint8_t* mat, uint8_t mat_index, uint32_t* id, uint32_t id0,
+                                 cudaStream_t stream) {
+  if (k <= 0) return cudaSuccess;
+  const int blocks = (int)std::min<int64_t>((k + kThreads - 1) / kThreads, 4096);
+  append_object_kernel<<<blocks, kThreads, 0, stream>>>(s, st, n0, k, xs, v[0], v[1], v[2], liquid ? 1 : 0, mat,
+                                                          mat_index, id, id0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_remove_ids(const float* sA, float* sB, int64_t st, int64_t n, const uint32_t* idA, uint32_t* idB,
+                              const uint8_t* matA, uint8_t* matB, uint32_t lo, uint32_t hi, bool liquid, int* flags,
+                              int* scratch, cudaStream_t stream, int64_t* launches) {
+  const int blocks = (int)std::min<int64_t>((n + kThreads) / kThreads, 4096);
+  keep_flags_kernel<<<blocks, kThreads, 0, stream>>>(idA, n, lo, hi, flags);
+  cudaError_t e = launch_exclusive_scan(flags, n + 1, scratch, stream, launches);
+  if (e != cudaSuccess) return e;
+  if (liquid)
+    compact_kernel<true><<<blocks, kThreads, 0, stream>>>(sA, sB, st, n, flags, idA, idB, matA, matB, lo, hi);
+  else
+    compact_kernel<false><<<blocks, kThreads, 0, stream>>>(sA, sB, st, n, flags, idA, idB, matA, matB, lo, hi);
+  if (launches) *launches += 2;
+  return cudaGetLastError();
+}
+
+int64_t scan_scratch_ints(int64_t m) { return (m + kThreads * kScanItems - 1) / (kThreads * kScanItems) + 1; }
+
+cudaError_t launch_exclusive_scan(int* data, int64_t m, int* scratch, cudaStream_t st, int64_t* launches) {
+  if (m <= 0) return cudaSuccess;
+  const int per = kThreads * kScanItems;
+  const int nb = (int)((m + per - 1) / per);
+  scan_blocks<<<nb, kThreads, 0, st>>>(data, m, scratch);
+  scan_block_sums<<<1, kThreads, 0, st>>>(scratch, nb);
+  scan_add<<<nb, kThreads, 0, st>>>(data, m, scratch);
+  if (launches) *launches += 3;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_grid_op(const float4* in, float4* out, GridConsts K, cudaStream_t st) {
   const int64_t cells = (int64_t)K.N * K.N * K.N;
   grid_op_kernel<<<grid_for(cells), 256, 0, st>>>(in, out, K);

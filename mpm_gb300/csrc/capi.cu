@@ -13,8 +13,19 @@
 
 #include "mpm_gb300.h"
 #include "mpm_internal.h"
+#include "seeding.h"
 
 using namespace mpm;
+
+// A scene object: its seeded particle positions (device) and, while active, the id range
+// its particles hold in the context.
+struct ObjectRec {
+  mpm_object desc{};  // host mesh pointers are not kept
+  float* d_x = nullptr;
+  int64_t count = 0;
+  bool active = false;
+  uint32_t id0 = 0;
+};
 
 struct mpm_ctx {
   mpm_params params{};
@@ -65,6 +76,9 @@ struct mpm_ctx {
   int64_t launches = 0;
   int steps_per_warp = 2;
   std::string last_error;
+
+  double t = 0.0;  // simulated time (Simulation::t)
+  std::vector<ObjectRec> objects;
 };
 
 namespace {
@@ -154,6 +168,115 @@ mpm_status ensure_particles(mpm_ctx* c, int64_t n) {
   MPM_CUDA(c, cudaMalloc(&c->keys, sizeof(uint32_t) * cap));
   c->capacity = cap;
   c->stride = cap;
+  return MPM_OK;
+}
+
+// Grows the particle arrays to hold `need` particles, keeping the current ones.
+mpm_status grow_particles(mpm_ctx* c, int64_t need) {
+  if (need <= c->capacity && c->sA) return MPM_OK;
+  if (!c->sA || c->n == 0) return ensure_particles(c, need);
+  const int64_t cap = std::max<int64_t>((need + 63) / 64 * 64, 2 * c->capacity);
+  const size_t fbytes = sizeof(float) * (size_t)kNumComps * cap;
+  float *sA = nullptr, *sB = nullptr;
+  uint8_t *mA = nullptr, *mB = nullptr;
+  uint32_t *iA = nullptr, *iB = nullptr, *keys = nullptr;
+  auto undo = [&]() {
+    for (void* p : {(void*)sA, (void*)sB, (void*)mA, (void*)mB, (void*)iA, (void*)iB, (void*)keys}) cudaFree(p);
+    return fail(c, MPM_ERR_NOMEM, "cannot grow the particle arrays");
+  };
+  if (cudaMalloc(&sA, fbytes) || cudaMalloc(&sB, fbytes) || cudaMalloc(&mA, cap) || cudaMalloc(&mB, cap) ||
+      cudaMalloc(&iA, sizeof(uint32_t) * cap) || cudaMalloc(&iB, sizeof(uint32_t) * cap) ||
+      cudaMalloc(&keys, sizeof(uint32_t) * cap))
+    return undo();
+  for (int k = 0; k < kNumComps; ++k)
+    MPM_CUDA(c, cudaMemcpyAsync(sA + (size_t)k * cap, c->sA + (size_t)k * c->stride, sizeof(float) * c->n,
+                                cudaMemcpyDeviceToDevice, c->stream));
+  MPM_CUDA(c, cudaMemcpyAsync(mA, c->matA, c->n, cudaMemcpyDeviceToDevice, c->stream));
+  MPM_CUDA(c, cudaMemcpyAsync(iA, c->idA, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToDevice, c->stream));
+  MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+  free_particles(c);
+  c->sA = sA;
+  c->sB = sB;
+  c->matA = mA;
+  c->matB = mB;
+  c->idA = iA;
+  c->idB = iB;
+  c->keys = keys;
+  c->capacity = c->stride = cap;
+  return MPM_OK;
+}
+
+void free_objects(mpm_ctx* c) {
+  for (auto& o : c->objects) cudaFree(o.d_x);
+  c->objects.clear();
+}
+
+// The particle set changed: the next substep re-sorts and restarts with a P2G launch.
+void particles_changed(mpm_ctx* c) {
+  c->pending = false;
+  c->since_sort = c->params.sort_interval;
+}
+
+mpm_status activate_object(mpm_ctx* c, ObjectRec& o) {
+  const int64_t k = o.count;
+  if (k > 0) {
+    if (c->n + k > (int64_t)0xffffffffLL) return fail(c, MPM_ERR_INVALID, "too many particles");
+    mpm_status st = grow_particles(c, c->n + k);
+    if (st != MPM_OK) return st;
+    const uint8_t mi = (uint8_t)o.desc.material;
+    if (!c->liquid_layout && mi != 0 && !c->have_mat) {
+      if (c->n > 0) MPM_CUDA(c, cudaMemsetAsync(c->matA, 0, c->n, c->stream));
+      c->have_mat = true;
+    }
+    MPM_CUDA(c, launch_append_object(c->sA, c->stride, c->n, k, o.d_x, o.desc.velocity, c->liquid_layout,
+                                     c->have_mat ? c->matA : nullptr, mi, c->idA, (uint32_t)c->n, c->stream));
+    c->launches += 1;
+    o.id0 = (uint32_t)c->n;
+    c->n += k;
+    particles_changed(c);
+  }
+  o.active = true;
+  return MPM_OK;
+}
+
+mpm_status retire_object(mpm_ctx* c, ObjectRec& o) {
+  const int64_t k = o.count;
+  if (k > 0) {
+    const int64_t n = c->n;
+    int* flags = nullptr;
+    int* scratch = nullptr;
+    if (cudaMalloc(&flags, sizeof(int) * (n + 1)) || cudaMalloc(&scratch, sizeof(int) * scan_scratch_ints(n + 1))) {
+      cudaFree(flags);
+      return fail(c, MPM_ERR_NOMEM, "cannot allocate the compaction scratch");
+    }
+    const uint32_t lo = o.id0, hi = o.id0 + (uint32_t)k;
+    cudaError_t e = launch_remove_ids(c->sA, c->sB, c->stride, n, c->idA, c->idB, c->have_mat ? c->matA : nullptr,
+                                      c->matB, lo, hi, c->liquid_layout, flags, scratch, c->stream, &c->launches);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(flags);
+    cudaFree(scratch);
+    if (e != cudaSuccess) return fail(c, MPM_ERR_CUDA, std::string("object removal: ") + cudaGetErrorString(e));
+    std::swap(c->sA, c->sB);
+    std::swap(c->matA, c->matB);
+    std::swap(c->idA, c->idB);
+    c->n = n - k;
+    for (auto& other : c->objects)
+      if (other.active && other.id0 > lo) other.id0 -= (uint32_t)k;
+    particles_changed(c);
+  }
+  o.active = false;
+  return MPM_OK;
+}
+
+// SimObject::isActive (include/mpm.cuh:36-38) at the current time, for every object.
+mpm_status update_objects(mpm_ctx* c) {
+  for (auto& o : c->objects) {
+    const bool want = c->t >= o.desc.lifetime_begin && c->t < o.desc.lifetime_end;
+    mpm_status st = MPM_OK;
+    if (want && !o.active) st = activate_object(c, o);
+    if (!want && o.active) st = retire_object(c, o);
+    if (st != MPM_OK) return st;
+  }
   return MPM_OK;
 }
 
@@ -338,6 +461,7 @@ mpm_status mpm_create(const mpm_params* params, mpm_ctx** out) {
 mpm_status mpm_destroy(mpm_ctx* c) {
   if (!c) return MPM_ERR_INVALID;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  free_objects(c);
   free_particles(c);
   for (auto& g : c->grid) cudaFree(g);
   cudaFree(c->vgrid_mem);
@@ -406,6 +530,8 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   c->prev = -1;
   c->substeps = 0;
   c->since_sort = c->params.sort_interval;  // sort before the first substep
+  c->t = 0.0;
+  free_objects(c);
   if (n == 0) return MPM_OK;
   const size_t per = 25 * sizeof(float);
   st = ensure_stage(c, per * (size_t)n);
@@ -476,6 +602,10 @@ mpm_status mpm_substep(mpm_ctx* c, int32_t nsteps) {
   if (st != MPM_OK) return st;
   if (nsteps < 0) return fail(c, MPM_ERR_INVALID, "nsteps must be >= 0");
   for (int32_t i = 0; i < nsteps; ++i) {
+    if (!c->objects.empty()) {
+      st = update_objects(c);
+      if (st != MPM_OK) return st;
+    }
     if (c->n > 0) {
       if (c->params.sort_interval > 0 && c->since_sort >= c->params.sort_interval) {
         st = run_sort(c);
@@ -490,7 +620,54 @@ mpm_status mpm_substep(mpm_ctx* c, int32_t nsteps) {
     }
     c->substeps += 1;
     c->since_sort += 1;
+    c->t += c->params.dt;  // Simulation::advance, src/mpm.cu:328
   }
+  return MPM_OK;
+}
+
+mpm_status mpm_add_object(mpm_ctx* c, const mpm_object* obj, int64_t* n_particles) {
+  mpm_status st = check_ready(c);
+  if (st != MPM_OK) return st;
+  if (!obj) return fail(c, MPM_ERR_INVALID, "object is NULL");
+  if (obj->material < 0 || obj->material >= c->n_materials)
+    return fail(c, MPM_ERR_INVALID, "object material index out of range");
+  if (!(obj->lifetime_end > obj->lifetime_begin)) return fail(c, MPM_ERR_INVALID, "empty object lifetime");
+  // density = u32(1.0 / particleVolume) (Simulation::addObject, src/mpm.cu:247)
+  const double dens = 1.0 / (double)c->mats[obj->material].particle_volume;
+  if (!(dens >= 1.0) || dens > 4294967295.0) return fail(c, MPM_ERR_INVALID, "particle volume out of range");
+  SeedShapeOwner shape;
+  st = build_seed_shape(*obj, (uint32_t)dens, shape);
+  if (st != MPM_OK) return fail(c, st, "invalid object shape");
+  ObjectRec rec;
+  rec.desc = *obj;
+  rec.desc.vertices = nullptr;
+  rec.desc.triangles = nullptr;
+  MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+  MPM_CUDA(c, seed_shape_gpu(shape.sh, c->stream, &rec.d_x, &rec.count));
+  c->launches += 5;
+  c->objects.push_back(rec);
+  if (n_particles) *n_particles = rec.count;
+  if (c->t >= obj->lifetime_begin && c->t < obj->lifetime_end) return activate_object(c, c->objects.back());
+  return MPM_OK;
+}
+
+double mpm_time(const mpm_ctx* c) { return c ? c->t : 0.0; }
+
+int32_t mpm_object_count(const mpm_ctx* c) { return c ? (int32_t)c->objects.size() : -1; }
+
+mpm_status mpm_seed_object(const mpm_object* obj, uint32_t density, float* x, int64_t capacity, int64_t* n) {
+  if (!obj || !n || capacity < 0 || (capacity > 0 && !x)) return MPM_ERR_INVALID;
+  SeedShapeOwner shape;
+  mpm_status st = build_seed_shape(*obj, density, shape);
+  if (st != MPM_OK) return st;
+  float* d_x = nullptr;
+  int64_t count = 0;
+  if (seed_shape_gpu(shape.sh, nullptr, &d_x, &count) != cudaSuccess) return MPM_ERR_CUDA;
+  const int64_t copy = std::min(count, capacity);
+  cudaError_t e = copy > 0 ? cudaMemcpy(x, d_x, sizeof(float) * 3 * copy, cudaMemcpyDeviceToHost) : cudaSuccess;
+  cudaFree(d_x);
+  if (e != cudaSuccess) return MPM_ERR_CUDA;
+  *n = count;
   return MPM_OK;
 }
 

@@ -132,6 +132,19 @@ cudaError_t launch_interleave(const float* s, int64_t stride, const uint32_t* id
                               int liquid_layout, cudaStream_t st);
 cudaError_t launch_iota(uint32_t* id, int64_t n, cudaStream_t st);
 cudaError_t launch_scatter_u8(const uint8_t* src, const uint32_t* id, int64_t n, uint8_t* dst, cudaStream_t st);
+// Scene objects: append k seeded particles (positions xs, 3 floats each) at index n0 with
+// velocity v, C = 0, F = I, Jp = 1, material mat_index and ids id0.., and remove the
+// particles with ids in [lo, hi) into the other SoA copy (ids above hi shift down;
+// flags holds n + 1 ints, scratch scan_scratch_ints(n + 1)).
+cudaError_t launch_append_object(float* s, int64_t st, int64_t n0, int64_t k, const float* xs, const float v[3],
+                                 bool liquid, uint8_t* mat, uint8_t mat_index, uint32_t* id, uint32_t id0,
+                                 cudaStream_t stream);
+cudaError_t launch_remove_ids(const float* sA, float* sB, int64_t st, int64_t n, const uint32_t* idA, uint32_t* idB,
+                              const uint8_t* matA, uint8_t* matB, uint32_t lo, uint32_t hi, bool liquid, int* flags,
+                              int* scratch, cudaStream_t stream, int64_t* launches);
+// In-place exclusive scan of m ints (three kernels); scratch holds scan_scratch_ints(m) ints.
+int64_t scan_scratch_ints(int64_t m);
+cudaError_t launch_exclusive_scan(int* data, int64_t m, int* scratch, cudaStream_t st, int64_t* launches);
 // Post-op grid with the reference's mass slot (src/mpm.cu:86-88).
 cudaError_t launch_grid_op(const float4* in, float4* out, GridConsts K, cudaStream_t st);
 

@@ -44,7 +44,6 @@ class Simulation:
             raise _lib.MpmError(code, "mpm_create failed")
         self.ctx = ctx
         self.N = int(N)
-        self.n = 0
         self.materials = []
         if materials is not None:
             self.set_materials(materials)
@@ -95,7 +94,6 @@ class Simulation:
             mat = np.ascontiguousarray(np.asarray(mat, dtype=np.uint8).reshape(n))
         _lib.check(self.L.mpm_upload_soa(self.ctx, n, _ptr(x), _ptr(v), _ptr(C), _ptr(F), _ptr(J), _ptr(mat)),
                    self.ctx)
-        self.n = n
 
     initCuda = upload
 
@@ -104,7 +102,31 @@ class Simulation:
         rec = np.ascontiguousarray(records)
         n = rec.nbytes // 104
         _lib.check(self.L.mpm_upload_aos(self.ctx, _ptr(rec), n), self.ctx)
-        self.n = n
+
+    # -- scene objects -----------------------------------------------------
+    def add_object(self, obj) -> int:
+        """Simulation::addObject (src/mpm.cu:237-251): seed a
+        :class:`mpm_gb300.scene_file.SceneObject` on the GPU; its particles join the
+        simulation while lifetime_begin <= t < lifetime_end.  Returns its particle count."""
+        o, keep = obj.to_c()
+        count = ctypes.c_int64()
+        _lib.check(self.L.mpm_add_object(self.ctx, ctypes.byref(o), ctypes.byref(count)), self.ctx)
+        del keep
+        return int(count.value)
+
+    @property
+    def t(self) -> float:
+        """Simulated time (Simulation::t)."""
+        return float(self.L.mpm_time(self.ctx))
+
+    @property
+    def object_count(self) -> int:
+        return int(self.L.mpm_object_count(self.ctx))
+
+    @property
+    def n(self) -> int:
+        """Particles currently simulated (uploaded plus active objects)."""
+        return int(self.L.mpm_particle_count(self.ctx))
 
     # -- stepping ----------------------------------------------------------
     def advance(self, nsteps: int = 1):

@@ -78,6 +78,9 @@ def lib():
         L.oracle_det_f32.restype = ctypes.c_float
         L.oracle_det_f32.argtypes = [P]
         L.oracle_max_threads.restype = ctypes.c_int
+        L.oracle_seed_object.restype = ctypes.c_int64
+        L.oracle_seed_object.argtypes = [ctypes.c_int, ctypes.c_float, P, P, ctypes.c_uint64, ctypes.c_uint32, P,
+                                         ctypes.c_int64, P, ctypes.c_int64, P, ctypes.c_int64]
         _lib = L
     return _lib
 
@@ -183,3 +186,25 @@ def det_f32(M: np.ndarray) -> float:
 
 def max_threads() -> int:
     return int(lib().oracle_max_threads())
+
+
+def seed_object(shape: int, size: float, position, box_extent=(1.0, 1.0, 1.0), seed: int = 0, density: int = 1000,
+                vertices=None, triangles=None) -> np.ndarray:
+    """Positions (n, 3) float32 of the restated rejection sampler (oracle/seed_oracle.cpp)."""
+    L = lib()
+    pos = np.ascontiguousarray(np.asarray(position, np.float32).reshape(3))
+    ext = np.ascontiguousarray(np.asarray(box_extent, np.float32).reshape(3))
+    V = T = None
+    nv = nt = 0
+    if vertices is not None:
+        V = np.ascontiguousarray(np.asarray(vertices, np.float32).reshape(-1, 3))
+        T = np.ascontiguousarray(np.asarray(triangles, np.int32).reshape(-1, 3))
+        nv, nt = V.shape[0], T.shape[0]
+    args = (int(shape), float(size), _ptr(pos), _ptr(ext), int(seed) & 0xFFFFFFFFFFFFFFFF, int(density), _ptr(V),
+            nv, _ptr(T), nt)
+    n = L.oracle_seed_object(*args, None, 0)
+    if n < 0:
+        raise ValueError("invalid object")
+    x = np.empty((max(n, 1), 3), np.float32)
+    L.oracle_seed_object(*args, _ptr(x), n)
+    return x[:n]

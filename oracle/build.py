@@ -27,11 +27,12 @@ def _run(cmd):
 def build_oracle(force: bool = False) -> str:
     out = os.path.join(HERE, "libmpm_oracle.so")
     src = os.path.join(HERE, "mpm_oracle.cpp")
+    seed = os.path.join(HERE, "seed_oracle.cpp")
     hdr = os.path.join(HERE, "mpm_oracle.h")
-    if force or not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(src), os.path.getmtime(hdr)):
+    if force or not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(f) for f in (src, seed, hdr)):
         tmp = out + ".tmp"
         _run(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
-              "-o", tmp, src])
+              "-o", tmp, src, seed])
         os.replace(tmp, out)
     return out
 

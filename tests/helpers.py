@@ -49,3 +49,41 @@ def golden_substep_cases():
         cfg = {"params": {"dt": float(dt), "N": int(N), "g2p_guard": 1}, "materials": mats, "state": state}
         cases.append((name, cfg, int(nsteps), expect, d[name + "_grid"]))
     return cases
+
+
+def icosphere(subdivisions=2):
+    """A closed triangle mesh of the unit sphere: an icosahedron with each triangle split
+    into four `subdivisions` times, vertices pushed onto the sphere; outward winding."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    V = [[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+         [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]]
+    F = [[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2], [10, 7, 6],
+         [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5], [2, 4, 11], [6, 2, 10],
+         [8, 6, 7], [9, 8, 1]]
+    V = [list(np.asarray(v, np.float64) / np.linalg.norm(v)) for v in V]
+    for _ in range(subdivisions):
+        mid = {}
+
+        def midpoint(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                m = (np.asarray(V[a]) + np.asarray(V[b])) / 2.0
+                V.append(list(m / np.linalg.norm(m)))
+                mid[key] = len(V) - 1
+            return mid[key]
+
+        nf = []
+        for a, b, c in F:
+            ab, bc, ca = midpoint(a, b), midpoint(b, c), midpoint(c, a)
+            nf += [[a, ab, ca], [b, bc, ab], [c, ca, bc], [ab, bc, ca]]
+        F = nf
+    return np.asarray(V, np.float32), np.asarray(F, np.int32)
+
+
+def write_obj(path, V, F, quads=False):
+    with open(path, "w") as f:
+        f.write("# test mesh\n")
+        for v in V:
+            f.write(f"v {v[0]:.7f} {v[1]:.7f} {v[2]:.7f}\n")
+        for tri in F:
+            f.write("f " + " ".join(f"{i + 1}/{i + 1}" for i in tri) + "\n")

@@ -81,3 +81,47 @@ def test_struct_layouts_match_header():
     body = re.search(r"typedef struct mpm_material \{(.*?)\} mpm_material;", src, re.S).group(1)
     fields = re.findall(r"\b(\w+);", re.sub(r"/\*.*?\*/", "", body, flags=re.S))
     assert fields == [f for f, _ in _lib.MpmMaterial._fields_]
+
+
+FACADE_PROGRAM = r"""
+#include <cstdio>
+#include "mpm_gb300.hpp"
+
+int main(int argc, char** argv) {
+  mpm_params p{};
+  p.dt = 1e-4f; p.N = 32; p.gravity = -9.81f; p.sort_interval = 16;
+  std::vector<mpm_material> mats(1);
+  mats[0] = {MPM_MAT_SNOW, 1.0f / 200000, 400.f, 1.4e5f, 0.2f, 10.f, 0.975f, 1.0075f, 0.f};
+  if (argc < 2) return 0;  // built and linked; running needs a GPU
+  mpm_gb300::Simulation sim(p, mats);
+  mpm_object o{};
+  o.shape = MPM_SHAPE_SPHERE; o.size = 0.2f; o.position[0] = o.position[1] = o.position[2] = 0.4f;
+  o.lifetime_end = 1e300;
+  sim.addObject(o);
+  for (int i = 0; i < 10; ++i) sim.advance();
+  auto& ps = sim.syncDevice();
+  std::printf("%zu %f\n", ps.size(), ps.empty() ? 0.f : ps[0].x[1]);
+  return 0;
+}
+"""
+
+
+def test_cpp_facade_compiles_and_links(tmp_path):
+    """include/mpm_gb300.hpp (the Simulation facade) compiles against the C ABI and the
+    program links against the built library (running it needs a GPU)."""
+    import shutil
+    import subprocess
+
+    from mpm_gb300 import build
+
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    lib = build.build()
+    src = tmp_path / "facade.cpp"
+    src.write_text(FACADE_PROGRAM)
+    inc = os.path.join(ROOT, "include")
+    exe = tmp_path / "facade"
+    r = subprocess.run(["g++", "-std=c++17", "-I", inc, str(src), "-o", str(exe), lib,
+                        "-Wl,-rpath," + os.path.dirname(lib)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(exe)]).returncode == 0

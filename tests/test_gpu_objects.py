@@ -1,0 +1,130 @@
+"""GPU tests of scene objects: the GPU rejection sampler against the oracle's
+restatement (bit-exact positions, same order), objects joining and leaving a context
+at their lifetimes (SimObject::isActive, include/mpm.cuh:36-38), and substep parity of
+a scene built from objects."""
+import numpy as np
+import pytest
+
+from helpers import compare_states, icosphere
+
+pytestmark = pytest.mark.gpu
+
+
+def _objs():
+    from mpm_gb300 import _lib
+    from mpm_gb300.scene_file import SceneObject
+
+    V, F = icosphere(3)
+    return {
+        "box": SceneObject(shape=_lib.SHAPE_BOX, size=0.3, position=(0.1, 0.2, 0.3), box_extent=(1.0, 0.5, 2.0), seed=3),
+        "sphere": SceneObject(shape=_lib.SHAPE_SPHERE, size=0.25, position=(0.4, 0.3, 0.35), seed=17),
+        "mesh": SceneObject(shape=_lib.SHAPE_MESH, size=0.3, position=(0.2, 0.25, 0.3), seed=29, vertices=V,
+                            triangles=F),
+    }
+
+
+@pytest.mark.parametrize("name", ["box", "sphere", "mesh"])
+def test_gpu_seeding_matches_oracle(gpu_lib, oracle_lib, name):
+    from mpm_gb300.scene_file import seed_object
+
+    o = _objs()[name]
+    dens = 300000
+    g = seed_object(o, dens)
+    r = oracle_lib.seed_object(o.shape, o.size, o.position, o.box_extent, o.seed, dens, o.vertices, o.triangles)
+    assert len(g) > 1000
+    assert g.shape == r.shape
+    assert np.array_equal(g, r)
+
+
+def test_objects_join_and_leave_at_their_lifetimes(gpu_lib):
+    from mpm_gb300 import _lib, materials as M
+    from mpm_gb300.scene_file import SceneObject
+
+    dt = 1e-4
+    from mpm_gb300.simulation import Simulation
+
+    sim = Simulation(dt=dt, N=32, sort_interval=4)
+    vol = 1.0 / 200000
+    sim.set_materials([M.elastic(vol), M.snow(vol)])
+    a = SceneObject(shape=_lib.SHAPE_SPHERE, material=0, size=0.2, position=(0.3, 0.3, 0.3), seed=1)
+    b = SceneObject(shape=_lib.SHAPE_BOX, material=1, size=0.15, position=(0.6, 0.5, 0.5), seed=2,
+                    lifetime_begin=3.5 * dt)
+    c = SceneObject(shape=_lib.SHAPE_SPHERE, material=1, size=0.1, position=(0.2, 0.7, 0.6), seed=3,
+                    lifetime_end=5.5 * dt, velocity=(0.5, 0.0, 0.0))
+    na, nb, nc = sim.add_object(a), sim.add_object(b), sim.add_object(c)
+    assert sim.object_count == 3 and min(na, nb, nc) > 50
+    assert sim.n == na + nc  # b starts later
+    counts = []
+    for _ in range(8):
+        sim.advance(1)
+        counts.append(sim.n)
+    # after k substeps t = k dt; activation is checked before each substep
+    assert counts == [na + nc] * 4 + [na + nc + nb] * 2 + [na + nb] * 2, counts
+    st = sim.syncDevice()
+    assert st["x"].shape == (na + nb, 3)
+    # download order: a (active from the start), then b (activated later); c left
+    assert np.all(st["mat"][:na] == 0) and np.all(st["mat"][na:] == 1)
+    assert np.all(np.isfinite(st["x"]))
+    assert abs(sim.t - 8 * float(np.float32(dt))) < 1e-15  # t sums the float32 dt in double
+    sim.close()
+
+
+def test_scene_from_objects_matches_oracle(gpu_lib, oracle_lib):
+    """Objects seeded on the GPU and advanced together give the oracle's result on the
+    same particles (the oracle's own seeding, concatenated in activation order)."""
+    from mpm_gb300 import _lib, materials as M
+    from mpm_gb300.scene_file import SceneObject
+    from mpm_gb300.simulation import Simulation
+
+    dt, N = 1e-4, 32
+    vol = 1.0 / 300000
+    mats = [M.elastic(vol), M.snow(vol)]
+    objs = [SceneObject(shape=_lib.SHAPE_SPHERE, material=0, size=0.2, position=(0.25, 0.3, 0.3), seed=4,
+                        velocity=(0.2, -0.5, 0.0)),
+            SceneObject(shape=_lib.SHAPE_BOX, material=1, size=0.2, position=(0.55, 0.3, 0.4), seed=5,
+                        box_extent=(1.0, 1.0, 0.6))]
+    sim = Simulation(dt=dt, N=N, sort_interval=2, materials=mats)
+    for o in objs:
+        sim.add_object(o)
+    sim.advance(5)
+    out = sim.syncDevice()
+    sim.close()
+    dens = int(1.0 / np.float64(np.float32(vol)))
+    xs, vs, ms = [], [], []
+    for o in objs:
+        x = oracle_lib.seed_object(o.shape, o.size, o.position, o.box_extent, o.seed, dens)
+        xs.append(x)
+        vs.append(np.tile(np.asarray(o.velocity, np.float32), (len(x), 1)))
+        ms.append(np.full(len(x), o.material, np.uint8))
+    n = sum(len(x) for x in xs)
+    st = {"x": np.concatenate(xs), "v": np.concatenate(vs), "C": np.zeros((n, 3, 3), np.float32),
+          "F": np.tile(np.eye(3, dtype=np.float32), (n, 1, 1)), "Jp": np.ones(n, np.float32), "mat": np.concatenate(ms)}
+    params = {"dt": dt, "N": N}
+    o32, _, _ = oracle_lib.substep(st, params, [m.derived() for m in mats], 5, np.float32)
+    errs = compare_states(out, o32, params, st)
+    assert max(errs.values()) < 1e-5, errs
+
+
+def test_cpp_facade_runs(gpu_lib, tmp_path):
+    """The C++ Simulation facade (include/mpm_gb300.hpp) seeds an object, advances and
+    reads the particles back in the reference's record layout."""
+    import os
+    import shutil
+    import subprocess
+
+    from test_capi import FACADE_PROGRAM, ROOT
+    from mpm_gb300 import build
+
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    lib = build.build()
+    src = tmp_path / "facade.cpp"
+    src.write_text(FACADE_PROGRAM)
+    exe = tmp_path / "facade"
+    r = subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe), lib,
+                        "-Wl,-rpath," + os.path.dirname(lib)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe), "run"], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    n, y = out.stdout.split()
+    assert int(n) > 500 and 0.3 < float(y) < 0.7
