@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="liquid",
-                    choices=["liquid", "snow", "elastic", "batched", "differentiable", "seeding"])
+                    choices=["liquid", "snow", "elastic", "batched", "differentiable", "seeding", "mesh"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -550,6 +550,110 @@ def run_seeding(args):
     print(json.dumps(line), flush=True)
 
 
+def run_mesh(args):
+    """Surface reconstruction at the reference's mesh defaults (include/options.h:30-31:
+    a 250^3 voxel grid, particle radius 5 voxels) of 500,000 particles (the reference's
+    default particle count) filling a ball of radius 0.25 in an N=60 domain, after 10
+    snow substeps.  A step is one mpm_surface_mesh call: distance field, level-set count,
+    scan, triangle write and the copy of the triangles to host memory.  value: device
+    time of the call's work on the context's stream (CUDA events); e2e: wall clock of the
+    call.  The oracle meshes the same particles on one host thread."""
+    from mpm_gb300 import build
+
+    build.build()
+    import ctypes
+
+    import torch
+
+    import oracle
+    from mpm_gb300 import _lib
+    from mpm_gb300 import materials as M
+    from mpm_gb300.simulation import Simulation
+
+    G, radius, n, N = 250, 5, 500_000, 60
+    rng = np.random.default_rng(0)
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    x = (0.5 + u * 0.25 * rng.random(n)[:, None] ** (1.0 / 3.0)).astype(np.float32)
+    sim = Simulation(dt=1e-4, N=N, materials=[M.snow(1.0 / n)])
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.upload({"x": x})
+    sim.advance(10)
+    sim.sync()
+    cap = 4 * 1024 * 1024
+    tris = np.empty((cap, 3, 3), np.float32)
+    cnt = ctypes.c_int64()
+    L = sim.L
+
+    def call():
+        _lib.check(L.mpm_surface_mesh(sim.ctx, G, radius, tris.ctypes.data_as(ctypes.c_void_p), cap,
+                                      ctypes.byref(cnt)), sim.ctx)
+
+    for _ in range(max(args.warmup, 3)):
+        call()
+    steps = max(1, min(args.steps, 20))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(0)
+    clocks.start()
+    dev, wall = [], []
+    launches0 = sim.launches
+    t_start = time.time()
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        call()
+        e1.record(stream)
+        t1 = time.perf_counter()
+        torch.cuda.synchronize()
+        dev.append(e0.elapsed_time(e1) * 1e-3)
+        wall.append(t1 - t0)
+    t_end = time.time()
+    clk = clocks.stop(t_start, t_end)
+    launches = (sim.launches - launches0) // steps
+    ntri = int(cnt.value)
+    d_s, w_s = statistics.median(dev), statistics.median(wall)
+    # distance kernel alone, for its roofline: minimal bytes = particle positions read once
+    # plus the field written once
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    field = np.empty((G, G, G), np.float32)
+    ev[0].record(stream)
+    _lib.check(L.mpm_surface_distance(sim.ctx, G, radius, field.ctypes.data_as(ctypes.c_void_p)), sim.ctx)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    peak, peak_kind = measured_peaks()
+    # oracle on one host thread: the same particles and grid
+    xs = sim.download(("x",))["x"]
+    vdx = oracle.voxel_dx(N, float(np.float32(1.0 / N)), G)
+    c0 = time.perf_counter()
+    f = oracle.distance_field(xs, G, radius, vdx)
+    ref = oracle.surface_mesh(f, radius, vdx)
+    cpu_s = time.perf_counter() - c0
+    alg = 12.0 * n + 4.0 * G ** 3 + 4.0 * G ** 3 + 36.0 * ntri
+    line = {"metric": "surface meshes/s", "value": 1.0 / d_s, "unit": "meshes/s", "n_gpus": 1, "steps": steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * d_s, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 field, f64 level set", "data": "synthetic",
+            "config": {"workload": "mesh_ball_500k_G250_r5", "particles": n, "grid_side": G, "radius": radius,
+                       "N": N, "triangles": ntri, "l2": "512 MiB flush between steps"},
+            "e2e": {"value": 1.0 / w_s, "unit": "meshes/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 36 * ntri + 8},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": alg / d_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / d_s / 1e9 / peak, "traffic": None,
+                         "note": f"whole call: particles read, field written and read, triangles written; "
+                                 f"peak of {peak_kind}"},
+            "distance_field_ms": ev[0].elapsed_time(ev[1]),
+            "clocks": clk,
+            "oracle_triangles": int(ref.shape[0]),
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "meshes/s", "cores": 1, "kind": "port",
+                             "sample": f"the same {n} particles on the same grid (oracle distance field and "
+                                       f"marching tetrahedra, 1 thread, {cpu_s:.1f} s)"}}
+    print(json.dumps(line), flush=True)
+
+
 def _icosphere(subdivisions):
     t = (1.0 + 5 ** 0.5) / 2.0
     V = [[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
@@ -587,6 +691,8 @@ def main():
         run_differentiable(args)
     elif args.config == "seeding":
         run_seeding(args)
+    elif args.config == "mesh":
+        run_mesh(args)
     else:
         run_ours(args)
 

@@ -184,6 +184,24 @@ int32_t mpm_object_count(const mpm_ctx* ctx);
  * (room for `capacity` particles); *n receives the count, which may exceed capacity. */
 mpm_status mpm_seed_object(const mpm_object* object, uint32_t density, float* x, int64_t capacity, int64_t* n);
 
+/* ---------------------------------------------------------------------------
+ * Surface reconstruction (MeshBuilder::computeMesh, include/mesh_builder.h:170-211).  A
+ * voxel grid of side grid_side (voxel_dx = N dx / grid_side) holds the distance from each
+ * node to the nearest particle within (radius + 1) voxels (fillVoxelGrid_distance,
+ * include/mesh_builder.h:89-137); the surface is the zero level of radius * voxel_dx -
+ * distance.  The reference extracts it with libigl's marching cubes; here marching
+ * tetrahedra (six per voxel cell, split along the main diagonal) give the same level set
+ * as a closed, oriented triangle soup.  Both calls synchronise.
+ * ------------------------------------------------------------------------- */
+/* grid_side in [2, 512], radius in [0, 64]; particles outside [0, grid_side voxel_dx)
+ * touch only the nodes inside the grid.
+ * The distance field (grid_side^3 floats, index (i grid_side + j) grid_side + k). */
+mpm_status mpm_surface_distance(mpm_ctx* ctx, int32_t grid_side, int32_t radius, float* field);
+/* Triangles of the surface, 9 floats each (3 vertices x y z), into host tris (room for
+ * `capacity` triangles); *n_tris receives the count, which may exceed capacity. */
+mpm_status mpm_surface_mesh(mpm_ctx* ctx, int32_t grid_side, int32_t radius, float* tris, int64_t capacity,
+                            int64_t* n_tris);
+
 /* Self-check of failure detection (no counterpart in the reference): one warp waits on
  * an mbarrier that nothing completes, gives up after `polls` polls (1..2^20; each poll
  * may suspend for a hardware-defined interval, microseconds at most) and sets the status

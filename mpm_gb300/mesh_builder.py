@@ -1,0 +1,56 @@
+"""Surface meshes of the particles: the reference's MeshBuilder (include/mesh_builder.h).
+
+``MeshBuilder(N, dx, grid_side, particle_radius).computeMesh(filename, sim)`` follows
+MeshBuilder::computeMesh (include/mesh_builder.h:170-211) as src/main.cu:78-106 drives it
+once per saved frame: the distance field and the level set are computed on the GPU
+(``mpm_surface_mesh``), the triangle soup is welded into an indexed mesh on the host and
+written as an OBJ file (igl::writeOBJ's ``v`` / ``f`` lines).  The reference's optional
+libigl post-processing (``--laplacian_smooth``, ``--mesh-face-count`` decimation, both
+off by default) is not provided.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# command-line defaults of the reference (include/options.h:30-31)
+MESH_GRID = 250
+MESH_PARTICLE_RADIUS = 5
+
+
+def weld(tris: np.ndarray):
+    """Indexed mesh (V (n, 3) float32, F (T, 3) int32) of a triangle soup (T, 3, 3).
+    Vertices on the same voxel edge are bit-identical, so exact matching welds them.
+    Where the level set passes exactly through a voxel node, edge points coincide and
+    their triangles collapse to a repeated index; those faces are dropped."""
+    pts = np.ascontiguousarray(tris.reshape(-1, 3))
+    if pts.shape[0] == 0:
+        return np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)
+    V, inv = np.unique(pts.view(np.dtype((np.void, 12))).ravel(), return_inverse=True)
+    F = inv.reshape(-1, 3).astype(np.int32)
+    F = F[(F[:, 0] != F[:, 1]) & (F[:, 1] != F[:, 2]) & (F[:, 0] != F[:, 2])]
+    return np.ascontiguousarray(V.view(np.float32).reshape(-1, 3)), F
+
+
+def write_obj(filename: str, V: np.ndarray, F: np.ndarray) -> None:
+    """igl::writeOBJ's subset: ``v x y z`` lines, then 1-based ``f a b c`` lines."""
+    with open(filename, "w") as f:
+        np.savetxt(f, V, fmt="v %.9g %.9g %.9g")
+        np.savetxt(f, F + 1, fmt="f %d %d %d")
+
+
+class MeshBuilder:
+    """MeshBuilder(params, flags, grid_size) (include/mesh_builder.h:19-34)."""
+
+    def __init__(self, grid_side: int = MESH_GRID, particle_radius: int = MESH_PARTICLE_RADIUS):
+        self.grid_side = int(grid_side)
+        self.particle_radius = int(particle_radius)
+
+    def mesh(self, sim):
+        """(V, F) of the particles' surface."""
+        return weld(sim.surface_mesh(self.grid_side, self.particle_radius))
+
+    def computeMesh(self, filename: str, sim) -> int:
+        """Writes the surface of the simulation's active particles; returns the face count."""
+        V, F = self.mesh(sim)
+        write_obj(filename, V, F)
+        return int(F.shape[0])

@@ -170,6 +170,30 @@ class Simulation:
         _lib.check(self.L.mpm_get_grid(self.ctx, int(which), _ptr(out)), self.ctx)
         return out
 
+    # -- surface reconstruction ------------------------------------------
+    def surface_distance(self, grid_side: int = 250, radius: int = 5) -> np.ndarray:
+        """Distance field (G, G, G) float32 of fillVoxelGrid_distance
+        (include/mesh_builder.h:89-137) on the voxel grid of MeshBuilder::computeMesh."""
+        G = int(grid_side)
+        out = np.empty((G, G, G), np.float32)
+        _lib.check(self.L.mpm_surface_distance(self.ctx, G, int(radius), _ptr(out)), self.ctx)
+        return out
+
+    def surface_mesh(self, grid_side: int = 250, radius: int = 5) -> np.ndarray:
+        """Triangles (T, 3, 3) float32 of the particles' surface (the zero level of
+        radius voxel_dx - distance, include/mesh_builder.h:170-190), in cell order."""
+        G = int(grid_side)
+        n = ctypes.c_int64()
+        # a first guess of the triangle count (a surface crossing 16 G^2 cells); retried once if short
+        out = np.empty((max(1, min(12 * (G - 1) ** 3, 16 * G * G)), 3, 3), np.float32)
+        _lib.check(self.L.mpm_surface_mesh(self.ctx, G, int(radius), _ptr(out), out.shape[0], ctypes.byref(n)),
+                   self.ctx)
+        if n.value > out.shape[0]:
+            out = np.empty((n.value, 3, 3), np.float32)
+            _lib.check(self.L.mpm_surface_mesh(self.ctx, G, int(radius), _ptr(out), n.value, ctypes.byref(n)),
+                       self.ctx)
+        return out[:n.value]
+
     def getFullParticleCount(self) -> int:
         return int(self.L.mpm_particle_count(self.ctx))
 

@@ -81,6 +81,10 @@ def lib():
         L.oracle_seed_object.restype = ctypes.c_int64
         L.oracle_seed_object.argtypes = [ctypes.c_int, ctypes.c_float, P, P, ctypes.c_uint64, ctypes.c_uint32, P,
                                          ctypes.c_int64, P, ctypes.c_int64, P, ctypes.c_int64]
+        L.oracle_distance_field.restype = None
+        L.oracle_distance_field.argtypes = [P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, P]
+        L.oracle_surface_mesh.restype = ctypes.c_int64
+        L.oracle_surface_mesh.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, P, ctypes.c_int64]
         _lib = L
     return _lib
 
@@ -208,3 +212,27 @@ def seed_object(shape: int, size: float, position, box_extent=(1.0, 1.0, 1.0), s
     x = np.empty((max(n, 1), 3), np.float32)
     L.oracle_seed_object(*args, _ptr(x), n)
     return x[:n]
+
+
+def voxel_dx(N: int, dx: float, grid_side: int) -> float:
+    """voxel_dx = N dx / grid_side with N dx in float (include/mesh_builder.h:172)."""
+    return float(np.float32(np.float32(N) * np.float32(dx))) / float(grid_side)
+
+
+def distance_field(x: np.ndarray, grid_side: int, radius: int, vdx: float) -> np.ndarray:
+    """Distance field (G, G, G) float32 of oracle/surface_oracle.cpp."""
+    X = np.ascontiguousarray(np.asarray(x, np.float32).reshape(-1, 3))
+    f = np.empty((grid_side,) * 3, np.float32)
+    lib().oracle_distance_field(_ptr(X), X.shape[0], int(grid_side), int(radius), float(vdx), _ptr(f))
+    return f
+
+
+def surface_mesh(field: np.ndarray, radius: int, vdx: float) -> np.ndarray:
+    """Triangles (T, 3, 3) float32 of the level set radius vdx - field = 0."""
+    f = np.ascontiguousarray(field, np.float32)
+    G = f.shape[0]
+    L = lib()
+    n = L.oracle_surface_mesh(_ptr(f), G, int(radius), float(vdx), None, 0)
+    t = np.empty((max(n, 1), 3, 3), np.float32)
+    L.oracle_surface_mesh(_ptr(f), G, int(radius), float(vdx), _ptr(t), n)
+    return t[:n]

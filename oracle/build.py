@@ -1,6 +1,7 @@
 """Build recipe for the oracle (test infrastructure).
 
-* ``libmpm_oracle.so`` — the C++ restatement of the reference substep (always).
+* ``libmpm_oracle.so`` — the C++ restatements of the reference substep, of particle
+  seeding and of surface reconstruction (always).
 * ``_ref/libref_svd.so`` — the reference's own ``include/svd3_cuda.h`` compiled
   for the host from where it lies in the reference checkout, through
   ``ref_shim/`` (host definitions of the three CUDA rounding intrinsics it uses).
@@ -28,11 +29,13 @@ def build_oracle(force: bool = False) -> str:
     out = os.path.join(HERE, "libmpm_oracle.so")
     src = os.path.join(HERE, "mpm_oracle.cpp")
     seed = os.path.join(HERE, "seed_oracle.cpp")
+    surface = os.path.join(HERE, "surface_oracle.cpp")
     hdr = os.path.join(HERE, "mpm_oracle.h")
-    if force or not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(f) for f in (src, seed, hdr)):
+    srcs = (src, seed, surface)
+    if force or not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(f) for f in srcs + (hdr,)):
         tmp = out + ".tmp"
         _run(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
-              "-o", tmp, src, seed])
+              "-o", tmp, *srcs])
         os.replace(tmp, out)
     return out
 
