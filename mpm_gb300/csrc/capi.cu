@@ -80,6 +80,7 @@ struct mpm_ctx {
 
   double t = 0.0;  // simulated time (Simulation::t)
   std::vector<ObjectRec> objects;
+  SurfaceBuffers surf;
 };
 
 namespace {
@@ -466,6 +467,7 @@ mpm_status mpm_destroy(mpm_ctx* c) {
   free_particles(c);
   for (auto& g : c->grid) cudaFree(g);
   cudaFree(c->vgrid_mem);
+  c->surf.release();
   cudaFree(c->counts);
   cudaFree(c->block_sums);
   cudaFree(c->stage);
@@ -770,18 +772,12 @@ namespace {
 // voxel_dx = N dx / grid_side in the reference's types (include/mesh_builder.h:172).
 double voxel_dx_of(const mpm_ctx* c, int G) { return (double)((float)c->params.N * c->K.g.dx) / (double)G; }
 
-mpm_status surface_field(mpm_ctx* c, int32_t G, int32_t radius, float** field) {
-  *field = nullptr;
+mpm_status surface_field(mpm_ctx* c, int32_t G, int32_t radius, bool finish) {
   // G <= 512 keeps 12 (G-1)^3, the most triangles a field can give, within int32
   if (G < 2 || G > 512 || radius < 0 || radius > 64) return fail(c, MPM_ERR_INVALID, "grid_side or radius out of range");
-  MPM_CUDA(c, cudaMalloc(field, sizeof(float) * (size_t)G * G * G));
-  cudaError_t e = launch_distance_field(c->sA, c->stride, c->n, G, radius, voxel_dx_of(c, G), *field, c->stream);
-  c->launches += 2;
-  if (e != cudaSuccess) {
-    cudaFree(*field);
-    *field = nullptr;
-    return fail(c, MPM_ERR_CUDA, std::string("distance field: ") + cudaGetErrorString(e));
-  }
+  cudaError_t e = launch_distance_field(c->sA, c->stride, c->n, G, radius, voxel_dx_of(c, G), finish, c->surf,
+                                        c->stream, &c->launches);
+  if (e != cudaSuccess) return fail(c, MPM_ERR_CUDA, std::string("distance field: ") + cudaGetErrorString(e));
   return MPM_OK;
 }
 
@@ -789,30 +785,25 @@ mpm_status surface_field(mpm_ctx* c, int32_t G, int32_t radius, float** field) {
 
 mpm_status mpm_surface_distance(mpm_ctx* c, int32_t G, int32_t radius, float* out) {
   if (!c || !out) return MPM_ERR_INVALID;
-  float* field = nullptr;
-  mpm_status st = surface_field(c, G, radius, &field);
+  mpm_status st = surface_field(c, G, radius, true);
   if (st != MPM_OK) return st;
-  cudaError_t e = cudaMemcpyAsync(out, field, sizeof(float) * (size_t)G * G * G, cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e =
+      cudaMemcpyAsync(out, c->surf.field, sizeof(float) * (size_t)G * G * G, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  cudaFree(field);
   if (e != cudaSuccess) return fail(c, MPM_ERR_CUDA, cudaGetErrorString(e));
   return MPM_OK;
 }
 
 mpm_status mpm_surface_mesh(mpm_ctx* c, int32_t G, int32_t radius, float* tris, int64_t capacity, int64_t* n_tris) {
   if (!c || !n_tris || capacity < 0 || (capacity > 0 && !tris)) return MPM_ERR_INVALID;
-  float* field = nullptr;
-  mpm_status st = surface_field(c, G, radius, &field);
+  mpm_status st = surface_field(c, G, radius, false);
   if (st != MPM_OK) return st;
-  float* d_tris = nullptr;
   int64_t n = 0;
-  cudaError_t e = extract_surface(field, G, radius, voxel_dx_of(c, G), c->stream, &d_tris, &n);
-  c->launches += 5;
+  cudaError_t e = extract_surface(G, radius, voxel_dx_of(c, G), c->surf, c->stream, &n, &c->launches);
   const int64_t copy = std::min(n, capacity);
   if (e == cudaSuccess && copy > 0)
-    e = cudaMemcpy(tris, d_tris, sizeof(float) * 9 * (size_t)copy, cudaMemcpyDeviceToHost);
-  cudaFree(field);
-  cudaFree(d_tris);
+    e = cudaMemcpyAsync(tris, c->surf.tris, sizeof(float) * 9 * (size_t)copy, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return fail(c, MPM_ERR_CUDA, std::string("surface: ") + cudaGetErrorString(e));
   *n_tris = n;
   return MPM_OK;

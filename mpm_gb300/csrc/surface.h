@@ -5,14 +5,31 @@
 
 namespace mpm {
 
-// Distance field of the particles on a G^3 voxel grid of spacing voxel_dx with cutoff
-// (radius + 1) voxels (MeshBuilder::computeMesh, include/mesh_builder.h:172-178).
+// Device buffers of the mesher, kept by the context between calls (grown, never shrunk).
+struct SurfaceBuffers {
+  float* field = nullptr;  // G^3 distance field
+  int64_t field_cap = 0;
+  int* counts = nullptr;   // triangles per block of cells, then their exclusive scan
+  int64_t counts_cap = 0;
+  int* scan = nullptr;     // scan scratch
+  int64_t scan_cap = 0;
+  float* tris = nullptr;   // 9 floats per triangle
+  int64_t tris_cap = 0;
+  int* total = nullptr;    // pinned host word: the triangle count
+  bool raw = false;        // field holds squared distances (not yet min(cutoff, sqrt(.)))
+  void release();
+};
+
+// Distance field of the particles into buf.field: a G^3 voxel grid of spacing voxel_dx
+// with cutoff (radius + 1) voxels (MeshBuilder::computeMesh, include/mesh_builder.h:172-178).
+// Without `finish` the buffer may be left holding the squared distances (buf.raw), which
+// extract_surface reads directly.
 cudaError_t launch_distance_field(const float* s, int64_t stride, int64_t n, int G, int radius, double voxel_dx,
-                                  float* field, cudaStream_t st);
+                                  bool finish, SurfaceBuffers& buf, cudaStream_t st, int64_t* launches);
 // Triangles (9 floats each: 3 vertices, cell order) of the level set
-// radius * voxel_dx - field = 0; *tris_out is device memory owned by the caller.
-cudaError_t extract_surface(const float* field, int G, int radius, double voxel_dx, cudaStream_t st, float** tris_out,
-                            int64_t* n_out);
+// radius * voxel_dx - field = 0 into buf.tris; synchronises the stream once (count).
+cudaError_t extract_surface(int G, int radius, double voxel_dx, SurfaceBuffers& buf, cudaStream_t st,
+                            int64_t* n_out, int64_t* launches);
 
 #ifdef __CUDACC__
 // The six tetrahedra of a voxel cell around its diagonal from corner 0 to corner 7
@@ -23,78 +40,100 @@ __device__ __forceinline__ int tet_corner(int t, int v) {
   return kTets[t][v];
 }
 
-// Point where the level set crosses edge (qa, qb) of the cell at (i, j, k), in world units.
-__device__ __forceinline__ void edge_point(const double v[8], int qa, int qb, int i, int j, int k, double vdx,
-                                           double p[3]) {
-  const double t = __ddiv_rn(v[qa], __dsub_rn(v[qa], v[qb]));
-  const double a[3] = {(double)(i + (qa >> 2)), (double)(j + ((qa >> 1) & 1)), (double)(k + (qa & 1))};
-  const double b[3] = {(double)(i + (qb >> 2)), (double)(j + ((qb >> 1) & 1)), (double)(k + (qb & 1))};
-#pragma unroll
-  for (int c = 0; c < 3; ++c) p[c] = __dmul_rn(__dadd_rn(a[c], __dmul_rn(t, __dsub_rn(b[c], a[c]))), vdx);
-}
+// Corner q of the cell sits at offset (q >> 2, (q >> 1) & 1, q & 1).
+__device__ __forceinline__ int corner_bit(int q, int c) { return (q >> (2 - c)) & 1; }
 
-// Writes triangle (p0, p1, p2), swapping p1 and p2 when its normal does not point along
-// `away` (from the inside corners to the outside ones).
-__device__ __forceinline__ void put_triangle(const double p0[3], const double p1[3], const double p2[3],
-                                             const double away[3], float* out) {
-  const double e1[3] = {__dsub_rn(p1[0], p0[0]), __dsub_rn(p1[1], p0[1]), __dsub_rn(p1[2], p0[2])};
-  const double e2[3] = {__dsub_rn(p2[0], p0[0]), __dsub_rn(p2[1], p0[1]), __dsub_rn(p2[2], p0[2])};
-  const double nx = __dsub_rn(__dmul_rn(e1[1], e2[2]), __dmul_rn(e1[2], e2[1]));
-  const double ny = __dsub_rn(__dmul_rn(e1[2], e2[0]), __dmul_rn(e1[0], e2[2]));
-  const double nz = __dsub_rn(__dmul_rn(e1[0], e2[1]), __dmul_rn(e1[1], e2[0]));
-  const double dot = __dadd_rn(__dadd_rn(__dmul_rn(nx, away[0]), __dmul_rn(ny, away[1])), __dmul_rn(nz, away[2]));
-  const double* q1 = dot < 0.0 ? p2 : p1;
-  const double* q2 = dot < 0.0 ? p1 : p2;
+// Point where the level set crosses the edge from inside corner qi to outside corner qo of
+// the cell at (i, j, k), in world units.  Always interpolated from the inside corner, so
+// a vertex shared by neighbouring tetrahedra and cells comes out bit-identical:
+//   t = (iso - f_in) / (f_out - f_in),  p = (in + t (out - in)) dx   (float, no contraction)
+__device__ __forceinline__ void edge_point(const float f[8], int qi, int qo, int i, int j, int k, float iso,
+                                           float vdx, float* p) {
+  const float t = __fdiv_rn(__fsub_rn(iso, f[qi]), __fsub_rn(f[qo], f[qi]));
+  const int cell[3] = {i, j, k};
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    out[c] = (float)p0[c];
-    out[3 + c] = (float)q1[c];
-    out[6 + c] = (float)q2[c];
+    const float a = (float)(cell[c] + corner_bit(qi, c)), b = (float)(cell[c] + corner_bit(qo, c));
+    p[c] = __fmul_rn(__fadd_rn(a, __fmul_rn(t, __fsub_rn(b, a))), vdx);
   }
 }
 
-// Triangles of tetrahedron t of the cell (values v of the level-set function S at its 8
-// corners, inside where S > 0); writes them to out (9 floats each) unless out is null.
-__device__ __forceinline__ int tet_triangles(const double v[8], int t, int i, int j, int k, double vdx, float* out) {
+// det(A - L, B - L, C - L) of cell corners (integer offsets).
+__device__ __forceinline__ int corner_det(int L, int A, int B, int C) {
+  int u[3], v[3], w[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    u[c] = corner_bit(A, c) - corner_bit(L, c);
+    v[c] = corner_bit(B, c) - corner_bit(L, c);
+    w[c] = corner_bit(C, c) - corner_bit(L, c);
+  }
+  return u[0] * (v[1] * w[2] - v[2] * w[1]) - u[1] * (v[0] * w[2] - v[2] * w[0]) + u[2] * (v[0] * w[1] - v[1] * w[0]);
+}
+
+// Whether the quad (ac, ad, bd, bc) of a tetrahedron with a, b inside and c, d outside
+// must be reversed to face outward: the normal of its triangle (ac, ad, bd) at the edge
+// midpoints, (d - c) x (b + d - a - c), against the direction (c + d) - (a + b).
+__device__ __forceinline__ bool quad_flip(int a, int b, int c, int d) {
+  int e1[3], e2[3], aw[3];
+#pragma unroll
+  for (int x = 0; x < 3; ++x) {
+    e1[x] = corner_bit(d, x) - corner_bit(c, x);
+    e2[x] = corner_bit(b, x) + corner_bit(d, x) - corner_bit(a, x) - corner_bit(c, x);
+    aw[x] = corner_bit(c, x) + corner_bit(d, x) - corner_bit(a, x) - corner_bit(b, x);
+  }
+  const int n0 = e1[1] * e2[2] - e1[2] * e2[1], n1 = e1[2] * e2[0] - e1[0] * e2[2], n2 = e1[0] * e2[1] - e1[1] * e2[0];
+  return n0 * aw[0] + n1 * aw[1] + n2 * aw[2] < 0;
+}
+
+__device__ __forceinline__ void put_triangle(const float* p0, const float* p1, const float* p2, bool flip, float* out) {
+  const float* q1 = flip ? p2 : p1;
+  const float* q2 = flip ? p1 : p2;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    out[c] = p0[c];
+    out[3 + c] = q1[c];
+    out[6 + c] = q2[c];
+  }
+}
+
+// Triangles of tetrahedron t of the cell (field values f at its 8 corners, corner q inside
+// when bit q of `inside` is set), written to out (9 floats each), facing from the inside
+// corners to the outside ones; returns their number.  Each triangle's orientation is fixed
+// by the corners alone: the level set of the linear interpolant is a plane in the
+// tetrahedron, so the sign of its normal against the tetrahedron's edges does not depend
+// on where the plane cuts them.
+__device__ __forceinline__ int tet_triangles(const float f[8], unsigned inside, int t, int i, int j, int k, float iso,
+                                             float vdx, float* out) {
   int q[4], in[4], n_in = 0;
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     q[r] = tet_corner(t, r);
-    in[r] = v[q[r]] > 0.0;
+    in[r] = (inside >> q[r]) & 1;
     n_in += in[r];
   }
   if (n_in == 0 || n_in == 4) return 0;
-  if (!out) return n_in == 2 ? 2 : 1;
-  // direction from the inside corners' centroid to the outside ones' (grid units)
-  double cin[3] = {0, 0, 0}, cout[3] = {0, 0, 0};
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const double o[3] = {(double)(q[r] >> 2), (double)((q[r] >> 1) & 1), (double)(q[r] & 1)};
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      if (in[r]) cin[c] = __dadd_rn(cin[c], o[c]);
-      else cout[c] = __dadd_rn(cout[c], o[c]);
-    }
-  }
-  const double ni = (double)n_in, no = (double)(4 - n_in);
-  const double away[3] = {__dsub_rn(__ddiv_rn(cout[0], no), __ddiv_rn(cin[0], ni)),
-                          __dsub_rn(__ddiv_rn(cout[1], no), __ddiv_rn(cin[1], ni)),
-                          __dsub_rn(__ddiv_rn(cout[2], no), __ddiv_rn(cin[2], ni))};
   if (n_in == 1 || n_in == 3) {
-    // the corner on its own side and the three edges from it
+    // the corner alone on its side (L) and the others in tetrahedron order (A, B, C);
+    // triangle (eLA, eLB, eLC) faces away from L when det(A - L, B - L, C - L) > 0
+    const int want_in = n_in == 1;
     int lone = 0;
 #pragma unroll
     for (int r = 0; r < 4; ++r)
-      if (in[r] == (n_in == 1)) lone = r;
-    double p[3][3];
-    int m = 0;
+      if (in[r] == want_in) lone = r;
+    int o[3], m = 0;
 #pragma unroll
     for (int r = 0; r < 4; ++r)
-      if (r != lone) {
-        edge_point(v, q[lone], q[r], i, j, k, vdx, p[m]);
-        ++m;
-      }
-    put_triangle(p[0], p[1], p[2], away, out);
+      if (r != lone) o[m++] = q[r];
+    float p[3][3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      if (n_in == 1) edge_point(f, q[lone], o[e], i, j, k, iso, vdx, p[e]);
+      else edge_point(f, o[e], q[lone], i, j, k, iso, vdx, p[e]);
+    }
+    const int det = corner_det(q[lone], o[0], o[1], o[2]);
+    // outward: away from an inside L, towards an outside L
+    const bool flip = n_in == 1 ? det < 0 : det > 0;
+    put_triangle(p[0], p[1], p[2], flip, out);
     return 1;
   }
   // two corners inside (a, b), two outside (c, d): the quad a-c, a-d, b-d, b-c
@@ -102,18 +141,19 @@ __device__ __forceinline__ int tet_triangles(const double v[8], int t, int i, in
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     if (in[r]) {
-      if (a < 0) a = r; else b = r;
+      if (a < 0) a = q[r]; else b = q[r];
     } else {
-      if (c < 0) c = r; else d = r;
+      if (c < 0) c = q[r]; else d = q[r];
     }
   }
-  double ac[3], ad[3], bd[3], bc[3];
-  edge_point(v, q[a], q[c], i, j, k, vdx, ac);
-  edge_point(v, q[a], q[d], i, j, k, vdx, ad);
-  edge_point(v, q[b], q[d], i, j, k, vdx, bd);
-  edge_point(v, q[b], q[c], i, j, k, vdx, bc);
-  put_triangle(ac, ad, bd, away, out);
-  put_triangle(ac, bd, bc, away, out + 9);
+  float ac[3], ad[3], bd[3], bc[3];
+  edge_point(f, a, c, i, j, k, iso, vdx, ac);
+  edge_point(f, a, d, i, j, k, iso, vdx, ad);
+  edge_point(f, b, d, i, j, k, iso, vdx, bd);
+  edge_point(f, b, c, i, j, k, iso, vdx, bc);
+  const bool flip = quad_flip(a, b, c, d);
+  put_triangle(ac, ad, bd, flip, out);
+  put_triangle(ac, bd, bc, flip, out + 9);
   return 2;
 }
 #endif

@@ -41,6 +41,26 @@ def test_distance_field_matches_oracle(gpu_lib, oracle_lib, N, G, radius):
     assert np.array_equal(g.view(np.int32), r.view(np.int32))
 
 
+@pytest.mark.parametrize("order,radius", [("sorted", 4), ("mixed", 4), ("sorted", 7)])
+def test_distance_field_of_cell_sorted_particles_matches_oracle(gpu_lib, oracle_lib, order, radius):
+    # cell-sorted particles take the shared-tile path (two particles per warp up to radius
+    # 6, one otherwise); a shuffled tail takes the direct one
+    N, G = 40, 120
+    x = _ball(60000, (0.5, 0.5, 0.5), 0.3, 5)
+    sim = _sim(x, N)
+    sim.sort()
+    if order == "mixed":
+        st = sim.download()
+        perm = np.arange(len(x))
+        tail = perm[len(x) // 2:]
+        perm[len(x) // 2:] = np.random.default_rng(0).permutation(tail)
+        sim.upload({k: v[perm] for k, v in st.items()})
+    g = sim.surface_distance(G, radius)
+    dx = float(np.float32(1.0 / N))
+    r = oracle_lib.distance_field(sim.download(("x",))["x"], G, radius, oracle_lib.voxel_dx(N, dx, G))
+    assert np.array_equal(g.view(np.int32), r.view(np.int32))
+
+
 @pytest.mark.parametrize("G,radius", [(48, 2), (33, 3)])
 def test_surface_triangles_match_oracle(gpu_lib, oracle_lib, G, radius):
     N = 32
