@@ -554,10 +554,11 @@ def run_mesh(args):
     """Surface reconstruction at the reference's mesh defaults (include/options.h:30-31:
     a 250^3 voxel grid, particle radius 5 voxels) of 500,000 particles (the reference's
     default particle count) filling a ball of radius 0.25 in an N=60 domain, after 10
-    snow substeps.  A step is one mpm_surface_mesh call: distance field, level-set count,
-    scan, triangle write and the copy of the triangles to host memory.  value: device
-    time of the call's work on the context's stream (CUDA events); e2e: wall clock of the
-    call.  The oracle meshes the same particles on one host thread."""
+    snow substeps.  A step is one surface extraction: distance field, level-set count,
+    scans, compaction and triangle write.  value: device time (CUDA events on the context's
+    stream) of mpm_surface_mesh_device, the triangles left in HBM; e2e: wall clock of
+    mpm_surface_mesh, which also copies the triangles to host memory.  The oracle meshes
+    the same particles on one host thread."""
     from mpm_gb300 import build
 
     build.build()
@@ -586,44 +587,50 @@ def run_mesh(args):
     cnt = ctypes.c_int64()
     L = sim.L
 
-    def call():
+    dptr = ctypes.c_void_p()
+
+    def call_host():
         _lib.check(L.mpm_surface_mesh(sim.ctx, G, radius, tris.ctypes.data_as(ctypes.c_void_p), cap,
                                       ctypes.byref(cnt)), sim.ctx)
 
+    def call_device():
+        _lib.check(L.mpm_surface_mesh_device(sim.ctx, G, radius, ctypes.byref(dptr), ctypes.byref(cnt)), sim.ctx)
+
+    def call_field():
+        _lib.check(L.mpm_surface_distance_device(sim.ctx, G, radius, ctypes.byref(dptr)), sim.ctx)
+
     for _ in range(max(args.warmup, 3)):
-        call()
+        call_host()
+        call_device()
+        call_field()
     steps = max(1, min(args.steps, 20))
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    clocks = ClockSampler(0)
-    clocks.start()
-    dev, wall = [], []
-    launches0 = sim.launches
-    t_start = time.time()
-    for _ in range(steps):
+
+    def timed(fn):
+        """Device time (CUDA events on the context's stream) and wall time of fn, L2 flushed before."""
         flush.fill_(1.0)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
         e0.record(stream)
-        call()
+        fn()
         e1.record(stream)
+        e1.synchronize()
         t1 = time.perf_counter()
-        torch.cuda.synchronize()
-        dev.append(e0.elapsed_time(e1) * 1e-3)
-        wall.append(t1 - t0)
+        return e0.elapsed_time(e1) * 1e-3, t1 - t0
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    launches0 = sim.launches
+    t_start = time.time()
+    dev = [timed(call_device)[0] for _ in range(steps)]
     t_end = time.time()
-    clk = clocks.stop(t_start, t_end)
     launches = (sim.launches - launches0) // steps
+    wall = [timed(call_host)[1] for _ in range(steps)]
+    field_s = statistics.median([timed(call_field)[0] for _ in range(steps)])
+    clk = clocks.stop(t_start, t_end)
     ntri = int(cnt.value)
     d_s, w_s = statistics.median(dev), statistics.median(wall)
-    # distance kernel alone, for its roofline: minimal bytes = particle positions read once
-    # plus the field written once
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-    field = np.empty((G, G, G), np.float32)
-    ev[0].record(stream)
-    _lib.check(L.mpm_surface_distance(sim.ctx, G, radius, field.ctypes.data_as(ctypes.c_void_p)), sim.ctx)
-    ev[1].record(stream)
-    torch.cuda.synchronize()
     peak, peak_kind = measured_peaks()
     # oracle on one host thread: the same particles and grid
     xs = sim.download(("x",))["x"]
@@ -632,7 +639,9 @@ def run_mesh(args):
     f = oracle.distance_field(xs, G, radius, vdx)
     ref = oracle.surface_mesh(f, radius, vdx)
     cpu_s = time.perf_counter() - c0
-    alg = 12.0 * n + 4.0 * G ** 3 + 4.0 * G ** 3 + 36.0 * ntri
+    # distance-field pass (fill, scatter, finish): minimal bytes = positions read once and
+    # the field written once
+    alg = 12.0 * n + 4.0 * G ** 3
     line = {"metric": "surface meshes/s", "value": 1.0 / d_s, "unit": "meshes/s", "n_gpus": 1, "steps": steps,
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * d_s, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 field, f64 level set", "data": "synthetic",
@@ -641,11 +650,13 @@ def run_mesh(args):
             "e2e": {"value": 1.0 / w_s, "unit": "meshes/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 36 * ntri + 8},
             "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "achieved": alg / d_s / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": alg / d_s / 1e9 / peak, "traffic": None,
-                         "note": f"whole call: particles read, field written and read, triangles written; "
-                                 f"peak of {peak_kind}"},
-            "distance_field_ms": ev[0].elapsed_time(ev[1]),
+            "roofline": {"bound": "hbm", "achieved": alg / field_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / field_s / 1e9 / peak, "traffic": None,
+                         "kernel": "distance field (fill + distance_kernel + finish)",
+                         "note": f"positions read + field written once per pass; the scatter is bound by "
+                                 f"shared-memory reductions (one per particle-node pair), not HBM; peak of "
+                                 f"{peak_kind}"},
+            "distance_field_ms": 1e3 * field_s,
             "clocks": clk,
             "oracle_triangles": int(ref.shape[0]),
             "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "meshes/s", "cores": 1, "kind": "port",

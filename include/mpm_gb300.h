@@ -201,6 +201,14 @@ mpm_status mpm_surface_distance(mpm_ctx* ctx, int32_t grid_side, int32_t radius,
  * `capacity` triangles); *n_tris receives the count, which may exceed capacity. */
 mpm_status mpm_surface_mesh(mpm_ctx* ctx, int32_t grid_side, int32_t radius, float* tris, int64_t capacity,
                             int64_t* n_tris);
+/* The distance field left in device memory (the context's buffer, valid until the next
+ * surface call or mpm_destroy), written asynchronously on the context's stream. */
+mpm_status mpm_surface_distance_device(mpm_ctx* ctx, int32_t grid_side, int32_t radius, const float** field);
+/* The same triangles left in device memory: *tris receives the context's buffer (valid
+ * until the next surface call or mpm_destroy), written asynchronously on the context's
+ * stream after the call returns (the call itself waits once, for the count). */
+mpm_status mpm_surface_mesh_device(mpm_ctx* ctx, int32_t grid_side, int32_t radius, const float** tris,
+                                   int64_t* n_tris);
 
 /* Self-check of failure detection (no counterpart in the reference): one warp waits on
  * an mbarrier that nothing completes, gives up after `polls` polls (1..2^20; each poll

@@ -91,6 +91,8 @@ SIGNATURES = [
     ("mpm_object_count", I32, [P]),
     ("mpm_surface_distance", I32, [P, I32, I32, P]),
     ("mpm_surface_mesh", I32, [P, I32, I32, P, I64, ctypes.POINTER(I64)]),
+    ("mpm_surface_mesh_device", I32, [P, I32, I32, ctypes.POINTER(P), ctypes.POINTER(I64)]),
+    ("mpm_surface_distance_device", I32, [P, I32, I32, ctypes.POINTER(P)]),
     ("mpm_seed_object", I32, [ctypes.POINTER(MpmObject), ctypes.c_uint32, P, I64, ctypes.POINTER(I64)]),
     ("mpm_particle_count", I64, [P]),
     ("mpm_substep_count", I64, [P]),

@@ -809,6 +809,26 @@ mpm_status mpm_surface_mesh(mpm_ctx* c, int32_t G, int32_t radius, float* tris, 
   return MPM_OK;
 }
 
+mpm_status mpm_surface_distance_device(mpm_ctx* c, int32_t G, int32_t radius, const float** field) {
+  if (!c || !field) return MPM_ERR_INVALID;
+  mpm_status st = surface_field(c, G, radius, true);
+  if (st != MPM_OK) return st;
+  *field = c->surf.field;
+  return MPM_OK;
+}
+
+mpm_status mpm_surface_mesh_device(mpm_ctx* c, int32_t G, int32_t radius, const float** tris, int64_t* n_tris) {
+  if (!c || !tris || !n_tris) return MPM_ERR_INVALID;
+  mpm_status st = surface_field(c, G, radius, false);
+  if (st != MPM_OK) return st;
+  int64_t n = 0;
+  cudaError_t e = extract_surface(G, radius, voxel_dx_of(c, G), c->surf, c->stream, &n, &c->launches);
+  if (e != cudaSuccess) return fail(c, MPM_ERR_CUDA, std::string("surface: ") + cudaGetErrorString(e));
+  *tris = c->surf.tris;
+  *n_tris = n;
+  return MPM_OK;
+}
+
 mpm_status mpm_check_wait_timeout(mpm_ctx* c, int32_t polls) {
   if (!c || polls < 1 || polls > (1 << 20)) return MPM_ERR_INVALID;
   MPM_CUDA(c, launch_wait_timeout_probe(c->status, polls, c->stream));

@@ -9,13 +9,15 @@ namespace mpm {
 struct SurfaceBuffers {
   float* field = nullptr;  // G^3 distance field
   int64_t field_cap = 0;
-  int* counts = nullptr;   // triangles per block of cells, then their exclusive scan
+  int* counts = nullptr;   // triangles and surface cells per block of cells, then their exclusive scans
   int64_t counts_cap = 0;
+  int2* cells = nullptr;   // surface cells in cell order: packed (i, j, k), first triangle
+  int64_t cells_cap = 0;
   int* scan = nullptr;     // scan scratch
   int64_t scan_cap = 0;
   float* tris = nullptr;   // 9 floats per triangle
   int64_t tris_cap = 0;
-  int* total = nullptr;    // pinned host word: the triangle count
+  int* total = nullptr;    // pinned host words: the triangle and surface-cell counts
   bool raw = false;        // field holds squared distances (not yet min(cutoff, sqrt(.)))
   void release();
 };

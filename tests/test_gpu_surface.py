@@ -41,7 +41,7 @@ def test_distance_field_matches_oracle(gpu_lib, oracle_lib, N, G, radius):
     assert np.array_equal(g.view(np.int32), r.view(np.int32))
 
 
-@pytest.mark.parametrize("order,radius", [("sorted", 4), ("mixed", 4), ("sorted", 7)])
+@pytest.mark.parametrize("order,radius", [("sorted", 4), ("mixed", 4), ("sorted", 6), ("sorted", 7)])
 def test_distance_field_of_cell_sorted_particles_matches_oracle(gpu_lib, oracle_lib, order, radius):
     # cell-sorted particles take the shared-tile path (two particles per warp up to radius
     # 6, one otherwise); a shuffled tail takes the direct one
@@ -106,3 +106,20 @@ def test_mesh_builder_writes_obj(gpu_lib, tmp_path):
     faces = MeshBuilder(64, 2).computeMesh(str(p), sim)
     text = p.read_text()
     assert faces > 500 and text.count("\nf ") + text.startswith("f ") == faces
+
+
+def test_device_outputs_match_host_calls(gpu_lib):
+    import ctypes
+
+    from mpm_gb300 import _lib
+
+    sim = _sim(_ball(20000, (0.5, 0.5, 0.5), 0.2, 6), 32)
+    tris = sim.surface_mesh(64, 3)
+    ptr, n = ctypes.c_void_p(), ctypes.c_int64()
+    _lib.check(sim.L.mpm_surface_mesh_device(sim.ctx, 64, 3, ctypes.byref(ptr), ctypes.byref(n)), sim.ctx)
+    assert ptr.value and n.value == len(tris)
+    _lib.check(sim.L.mpm_surface_distance_device(sim.ctx, 64, 3, ctypes.byref(ptr)), sim.ctx)
+    sim.sync()
+    assert ptr.value
+    # the device calls leave the host calls' results unchanged
+    assert np.array_equal(sim.surface_mesh(64, 3), tris)
