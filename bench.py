@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="liquid",
-                    choices=["liquid", "snow", "elastic", "batched", "differentiable", "seeding", "mesh"])
+                    choices=["liquid", "snow", "elastic", "batched", "differentiable", "seeding", "mesh", "export",
+                             "render"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -665,6 +666,186 @@ def run_mesh(args):
     print(json.dumps(line), flush=True)
 
 
+def _liquid_sim(stream):
+    """The liquid throughput scene (1M particles, N=32) advanced 16 substeps, on `stream`."""
+    from mpm_gb300.simulation import Simulation
+
+    cfg, _ = make_cfg("liquid")
+    sim = Simulation.from_config(cfg)
+    sim.set_stream(stream.cuda_stream)
+    sim.upload(cfg["state"])
+    sim.advance(16)
+    sim.sync()
+    return sim, cfg
+
+
+def run_export(args):
+    """Particle export of the liquid scene (1M particles): the reference's per-frame
+    ParticleWriter::writeParticles (include/particle_writer.h:19-43) as .bgeo point records.
+    A step is one frame: mpm_export_particles (records packed on the GPU in active-list
+    order, copied to pinned memory on a copy stream) and mpm_export_wait.  value: exported
+    particles/s of that pair (wall clock: the copy ends it); roofline: the packing kernel
+    (24 B of x, v and 4 B of id read, 36 B written per particle) by CUDA events on the
+    context's stream; e2e: the same frame with the uncompressed file written to /dev/shm
+    (or the temp directory).  overlap: 16 substeps with and without a frame export between
+    them.  The oracle writes the same file from host arrays with numpy (1 core)."""
+    from mpm_gb300 import build
+
+    build.build()
+    import ctypes
+    import tempfile
+
+    import torch
+
+    import oracle.export_oracle as E
+    from mpm_gb300 import particle_writer as W
+
+    stream = torch.cuda.Stream()
+    sim, cfg = _liquid_sim(stream)
+    n = sim.n
+    for _ in range(max(args.warmup, 3)):
+        W.export_records(sim, 0)
+        W.wait_records(sim, 0)
+    steps = max(1, min(args.steps, 50))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(0)
+    clocks.start()
+    t_start = time.time()
+    wall, pack = [], []
+    launches0 = sim.launches
+    for k in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        W.export_records(sim, k & 1)
+        e1.record(stream)
+        W.wait_records(sim, k & 1)
+        wall.append(time.perf_counter() - t0)
+        torch.cuda.synchronize()
+        pack.append(e0.elapsed_time(e1) * 1e-3)
+    t_end = time.time()
+    clk = clocks.stop(t_start, t_end)
+    launches = (sim.launches - launches0) // steps
+    outdir = "/dev/shm" if os.path.isdir("/dev/shm") else tempfile.gettempdir()
+    path = os.path.join(outdir, f"mpm_export_{os.getpid()}.bgeo")
+    e2e = []
+    writer = W.ParticleWriter()
+    for _ in range(min(steps, 10)):
+        t0 = time.perf_counter()
+        writer.writeParticles(path, sim)
+        e2e.append(time.perf_counter() - t0)
+    size = os.path.getsize(path)
+    os.remove(path)
+    # overlap: 16 substeps alone, then 16 substeps with a frame exported after the first
+    def loop(export):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.advance(1)
+        if export:
+            W.export_records(sim, 0)
+        sim.advance(15)
+        if export:
+            W.wait_records(sim, 0)
+        sim.sync()
+        return time.perf_counter() - t0
+    loop(False), loop(True)
+    plain = statistics.median([loop(False) for _ in range(5)])
+    with_export = statistics.median([loop(True) for _ in range(5)])
+    # oracle: the same file from host arrays
+    st = sim.download(("x", "v"))
+    c0 = time.perf_counter()
+    ref = E.bgeo_file(st["x"], st["v"])
+    cpu_s = time.perf_counter() - c0
+    w_s, p_s = statistics.median(wall), statistics.median(pack)
+    peak, peak_kind = measured_peaks()
+    alg = 64.0 * n
+    line = {"metric": "exported particles/s", "value": n / w_s, "unit": "particles/s", "n_gpus": 1, "steps": steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * w_s, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 records (big-endian)", "data": "synthetic",
+            "config": {"workload": "export_liquid_1M", "particles": n, "record_bytes": 36, "file_bytes": size,
+                       "l2": "512 MiB flush between steps"},
+            "e2e": {"value": n / statistics.median(e2e), "unit": "particles/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 36 * n, "file": outdir},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": alg / p_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / p_s / 1e9 / peak, "traffic": None, "kernel": "bgeo_pack_kernel",
+                         "note": f"64 B per particle (x, v, id read; record written); peak of {peak_kind}"},
+            "pack_ms": 1e3 * p_s, "copy_GBps": 36.0 * n / w_s / 1e9,
+            "overlap": {"substeps_16_ms": 1e3 * plain, "substeps_16_with_export_ms": 1e3 * with_export},
+            "clocks": clk, "oracle_bytes_equal": bool(len(ref) == size),
+            "cpu_baseline": {"value": n / cpu_s, "unit": "particles/s", "cores": 1, "kind": "port",
+                             "sample": f"the same {n} particles: numpy writer of the oracle from host arrays "
+                                       f"({cpu_s:.3f} s)"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_render(args):
+    """Headless point rendering of the liquid scene (1M particles): the reference's
+    Renderer::render (include/renderer.h:43-63) at 800 x 600 with 2-pixel points.  A step is
+    one mpm_render_points call (clear, splat, colour, copy of the RGB8 image to host).
+    value: frames/s by CUDA events on the context's stream (the copy included); e2e: wall
+    clock of the call.  The oracle rasterises the same particles with numpy (1 core)."""
+    from mpm_gb300 import build
+
+    build.build()
+    import torch
+
+    import oracle.export_oracle as E
+    from mpm_gb300.renderer import Renderer
+
+    stream = torch.cuda.Stream()
+    sim, cfg = _liquid_sim(stream)
+    n = sim.n
+    r = Renderer()
+    for _ in range(max(args.warmup, 3)):
+        r.render(sim)
+    steps = max(1, min(args.steps, 50))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(0)
+    clocks.start()
+    t_start = time.time()
+    dev, wall = [], []
+    launches0 = sim.launches
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        img = r.render(sim)
+        e1.record(stream)
+        wall.append(time.perf_counter() - t0)
+        torch.cuda.synchronize()
+        dev.append(e0.elapsed_time(e1) * 1e-3)
+    t_end = time.time()
+    clk = clocks.stop(t_start, t_end)
+    launches = (sim.launches - launches0) // steps
+    x = sim.download(("x",))["x"]
+    c0 = time.perf_counter()
+    ref = E.render_points(x)
+    cpu_s = time.perf_counter() - c0
+    d_s, w_s = statistics.median(dev), statistics.median(wall)
+    peak, peak_kind = measured_peaks()
+    alg = 12.0 * n + 4.0 * 800 * 600
+    line = {"metric": "rendered frames/s", "value": 1.0 / d_s, "unit": "frames/s", "n_gpus": 1, "steps": steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * d_s, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 positions, u8 image", "data": "synthetic",
+            "config": {"workload": "render_liquid_1M_800x600", "particles": n, "width": 800, "height": 600,
+                       "point_size": 2.0, "l2": "512 MiB flush between steps"},
+            "e2e": {"value": 1.0 / w_s, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 3 * 800 * 600},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": alg / d_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / d_s / 1e9 / peak, "traffic": None, "kernel": "whole call",
+                         "note": f"positions read, mask and image written once; peak of {peak_kind}"},
+            "clocks": clk, "oracle_image_equal": bool(np.array_equal(img, ref)),
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "frames/s", "cores": 1, "kind": "port",
+                             "sample": f"the same {n} particles, numpy rasteriser of the oracle ({cpu_s:.3f} s)"}}
+    print(json.dumps(line), flush=True)
+
+
 def _icosphere(subdivisions):
     t = (1.0 + 5 ** 0.5) / 2.0
     V = [[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
@@ -704,6 +885,10 @@ def main():
         run_seeding(args)
     elif args.config == "mesh":
         run_mesh(args)
+    elif args.config == "export":
+        run_export(args)
+    elif args.config == "render":
+        run_render(args)
     else:
         run_ours(args)
 

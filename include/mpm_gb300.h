@@ -36,7 +36,8 @@ typedef enum mpm_status {
   MPM_ERR_STATE = 3,       /* device status word: non-finite particle / index out of range */
   MPM_ERR_TIMEOUT = 4,     /* a bounded device-side wait expired */
   MPM_ERR_NOMEM = 5,       /* device allocation failed */
-  MPM_ERR_UNSUPPORTED = 6  /* configuration not supported by this build */
+  MPM_ERR_UNSUPPORTED = 6, /* configuration not supported by this build */
+  MPM_ERR_IO = 7           /* a file could not be written */
 } mpm_status;
 
 /* Material kinds. MMSnow is the only model the reference instantiates
@@ -209,6 +210,46 @@ mpm_status mpm_surface_distance_device(mpm_ctx* ctx, int32_t grid_side, int32_t 
  * stream after the call returns (the call itself waits once, for the count). */
 mpm_status mpm_surface_mesh_device(mpm_ctx* ctx, int32_t grid_side, int32_t radius, const float** tris,
                                    int64_t* n_tris);
+
+/* ---------------------------------------------------------------------------
+ * Particle export (ParticleWriter::writeParticles, include/particle_writer.h:19-43).  The
+ * reference writes each saved frame through Partio as a .bgeo file: per active particle
+ * its index "id", "position", "velocity" and "radius" 0.1.  Here the point records of that
+ * file (Houdini classic binary geometry v5 as Partio writes it: P = x y z 1, id,
+ * velocity, radius; 36 bytes, big-endian) are packed on the GPU from the particle arrays,
+ * in the active-list order of mpm_download_*, and copied to pinned host memory on a copy
+ * stream that waits only for the packing, so substeps enqueued after the export overlap
+ * the copy.  Two slots let one frame be written to disk while the next is copied.
+ * ------------------------------------------------------------------------- */
+#define MPM_BGEO_RECORD_BYTES 36
+/* Packs the records into slot (0 or 1) and starts their copy; *n receives the count.
+ * Reusing a slot first waits for its previous copy (on the GPU). */
+mpm_status mpm_export_particles(mpm_ctx* ctx, int32_t slot, float radius, int64_t* n);
+/* Waits for slot's copy; *records = its n records in pinned host memory, valid until the
+ * slot is exported into again or the context is destroyed. */
+mpm_status mpm_export_wait(mpm_ctx* ctx, int32_t slot, const void** records, int64_t* n);
+/* Writes a .bgeo file: header, the n records, terminator (uncompressed; readers of the
+ * format also accept the gzip-compressed form the reference writes). */
+mpm_status mpm_write_bgeo(const char* path, const void* records, int64_t n);
+/* The .bgeo header for n points into out (when capacity allows); returns its size. */
+int64_t mpm_bgeo_header(int64_t n, uint8_t* out, int64_t capacity);
+
+/* ---------------------------------------------------------------------------
+ * Headless point rendering (Renderer::render, include/renderer.h:43-63, and its shaders).
+ * The reference uploads (x - 0.5) * 1.8 per particle as clip-space positions and draws
+ * 2-pixel points of colour (0.59, 0.54, 0.2) on an 800 x 600 frame cleared to 0.1 grey,
+ * without depth test or blending.  No graphics API is used here.
+ * ------------------------------------------------------------------------- */
+/* The clip-space positions (3 floats per particle, active-list order) in the context's
+ * device buffer, valid until the next call; written asynchronously on its stream. */
+mpm_status mpm_render_positions_device(mpm_ctx* ctx, const float** positions);
+/* The same positions copied to host memory (3 floats per particle).  Synchronises. */
+mpm_status mpm_render_positions(mpm_ctx* ctx, float* positions);
+/* RGB8 image (width x height x 3 bytes, rows top to bottom) of the points: pixels whose
+ * centres fall inside a point_size square around a point inside the clip volume take
+ * `color`, the others `background`.  Synchronises. */
+mpm_status mpm_render_points(mpm_ctx* ctx, int32_t width, int32_t height, float point_size, const uint8_t color[3],
+                             const uint8_t background[3], uint8_t* rgb);
 
 /* Self-check of failure detection (no counterpart in the reference): one warp waits on
  * an mbarrier that nothing completes, gives up after `polls` polls (1..2^20; each poll

@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(_HERE, "libmpm_gb300.so")
 
 MPM_MAX_MATERIALS = 16
 STATUS_NAMES = {0: "MPM_OK", 1: "MPM_ERR_INVALID", 2: "MPM_ERR_CUDA", 3: "MPM_ERR_STATE", 4: "MPM_ERR_TIMEOUT",
-                5: "MPM_ERR_NOMEM", 6: "MPM_ERR_UNSUPPORTED"}
+                5: "MPM_ERR_NOMEM", 6: "MPM_ERR_UNSUPPORTED", 7: "MPM_ERR_IO"}
 
 
 class MpmParams(ctypes.Structure):
@@ -93,6 +93,13 @@ SIGNATURES = [
     ("mpm_surface_mesh", I32, [P, I32, I32, P, I64, ctypes.POINTER(I64)]),
     ("mpm_surface_mesh_device", I32, [P, I32, I32, ctypes.POINTER(P), ctypes.POINTER(I64)]),
     ("mpm_surface_distance_device", I32, [P, I32, I32, ctypes.POINTER(P)]),
+    ("mpm_export_particles", I32, [P, I32, ctypes.c_float, ctypes.POINTER(I64)]),
+    ("mpm_export_wait", I32, [P, I32, ctypes.POINTER(P), ctypes.POINTER(I64)]),
+    ("mpm_write_bgeo", I32, [ctypes.c_char_p, P, I64]),
+    ("mpm_bgeo_header", I64, [I64, P, I64]),
+    ("mpm_render_positions_device", I32, [P, ctypes.POINTER(P)]),
+    ("mpm_render_positions", I32, [P, P]),
+    ("mpm_render_points", I32, [P, I32, I32, ctypes.c_float, P, P, P]),
     ("mpm_seed_object", I32, [ctypes.POINTER(MpmObject), ctypes.c_uint32, P, I64, ctypes.POINTER(I64)]),
     ("mpm_particle_count", I64, [P]),
     ("mpm_substep_count", I64, [P]),

@@ -15,6 +15,7 @@
 #include "mpm_internal.h"
 #include "seeding.h"
 #include "surface.h"
+#include "export.h"
 
 using namespace mpm;
 
@@ -81,6 +82,19 @@ struct mpm_ctx {
   double t = 0.0;  // simulated time (Simulation::t)
   std::vector<ObjectRec> objects;
   SurfaceBuffers surf;
+  struct ExportSlot {
+    void* dev = nullptr;   // packed records on the device
+    void* host = nullptr;  // pinned copy
+    int64_t cap = 0;       // records both hold
+    int64_t n = 0;
+    cudaEvent_t packed = nullptr, copied = nullptr;
+    bool pending = false;
+  } exports[2];
+  cudaStream_t copy_stream = nullptr;
+  float* positions = nullptr;  // clip-space positions of the renderer
+  int64_t positions_cap = 0;
+  uint8_t* image = nullptr;  // mask (W H) then RGB (3 W H)
+  int64_t image_cap = 0;
 };
 
 namespace {
@@ -468,6 +482,18 @@ mpm_status mpm_destroy(mpm_ctx* c) {
   for (auto& g : c->grid) cudaFree(g);
   cudaFree(c->vgrid_mem);
   c->surf.release();
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
+  for (auto& x : c->exports) {
+    cudaFree(x.dev);
+    cudaFreeHost(x.host);
+    if (x.packed) cudaEventDestroy(x.packed);
+    if (x.copied) cudaEventDestroy(x.copied);
+  }
+  cudaFree(c->positions);
+  cudaFree(c->image);
   cudaFree(c->counts);
   cudaFree(c->block_sums);
   cudaFree(c->stage);
@@ -826,6 +852,120 @@ mpm_status mpm_surface_mesh_device(mpm_ctx* c, int32_t G, int32_t radius, const 
   if (e != cudaSuccess) return fail(c, MPM_ERR_CUDA, std::string("surface: ") + cudaGetErrorString(e));
   *tris = c->surf.tris;
   *n_tris = n;
+  return MPM_OK;
+}
+
+mpm_status mpm_export_particles(mpm_ctx* c, int32_t slot, float radius, int64_t* n) {
+  if (!c || !n || slot < 0 || slot > 1) return MPM_ERR_INVALID;
+  auto& x = c->exports[slot];
+  if (!c->copy_stream) MPM_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  if (!x.packed) {
+    MPM_CUDA(c, cudaEventCreateWithFlags(&x.packed, cudaEventDisableTiming));
+    MPM_CUDA(c, cudaEventCreateWithFlags(&x.copied, cudaEventDisableTiming));
+  }
+  const int64_t cnt = c->n;
+  if (x.pending) {
+    if (cnt > x.cap) {
+      MPM_CUDA(c, cudaEventSynchronize(x.copied));  // the buffers are about to be replaced
+    } else {
+      MPM_CUDA(c, cudaStreamWaitEvent(c->stream, x.copied, 0));  // the device buffer is still being read
+    }
+  }
+  if (cnt > x.cap) {
+    cudaFree(x.dev);
+    cudaFreeHost(x.host);
+    x.dev = x.host = nullptr;
+    x.cap = 0;
+    const size_t bytes = (size_t)kBgeoRecordBytes * (size_t)cnt;
+    if (cudaMalloc(&x.dev, bytes) != cudaSuccess) return fail(c, MPM_ERR_NOMEM, "export: device buffer");
+    if (cudaMallocHost(&x.host, bytes) != cudaSuccess) return fail(c, MPM_ERR_NOMEM, "export: pinned buffer");
+    x.cap = cnt;
+  }
+  MPM_CUDA(c, launch_bgeo_pack(c->sA, c->stride, c->idA, cnt, radius, x.dev, c->stream));
+  MPM_CUDA(c, cudaEventRecord(x.packed, c->stream));
+  MPM_CUDA(c, cudaStreamWaitEvent(c->copy_stream, x.packed, 0));
+  if (cnt > 0)
+    MPM_CUDA(c, cudaMemcpyAsync(x.host, x.dev, (size_t)kBgeoRecordBytes * (size_t)cnt, cudaMemcpyDeviceToHost,
+                                c->copy_stream));
+  MPM_CUDA(c, cudaEventRecord(x.copied, c->copy_stream));
+  c->launches += cnt > 0;
+  x.n = cnt;
+  x.pending = true;
+  *n = cnt;
+  return MPM_OK;
+}
+
+mpm_status mpm_export_wait(mpm_ctx* c, int32_t slot, const void** records, int64_t* n) {
+  if (!c || !records || !n || slot < 0 || slot > 1) return MPM_ERR_INVALID;
+  auto& x = c->exports[slot];
+  if (!x.pending) return fail(c, MPM_ERR_INVALID, "export_wait: nothing exported into this slot");
+  MPM_CUDA(c, cudaEventSynchronize(x.copied));
+  *records = x.host;
+  *n = x.n;
+  return MPM_OK;
+}
+
+int64_t mpm_bgeo_header(int64_t n, uint8_t* out, int64_t capacity) { return bgeo_header(n, out, capacity); }
+
+mpm_status mpm_write_bgeo(const char* path, const void* records, int64_t n) {
+  if (!path || n < 0 || (n > 0 && !records)) return MPM_ERR_INVALID;
+  uint8_t head[256];
+  const int64_t hn = bgeo_header(n, head, sizeof(head));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return MPM_ERR_IO;
+  bool ok = std::fwrite(head, 1, (size_t)hn, f) == (size_t)hn;
+  if (ok && n > 0)
+    ok = std::fwrite(records, 1, (size_t)kBgeoRecordBytes * (size_t)n, f) == (size_t)kBgeoRecordBytes * (size_t)n;
+  if (ok) ok = std::fwrite(kBgeoTerminator, 1, 2, f) == 2;
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? MPM_OK : MPM_ERR_IO;
+}
+
+mpm_status mpm_render_positions_device(mpm_ctx* c, const float** positions) {
+  if (!c || !positions) return MPM_ERR_INVALID;
+  if (c->n > c->positions_cap) {
+    cudaFree(c->positions);
+    c->positions = nullptr;
+    c->positions_cap = 0;
+    if (cudaMalloc(&c->positions, sizeof(float) * 3 * (size_t)c->n) != cudaSuccess)
+      return fail(c, MPM_ERR_NOMEM, "render: positions");
+    c->positions_cap = c->n;
+  }
+  MPM_CUDA(c, launch_project(c->sA, c->stride, c->idA, c->n, c->positions, c->stream));
+  c->launches += c->n > 0;
+  *positions = c->positions;
+  return MPM_OK;
+}
+
+mpm_status mpm_render_positions(mpm_ctx* c, float* out) {
+  if (!c || (!out && c->n > 0)) return MPM_ERR_INVALID;
+  const float* d = nullptr;
+  mpm_status st = mpm_render_positions_device(c, &d);
+  if (st != MPM_OK) return st;
+  if (c->n > 0)
+    MPM_CUDA(c, cudaMemcpyAsync(out, d, sizeof(float) * 3 * (size_t)c->n, cudaMemcpyDeviceToHost, c->stream));
+  MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+mpm_status mpm_render_points(mpm_ctx* c, int32_t W, int32_t H, float point_size, const uint8_t color[3],
+                             const uint8_t background[3], uint8_t* rgb) {
+  if (!c || !rgb || !color || !background || W <= 0 || H <= 0 || W > 16384 || H > 16384 || !(point_size > 0.f) ||
+      !(point_size <= 64.f))
+    return fail(c, MPM_ERR_INVALID, "render: bad image size, point size or buffer");
+  const int64_t pixels = (int64_t)W * H;
+  if (4 * pixels > c->image_cap) {
+    cudaFree(c->image);
+    c->image = nullptr;
+    c->image_cap = 0;
+    if (cudaMalloc(&c->image, (size_t)(4 * pixels)) != cudaSuccess) return fail(c, MPM_ERR_NOMEM, "render: image");
+    c->image_cap = 4 * pixels;
+  }
+  MPM_CUDA(c, launch_render_points(c->sA, c->stride, c->n, W, H, point_size, color, background, c->image,
+                                   c->image + pixels, c->stream));
+  c->launches += 2 + (c->n > 0);
+  MPM_CUDA(c, cudaMemcpyAsync(rgb, c->image + pixels, (size_t)(3 * pixels), cudaMemcpyDeviceToHost, c->stream));
+  MPM_CUDA(c, cudaStreamSynchronize(c->stream));
   return MPM_OK;
 }
 
