@@ -606,7 +606,9 @@ mpm_status mpm_diff_forward(mpm_diff* d, const float* x0, const float* v0, const
   }
   d->nsteps = nsteps;
   if (x_out || v_out) {
-    if (launch_interleave(work, d->stride, d->id, n, d->stage, 0, s) != cudaSuccess) return MPM_ERR_CUDA;
+    // the differentiable context never reorders its particles (d->id is the identity)
+    if (launch_interleave(work, d->stride, nullptr, n, d->stage, 0, kFieldX | kFieldV, s) != cudaSuccess)
+      return MPM_ERR_CUDA;
     if (x_out && cudaMemcpyAsync(x_out, d->stage, 12 * n, cudaMemcpyDeviceToHost, s)) return MPM_ERR_CUDA;
     if (v_out && cudaMemcpyAsync(v_out, d->stage + 3 * n, 12 * n, cudaMemcpyDeviceToHost, s)) return MPM_ERR_CUDA;
   }
@@ -672,7 +674,7 @@ mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv
     }
   }
   // out: adjoint of the initial state, host interleaved
-  if (launch_interleave(d->adj, d->stride, d->id, n, d->stage, 0, s) != cudaSuccess) return MPM_ERR_CUDA;
+  if (launch_interleave(d->adj, d->stride, nullptr, n, d->stage, 0, kFieldAll, s) != cudaSuccess) return MPM_ERR_CUDA;
   float* Cs = vs + 3 * n;
   float* Fs = Cs + 9 * n;
   if ((gx0 && cudaMemcpyAsync(gx0, xs, 12 * n, cudaMemcpyDeviceToHost, s)) ||

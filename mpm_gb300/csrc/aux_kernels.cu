@@ -275,26 +275,37 @@ __global__ void deinterleave_kernel(const float* stage, float* s, int64_t st, in
   }
 }
 
-__global__ void interleave_kernel(const float* s, int64_t st, const uint32_t* id, int64_t n, float* stage,
-                                  int liquid_layout) {
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t q = id[p];
+__global__ void inverse_kernel(const uint32_t* __restrict__ id, int64_t n, uint32_t* __restrict__ inv) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+    inv[id[p]] = (uint32_t)p;
+}
+
+// Staging arrays in upload order: thread r gathers particle inv[r] (scattered reads) and
+// writes its own entries of the requested fields (coalesced writes).
+__global__ void interleave_kernel(const float* __restrict__ s, int64_t st, const uint32_t* __restrict__ inv, int64_t n,
+                                  float* __restrict__ stage, int liquid_layout, unsigned fields) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = inv ? inv[r] : r;
     float* xs = stage;
     float* vs = xs + 3 * n;
     float* Cs = vs + 3 * n;
     float* Fs = Cs + 9 * n;
     float* Js = Fs + 9 * n;
-    for (int d = 0; d < 3; ++d) {
-      xs[3 * q + d] = s[(kX + d) * st + p];
-      vs[3 * q + d] = s[(kV + d) * st + p];
+    if (fields & kFieldX)
+      for (int d = 0; d < 3; ++d) xs[3 * r + d] = s[(kX + d) * st + p];
+    if (fields & kFieldV)
+      for (int d = 0; d < 3; ++d) vs[3 * r + d] = s[(kV + d) * st + p];
+    if (fields & kFieldC)
+      for (int i = 0; i < 9; ++i) Cs[9 * r + i] = s[(kC + i) * st + p];
+    if (fields & (kFieldF | kFieldJ)) {
+      const float J = s[kJp * st + p];
+      if (fields & kFieldJ) Js[r] = J;
+      if (fields & kFieldF) {
+        const float cr = liquid_layout ? cbrtf(J) : 0.f;
+        for (int i = 0; i < 9; ++i)
+          Fs[9 * r + i] = liquid_layout ? ((i % 4 == 0) ? cr : 0.f) : s[(kF + i) * st + p];
+      }
     }
-    const float J = s[kJp * st + p];
-    const float cr = liquid_layout ? cbrtf(J) : 0.f;
-    for (int i = 0; i < 9; ++i) {
-      Cs[9 * q + i] = s[(kC + i) * st + p];
-      Fs[9 * q + i] = liquid_layout ? ((i % 4 == 0) ? cr : 0.f) : s[(kF + i) * st + p];
-    }
-    Js[q] = J;
   }
 }
 
@@ -317,10 +328,30 @@ cudaError_t launch_deinterleave(const float* stage, float* s, int64_t stride, in
   return cudaGetLastError();
 }
 
-cudaError_t launch_interleave(const float* s, int64_t stride, const uint32_t* id, int64_t n, float* stage,
-                              int liquid_layout, cudaStream_t st) {
+cudaError_t launch_inverse(const uint32_t* id, int64_t n, uint32_t* inv, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  interleave_kernel<<<grid_for(n), 256, 0, st>>>(s, stride, id, n, stage, liquid_layout);
+  inverse_kernel<<<grid_for(n), 256, 0, st>>>(id, n, inv);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_interleave(const float* s, int64_t stride, const uint32_t* inv, int64_t n, float* stage,
+                              int liquid_layout, unsigned fields, cudaStream_t st) {
+  if (n == 0 || fields == 0) return cudaSuccess;
+  interleave_kernel<<<grid_for(n), 256, 0, st>>>(s, stride, inv, n, stage, liquid_layout, fields);
+  return cudaGetLastError();
+}
+
+namespace {
+__global__ void check_finite_kernel(const float* __restrict__ x, int64_t m, int* flag) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+    if (!isfinite(x[i])) *flag = 1;  // every writer stores the same value
+}
+}  // namespace
+
+cudaError_t launch_check_finite(const float* x, int64_t m, int* flag, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
+  if (e != cudaSuccess || m == 0) return e;
+  check_finite_kernel<<<(int)std::min<int64_t>(grid_for(m), 2048), 256, 0, st>>>(x, m, flag);
   return cudaGetLastError();
 }
 

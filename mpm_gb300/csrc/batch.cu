@@ -426,8 +426,12 @@ mpm_status mpm_batch_download_soa(mpm_batch* b, float* x, float* v, float* C, fl
   if (!b) return MPM_ERR_INVALID;
   const int64_t n = b->n;
   if (n == 0) return MPM_OK;
-  BCUDA(b, launch_interleave(b->sA, b->stride, b->idA, n, b->stage, 0, b->stream));
-  b->launches += 1;
+  const unsigned fields = (x ? kFieldX : 0) | (v ? kFieldV : 0) | (C ? kFieldC : 0) | (F ? kFieldF : 0) |
+                          (Jp ? kFieldJ : 0);
+  uint32_t* inv = b->keys;  // free outside the sort
+  BCUDA(b, launch_inverse(b->idA, n, inv, b->stream));
+  BCUDA(b, launch_interleave(b->sA, b->stride, inv, n, b->stage, 0, fields, b->stream));
+  b->launches += 2;
   float* xs = b->stage;
   float* vs = xs + 3 * n;
   float* Cs = vs + 3 * n;

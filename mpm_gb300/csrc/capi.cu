@@ -70,7 +70,7 @@ struct mpm_ctx {
   float* stage = nullptr;
   size_t stage_bytes = 0;
   int* status = nullptr;
-  int* work = nullptr;  // two range counters, alternating between substep launches
+  int* work = nullptr;  // two range counters, alternating between substep launches; [2]: upload check
   int launch_parity = 0;
 
   int64_t substeps = 0;
@@ -464,7 +464,7 @@ mpm_status mpm_create(const mpm_params* params, mpm_ctx** out) {
   if (cudaMalloc(&c->counts, sizeof(int) * c->sort_keys) != cudaSuccess) return bail(MPM_ERR_NOMEM);
   if (cudaMalloc(&c->block_sums, sizeof(int) * std::max<int64_t>(nb, 1)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
   if (cudaMalloc(&c->status, sizeof(int)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
-  if (cudaMalloc(&c->work, 2 * sizeof(int)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
+  if (cudaMalloc(&c->work, 4 * sizeof(int)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
   if (cudaMemsetAsync(c->work, 0, 2 * sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
 
   if (cudaMemsetAsync(c->status, 0, sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
@@ -550,8 +550,31 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   if (mat)
     for (int64_t p = 0; p < n; ++p)
       if (mat[p] >= c->n_materials) return fail(c, MPM_ERR_INVALID, "material index out of range");
-  for (int64_t i = 0; i < 3 * n; ++i)
-    if (!std::isfinite(x[i])) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
+  // The arrays go to the staging buffer first; positions are checked there on the GPU (a
+  // host loop over them cost more than the copies), and the context is changed only once
+  // they pass.
+  float *xs = nullptr, *vs = nullptr, *Cs = nullptr, *Fs = nullptr, *Js = nullptr;
+  if (n > 0) {
+    st = ensure_stage(c, 25 * sizeof(float) * (size_t)n);
+    if (st != MPM_OK) return st;
+    xs = c->stage;
+    vs = xs + 3 * n;
+    Cs = vs + 3 * n;
+    Fs = Cs + 9 * n;
+    Js = Fs + 9 * n;
+    MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // the stage may still feed an earlier call
+    MPM_CUDA(c, cudaMemcpyAsync(xs, x, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+    if (v) MPM_CUDA(c, cudaMemcpyAsync(vs, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+    if (C) MPM_CUDA(c, cudaMemcpyAsync(Cs, C, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, c->stream));
+    if (F) MPM_CUDA(c, cudaMemcpyAsync(Fs, F, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, c->stream));
+    if (Jp) MPM_CUDA(c, cudaMemcpyAsync(Js, Jp, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+    MPM_CUDA(c, launch_check_finite(xs, 3 * n, c->work + 2, c->stream));
+    int bad = 0;
+    MPM_CUDA(c, cudaMemcpyAsync(&bad, c->work + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->launches += 1;
+    if (bad) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
+  }
   st = ensure_particles(c, n);
   if (st != MPM_OK) return st;
   c->n = n;
@@ -562,19 +585,6 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   c->t = 0.0;
   free_objects(c);
   if (n == 0) return MPM_OK;
-  const size_t per = 25 * sizeof(float);
-  st = ensure_stage(c, per * (size_t)n);
-  if (st != MPM_OK) return st;
-  float* xs = c->stage;
-  float* vs = xs + 3 * n;
-  float* Cs = vs + 3 * n;
-  float* Fs = Cs + 9 * n;
-  float* Js = Fs + 9 * n;
-  MPM_CUDA(c, cudaMemcpyAsync(xs, x, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
-  if (v) MPM_CUDA(c, cudaMemcpyAsync(vs, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
-  if (C) MPM_CUDA(c, cudaMemcpyAsync(Cs, C, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, c->stream));
-  if (F) MPM_CUDA(c, cudaMemcpyAsync(Fs, F, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, c->stream));
-  if (Jp) MPM_CUDA(c, cudaMemcpyAsync(Js, Jp, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
   MPM_CUDA(c, launch_deinterleave(c->stage, c->sA, c->stride, n, v != nullptr, C != nullptr, F != nullptr,
                                   Jp != nullptr, c->stream));
   MPM_CUDA(c, launch_iota(c->idA, n, c->stream));
@@ -720,8 +730,13 @@ mpm_status mpm_download_soa(mpm_ctx* c, float* x, float* v, float* C, float* F, 
   if (n == 0) return MPM_OK;
   mpm_status st = ensure_stage(c, 25 * sizeof(float) * (size_t)n + (size_t)n);
   if (st != MPM_OK) return st;
-  MPM_CUDA(c, launch_interleave(c->sA, c->stride, c->idA, n, c->stage, c->liquid_layout, c->stream));
-  c->launches += 1;
+  const unsigned fields = (x ? kFieldX : 0) | (v ? kFieldV : 0) | (C ? kFieldC : 0) | (F ? kFieldF : 0) |
+                          (Jp ? kFieldJ : 0);
+  // the particles sit in cell order: invert the id array into the other id copy (free
+  // outside sorts and object updates) and gather in upload order
+  MPM_CUDA(c, launch_inverse(c->idA, n, c->idB, c->stream));
+  MPM_CUDA(c, launch_interleave(c->sA, c->stride, c->idB, n, c->stage, c->liquid_layout, fields, c->stream));
+  c->launches += 2;
   float* xs = c->stage;
   float* vs = xs + 3 * n;
   float* Cs = vs + 3 * n;
@@ -881,14 +896,15 @@ mpm_status mpm_export_particles(mpm_ctx* c, int32_t slot, float radius, int64_t*
     if (cudaMallocHost(&x.host, bytes) != cudaSuccess) return fail(c, MPM_ERR_NOMEM, "export: pinned buffer");
     x.cap = cnt;
   }
-  MPM_CUDA(c, launch_bgeo_pack(c->sA, c->stride, c->idA, cnt, radius, x.dev, c->stream));
+  MPM_CUDA(c, launch_inverse(c->idA, cnt, c->idB, c->stream));
+  MPM_CUDA(c, launch_bgeo_pack(c->sA, c->stride, c->idB, cnt, radius, x.dev, c->stream));
   MPM_CUDA(c, cudaEventRecord(x.packed, c->stream));
   MPM_CUDA(c, cudaStreamWaitEvent(c->copy_stream, x.packed, 0));
   if (cnt > 0)
     MPM_CUDA(c, cudaMemcpyAsync(x.host, x.dev, (size_t)kBgeoRecordBytes * (size_t)cnt, cudaMemcpyDeviceToHost,
                                 c->copy_stream));
   MPM_CUDA(c, cudaEventRecord(x.copied, c->copy_stream));
-  c->launches += cnt > 0;
+  c->launches += 2 * (cnt > 0);
   x.n = cnt;
   x.pending = true;
   *n = cnt;
@@ -931,8 +947,9 @@ mpm_status mpm_render_positions_device(mpm_ctx* c, const float** positions) {
       return fail(c, MPM_ERR_NOMEM, "render: positions");
     c->positions_cap = c->n;
   }
-  MPM_CUDA(c, launch_project(c->sA, c->stride, c->idA, c->n, c->positions, c->stream));
-  c->launches += c->n > 0;
+  MPM_CUDA(c, launch_inverse(c->idA, c->n, c->idB, c->stream));
+  MPM_CUDA(c, launch_project(c->sA, c->stride, c->idB, c->n, c->positions, c->stream));
+  c->launches += 2 * (c->n > 0);
   *positions = c->positions;
   return MPM_OK;
 }

@@ -8,8 +8,9 @@
 // Houdini's classic binary geometry, version 5: a big-endian header, one definition per
 // non-position attribute, then per point its homogeneous position (x, y, z, 1) followed by
 // the attributes in definition order, then two terminator bytes.  bgeo_pack_kernel writes
-// those point records (36 bytes: P, id, velocity, radius) already byte-swapped, each at its
-// particle's active-list index, so the host only adds the header and the terminator.
+// those point records (36 bytes: P, id, velocity, radius) already byte-swapped, in
+// active-list order (gathering through the inverse of the id array), so the host only adds
+// the header and the terminator.
 //
 // Render: the reference draws the particles with OpenGL (Renderer::render,
 // include/renderer.h:43-63; shaders/cube_vertex.glsl, shaders/constant_fragment.glsl): the
@@ -32,40 +33,45 @@ constexpr int kExportThreads = 256;
 
 __device__ __forceinline__ uint32_t be32(uint32_t v) { return __byte_perm(v, 0, 0x0123); }
 
-__global__ void bgeo_pack_kernel(const float* __restrict__ s, int64_t st, const uint32_t* __restrict__ id,
-                                 int64_t n, float radius, uint32_t* __restrict__ out) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const uint32_t r = id ? id[p] : (uint32_t)p;
-  const uint32_t w[9] = {be32(__float_as_uint(s[(kX + 0) * st + p])), be32(__float_as_uint(s[(kX + 1) * st + p])),
-                         be32(__float_as_uint(s[(kX + 2) * st + p])), be32(__float_as_uint(1.f)),
-                         be32(r),
-                         be32(__float_as_uint(s[(kV + 0) * st + p])), be32(__float_as_uint(s[(kV + 1) * st + p])),
-                         be32(__float_as_uint(s[(kV + 2) * st + p])), be32(__float_as_uint(radius))};
-  // the records land at scattered places: 8-byte stores (a record at 36 r starts 8-byte
-  // aligned for even r, 4 bytes past it for odd r) halve the write requests
-  uint32_t* o = out + 9 * (int64_t)r;
-  if ((r & 1u) == 0) {
-    uint2* q = reinterpret_cast<uint2*>(o);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) q[c] = make_uint2(w[2 * c], w[2 * c + 1]);
-    o[8] = w[8];
-  } else {
-    o[0] = w[0];
-    uint2* q = reinterpret_cast<uint2*>(o + 1);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) q[c] = make_uint2(w[2 * c + 1], w[2 * c + 2]);
+// Thread r writes record r (the particle at device slot inv[r]): the block's records are
+// staged in shared memory and stored as 16-byte chunks (a block's 256 records, 9216 bytes,
+// start 16-byte aligned).
+__global__ void __launch_bounds__(kExportThreads) bgeo_pack_kernel(const float* __restrict__ s, int64_t st,
+                                                                   const uint32_t* __restrict__ inv, int64_t n,
+                                                                   float radius, uint32_t* __restrict__ out) {
+  __shared__ __align__(16) uint32_t rec[kExportThreads * 9];
+  const int64_t r0 = (int64_t)blockIdx.x * kExportThreads;
+  const int64_t r = r0 + threadIdx.x;
+  if (r < n) {
+    const int64_t p = inv ? inv[r] : r;
+    uint32_t* w = rec + 9 * threadIdx.x;
+    w[0] = be32(__float_as_uint(s[(kX + 0) * st + p]));
+    w[1] = be32(__float_as_uint(s[(kX + 1) * st + p]));
+    w[2] = be32(__float_as_uint(s[(kX + 2) * st + p]));
+    w[3] = be32(__float_as_uint(1.f));
+    w[4] = be32((uint32_t)r);
+    w[5] = be32(__float_as_uint(s[(kV + 0) * st + p]));
+    w[6] = be32(__float_as_uint(s[(kV + 1) * st + p]));
+    w[7] = be32(__float_as_uint(s[(kV + 2) * st + p]));
+    w[8] = be32(__float_as_uint(radius));
   }
+  __syncthreads();
+  const int64_t cnt = n - r0 < kExportThreads ? n - r0 : kExportThreads;
+  const int words = (int)(9 * cnt);
+  uint4* dst = reinterpret_cast<uint4*>(out + 9 * r0);
+  const uint4* src = reinterpret_cast<const uint4*>(rec);
+  for (int q = threadIdx.x; q < words / 4; q += kExportThreads) dst[q] = src[q];
+  for (int q = (words / 4) * 4 + threadIdx.x; q < words; q += kExportThreads) out[9 * r0 + q] = rec[q];
 }
 
 // (x - 0.5) * 1.8 per coordinate (Renderer::setParticlePositions), active-list order.
 __device__ __forceinline__ float clip_coord(float x) { return __fmul_rn(__fsub_rn(x, 0.5f), 1.8f); }
 
-__global__ void project_kernel(const float* __restrict__ s, int64_t st, const uint32_t* __restrict__ id, int64_t n,
+__global__ void project_kernel(const float* __restrict__ s, int64_t st, const uint32_t* __restrict__ inv, int64_t n,
                                float* __restrict__ out) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const int64_t r = id ? id[p] : p;
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int64_t p = inv ? inv[r] : r;
 #pragma unroll
   for (int c = 0; c < 3; ++c) out[3 * r + c] = clip_coord(s[(kX + c) * st + p]);
 }
@@ -112,17 +118,17 @@ int blocks_for(int64_t n) { return (int)std::max<int64_t>(1, (n + kExportThreads
 
 }  // namespace
 
-cudaError_t launch_bgeo_pack(const float* s, int64_t stride, const uint32_t* id, int64_t n, float radius,
+cudaError_t launch_bgeo_pack(const float* s, int64_t stride, const uint32_t* inv, int64_t n, float radius,
                              void* records, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  bgeo_pack_kernel<<<blocks_for(n), kExportThreads, 0, st>>>(s, stride, id, n, radius, (uint32_t*)records);
+  bgeo_pack_kernel<<<blocks_for(n), kExportThreads, 0, st>>>(s, stride, inv, n, radius, (uint32_t*)records);
   return cudaGetLastError();
 }
 
-cudaError_t launch_project(const float* s, int64_t stride, const uint32_t* id, int64_t n, float* out,
+cudaError_t launch_project(const float* s, int64_t stride, const uint32_t* inv, int64_t n, float* out,
                            cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  project_kernel<<<blocks_for(n), kExportThreads, 0, st>>>(s, stride, id, n, out);
+  project_kernel<<<blocks_for(n), kExportThreads, 0, st>>>(s, stride, inv, n, out);
   return cudaGetLastError();
 }
 

@@ -128,9 +128,17 @@ cudaError_t launch_sort(const SortArgs& a, int num_sms, cudaStream_t st, int64_t
 // Host-interleaved <-> component-major conversion.
 cudaError_t launch_deinterleave(const float* stage, float* s, int64_t stride, int64_t n, int has_v,
                                 int has_C, int has_F, int has_Jp, cudaStream_t st);
-cudaError_t launch_interleave(const float* s, int64_t stride, const uint32_t* id, int64_t n, float* stage,
-                              int liquid_layout, cudaStream_t st);
+// Fields of launch_interleave.
+constexpr unsigned kFieldX = 1, kFieldV = 2, kFieldC = 4, kFieldF = 8, kFieldJ = 16, kFieldAll = 31;
+// inv[id[p]] = p: the device slot of each particle in upload order.
+cudaError_t launch_inverse(const uint32_t* id, int64_t n, uint32_t* inv, cudaStream_t st);
+// Staging arrays (x, v, C, F, Jp blocks) in upload order from the particle arrays, inv as
+// from launch_inverse (null: device order is upload order), only the requested fields.
+cudaError_t launch_interleave(const float* s, int64_t stride, const uint32_t* inv, int64_t n, float* stage,
+                              int liquid_layout, unsigned fields, cudaStream_t st);
 cudaError_t launch_iota(uint32_t* id, int64_t n, cudaStream_t st);
+// *flag = 1 when any of the m floats is not finite (0 otherwise).
+cudaError_t launch_check_finite(const float* x, int64_t m, int* flag, cudaStream_t st);
 cudaError_t launch_scatter_u8(const uint8_t* src, const uint32_t* id, int64_t n, uint8_t* dst, cudaStream_t st);
 // Scene objects: append k seeded particles (positions xs, 3 floats each) at index n0 with
 // velocity v, C = 0, F = I, Jp = 1, material mat_index and ids id0.., and remove the

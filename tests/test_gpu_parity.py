@@ -222,12 +222,26 @@ def test_check_finite_flags_non_finite_state(gpu_lib):
             sim.sync()
         assert ei.value.code == 3
         sim.sync()  # the status word is cleared once reported
-    # non-finite positions are rejected on the host
-    cfg["state"]["x"][3] = [np.nan, 0.5, 0.5]
+    # non-finite positions are rejected before the context changes
+    cfg = scenes.config_elastic(n=2000, seed=9)
+    good = {k: v.copy() for k, v in cfg["state"].items()}
     with Simulation.from_config(cfg) as sim:
-        with pytest.raises(_lib.MpmError) as ei:
-            sim.upload(cfg["state"])
-        assert ei.value.code == 1
+        sim.upload(good)
+        sim.advance(2)
+        before = sim.download()
+        bad = dict(cfg["state"])
+        for row, val in ((3, [np.nan, 0.5, 0.5]), (1999, [0.5, np.inf, 0.5])):
+            bad["x"] = good["x"].copy()
+            bad["x"][row] = val
+            bad["x"] = np.concatenate([bad["x"], good["x"][:100]])  # a larger count as well
+            bad = {k: (np.concatenate([good[k], good[k][:100]]) if k != "x" else bad["x"]) for k in good}
+            with pytest.raises(_lib.MpmError) as ei:
+                sim.upload(bad)
+            assert ei.value.code == 1
+        assert sim.n == len(good["x"]) and sim.substeps == 2
+        after = sim.download()
+        for k in before:
+            assert np.array_equal(before[k], after[k]), k
 
 
 def test_api_errors(gpu_lib):
