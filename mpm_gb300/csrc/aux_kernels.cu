@@ -328,6 +328,118 @@ cudaError_t launch_deinterleave(const float* stage, float* s, int64_t stride, in
   return cudaGetLastError();
 }
 
+namespace {
+
+// The block's part of a host array (w floats per particle) through shared memory: 16-byte
+// loads or stores of the contiguous range when it is 16-byte aligned, plain ones otherwise.
+template <int W>
+__device__ __forceinline__ void load_rows(const float* __restrict__ src, int64_t r0, int cnt, float* tile) {
+  const float* base = src + W * r0;
+  const int words = W * cnt;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) == 0) {
+    const float4* b4 = reinterpret_cast<const float4*>(base);
+    for (int q = threadIdx.x; q < words / 4; q += blockDim.x) reinterpret_cast<float4*>(tile)[q] = b4[q];
+    for (int q = (words / 4) * 4 + threadIdx.x; q < words; q += blockDim.x) tile[q] = base[q];
+  } else {
+    for (int q = threadIdx.x; q < words; q += blockDim.x) tile[q] = base[q];
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void store_rows(float* __restrict__ dst, int64_t r0, int cnt, const float* tile) {
+  float* base = dst + W * r0;
+  const int words = W * cnt;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) == 0) {
+    float4* b4 = reinterpret_cast<float4*>(base);
+    for (int q = threadIdx.x; q < words / 4; q += blockDim.x) b4[q] = reinterpret_cast<const float4*>(tile)[q];
+    for (int q = (words / 4) * 4 + threadIdx.x; q < words; q += blockDim.x) base[q] = tile[q];
+  } else {
+    for (int q = threadIdx.x; q < words; q += blockDim.x) base[q] = tile[q];
+  }
+}
+
+constexpr int kRowsPerBlock = 256;
+
+// Host-interleaved arrays (device-visible host memory, or device memory) -> component-major
+// particle arrays; *bad = 1 when a position is not finite.  One block per 256 particles,
+// each array moved through shared memory in contiguous 16-byte pieces.
+__global__ void __launch_bounds__(kRowsPerBlock) deinterleave_arrays_kernel(HostArrays a, float* __restrict__ s,
+                                                                            int64_t st, int64_t n, int* bad) {
+  __shared__ __align__(16) float tile[9 * kRowsPerBlock];
+  const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
+  const int cnt = (int)(n - r0 < kRowsPerBlock ? n - r0 : kRowsPerBlock);
+  const int t = threadIdx.x;
+  const int64_t p = r0 + t;
+  auto field = [&](const float* src, int W, int comp0, auto def) {
+    if (src) {
+      if (W == 1) load_rows<1>(src, r0, cnt, tile);
+      else if (W == 3) load_rows<3>(src, r0, cnt, tile);
+      else load_rows<9>(src, r0, cnt, tile);
+    }
+    __syncthreads();
+    if (t < cnt)
+      for (int d = 0; d < W; ++d) {
+        const float v = src ? tile[W * t + d] : def(d);
+        if (comp0 == kX && !isfinite(v)) *bad = 1;
+        s[(int64_t)(comp0 + d) * st + p] = v;
+      }
+    __syncthreads();
+  };
+  field(a.x, 3, kX, [](int) { return 0.f; });
+  field(a.v, 3, kV, [](int) { return 0.f; });
+  field(a.C, 9, kC, [](int) { return 0.f; });
+  field(a.F, 9, kF, [](int d) { return (d % 4 == 0) ? 1.f : 0.f; });
+  field(a.J, 1, kJp, [](int) { return 1.f; });
+}
+
+// Component-major particle arrays -> host arrays in upload order (record r from device slot
+// inv[r]), written through shared memory in contiguous 16-byte pieces.
+__global__ void __launch_bounds__(kRowsPerBlock) interleave_arrays_kernel(const float* __restrict__ s, int64_t st,
+                                                                          const uint32_t* __restrict__ inv, int64_t n,
+                                                                          OutArrays o, int liquid_layout) {
+  __shared__ __align__(16) float tile[9 * kRowsPerBlock];
+  const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
+  const int cnt = (int)(n - r0 < kRowsPerBlock ? n - r0 : kRowsPerBlock);
+  const int t = threadIdx.x;
+  const int64_t p = t < cnt ? (inv ? (int64_t)inv[r0 + t] : r0 + t) : 0;
+  auto field = [&](float* dst, int W, auto value) {
+    if (!dst) return;
+    if (t < cnt)
+      for (int d = 0; d < W; ++d) tile[W * t + d] = value(d);
+    __syncthreads();
+    if (W == 1) store_rows<1>(dst, r0, cnt, tile);
+    else if (W == 3) store_rows<3>(dst, r0, cnt, tile);
+    else store_rows<9>(dst, r0, cnt, tile);
+    __syncthreads();
+  };
+  field(o.x, 3, [&](int d) { return s[(int64_t)(kX + d) * st + p]; });
+  field(o.v, 3, [&](int d) { return s[(int64_t)(kV + d) * st + p]; });
+  field(o.C, 9, [&](int d) { return s[(int64_t)(kC + d) * st + p]; });
+  field(o.F, 9, [&](int d) {
+    if (!liquid_layout) return s[(int64_t)(kF + d) * st + p];
+    return (d % 4 == 0) ? cbrtf(s[(int64_t)kJp * st + p]) : 0.f;
+  });
+  field(o.J, 1, [&](int) { return s[(int64_t)kJp * st + p]; });
+}
+
+}  // namespace
+
+cudaError_t launch_deinterleave_arrays(HostArrays a, float* s, int64_t stride, int64_t n, int* bad, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), st);
+  if (e != cudaSuccess || n == 0) return e;
+  deinterleave_arrays_kernel<<<(unsigned)((n + kRowsPerBlock - 1) / kRowsPerBlock), kRowsPerBlock, 0, st>>>(a, s, stride,
+                                                                                                        n, bad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_interleave_arrays(const float* s, int64_t stride, const uint32_t* inv, int64_t n, OutArrays o,
+                                     int liquid_layout, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  interleave_arrays_kernel<<<(unsigned)((n + kRowsPerBlock - 1) / kRowsPerBlock), kRowsPerBlock, 0, st>>>(
+      s, stride, inv, n, o, liquid_layout);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_inverse(const uint32_t* id, int64_t n, uint32_t* inv, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   inverse_kernel<<<grid_for(n), 256, 0, st>>>(id, n, inv);

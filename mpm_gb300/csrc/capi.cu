@@ -145,6 +145,27 @@ void derive_consts(mpm_ctx* c) { mpm::make_sim_consts(c->params, c->mats, c->n_m
 // The compact liquid layout (x, v, C, J) is used when the table is a single liquid.
 bool all_liquid(const mpm_ctx* c) { return c->n_materials == 1 && c->mats[0].kind == MPM_MAT_LIQUID; }
 
+// Whether [p, p + bytes) lies in one pinned host allocation the device can address; *dev
+// receives the device view of p.  Pageable or unknown memory goes through copies instead.
+bool device_view(const void* p, size_t bytes, const void** dev) {
+  if (!p || bytes == 0) return false;
+  cudaPointerAttributes a{}, b{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const char* last = (const char*)p + bytes - 1;
+  if (cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost || !a.devicePointer || !b.devicePointer)
+    return false;
+  if ((const char*)b.devicePointer - (const char*)a.devicePointer != (ptrdiff_t)(bytes - 1)) return false;
+  *dev = a.devicePointer;
+  return true;
+}
+
 mpm_status ensure_stage(mpm_ctx* c, size_t bytes) {
   if (c->stage_bytes >= bytes) return MPM_OK;
   if (c->stage) cudaFree(c->stage);
@@ -550,33 +571,63 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   if (mat)
     for (int64_t p = 0; p < n; ++p)
       if (mat[p] >= c->n_materials) return fail(c, MPM_ERR_INVALID, "material index out of range");
-  // The arrays go to the staging buffer first; positions are checked there on the GPU (a
-  // host loop over them cost more than the copies), and the context is changed only once
-  // they pass.
-  float *xs = nullptr, *vs = nullptr, *Cs = nullptr, *Fs = nullptr, *Js = nullptr;
-  if (n > 0) {
+  // The positions are checked on the GPU (a host loop over them cost more than the
+  // copies) and the context changes only once they pass.  Arrays in pinned host memory are
+  // read by the conversion kernel itself over the host link; others go through the staging
+  // buffer with copies.  When the particle arrays keep their size, the conversion writes
+  // the spare copy, which replaces the current one after the check.
+  const bool grow = n > c->capacity || !c->sA;
+  HostArrays arr{};
+  bool direct = false;
+  if (n > 0 && !grow) {
+    const void *dx = nullptr, *dv = nullptr, *dC = nullptr, *dF = nullptr, *dJ = nullptr;
+    direct = device_view(x, 12 * n, &dx) && (!v || device_view(v, 12 * n, &dv)) &&
+             (!C || device_view(C, 36 * n, &dC)) && (!F || device_view(F, 36 * n, &dF)) &&
+             (!Jp || device_view(Jp, 4 * n, &dJ));
+    if (direct) arr = HostArrays{(const float*)dx, (const float*)dv, (const float*)dC, (const float*)dF, (const float*)dJ};
+  }
+  if (n > 0 && !direct) {
     st = ensure_stage(c, 25 * sizeof(float) * (size_t)n);
     if (st != MPM_OK) return st;
-    xs = c->stage;
-    vs = xs + 3 * n;
-    Cs = vs + 3 * n;
-    Fs = Cs + 9 * n;
-    Js = Fs + 9 * n;
+    float* xs = c->stage;
+    float* vs = xs + 3 * n;
+    float* Cs = vs + 3 * n;
+    float* Fs = Cs + 9 * n;
+    float* Js = Fs + 9 * n;
     MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // the stage may still feed an earlier call
     MPM_CUDA(c, cudaMemcpyAsync(xs, x, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
     if (v) MPM_CUDA(c, cudaMemcpyAsync(vs, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, c->stream));
     if (C) MPM_CUDA(c, cudaMemcpyAsync(Cs, C, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, c->stream));
     if (F) MPM_CUDA(c, cudaMemcpyAsync(Fs, F, sizeof(float) * 9 * n, cudaMemcpyHostToDevice, c->stream));
     if (Jp) MPM_CUDA(c, cudaMemcpyAsync(Js, Jp, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
-    MPM_CUDA(c, launch_check_finite(xs, 3 * n, c->work + 2, c->stream));
-    int bad = 0;
-    MPM_CUDA(c, cudaMemcpyAsync(&bad, c->work + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    MPM_CUDA(c, cudaStreamSynchronize(c->stream));
-    c->launches += 1;
-    if (bad) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
+    arr = HostArrays{xs, v ? vs : nullptr, C ? Cs : nullptr, F ? Fs : nullptr, Jp ? Js : nullptr};
   }
-  st = ensure_particles(c, n);
-  if (st != MPM_OK) return st;
+  if (n > 0) {
+    int bad = 0;
+    if (grow) {
+      // check the staged positions before the old arrays are released
+      MPM_CUDA(c, launch_check_finite(arr.x, 3 * n, c->work + 2, c->stream));
+      MPM_CUDA(c, cudaMemcpyAsync(&bad, c->work + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+      c->launches += 1;
+      if (bad) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
+      st = ensure_particles(c, n);
+      if (st != MPM_OK) return st;
+      MPM_CUDA(c, launch_deinterleave_arrays(arr, c->sA, c->stride, n, c->work + 2, c->stream));
+    } else {
+      if (direct) MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // earlier work may read the spare copy
+      MPM_CUDA(c, launch_deinterleave_arrays(arr, c->sB, c->stride, n, c->work + 2, c->stream));
+      MPM_CUDA(c, cudaMemcpyAsync(&bad, c->work + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (bad) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
+      std::swap(c->sA, c->sB);
+    }
+    c->launches += 1;
+  }
+  if (n == 0) {
+    st = ensure_particles(c, 0);
+    if (st != MPM_OK) return st;
+  }
   c->n = n;
   c->pending = false;
   c->prev = -1;
@@ -585,10 +636,8 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   c->t = 0.0;
   free_objects(c);
   if (n == 0) return MPM_OK;
-  MPM_CUDA(c, launch_deinterleave(c->stage, c->sA, c->stride, n, v != nullptr, C != nullptr, F != nullptr,
-                                  Jp != nullptr, c->stream));
   MPM_CUDA(c, launch_iota(c->idA, n, c->stream));
-  c->launches += 2;
+  c->launches += 1;
   c->have_mat = !c->liquid_layout && c->n_materials > 1;
   if (c->have_mat) {
     if (mat) {
@@ -728,15 +777,29 @@ mpm_status mpm_download_soa(mpm_ctx* c, float* x, float* v, float* C, float* F, 
   if (!c) return MPM_ERR_INVALID;
   const int64_t n = c->n;
   if (n == 0) return MPM_OK;
+  // the particles sit in cell order: invert the id array into the other id copy (free
+  // outside sorts and object updates) and gather in upload order
+  MPM_CUDA(c, launch_inverse(c->idA, n, c->idB, c->stream));
+  c->launches += 1;
+  {
+    // pinned host arrays are written by the conversion kernel itself over the host link
+    const void *dx = nullptr, *dv = nullptr, *dC = nullptr, *dF = nullptr, *dJ = nullptr;
+    const bool direct = (x || v || C || F || Jp) && (!x || device_view(x, 12 * n, &dx)) &&
+                        (!v || device_view(v, 12 * n, &dv)) && (!C || device_view(C, 36 * n, &dC)) &&
+                        (!F || device_view(F, 36 * n, &dF)) && (!Jp || device_view(Jp, 4 * n, &dJ));
+    if (direct) {
+      const OutArrays o{(float*)dx, (float*)dv, (float*)dC, (float*)dF, (float*)dJ};
+      MPM_CUDA(c, launch_interleave_arrays(c->sA, c->stride, c->idB, n, o, c->liquid_layout, c->stream));
+      c->launches += 1;
+      x = v = C = F = Jp = nullptr;  // written
+    }
+  }
   mpm_status st = ensure_stage(c, 25 * sizeof(float) * (size_t)n + (size_t)n);
   if (st != MPM_OK) return st;
   const unsigned fields = (x ? kFieldX : 0) | (v ? kFieldV : 0) | (C ? kFieldC : 0) | (F ? kFieldF : 0) |
                           (Jp ? kFieldJ : 0);
-  // the particles sit in cell order: invert the id array into the other id copy (free
-  // outside sorts and object updates) and gather in upload order
-  MPM_CUDA(c, launch_inverse(c->idA, n, c->idB, c->stream));
   MPM_CUDA(c, launch_interleave(c->sA, c->stride, c->idB, n, c->stage, c->liquid_layout, fields, c->stream));
-  c->launches += 2;
+  c->launches += fields != 0;
   float* xs = c->stage;
   float* vs = xs + 3 * n;
   float* Cs = vs + 3 * n;

@@ -128,6 +128,21 @@ cudaError_t launch_sort(const SortArgs& a, int num_sms, cudaStream_t st, int64_t
 // Host-interleaved <-> component-major conversion.
 cudaError_t launch_deinterleave(const float* stage, float* s, int64_t stride, int64_t n, int has_v,
                                 int has_C, int has_F, int has_Jp, cudaStream_t st);
+// Per-particle host-layout arrays (x, v: 3 floats; C, F: 9 row-major; J: 1), any of them
+// null, in memory the device can read (device memory or mapped pinned host memory).
+struct HostArrays {
+  const float *x, *v, *C, *F, *J;
+};
+struct OutArrays {
+  float *x, *v, *C, *F, *J;
+};
+// Arrays -> component-major particle arrays in one pass (missing fields take their rest
+// values); *bad = 1 when a position is not finite.
+cudaError_t launch_deinterleave_arrays(HostArrays a, float* s, int64_t stride, int64_t n, int* bad, cudaStream_t st);
+// Component-major particle arrays -> the non-null arrays in upload order (inv as from
+// launch_inverse, null for the identity).
+cudaError_t launch_interleave_arrays(const float* s, int64_t stride, const uint32_t* inv, int64_t n, OutArrays o,
+                                     int liquid_layout, cudaStream_t st);
 // Fields of launch_interleave.
 constexpr unsigned kFieldX = 1, kFieldV = 2, kFieldC = 4, kFieldF = 8, kFieldJ = 16, kFieldAll = 31;
 // inv[id[p]] = p: the device slot of each particle in upload order.

@@ -279,3 +279,48 @@ def test_matches_reference_policy_vectors(gpu_lib, case):
     errs = compare_states(out, expect, cfg["params"], cfg["state"])
     assert max(errs.values()) < 1e-5, errs
     assert rel_err(g_p2g, grid) < 1e-5
+
+
+def test_pinned_host_arrays_take_the_direct_path(gpu_lib):
+    """Pinned host arrays are read and written by the conversion kernels over the host link;
+    the results equal those of pageable arrays (staged copies), for both layouts, and a
+    rejected upload leaves the context unchanged."""
+    import ctypes
+
+    import torch
+
+    from mpm_gb300 import _lib, scenes
+    from mpm_gb300.simulation import Simulation
+
+    for cfg in (scenes.config_elastic(n=3000, seed=4), scenes.config_liquid(n=5000, seed=4)):
+        st = cfg["state"]
+        n = len(st["x"])
+        liquid = cfg["materials"][0].kind == 3
+        keys = ("x", "v", "C", "Jp") if liquid else ("x", "v", "C", "F", "Jp")
+        width = {"x": 3, "v": 3, "C": 9, "F": 9, "Jp": 1}
+        pin = {k: torch.from_numpy(np.ascontiguousarray(np.asarray(st[k], np.float32).reshape(n, width[k])))
+               .pin_memory() for k in keys}
+        P = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+        with Simulation.from_config(cfg) as b:
+            b.upload(st)  # staged; sizes the arrays
+            staged = b.download()
+            _lib.check(b.L.mpm_upload_soa(b.ctx, n, P(pin["x"]), P(pin["v"]), P(pin["C"]), P(pin.get("F")),
+                                          P(pin["Jp"]), None), b.ctx)
+            direct = b.download()
+            for k in staged:
+                assert np.array_equal(direct[k], staged[k]), k
+            b.advance(20)
+            ref = b.download()  # pageable: staged copies
+            out = {k: torch.empty((n, width[k]), dtype=torch.float32).pin_memory() for k in keys}
+            _lib.check(b.L.mpm_download_soa(b.ctx, P(out["x"]), P(out["v"]), P(out["C"]), P(out.get("F")),
+                                            P(out["Jp"]), None), b.ctx)
+            for k in keys:
+                assert np.array_equal(out[k].numpy().reshape(ref[k].shape), ref[k]), k
+            # a non-finite position in pinned arrays: rejected, state kept
+            pin["x"][17, 1] = float("nan")
+            code = b.L.mpm_upload_soa(b.ctx, n, P(pin["x"]), P(pin["v"]), P(pin["C"]), P(pin.get("F")),
+                                      P(pin["Jp"]), None)
+            assert code == 1 and b.substeps == 20
+            after = b.download()
+            for k in ref:
+                assert np.array_equal(after[k], ref[k]), k
