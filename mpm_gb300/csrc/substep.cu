@@ -40,6 +40,8 @@
 #include <algorithm>
 #include <climits>
 #include <mutex>
+#include <tuple>
+#include <vector>
 
 #include "mpm_internal.h"
 #include "particle_ops.cuh"
@@ -642,12 +644,27 @@ size_t step_smem_bytes(StepKind kind, bool batch) {
   return b + 128;  // alignment of the TMA tiles
 }
 
+// The kernel's dynamic shared memory limit, set once per kernel, size and device.
+cudaError_t prepare_step_kernel(void* fn, size_t smem) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  static std::mutex mu;
+  static std::vector<std::tuple<void*, size_t, int>> done;
+  std::lock_guard<std::mutex> lock(mu);
+  for (const auto& d : done)
+    if (std::get<0>(d) == fn && std::get<1>(d) == smem && std::get<2>(d) == dev) return cudaSuccess;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) done.emplace_back(fn, smem, dev);
+  return e;
+}
+
 cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guard, int grid_blocks, cudaStream_t st,
                         int64_t* launches) {
   const bool batch = a.nscenes > 0;
   void* fn = select_kernel(kind, liquid, guard, batch);
   const size_t smem = step_smem_bytes(kind, batch);
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = prepare_step_kernel(fn, smem);
   if (e != cudaSuccess) return e;
   if (!batch && kind != kStepP2GOnly) {
     if (!a.vgrid || !a.grid_in) return cudaErrorInvalidValue;
@@ -676,9 +693,18 @@ cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guar
 
 int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem, bool batch) {
   void* fn = select_kernel(kind, liquid, guard, batch);
-  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
+  if (prepare_step_kernel(fn, smem) != cudaSuccess) return 1;
+  // the answer depends on the kernel, its shared memory and the device only: ask once
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static std::mutex mu;
+  static std::vector<std::tuple<void*, size_t, int, int>> known;
+  std::lock_guard<std::mutex> lock(mu);
+  for (const auto& k : known)
+    if (std::get<0>(k) == fn && std::get<1>(k) == smem && std::get<2>(k) == dev) return std::get<3>(k);
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kStepThreads, smem) != cudaSuccess || nb < 1) nb = 1;
+  known.emplace_back(fn, smem, dev, nb);
   return nb;
 }
 
