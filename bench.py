@@ -70,10 +70,9 @@ def make_cfg(name):
 
 
 def dist_setup(args):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from mpm_gb300 import distributed as D
+
+    return D.env()
 
 
 class ClockSampler:
@@ -225,18 +224,14 @@ def run_reference(args):
 def run_ours(args):
     import torch
 
-    world, rank, local = dist_setup(args)
-    if world > 1:
-        import torch.distributed as dist
+    from mpm_gb300 import distributed as D
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+    world, rank, local = D.init("nccl")
     from mpm_gb300 import build
 
     if rank == 0 or world == 1:
         build.build()
-    if world > 1:
-        torch.distributed.barrier()
+    D.barrier()
     from mpm_gb300.simulation import Simulation
 
     cfg, workload = make_cfg(args.config)
@@ -255,8 +250,7 @@ def run_ours(args):
         flush.fill_(1.0)
         sim.advance(1)
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    D.barrier()
     torch.cuda.synchronize()
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -281,13 +275,11 @@ def run_ours(args):
     clocks = sampler.stop(wall0_abs, wall0_abs + wall)
     ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     sim.sync()
-    dev_ms = sum(ms)
-    if world > 1:
-        t = torch.tensor([dev_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = float(t.item())
+    torch.cuda.synchronize()
+    D.barrier()
+    dev_ms = D.max_over_ranks(sum(ms))  # the slowest replica
     ms_per_step = dev_ms / args.steps
-    value = world * n * args.steps / (dev_ms * 1e-3)
+    value = D.job_rate(world * n * args.steps, dev_ms * 1e-3)
 
     fused_ms = [m for m, p in zip(ms, pure) if p]
     kernel_ms = statistics.mean(fused_ms) if fused_ms else ms_per_step
@@ -354,9 +346,11 @@ def run_e2e(sim, cfg, steps, world):
             raise RuntimeError("e2e C ABI call failed")
         if k > 0:
             times.append(t1 - t0)
-    per = statistics.median(times)
+    from mpm_gb300 import distributed as D
+
+    per = D.max_over_ranks(statistics.median(times))  # the slowest replica
     nbytes = 4 * n * sum(fields.values())
-    return {"value": world * n / per, "unit": "particle-substeps/s", "h2d_bytes_per_step": nbytes,
+    return {"value": D.job_rate(world * n, per), "unit": "particle-substeps/s", "h2d_bytes_per_step": nbytes,
             "d2h_bytes_per_step": nbytes, "ms_per_step": 1e3 * per,
             "path": "mpm_upload_soa + mpm_substep(1) + mpm_download_soa, pinned host buffers"}
 
@@ -366,16 +360,14 @@ def run_batched(args):
     against looping plain launches scene by scene (one context per scene)."""
     import torch
 
-    world, rank, local = dist_setup(args)
-    if world > 1:
-        torch.cuda.set_device(local)
-        torch.distributed.init_process_group("nccl")
+    from mpm_gb300 import distributed as D
+
+    world, rank, local = D.init("nccl")
     from mpm_gb300 import build
 
     if rank == 0 or world == 1:
         build.build()
-    if world > 1:
-        torch.distributed.barrier()
+    D.barrier()
     from mpm_gb300 import scenes
     from mpm_gb300.batch import Batch
     from mpm_gb300.simulation import Simulation
@@ -383,7 +375,7 @@ def run_batched(args):
     all_scenes = scenes.config_batched(nscenes=256, seed=0)
     n_all = sum(s["state"]["x"].shape[0] for s in all_scenes)
     # scenes are independent: rank r takes scenes r, r + world, ... (no collective on the data path)
-    scs = all_scenes[rank::world]
+    scs = D.shard(all_scenes, rank, world)
     n = sum(s["state"]["x"].shape[0] for s in scs)
     sub = 50
     stream = torch.cuda.Stream()
@@ -394,8 +386,7 @@ def run_batched(args):
     for _ in range(max(args.warmup, 3)):
         b.advance(sub, graph=True)
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    D.barrier()
     torch.cuda.synchronize()
     steps = max(1, min(args.steps, 20))
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -407,14 +398,11 @@ def run_batched(args):
     torch.cuda.synchronize()
     batched_ms = sum(a.elapsed_time(e) for a, e in ev)
     local_rate = n * sub * steps / (batched_ms * 1e-3)
-    if world > 1:
-        t = torch.tensor([batched_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        batched_ms = float(t.item())
+    batched_ms = D.max_over_ranks(batched_ms)  # the slowest rank's share
     launches = b.launches - l0
     b.sync()
     b.close()
-    value = n_all * sub * steps / (batched_ms * 1e-3)
+    value = D.job_rate(n_all * sub * steps, batched_ms * 1e-3)
 
     # looped plain launches: one context per scene, substep by substep over the scenes
     sims = []
