@@ -5,7 +5,8 @@
 // the bounding box of the scaled mesh (Simulation::loadMesh, src/mpm.cu:330-344), each
 // kept when libigl's winding number says it is inside.  Here the same rejection sampler
 // runs as two GPU passes over the candidates (count, exclusive scan over blocks, write),
-// so the kept particles come out in candidate order.  Candidate i's coordinates come from
+// so the kept particles come out in candidate order; the count pass keeps one bit per
+// candidate, and the write pass regenerates only the kept candidates.  Candidate i's coordinates come from
 // SplitMix64 (Steele, Lea and Flood, "Fast splittable pseudorandom number generators",
 // OOPSLA 2014) of seed + 3 i + axis, so seeding is reproducible on any device and on the
 // host.  Inside tests: boxes keep every candidate, spheres compare the squared distance
@@ -67,18 +68,22 @@ __device__ __forceinline__ bool inside(const SeedShape& sh, const float p[3]) {
   return inside_mesh(sh, p);
 }
 
-// Pass 1: kept candidates per block.
-__global__ void __launch_bounds__(kSeedThreads) seed_count_kernel(SeedShape sh, int* block_counts) {
+// Pass 1: kept candidates per block, and per thread the mask of its kept candidates (the
+// write pass reads it instead of testing again; the mesh test dominates seeding).
+__global__ void __launch_bounds__(kSeedThreads) seed_count_kernel(SeedShape sh, int* block_counts,
+                                                                  uint8_t* masks) {
   __shared__ int warp_sum[kSeedThreads / 32];
   const uint64_t base = (uint64_t)blockIdx.x * kSeedPerBlock + (uint64_t)threadIdx.x * kSeedPerThread;
-  int kept = 0;
+  unsigned mask = 0;
   for (int j = 0; j < kSeedPerThread; ++j) {
     const uint64_t i = base + j;
     if (i >= sh.candidates) break;
     float p[3];
     candidate(sh, i, p);
-    kept += inside(sh, p) ? 1 : 0;
+    if (inside(sh, p)) mask |= 1u << j;
   }
+  masks[(uint64_t)blockIdx.x * kSeedThreads + threadIdx.x] = (uint8_t)mask;
+  int kept = __popc(mask);
 #pragma unroll
   for (int o = 16; o; o >>= 1) kept += __shfl_xor_sync(kFull, kept, o);
   if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = kept;
@@ -92,18 +97,11 @@ __global__ void __launch_bounds__(kSeedThreads) seed_count_kernel(SeedShape sh, 
 
 // Pass 2: write kept candidates in candidate order (block offsets from the scan).
 __global__ void __launch_bounds__(kSeedThreads) seed_write_kernel(SeedShape sh, const int* block_offsets,
-                                                                  float* x) {
+                                                                  const uint8_t* masks, float* x) {
   __shared__ int warp_sum[kSeedThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint64_t base = (uint64_t)blockIdx.x * kSeedPerBlock + (uint64_t)threadIdx.x * kSeedPerThread;
-  unsigned mask = 0;
-  float pts[kSeedPerThread][3];
-  for (int j = 0; j < kSeedPerThread; ++j) {
-    const uint64_t i = base + j;
-    if (i >= sh.candidates) break;
-    candidate(sh, i, pts[j]);
-    if (inside(sh, pts[j])) mask |= 1u << j;
-  }
+  const unsigned mask = masks[(uint64_t)blockIdx.x * kSeedThreads + threadIdx.x];
   const int kept = __popc(mask);
   int inc = kept;
 #pragma unroll
@@ -118,9 +116,11 @@ __global__ void __launch_bounds__(kSeedThreads) seed_write_kernel(SeedShape sh, 
   int64_t out = (int64_t)block_offsets[blockIdx.x] + wpre + inc - kept;
   for (int j = 0; j < kSeedPerThread; ++j) {
     if (!(mask & (1u << j))) continue;
-    x[3 * out + 0] = pts[j][0];
-    x[3 * out + 1] = pts[j][1];
-    x[3 * out + 2] = pts[j][2];
+    float p[3];
+    candidate(sh, base + j, p);
+    x[3 * out + 0] = p[0];
+    x[3 * out + 1] = p[1];
+    x[3 * out + 2] = p[2];
     ++out;
   }
 }
@@ -274,11 +274,13 @@ cudaError_t seed_shape_gpu(const SeedShape& sh, cudaStream_t st, float** x_out, 
   if (nblocks > (int64_t)INT32_MAX) return cudaErrorInvalidValue;
   int* counts = nullptr;
   int* scratch = nullptr;
+  uint8_t* masks = nullptr;
   cudaError_t e = cudaMalloc(&counts, sizeof(int) * (nblocks + 1));
   if (e == cudaSuccess) e = cudaMalloc(&scratch, sizeof(int) * scan_scratch_ints(nblocks + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&masks, (size_t)nblocks * kSeedThreads);
   if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, sizeof(int) * (nblocks + 1), st);
   if (e == cudaSuccess) {
-    seed_count_kernel<<<(unsigned)nblocks, kSeedThreads, 0, st>>>(sh, counts);
+    seed_count_kernel<<<(unsigned)nblocks, kSeedThreads, 0, st>>>(sh, counts, masks);
     e = cudaGetLastError();
   }
   // exclusive scan over nblocks + 1 entries: the last one is the total
@@ -290,13 +292,14 @@ cudaError_t seed_shape_gpu(const SeedShape& sh, cudaStream_t st, float** x_out, 
   if (e == cudaSuccess && total > 0) {
     e = cudaMalloc(&x, sizeof(float) * 3 * (size_t)total);
     if (e == cudaSuccess) {
-      seed_write_kernel<<<(unsigned)nblocks, kSeedThreads, 0, st>>>(sh, counts, x);
+      seed_write_kernel<<<(unsigned)nblocks, kSeedThreads, 0, st>>>(sh, counts, masks, x);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   }
   cudaFree(counts);
   cudaFree(scratch);
+  cudaFree(masks);
   if (e != cudaSuccess) {
     cudaFree(x);
     return e;
