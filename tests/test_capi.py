@@ -101,6 +101,14 @@ int main(int argc, char** argv) {
   for (int i = 0; i < 10; ++i) sim.advance();
   auto& ps = sim.syncDevice();
   std::printf("%zu %f\n", ps.size(), ps.empty() ? 0.f : ps[0].x[1]);
+  // the frame outputs of the reference's main loop
+  const std::string dir = argv[1];
+  const size_t faces = mpm_gb300::MeshBuilder(64, 2).computeMesh(dir + "/mesh_00000.obj", sim);
+  mpm_gb300::ParticleWriter().writeParticles(dir + "/particles_0.bgeo", sim);
+  mpm_gb300::Renderer r;
+  const auto& img = r.render(sim);
+  r.writePPM(dir + "/frame.ppm");
+  std::printf("%zu %zu\n", faces, img.size());
   return 0;
 }
 """

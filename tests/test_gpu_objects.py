@@ -107,7 +107,8 @@ def test_scene_from_objects_matches_oracle(gpu_lib, oracle_lib):
 
 def test_cpp_facade_runs(gpu_lib, tmp_path):
     """The C++ Simulation facade (include/mpm_gb300.hpp) seeds an object, advances and
-    reads the particles back in the reference's record layout."""
+    reads the particles back in the reference's record layout, then writes the frame
+    outputs of the reference's main loop (MeshBuilder, ParticleWriter, Renderer)."""
     import os
     import shutil
     import subprocess
@@ -124,7 +125,15 @@ def test_cpp_facade_runs(gpu_lib, tmp_path):
     r = subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe), lib,
                         "-Wl,-rpath," + os.path.dirname(lib)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    out = subprocess.run([str(exe), "run"], capture_output=True, text=True)
+    out = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True)
     assert out.returncode == 0, out.stderr
-    n, y = out.stdout.split()
+    n, y, faces, img = out.stdout.split()
     assert int(n) > 500 and 0.3 < float(y) < 0.7
+    from oracle import export_oracle as E
+
+    obj = (tmp_path / "mesh_00000.obj").read_text().splitlines()
+    assert int(faces) > 100 and sum(l.startswith("f ") for l in obj) == int(faces)
+    parsed = E.parse_bgeo((tmp_path / "particles_0.bgeo").read_bytes())
+    assert parsed["n"] == int(n) and parsed["tail"] == b"\x00\xff"
+    ppm = (tmp_path / "frame.ppm").read_bytes()
+    assert int(img) == 800 * 600 * 3 and ppm.startswith(b"P6 800 600 255\n") and len(ppm) == 15 + 800 * 600 * 3
