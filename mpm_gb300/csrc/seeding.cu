@@ -41,7 +41,7 @@ __device__ __forceinline__ void candidate(const SeedShape& sh, uint64_t i, float
 }
 
 __device__ bool inside_mesh(const SeedShape& sh, const float p[3]) {
-  const double px = p[0], py = p[1], pz = p[2];
+  const double py = p[1], pz = p[2];
   // the point's bin, clamped like the triangles' bin ranges
   const int by = min(max((int)floor(dmul(dsub(py, sh.bin_y0), sh.bin_inv_dy)), 0), sh.bins_y - 1);
   const int bz = min(max((int)floor(dmul(dsub(pz, sh.bin_z0), sh.bin_inv_dz)), 0), sh.bins_z - 1);
@@ -52,7 +52,7 @@ __device__ bool inside_mesh(const SeedShape& sh, const float p[3]) {
     const float* a = sh.verts + 3 * sh.tris[3 * t + 0];
     const float* b = sh.verts + 3 * sh.tris[3 * t + 1];
     const float* c = sh.verts + 3 * sh.tris[3 * t + 2];
-    if (ray_crosses(a, b, c, px, py, pz)) ++crossings;
+    if (ray_crosses(a, b, c, p[0], p[1], p[2])) ++crossings;
   }
   return (crossings & 1) != 0;
 }

@@ -40,11 +40,36 @@ __host__ __device__ __forceinline__ double seed_uniform(uint64_t seed, uint64_t 
 }
 
 #ifdef __CUDACC__
+// Sign of the edge function (by - ay)(qz - az) - (bz - az)(qy - ay) of float inputs when a
+// float evaluation decides it, 0 when it does not.  Each subtraction, product and the final
+// difference rounds by at most u = 2^-24 relative, so the float result is within
+// 4u (|t1| + |t2|) of the exact value; outside 4e-7 (|t1| + |t2|) the exact value has the
+// float result's sign and is far above the double evaluation's error, so the double edge
+// function has that sign too.  (Infinities and NaN compare false: undecided.)
+__device__ __forceinline__ int orient_sign_f(float ay, float az, float by, float bz, float qy, float qz) {
+  const float t1 = __fmul_rn(__fsub_rn(by, ay), __fsub_rn(qz, az));
+  const float t2 = __fmul_rn(__fsub_rn(bz, az), __fsub_rn(qy, ay));
+  const float o = __fsub_rn(t1, t2);
+  const float bound = 4.0e-7f * (fabsf(t1) + fabsf(t2));
+  return o > bound ? 1 : (o < -bound ? -1 : 0);
+}
+
 // Does the +x ray from (px, py, pz) cross triangle abc?  Its (y, z) projection must
 // contain (py, pz) strictly (all three edge functions of one sign; points on an edge are
-// a measure-zero set), and the plane's x above (py, pz) must exceed px.
-__device__ __forceinline__ bool ray_crosses(const float* a, const float* b, const float* c, double px, double py,
-                                            double pz) {
+// a measure-zero set), and the plane's x above (py, pz) must exceed px.  The decision is
+// the double evaluation's; a float pre-test (orient_sign_f) rejects, with the same answer,
+// the triangles whose edge functions have decided, differing signs, which is nearly all of
+// them (FP64 runs at a small fraction of the FP32 rate on this part).
+__device__ __forceinline__ bool ray_crosses(const float* a, const float* b, const float* c, float qx, float qy,
+                                            float qz) {
+  {
+    const int s0 = orient_sign_f(b[1], b[2], c[1], c[2], qy, qz);
+    const int s1 = orient_sign_f(c[1], c[2], a[1], a[2], qy, qz);
+    if (s0 * s1 < 0) return false;
+    const int s2 = orient_sign_f(a[1], a[2], b[1], b[2], qy, qz);
+    if (s0 * s2 < 0 || s1 * s2 < 0) return false;
+  }
+  const double px = qx, py = qy, pz = qz;
   auto orient = [](double ay, double az, double by, double bz, double qy, double qz) {
     return __dsub_rn(__dmul_rn(__dsub_rn(by, ay), __dsub_rn(qz, az)), __dmul_rn(__dsub_rn(bz, az), __dsub_rn(qy, ay)));
   };
