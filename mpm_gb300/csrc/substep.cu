@@ -79,22 +79,21 @@ enum TileState { kTileNone = 0, kTileSmem = 1, kTileGlobal = 2 };
 // The substep kernel is launched as its programmatic dependent: it may start (claim
 // ranges, load its first positions) while this pass runs, and waits for the pass
 // with griddepcontrol.wait before it reads the velocity grid.
+// One thread per padded node: grid (rows of the padded k extent, P, P), so the indices
+// need no division (padded grids stay far below 2^31 nodes).
 __global__ void grid_velocity_kernel(const float4* __restrict__ grid, float4* __restrict__ vgrid, GridConsts K) {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   const int N = K.N, P = N + kPadLo + kPadHi;
-  const int64_t PP = (int64_t)P * P, tot = PP * P;
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
-    const int pi = (int)(q / PP);
-    const int rem = (int)(q - (int64_t)pi * PP);
-    const int pj = rem / P;
-    const int i = pi - kPadLo, j = pj - kPadLo, k = rem - pj * P - kPadLo;
-    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
-    if ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N) {
-      const float3 v = grid_node_velocity(grid[((int64_t)i * N + j) * N + k], i, j, k, K);
-      out = make_float4(v.x, v.y, v.z, 0.f);
-    }
-    vgrid[q] = out;
+  const int pk = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (pk >= P) return;
+  const int pj = (int)blockIdx.y, pi = (int)blockIdx.z;
+  const int i = pi - kPadLo, j = pj - kPadLo, k = pk - kPadLo;
+  float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+  if ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N) {
+    const float3 v = grid_node_velocity(grid[(i * N + j) * N + k], i, j, k, K);
+    out = make_float4(v.x, v.y, v.z, 0.f);
   }
+  vgrid[(pi * P + pj) * P + pk] = out;
 }
 
 // G2P gather straight from the velocity grid, for steps whose box exceeds the tile;
@@ -668,9 +667,10 @@ cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guar
   if (e != cudaSuccess) return e;
   if (!batch && kind != kStepP2GOnly) {
     if (!a.vgrid || !a.grid_in) return cudaErrorInvalidValue;
-    const int64_t tot = vgrid_nodes(a.K.g.N);
-    const int vb = (int)std::min<int64_t>((tot + kThreads - 1) / kThreads, 4096);
-    grid_velocity_kernel<<<vb, kThreads, 0, st>>>(a.grid_in, a.vgrid, a.K.g);
+    const int P = a.K.g.N + kPadLo + kPadHi;
+    const int tx = P <= 64 ? 64 : 128;
+    grid_velocity_kernel<<<dim3((unsigned)((P + tx - 1) / tx), (unsigned)P, (unsigned)P), tx, 0, st>>>(a.grid_in, a.vgrid,
+                                                                                                   a.K.g);
     if (launches) *launches += 1;
   }
   StepArgs copy = a;
