@@ -164,6 +164,42 @@ __global__ void sort_scatter(SortArgs a) {
   }
 }
 
+// The sort for particles in arbitrary order (after an upload): scattering them would write
+// every component to a random slot, so sort_rank only writes the permutation (slot q holds
+// particle perm[q]) and sort_gather fills each slot with coalesced writes.
+__global__ void sort_rank(SortArgs a) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < a.n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = base + threadIdx.x;
+    const bool valid = p < a.n;
+    const uint32_t key = valid ? a.keys[p] : 0xffffffffu;
+    const unsigned same = __match_any_sync(kFull, key);
+    const int leader = __ffs(same) - 1;
+    int start = 0;
+    if (valid && lane == leader) start = atomicAdd(a.counts + key, __popc(same));
+    start = __shfl_sync(kFull, start, leader);
+    if (valid) a.perm[(int64_t)start + __popc(same & ((1u << lane) - 1u))] = (uint32_t)p;
+  }
+}
+
+template <bool LIQ>
+__global__ void sort_gather(SortArgs a) {
+  constexpr int NC = LIQ ? kLiquidComps : kNumComps;
+  const float* __restrict__ sA = a.sA;
+  float* __restrict__ sB = a.sB;
+  const int64_t st = a.stride;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < a.n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = a.perm[q];
+    float vals[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) vals[c] = __ldg(sA + moved_comp<LIQ>(c) * st + p);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) sB[moved_comp<LIQ>(c) * st + q] = vals[c];
+    if (a.matA) a.matB[q] = a.matA[p];
+    a.idB[q] = a.idA[p];
+  }
+}
+
 // Exclusive scan of a small key space (a multiple of 4 counts) by one CTA: each of
 // kScanThreads threads scans kScanRun consecutive counts in registers (int4 loads),
 // then the CTA scans the threads' totals; tiles of kScanThreads x kScanRun counts
@@ -243,10 +279,18 @@ cudaError_t launch_sort(const SortArgs& a, int num_sms, cudaStream_t st, int64_t
     scan_add<<<nb, kThreads, 0, st>>>(a.counts, a.cells, a.block_sums);
     n_launch = 5;
   }
-  if (a.ncomp == kLiquidComps)
+  if (a.perm) {
+    sort_rank<<<blocks, kThreads, 0, st>>>(a);
+    if (a.ncomp == kLiquidComps)
+      sort_gather<true><<<blocks, kThreads, 0, st>>>(a);
+    else
+      sort_gather<false><<<blocks, kThreads, 0, st>>>(a);
+    n_launch += 1;
+  } else if (a.ncomp == kLiquidComps) {
     sort_scatter<true><<<blocks, kThreads, 0, st>>>(a);
-  else
+  } else {
     sort_scatter<false><<<blocks, kThreads, 0, st>>>(a);
+  }
   if (launches) *launches += n_launch;
   return cudaGetLastError();
 }

@@ -72,6 +72,7 @@ struct mpm_ctx {
   int* status = nullptr;
   int* work = nullptr;  // two range counters, alternating between substep launches; [2]: upload check
   int launch_parity = 0;
+  bool unsorted = true;  // particle order unrelated to cells (upload, append): the next sort gathers
 
   int64_t substeps = 0;
   int64_t since_sort = 0;
@@ -202,7 +203,7 @@ mpm_status ensure_particles(mpm_ctx* c, int64_t n) {
   MPM_CUDA(c, cudaMalloc(&c->matB, cap));
   MPM_CUDA(c, cudaMalloc(&c->idA, sizeof(uint32_t) * cap));
   MPM_CUDA(c, cudaMalloc(&c->idB, sizeof(uint32_t) * cap));
-  MPM_CUDA(c, cudaMalloc(&c->keys, sizeof(uint32_t) * cap));
+  MPM_CUDA(c, cudaMalloc(&c->keys, sizeof(uint32_t) * 2 * cap));  // sort keys, then the sort's permutation
   c->capacity = cap;
   c->stride = cap;
   return MPM_OK;
@@ -223,7 +224,7 @@ mpm_status grow_particles(mpm_ctx* c, int64_t need) {
   };
   if (cudaMalloc(&sA, fbytes) || cudaMalloc(&sB, fbytes) || cudaMalloc(&mA, cap) || cudaMalloc(&mB, cap) ||
       cudaMalloc(&iA, sizeof(uint32_t) * cap) || cudaMalloc(&iB, sizeof(uint32_t) * cap) ||
-      cudaMalloc(&keys, sizeof(uint32_t) * cap))
+      cudaMalloc(&keys, sizeof(uint32_t) * 2 * cap))
     return undo();
   for (int k = 0; k < kNumComps; ++k)
     MPM_CUDA(c, cudaMemcpyAsync(sA + (size_t)k * cap, c->sA + (size_t)k * c->stride, sizeof(float) * c->n,
@@ -270,6 +271,7 @@ mpm_status activate_object(mpm_ctx* c, ObjectRec& o) {
     c->launches += 1;
     o.id0 = (uint32_t)c->n;
     c->n += k;
+    c->unsorted = true;  // the new particles sit at the end in seeding order
     particles_changed(c);
   }
   o.active = true;
@@ -369,6 +371,8 @@ mpm_status run_sort(mpm_ctx* c) {
   s.idA = c->idA;
   s.idB = c->idB;
   s.keys = c->keys;
+  // particles in arbitrary order (just uploaded or appended) sort faster by gathering
+  s.perm = c->unsorted ? c->keys + c->capacity : nullptr;
   s.counts = c->counts;
   s.block_sums = c->block_sums;
   s.cells = c->sort_keys;
@@ -381,6 +385,7 @@ mpm_status run_sort(mpm_ctx* c) {
   std::swap(c->matA, c->matB);
   std::swap(c->idA, c->idB);
   c->since_sort = 0;
+  c->unsorted = false;
   return MPM_OK;
 }
 
@@ -633,6 +638,7 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   c->prev = -1;
   c->substeps = 0;
   c->since_sort = c->params.sort_interval;  // sort before the first substep
+  c->unsorted = true;
   c->t = 0.0;
   free_objects(c);
   if (n == 0) return MPM_OK;

@@ -111,6 +111,7 @@ struct SortArgs {
   const uint32_t* idA;
   uint32_t* idB;
   uint32_t* keys;
+  uint32_t* perm;  // n words, or null: with it the sort ranks, then gathers (for unsorted input)
   int* counts;   // one per sort key
   int* block_sums;
   int64_t cells;  // sort key space (bricked cell index range)
