@@ -23,10 +23,11 @@
 //     Corners are classified as the reference's double S > 0 (one float compare against
 //     the equivalent float threshold); edge points are interpolated in float (the
 //     triangles are float anyway; the double path cost far more on this part, whose FP64
-//     rate is a small fraction of its FP32 rate).  A count sweep over the cells, exclusive
-//     scans over its blocks, a compaction sweep that lists the surface cells in cell order
-//     with their first triangle's index, and a dense emit pass (one thread per surface
-//     cell) write the triangles in cell order, so the mesh is deterministic.
+//     rate is a small fraction of its FP32 rate).  One sweep over the cells counts triangles
+//     and surface cells per block and lists each block's surface cells in its slots;
+//     exclusive scans over the blocks give their offsets; a dense emit pass (one thread per
+//     surface cell, which finds its block by binary search) writes the triangles in cell
+//     order, so the mesh is deterministic.
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -415,39 +416,13 @@ __device__ __forceinline__ int64_t block_linear() {
   return ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
 }
 
-// Sweep 1: triangles and surface cells (cells with triangles) per block.
+// The one sweep over the cells: per block, its triangle and surface-cell counts, and in the
+// block's slots (kSurfThreads of them) its surface cells in cell order, each with its first
+// triangle's offset inside the block.
 __global__ void __launch_bounds__(kSurfThreads) mc_count_kernel(const float* __restrict__ field, int G, float thr,
                                                                 int* __restrict__ block_tris,
-                                                                int* __restrict__ block_cells) {
-  __shared__ int warp_tris[kSurfThreads / 32], warp_cells[kSurfThreads / 32];
-  int i, j, k, cnt = 0;
-  if (block_cell(G, i, j, k)) cnt = mask_triangles(corner_mask(field, G, i, j, k, thr));
-  int cells = __popc(__ballot_sync(kFull, cnt > 0));
-#pragma unroll
-  for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
-  if ((threadIdx.x & 31) == 0) {
-    warp_tris[threadIdx.x >> 5] = cnt;
-    warp_cells[threadIdx.x >> 5] = cells;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int t = 0, c = 0;
-    for (int w = 0; w < kSurfThreads / 32; ++w) {
-      t += warp_tris[w];
-      c += warp_cells[w];
-    }
-    const int64_t b = block_linear();
-    block_tris[b] = t;
-    block_cells[b] = c;
-  }
-}
-
-// Sweep 2: the surface cells in cell order, each with its first triangle's index
-// (block_tris and block_cells now hold the exclusive scans of the per-block counts).
-__global__ void __launch_bounds__(kSurfThreads) mc_compact_kernel(const float* __restrict__ field, int G, float thr,
-                                                                  const int* __restrict__ block_tris,
-                                                                  const int* __restrict__ block_cells,
-                                                                  int2* __restrict__ cells_out) {
+                                                                int* __restrict__ block_cells,
+                                                                int2* __restrict__ slots) {
   __shared__ int warp_tris[kSurfThreads / 32], warp_cells[kSurfThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int i, j, k, cnt = 0;
@@ -464,28 +439,48 @@ __global__ void __launch_bounds__(kSurfThreads) mc_compact_kernel(const float* _
     warp_cells[warp] = __popc(surf);
   }
   __syncthreads();
+  const int64_t b = block_linear();
+  if (threadIdx.x == 0) {
+    int t = 0, c = 0;
+    for (int w = 0; w < kSurfThreads / 32; ++w) {
+      t += warp_tris[w];
+      c += warp_cells[w];
+    }
+    block_tris[b] = t;
+    block_cells[b] = c;
+  }
   if (cnt == 0) return;
   int tpre = 0, cpre = 0;
   for (int w = 0; w < warp; ++w) {
     tpre += warp_tris[w];
     cpre += warp_cells[w];
   }
-  const int64_t b = block_linear();
-  const int rank = block_cells[b] + cpre + __popc(surf & ((1u << lane) - 1u));
-  cells_out[rank] = make_int2((i << 20) | (j << 10) | k, block_tris[b] + tpre + inc - cnt);
+  const int rank = cpre + __popc(surf & ((1u << lane) - 1u));
+  slots[b * kSurfThreads + rank] = make_int2((i << 20) | (j << 10) | k, tpre + inc - cnt);
 }
 
 // Triangles of the surface cells, one thread per cell.  RAW: the buffer holds the squared
 // distances and a corner's field value is min(cutoff, sqrt(s)) (what
 // finish_distance_kernel stores).
+// Surface cell c (in cell order) is found in the slots of the block b whose exclusive scan
+// of surface cells, cell_off[b], is the last one <= c; tri_off[b] is the block's first
+// triangle.
 template <bool RAW>
 __global__ void __launch_bounds__(kSurfThreads) mc_emit_kernel(const float* __restrict__ field, int G, float thr,
                                                                float cutoff, float iso, float vdx,
-                                                               const int2* __restrict__ cells, int ncells,
+                                                               const int* __restrict__ tri_off,
+                                                               const int* __restrict__ cell_off, int64_t nblocks,
+                                                               const int2* __restrict__ slots, int ncells,
                                                                float* __restrict__ tris) {
   const int c = blockIdx.x * kSurfThreads + threadIdx.x;
   if (c >= ncells) return;
-  const int2 e = cells[c];
+  int64_t lo = 0, hi = nblocks - 1;  // cell_off[0] = 0 <= c < cell_off[nblocks] = ncells
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) >> 1;
+    if (cell_off[mid] <= c) lo = mid; else hi = mid - 1;
+  }
+  int2 e = slots[lo * kSurfThreads + (c - cell_off[lo])];
+  e.y += tri_off[lo];
   const int i = e.x >> 20, j = (e.x >> 10) & 1023, k = e.x & 1023;
   float f[8];
   unsigned m = 0;
@@ -626,7 +621,9 @@ cudaError_t extract_surface(int G, int radius, double voxel_dx, SurfaceBuffers& 
   if (e != cudaSuccess) return e;
   int* block_tris = buf.counts;
   int* block_cells = buf.counts + nblocks + 1;
-  mc_count_kernel<<<grid, kSurfThreads, 0, st>>>(buf.field, G, thr, block_tris, block_cells);
+  e = reserve(&buf.cells, &buf.cells_cap, nblocks * kSurfThreads);
+  if (e != cudaSuccess) return e;
+  mc_count_kernel<<<grid, kSurfThreads, 0, st>>>(buf.field, G, thr, block_tris, block_cells, buf.cells);
   e = cudaMemsetAsync(block_tris + nblocks, 0, sizeof(int), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(block_cells + nblocks, 0, sizeof(int), st);
   if (e == cudaSuccess) e = cudaGetLastError();
@@ -642,19 +639,17 @@ cudaError_t extract_surface(int G, int radius, double voxel_dx, SurfaceBuffers& 
   const int ncells = buf.total[1];
   if (total > 0) {
     e = reserve(&buf.tris, &buf.tris_cap, 9 * total);
-    if (e == cudaSuccess) e = reserve(&buf.cells, &buf.cells_cap, (int64_t)ncells);
     if (e != cudaSuccess) return e;
-    mc_compact_kernel<<<grid, kSurfThreads, 0, st>>>(buf.field, G, thr, block_tris, block_cells, buf.cells);
     const float iso = (float)K.iso;
     const unsigned eblocks = (unsigned)((ncells + kSurfThreads - 1) / kSurfThreads);
     if (buf.raw)
-      mc_emit_kernel<true><<<eblocks, kSurfThreads, 0, st>>>(buf.field, G, thr, K.cutoff, iso, K.vdx, buf.cells,
-                                                             ncells, buf.tris);
+      mc_emit_kernel<true><<<eblocks, kSurfThreads, 0, st>>>(buf.field, G, thr, K.cutoff, iso, K.vdx, block_tris,
+                                                             block_cells, nblocks, buf.cells, ncells, buf.tris);
     else
-      mc_emit_kernel<false><<<eblocks, kSurfThreads, 0, st>>>(buf.field, G, thr, K.cutoff, iso, K.vdx, buf.cells,
-                                                              ncells, buf.tris);
+      mc_emit_kernel<false><<<eblocks, kSurfThreads, 0, st>>>(buf.field, G, thr, K.cutoff, iso, K.vdx, block_tris,
+                                                              block_cells, nblocks, buf.cells, ncells, buf.tris);
     e = cudaGetLastError();
-    if (launches) *launches += 2;
+    if (launches) *launches += 1;
   }
   *n_out = total;
   return e;

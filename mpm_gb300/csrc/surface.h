@@ -11,7 +11,7 @@ struct SurfaceBuffers {
   int64_t field_cap = 0;
   int* counts = nullptr;   // triangles and surface cells per block of cells, then their exclusive scans
   int64_t counts_cap = 0;
-  int2* cells = nullptr;   // surface cells in cell order: packed (i, j, k), first triangle
+  int2* cells = nullptr;   // per block of cells, its surface cells: packed (i, j, k), first triangle in the block
   int64_t cells_cap = 0;
   int* scan = nullptr;     // scan scratch
   int64_t scan_cap = 0;
