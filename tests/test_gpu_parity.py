@@ -324,3 +324,52 @@ def test_pinned_host_arrays_take_the_direct_path(gpu_lib):
             after = b.download()
             for k in ref:
                 assert np.array_equal(after[k], ref[k]), k
+
+
+def test_argument_validation(gpu_lib, tmp_path):
+    """Every entry point rejects bad arguments with its status code (no device work)."""
+    import ctypes
+
+    from mpm_gb300 import _lib
+    from mpm_gb300 import materials as M
+    from mpm_gb300.simulation import Simulation
+
+    L = _lib.lib()
+    INVALID, IO = 1, 7
+    ctx = ctypes.c_void_p()
+    for kw in ({"N": 3}, {"N": 1001}, {"dt": 0.0}, {"dt": float("nan")}, {"boundary_mode": 3}):
+        p = _lib.MpmParams(float(kw.get("dt", 1e-4)), int(kw.get("N", 16)), -9.8, int(kw.get("boundary_mode", 0)), 3,
+                           0, 16, 0)
+        assert L.mpm_create(ctypes.byref(p), ctypes.byref(ctx)) == INVALID, kw
+    # null contexts and outputs
+    assert L.mpm_substep(None, 1) == INVALID
+    assert L.mpm_sync(None) == INVALID
+    assert L.mpm_surface_mesh(None, 16, 2, None, 0, None) == INVALID
+    assert L.mpm_export_particles(None, 0, 0.1, None) == INVALID
+    assert L.mpm_render_positions(None, None) == INVALID
+    with Simulation(N=16) as sim:
+        bad_mats = [(_lib.MpmMaterial * 1)(_lib.MpmMaterial(9, 1e-5, 1000, 1e4, 0.3, 0, 0, 1e30, 0)),
+                    (_lib.MpmMaterial * 1)(_lib.MpmMaterial(0, -1.0, 1000, 1e4, 0.3, 0, 0, 1e30, 0))]
+        for m in bad_mats:
+            assert L.mpm_set_materials(sim.ctx, m, 1) == INVALID
+        assert L.mpm_set_materials(sim.ctx, bad_mats[0], 0) == INVALID
+        sim.set_materials([M.elastic(1e-5)])
+        sim.upload({"x": np.full((100, 3), 0.5, np.float32)})
+        p = _lib.MpmParams(1e-4, 32, -9.8, 0, 3, 0, 16, 0)
+        assert L.mpm_set_params(sim.ctx, ctypes.byref(p)) == INVALID  # N of a live context
+        n = ctypes.c_int64()
+        assert L.mpm_export_particles(sim.ctx, 2, 0.1, ctypes.byref(n)) == INVALID
+        rec, cnt = ctypes.c_void_p(), ctypes.c_int64()
+        assert L.mpm_export_wait(sim.ctx, 1, ctypes.byref(rec), ctypes.byref(cnt)) == INVALID  # nothing exported
+        tri = ctypes.c_int64()
+        for G, r in ((1, 2), (513, 2), (16, -1), (16, 65)):
+            assert L.mpm_surface_mesh(sim.ctx, G, r, None, 0, ctypes.byref(tri)) == INVALID, (G, r)
+        col = (ctypes.c_uint8 * 3)(1, 2, 3)
+        img = np.empty(12, np.uint8)
+        for w, h, ps in ((0, 10, 2.0), (10, 0, 2.0), (2, 2, 0.0), (2, 2, 100.0)):
+            assert L.mpm_render_points(sim.ctx, w, h, ps, col, col, img.ctypes.data_as(ctypes.c_void_p)) == INVALID
+        assert L.mpm_write_bgeo(str(tmp_path / "no" / "dir.bgeo").encode(), None, 0) == IO
+        # the context still works after all of that
+        sim.advance(2)
+        sim.sync()
+        assert np.isfinite(sim.download(("x",))["x"]).all()
