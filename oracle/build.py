@@ -11,6 +11,10 @@
   (TransferScheme.h, MaterialModel.cuh, InterpolationKernel.cuh, types.h,
   svd3_cuda.h) compiled for the host against the project-written Eigen subset in
   ``ref_shim/``, driven by the loop skeleton in ``ref_substep.cpp``.
+* ``_ref/libref_mesh.so`` — the reference's own ``include/mesh_builder.h`` (its
+  distance field) compiled for the host against the same Eigen subset plus the
+  ``boost::multi_array`` and declaration-only libigl stand-ins in ``ref_shim/``,
+  driven by ``ref_mesh.cpp``; no OpenMP, so its particle loop runs sequentially.
 """
 from __future__ import annotations
 
@@ -54,7 +58,8 @@ def build_ref(force: bool = False) -> list:
     inc = os.path.join(REF_ROOT, "include")
     shim = os.path.join(HERE, "ref_shim")
     built = []
-    for name, src in (("libref_svd.so", "ref_svd.cpp"), ("libref_substep.so", "ref_substep.cpp")):
+    for name, src in (("libref_svd.so", "ref_svd.cpp"), ("libref_substep.so", "ref_substep.cpp"),
+                      ("libref_mesh.so", "ref_mesh.cpp")):
         srcp = os.path.join(HERE, src)
         if not os.path.exists(srcp):
             continue

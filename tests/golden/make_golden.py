@@ -10,6 +10,8 @@ Writes:
                      include/svd3_cuda.h, compiled for the host (oracle/_ref).
   ref_substep.npz  — (when oracle/_ref/libref_substep.so is built) small seeded
                      particle states advanced by the reference's own policy headers.
+  ref_mesh.npz     — (when oracle/_ref/libref_mesh.so is built) distance fields of
+                     seeded particle sets from the reference's include/mesh_builder.h.
 """
 import ctypes
 import json
@@ -73,6 +75,12 @@ def main():
         import ref_substep_vectors
 
         np.savez_compressed(os.path.join(HERE, "ref_substep.npz"), **ref_substep_vectors.make(sub))
+    mesh = os.path.join(ROOT, "oracle", "_ref", "libref_mesh.so")
+    if os.path.exists(mesh):
+        sys.path.insert(0, HERE)
+        import ref_mesh_vectors
+
+        np.savez_compressed(os.path.join(HERE, "ref_mesh.npz"), **ref_mesh_vectors.make(mesh))
     print("golden fixtures written")
 
 

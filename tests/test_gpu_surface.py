@@ -5,7 +5,9 @@ extraction of the same field, and a simulated body's surface closed and outward.
 import numpy as np
 import pytest
 
-from surface_checks import edge_balance, enclosed_volume, weld
+from surface_checks import edge_balance, enclosed_volume, golden_mesh_cases, matches_golden, weld
+
+MESH_CASES = golden_mesh_cases()
 
 pytestmark = pytest.mark.gpu
 
@@ -39,6 +41,15 @@ def test_distance_field_matches_oracle(gpu_lib, oracle_lib, N, G, radius):
     dx = float(np.float32(1.0 / N))
     r = oracle_lib.distance_field(sim.download(("x",))["x"], G, radius, oracle_lib.voxel_dx(N, dx, G))
     assert np.array_equal(g.view(np.int32), r.view(np.int32))
+
+
+@pytest.mark.parametrize("case", MESH_CASES, ids=[c[0] for c in MESH_CASES])
+def test_distance_field_matches_reference_golden(gpu_lib, case):
+    """The device field bit for bit against the reference's own fillVoxelGrid_distance
+    (tests/golden/ref_mesh.npz), particles reaching past both faces of the grid."""
+    name, x, N, G, r, vdx, field, sha = case
+    sim = _sim(x, N)
+    assert matches_golden(sim.surface_distance(G, r), field, sha)
 
 
 @pytest.mark.parametrize("order,radius", [("sorted", 4), ("mixed", 4), ("sorted", 6), ("sorted", 7)])

@@ -1,11 +1,33 @@
 """CPU tests of the surface-reconstruction oracle (oracle/surface_oracle.cpp): the
-distance field of fillVoxelGrid_distance (include/mesh_builder.h:89-137) restated once
-more in numpy float32 arithmetic and compared bit for bit, and the marching-tetrahedra
-surface checked for the properties of a closed, outward-oriented surface."""
+distance field of fillVoxelGrid_distance (include/mesh_builder.h:89-137) bit for bit
+against the reference's own header compiled for the host (tests/golden/ref_mesh.npz) and
+against a numpy float32 restatement, and the marching-tetrahedra surface checked for the
+properties of a closed, outward-oriented surface."""
 import numpy as np
 import pytest
 
-from surface_checks import edge_balance, enclosed_volume, weld
+from surface_checks import edge_balance, enclosed_volume, golden_mesh_cases, matches_golden, weld
+
+MESH_CASES = golden_mesh_cases()
+
+
+@pytest.mark.parametrize("case", MESH_CASES, ids=[c[0] for c in MESH_CASES])
+def test_distance_field_matches_reference_golden(oracle_lib, case):
+    """The reference's fillVoxelGrid_distance, called as MeshBuilder::computeMesh calls it
+    (include/mesh_builder.h:167-174), on seeded particles reaching past both faces of the
+    grid; the largest case is the reference's default mesh grid (G = 250, radius 5)."""
+    name, x, N, G, r, vdx, field, sha = case
+    assert oracle_lib.voxel_dx(N, float(np.float32(1.0 / N)), G) == vdx
+    assert matches_golden(oracle_lib.distance_field(x, G, r, vdx), field, sha)
+
+
+@pytest.mark.parametrize("stored", [True, False])
+def test_golden_distance_check_detects_a_changed_node(oracle_lib, stored):
+    name, x, N, G, r, vdx, field, sha = next(c for c in MESH_CASES if (c[6] is not None) == stored)
+    f = oracle_lib.distance_field(x, G, r, vdx)
+    hit = np.argwhere(f < f.max())[0]
+    f[tuple(hit)] = np.nextafter(f[tuple(hit)], np.float32(0))
+    assert not matches_golden(f, field, sha)
 
 
 def numpy_distance_field(x, G, radius, vdx):
