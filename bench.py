@@ -543,11 +543,12 @@ def run_mesh(args):
     """Surface reconstruction at the reference's mesh defaults (include/options.h:30-31:
     a 250^3 voxel grid, particle radius 5 voxels) of 500,000 particles (the reference's
     default particle count) filling a ball of radius 0.25 in an N=60 domain, after 10
-    snow substeps.  A step is one surface extraction: distance field, level-set count,
-    scans, compaction and triangle write.  value: device time (CUDA events on the context's
-    stream) of mpm_surface_mesh_device, the triangles left in HBM; e2e: wall clock of
-    mpm_surface_mesh, which also copies the triangles to host memory.  The oracle meshes
-    the same particles on one host thread."""
+    snow substeps.  A step is one surface extraction as MeshBuilder::computeMesh makes it
+    (up to the OBJ text): distance field, marching-cubes count, scan, and the emit of
+    libigl's vertex list and the faces.  value: device time (CUDA events on the context's
+    stream) of mpm_surface_mesh_indexed_device, the mesh left in HBM; e2e: wall clock of
+    mpm_surface_mesh_indexed, which also copies vertices and faces to pinned host memory.
+    The oracle meshes the same particles on one host thread."""
     from mpm_gb300 import build
 
     build.build()
@@ -572,18 +573,21 @@ def run_mesh(args):
     sim.advance(10)
     sim.sync()
     cap = 4 * 1024 * 1024
-    tris = np.empty((cap, 3, 3), np.float32)
-    cnt = ctypes.c_int64()
+    Vh = torch.empty((cap, 3), dtype=torch.float64, pin_memory=True)
+    Fh = torch.empty((cap, 3), dtype=torch.int32, pin_memory=True)
+    nv, cnt = ctypes.c_int64(), ctypes.c_int64()
     L = sim.L
 
-    dptr = ctypes.c_void_p()
+    dptr, fptr = ctypes.c_void_p(), ctypes.c_void_p()
 
     def call_host():
-        _lib.check(L.mpm_surface_mesh(sim.ctx, G, radius, tris.ctypes.data_as(ctypes.c_void_p), cap,
-                                      ctypes.byref(cnt)), sim.ctx)
+        _lib.check(L.mpm_surface_mesh_indexed(sim.ctx, G, radius, ctypes.c_void_p(Vh.data_ptr()), cap,
+                                              ctypes.c_void_p(Fh.data_ptr()), cap, ctypes.byref(nv),
+                                              ctypes.byref(cnt)), sim.ctx)
 
     def call_device():
-        _lib.check(L.mpm_surface_mesh_device(sim.ctx, G, radius, ctypes.byref(dptr), ctypes.byref(cnt)), sim.ctx)
+        _lib.check(L.mpm_surface_mesh_indexed_device(sim.ctx, G, radius, ctypes.byref(dptr), ctypes.byref(fptr),
+                                                     ctypes.byref(nv), ctypes.byref(cnt)), sim.ctx)
 
     def call_field():
         _lib.check(L.mpm_surface_distance_device(sim.ctx, G, radius, ctypes.byref(dptr)), sim.ctx)
@@ -618,7 +622,7 @@ def run_mesh(args):
     wall = [timed(call_host)[1] for _ in range(steps)]
     field_s = statistics.median([timed(call_field)[0] for _ in range(steps)])
     clk = clocks.stop(t_start, t_end)
-    ntri = int(cnt.value)
+    ntri, nvert = int(cnt.value), int(nv.value)
     d_s, w_s = statistics.median(dev), statistics.median(wall)
     peak, peak_kind = measured_peaks()
     # oracle on one host thread: the same particles and grid
@@ -626,18 +630,19 @@ def run_mesh(args):
     vdx = oracle.voxel_dx(N, float(np.float32(1.0 / N)), G)
     c0 = time.perf_counter()
     f = oracle.distance_field(xs, G, radius, vdx)
-    ref = oracle.surface_mesh(f, radius, vdx)
+    ref_V, ref_F = oracle.surface_indexed(f, radius, vdx)
     cpu_s = time.perf_counter() - c0
     # distance-field pass (fill, scatter, finish): minimal bytes = positions read once and
     # the field written once
     alg = 12.0 * n + 4.0 * G ** 3
     line = {"metric": "surface meshes/s", "value": 1.0 / d_s, "unit": "meshes/s", "n_gpus": 1, "steps": steps,
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * d_s, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 field, f64 level set", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32 field, f64 vertices", "data": "synthetic",
             "config": {"workload": "mesh_ball_500k_G250_r5", "particles": n, "grid_side": G, "radius": radius,
-                       "N": N, "triangles": ntri, "l2": "512 MiB flush between steps"},
+                       "N": N, "vertices": nvert, "faces": ntri,
+                       "l2": "512 MiB flush between steps"},
             "e2e": {"value": 1.0 / w_s, "unit": "meshes/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 36 * ntri + 8},
+                    "d2h_bytes_per_step": 24 * nvert + 12 * ntri + 12},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": alg / field_s / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": alg / field_s / 1e9 / peak, "traffic": None,
@@ -647,10 +652,10 @@ def run_mesh(args):
                                  f"{peak_kind}"},
             "distance_field_ms": 1e3 * field_s,
             "clocks": clk,
-            "oracle_triangles": int(ref.shape[0]),
+            "oracle_faces": int(ref_F.shape[0]),
             "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "meshes/s", "cores": 1, "kind": "port",
                              "sample": f"the same {n} particles on the same grid (oracle distance field and "
-                                       f"marching tetrahedra, 1 thread, {cpu_s:.1f} s)"}}
+                                       f"marching cubes, 1 thread, {cpu_s:.1f} s)"}}
     print(json.dumps(line), flush=True)
 
 

@@ -190,18 +190,32 @@ mpm_status mpm_seed_object(const mpm_object* object, uint32_t density, float* x,
  * voxel grid of side grid_side (voxel_dx = N dx / grid_side) holds the distance from each
  * node to the nearest particle within (radius + 1) voxels (fillVoxelGrid_distance,
  * include/mesh_builder.h:89-137); the surface is the zero level of radius * voxel_dx -
- * distance.  The reference extracts it with libigl's marching cubes; here marching
- * tetrahedra (six per voxel cell, split along the main diagonal) give the same level set
- * as a closed, oriented triangle soup.  Both calls synchronise.
+ * distance, extracted by libigl's marching cubes.  Here the vertices are libigl's, bit
+ * for bit and in its order; each cube's faces triangulate the same edge loops as
+ * libigl's (the fan inside a loop may differ).  Every call synchronises.
  * ------------------------------------------------------------------------- */
 /* grid_side in [2, 512], radius in [0, 64]; particles outside [0, grid_side voxel_dx)
  * touch only the nodes inside the grid.
  * The distance field (grid_side^3 floats, index (i grid_side + j) grid_side + k). */
 mpm_status mpm_surface_distance(mpm_ctx* ctx, int32_t grid_side, int32_t radius, float* field);
 /* Triangles of the surface, 9 floats each (3 vertices x y z), into host tris (room for
- * `capacity` triangles); *n_tris receives the count, which may exceed capacity. */
+ * `capacity` triangles); *n_tris receives the count, which may exceed capacity.  The
+ * triangles are the faces of mpm_surface_mesh_indexed with their vertices rounded to
+ * float, in the same order. */
 mpm_status mpm_surface_mesh(mpm_ctx* ctx, int32_t grid_side, int32_t radius, float* tris, int64_t capacity,
                             int64_t* n_tris);
+/* The surface as MeshBuilder::computeMesh hands it to igl::writeOBJ
+ * (include/mesh_builder.h:193-210, without smoothing or decimation): vertices (3 doubles
+ * each, world units) in the order libigl's marching cubes creates them, bit for bit, and
+ * faces (3 zero-based vertex indices each, outward).  Copies up to the capacities;
+ * *n_vertices and *n_faces receive the counts, which may exceed them. */
+mpm_status mpm_surface_mesh_indexed(mpm_ctx* ctx, int32_t grid_side, int32_t radius, double* vertices,
+                                    int64_t vertex_capacity, int32_t* faces, int64_t face_capacity,
+                                    int64_t* n_vertices, int64_t* n_faces);
+/* The marching-cubes triangle table (no context, no GPU): for each inside-corner mask m
+ * (bit n: libigl's corner n has S > 0), counts[m] triangles as edge-slot triples in
+ * slots[30 m ...] (-1 past them). */
+mpm_status mpm_surface_table(int32_t* counts, int32_t* slots);
 /* The distance field left in device memory (the context's buffer, valid until the next
  * surface call or mpm_destroy), written asynchronously on the context's stream. */
 mpm_status mpm_surface_distance_device(mpm_ctx* ctx, int32_t grid_side, int32_t radius, const float** field);
@@ -210,6 +224,11 @@ mpm_status mpm_surface_distance_device(mpm_ctx* ctx, int32_t grid_side, int32_t 
  * stream after the call returns (the call itself waits once, for the count). */
 mpm_status mpm_surface_mesh_device(mpm_ctx* ctx, int32_t grid_side, int32_t radius, const float** tris,
                                    int64_t* n_tris);
+/* The same vertices and faces left in device memory (the context's buffers, valid until
+ * the next surface call or mpm_destroy), written asynchronously on the context's stream
+ * after the call returns (the call itself waits once, for the counts). */
+mpm_status mpm_surface_mesh_indexed_device(mpm_ctx* ctx, int32_t grid_side, int32_t radius, const double** vertices,
+                                           const int32_t** faces, int64_t* n_vertices, int64_t* n_faces);
 
 /* ---------------------------------------------------------------------------
  * Particle export (ParticleWriter::writeParticles, include/particle_writer.h:19-43).  The

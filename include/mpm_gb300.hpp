@@ -26,7 +26,6 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 #include "mpm_gb300.h"
@@ -107,16 +106,15 @@ class Simulation {
 };
 
 /* MeshBuilder(params, flags, grid_size) / computeMesh (include/mesh_builder.h:19-34,
- * 170-211): the surface of the simulation's particles on a grid_side^3 voxel grid with the
- * given particle radius (in voxels), written as an OBJ file.  Vertices shared by triangles
- * are welded (they are bit-identical); triangles collapsed where the surface passes through
- * a voxel node are dropped. */
+ * 165-211): the surface of the simulation's particles on a grid_side^3 voxel grid with the
+ * given particle radius (in voxels), written as an OBJ file: libigl's marching-cubes
+ * vertex list (bit for bit, in its order) and outward faces over the same edge loops. */
 class MeshBuilder {
  public:
   explicit MeshBuilder(int32_t grid_side = 250, int32_t particle_radius = 5)
       : grid_side_(grid_side), radius_(particle_radius) {}
 
-  /* The triangle soup, 9 floats per triangle (cell order). */
+  /* The triangle soup, 9 floats per triangle (the faces of mesh(), in order). */
   std::vector<float> triangles(Simulation& sim) const {
     int64_t n = 0;
     std::vector<float> t(9 * 65536);
@@ -129,43 +127,33 @@ class MeshBuilder {
     return t;
   }
 
-  /* Writes the OBJ file; returns the number of faces. */
-  size_t computeMesh(const std::string& filename, Simulation& sim) const {
-    const std::vector<float> t = triangles(sim);
-    struct Key {
-      uint32_t b[3];
-      bool operator==(const Key& o) const { return b[0] == o.b[0] && b[1] == o.b[1] && b[2] == o.b[2]; }
-    };
-    struct Hash {
-      size_t operator()(const Key& k) const {
-        return ((size_t)k.b[0] * 73856093u) ^ ((size_t)k.b[1] * 19349663u) ^ ((size_t)k.b[2] * 83492791u);
-      }
-    };
-    std::unordered_map<Key, uint32_t, Hash> index;
-    std::vector<float> verts;
-    std::vector<uint32_t> faces;
-    for (size_t q = 0; q < t.size() / 9; ++q) {
-      uint32_t f[3];
-      for (int c = 0; c < 3; ++c) {
-        Key k;
-        std::memcpy(k.b, &t[9 * q + 3 * c], 12);
-        auto it = index.find(k);
-        if (it == index.end()) {
-          it = index.emplace(k, (uint32_t)(verts.size() / 3)).first;
-          verts.insert(verts.end(), &t[9 * q + 3 * c], &t[9 * q + 3 * c] + 3);
-        }
-        f[c] = it->second;
-      }
-      if (f[0] != f[1] && f[1] != f[2] && f[0] != f[2]) faces.insert(faces.end(), f, f + 3);
+  /* The indexed mesh: 3 doubles per vertex, 3 zero-based vertex indices per face. */
+  void mesh(Simulation& sim, std::vector<double>& V, std::vector<int32_t>& F) const {
+    int64_t nv = 0, nf = 0;
+    V.resize(3 * 65536);
+    F.resize(3 * 65536);
+    status(sim, mpm_surface_mesh_indexed(sim.handle(), grid_side_, radius_, V.data(), 65536, F.data(), 65536, &nv,
+                                         &nf));
+    if (nv > 65536 || nf > 65536) {
+      V.resize(3 * (size_t)nv);
+      F.resize(3 * (size_t)nf);
+      status(sim, mpm_surface_mesh_indexed(sim.handle(), grid_side_, radius_, V.data(), nv, F.data(), nf, &nv, &nf));
     }
+    V.resize(3 * (size_t)nv);
+    F.resize(3 * (size_t)nf);
+  }
+
+  /* Writes the OBJ file (igl::writeOBJ's v / f lines); returns the number of faces. */
+  size_t computeMesh(const std::string& filename, Simulation& sim) const {
+    std::vector<double> V;
+    std::vector<int32_t> F;
+    mesh(sim, V, F);
     FILE* out = std::fopen(filename.c_str(), "w");
     if (!out) throw Error(MPM_ERR_IO, "cannot write " + filename);
-    for (size_t v = 0; v < verts.size() / 3; ++v)
-      std::fprintf(out, "v %.9g %.9g %.9g\n", verts[3 * v], verts[3 * v + 1], verts[3 * v + 2]);
-    for (size_t q = 0; q < faces.size() / 3; ++q)
-      std::fprintf(out, "f %u %u %u\n", faces[3 * q] + 1, faces[3 * q + 1] + 1, faces[3 * q + 2] + 1);
+    for (size_t v = 0; v < V.size() / 3; ++v) std::fprintf(out, "v %.17g %.17g %.17g\n", V[3 * v], V[3 * v + 1], V[3 * v + 2]);
+    for (size_t q = 0; q < F.size() / 3; ++q) std::fprintf(out, "f %d %d %d\n", F[3 * q] + 1, F[3 * q + 1] + 1, F[3 * q + 2] + 1);
     if (std::fclose(out) != 0) throw Error(MPM_ERR_IO, "cannot write " + filename);
-    return faces.size() / 3;
+    return F.size() / 3;
   }
 
  private:

@@ -883,7 +883,8 @@ namespace {
 double voxel_dx_of(const mpm_ctx* c, int G) { return (double)((float)c->params.N * c->K.g.dx) / (double)G; }
 
 mpm_status surface_field(mpm_ctx* c, int32_t G, int32_t radius, bool finish) {
-  // G <= 512 keeps 12 (G-1)^3, the most triangles a field can give, within int32
+  // G <= 512 keeps the mesher's counts (at most 5 triangles, 3 vertices and one surface
+  // cube per cube of the (G-1)^3) within int32
   if (G < 2 || G > 512 || radius < 0 || radius > 64) return fail(c, MPM_ERR_INVALID, "grid_side or radius out of range");
   cudaError_t e = launch_distance_field(c->sA, c->stride, c->n, G, radius, voxel_dx_of(c, G), finish, c->surf,
                                         c->stream, &c->launches);
@@ -908,14 +909,42 @@ mpm_status mpm_surface_mesh(mpm_ctx* c, int32_t G, int32_t radius, float* tris, 
   if (!c || !n_tris || capacity < 0 || (capacity > 0 && !tris)) return MPM_ERR_INVALID;
   mpm_status st = surface_field(c, G, radius, false);
   if (st != MPM_OK) return st;
-  int64_t n = 0;
-  cudaError_t e = extract_surface(G, radius, voxel_dx_of(c, G), c->surf, c->stream, &n, &c->launches);
+  int64_t nv = 0, n = 0;
+  cudaError_t e = extract_surface(G, radius, voxel_dx_of(c, G), c->surf, c->stream, true, &nv, &n, &c->launches);
   const int64_t copy = std::min(n, capacity);
   if (e == cudaSuccess && copy > 0)
     e = cudaMemcpyAsync(tris, c->surf.tris, sizeof(float) * 9 * (size_t)copy, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return fail(c, MPM_ERR_CUDA, std::string("surface: ") + cudaGetErrorString(e));
   *n_tris = n;
+  return MPM_OK;
+}
+
+mpm_status mpm_surface_mesh_indexed(mpm_ctx* c, int32_t G, int32_t radius, double* vertices, int64_t vertex_capacity,
+                                    int32_t* faces, int64_t face_capacity, int64_t* n_vertices, int64_t* n_faces) {
+  if (!c || !n_vertices || !n_faces || vertex_capacity < 0 || face_capacity < 0 ||
+      (vertex_capacity > 0 && !vertices) || (face_capacity > 0 && !faces))
+    return MPM_ERR_INVALID;
+  mpm_status st = surface_field(c, G, radius, false);
+  if (st != MPM_OK) return st;
+  int64_t nv = 0, nf = 0;
+  cudaError_t e = extract_surface(G, radius, voxel_dx_of(c, G), c->surf, c->stream, false, &nv, &nf, &c->launches);
+  const int64_t vcopy = std::min(nv, vertex_capacity), fcopy = std::min(nf, face_capacity);
+  if (e == cudaSuccess && vcopy > 0)
+    e = cudaMemcpyAsync(vertices, c->surf.verts, sizeof(double) * 3 * (size_t)vcopy, cudaMemcpyDeviceToHost,
+                        c->stream);
+  if (e == cudaSuccess && fcopy > 0)
+    e = cudaMemcpyAsync(faces, c->surf.faces, sizeof(int32_t) * 3 * (size_t)fcopy, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail(c, MPM_ERR_CUDA, std::string("surface: ") + cudaGetErrorString(e));
+  *n_vertices = nv;
+  *n_faces = nf;
+  return MPM_OK;
+}
+
+mpm_status mpm_surface_table(int32_t* counts, int32_t* slots) {
+  if (!counts || !slots) return MPM_ERR_INVALID;
+  surface_table(counts, slots);
   return MPM_OK;
 }
 
@@ -931,11 +960,26 @@ mpm_status mpm_surface_mesh_device(mpm_ctx* c, int32_t G, int32_t radius, const 
   if (!c || !tris || !n_tris) return MPM_ERR_INVALID;
   mpm_status st = surface_field(c, G, radius, false);
   if (st != MPM_OK) return st;
-  int64_t n = 0;
-  cudaError_t e = extract_surface(G, radius, voxel_dx_of(c, G), c->surf, c->stream, &n, &c->launches);
+  int64_t nv = 0, n = 0;
+  cudaError_t e = extract_surface(G, radius, voxel_dx_of(c, G), c->surf, c->stream, true, &nv, &n, &c->launches);
   if (e != cudaSuccess) return fail(c, MPM_ERR_CUDA, std::string("surface: ") + cudaGetErrorString(e));
   *tris = c->surf.tris;
   *n_tris = n;
+  return MPM_OK;
+}
+
+mpm_status mpm_surface_mesh_indexed_device(mpm_ctx* c, int32_t G, int32_t radius, const double** vertices,
+                                           const int32_t** faces, int64_t* n_vertices, int64_t* n_faces) {
+  if (!c || !vertices || !faces || !n_vertices || !n_faces) return MPM_ERR_INVALID;
+  mpm_status st = surface_field(c, G, radius, false);
+  if (st != MPM_OK) return st;
+  int64_t nv = 0, nf = 0;
+  cudaError_t e = extract_surface(G, radius, voxel_dx_of(c, G), c->surf, c->stream, false, &nv, &nf, &c->launches);
+  if (e != cudaSuccess) return fail(c, MPM_ERR_CUDA, std::string("surface: ") + cudaGetErrorString(e));
+  *vertices = c->surf.verts;
+  *faces = c->surf.faces;
+  *n_vertices = nv;
+  *n_faces = nf;
   return MPM_OK;
 }
 

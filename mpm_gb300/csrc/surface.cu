@@ -15,19 +15,22 @@
 //     distances are non-negative floats, so integer order on their bits is float order;
 //     the float arithmetic per (particle, node) pair is the reference's, so the field
 //     matches its sequential loop bit for bit;
-//   * the level set is extracted by marching tetrahedra: each voxel cell is split into the
-//     six tetrahedra around its main diagonal (the same split in every cell, so the
-//     surface has no cracks), each tetrahedron gives 0, 1 or 2 triangles with vertices
-//     interpolated linearly on its edges, oriented from S > 0 to S < 0.  libigl is not
-//     available; marching tetrahedra yields the same level set with a finer triangulation.
-//     Corners are classified as the reference's double S > 0 (one float compare against
-//     the equivalent float threshold); edge points are interpolated in float (the
-//     triangles are float anyway; the double path cost far more on this part, whose FP64
-//     rate is a small fraction of its FP32 rate).  One sweep over the cells counts triangles
-//     and surface cells per block and lists each block's surface cells in its slots;
-//     exclusive scans over the blocks give their offsets; a dense emit pass (one thread per
-//     surface cell, which finds its block by binary search) writes the triangles in cell
-//     order, so the mesh is deterministic.
+//   * the level set is extracted by marching cubes in libigl's layout (the reference's
+//     vendored include/igl/copyleft/marching_cubes.cpp, fed by
+//     include/mesh_builder.h:181-194): cubes in node order with k fastest, a corner inside
+//     when S > 0 (one float compare against the equivalent float threshold), and a vertex
+//     created on each crossed edge the first time a cube sees it, at
+//     (1 - t) p0 + t p1, t = |S0| / (|S0| + |S1|), in double, then scaled by voxel_dx.
+//     So the vertex list is the reference's bit for bit and in its order: an edge is
+//     first seen by its lowest cube, and a cube's new vertices follow its edge slots.  The
+//     triangle table is this project's own (surface.h): it triangulates the same loops of
+//     crossed edges per cube as libigl's table, with a fan inside each loop.
+//     One sweep over the cubes counts triangles, new vertices and surface cubes per block
+//     of cubes and lists each block's surface cubes in its slots; one scan over the three
+//     counts gives the blocks' offsets; a dense emit pass (one thread per surface cube,
+//     which finds its block by binary search) writes the vertices it creates, its faces
+//     (a vertex created by an earlier cube is found through that cube's slot, again by
+//     binary search) and, when asked, the triangle soup, so the mesh is deterministic.
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -370,41 +373,61 @@ __global__ void finish_distance_kernel(unsigned* field, int64_t cells, float cut
     field[c] = __float_as_uint(fminf(cutoff, __fsqrt_rn(__uint_as_float(field[c]))));
 }
 
-// Bit q of the mask: corner q of cell (i, j, k) is inside, i.e. its value is below thr
-// (the field against the float threshold of S > 0, or the raw squared distance against
-// the squared threshold).  Indices fit in int (G <= 512).
+// The triangle table in global memory: threads of a warp read different entries, which
+// the read-only cache serves without the serialisation of divergent constant loads.
+__device__ const mc::Table kMc = mc::make_table();
+
+constexpr int kEmitThreads = 128;
+
+// Bit n of the mask: corner n of cube (i, j, k) (libigl's numbering) is inside, i.e. its
+// value is below thr (the field against the float threshold of S > 0, or the raw squared
+// distance against the squared threshold).  Indices fit in int (G <= 512).
 __device__ __forceinline__ unsigned corner_mask(const float* field, int G, int i, int j, int k, float thr) {
   const float* f = field + (i * G + j) * G + k;
   const int sj = G, si = G * G;
   unsigned m = 0;
   m |= (unsigned)(f[0] < thr) << 0;
   m |= (unsigned)(f[1] < thr) << 1;
-  m |= (unsigned)(f[sj] < thr) << 2;
-  m |= (unsigned)(f[sj + 1] < thr) << 3;
+  m |= (unsigned)(f[sj + 1] < thr) << 2;
+  m |= (unsigned)(f[sj] < thr) << 3;
   m |= (unsigned)(f[si] < thr) << 4;
   m |= (unsigned)(f[si + 1] < thr) << 5;
-  m |= (unsigned)(f[si + sj] < thr) << 6;
-  m |= (unsigned)(f[si + sj + 1] < thr) << 7;
+  m |= (unsigned)(f[si + sj + 1] < thr) << 6;
+  m |= (unsigned)(f[si + sj] < thr) << 7;
   return m;
 }
 
-// Triangles of a cell from its corner mask: per tetrahedron 1 when 1 or 3 corners are
-// inside, 2 when 2 are.
-__device__ __forceinline__ int mask_triangles(unsigned m) {
-  if (m == 0 || m == 0xffu) return 0;
-  int cnt = 0;
-#pragma unroll
-  for (int t = 0; t < 6; ++t) {
-    const unsigned tm = (1u << tet_corner(t, 0)) | (1u << tet_corner(t, 1)) | (1u << tet_corner(t, 2)) |
-                        (1u << tet_corner(t, 3));
-    const int k = __popc(m & tm);
-    cnt += (k == 2) ? 2 : (k == 1 || k == 3) ? 1 : 0;
-  }
-  return cnt;
+// Compile-time facts of edge slot E: its corners, axis and lower-corner offsets.
+template <int E>
+struct Edge {
+  static constexpr int a = mc::kEdge[E][0], b = mc::kEdge[E][1];
+  static constexpr int o0 = mc::kCorner[a][0], o1 = mc::kCorner[a][1], o2 = mc::kCorner[a][2];
+  static constexpr int ax = mc::kCorner[a][0] != mc::kCorner[b][0] ? 0 : mc::kCorner[a][1] != mc::kCorner[b][1] ? 1 : 2;
+  // owned by a cube whose coordinate is 0 on each perpendicular axis where the edge
+  // lies on the cube's lower side (bit p of `need_zero`)
+  static constexpr int need_zero = (ax != 0 && o0 == 0 ? 1 : 0) | (ax != 1 && o1 == 0 ? 2 : 0) | (ax != 2 && o2 == 0 ? 4 : 0);
+  static constexpr int slot_at(int s0, int s1, int s2) { return mc::slot_along(ax, o0 | s0, o1 | s1, o2 | s2); }
+  // the owner's slot for the shifts (s0, s1, s2), 4 bits per combination s0 * 4 + s1 * 2 + s2
+  static constexpr uint32_t owner_slots =
+      (uint32_t)slot_at(0, 0, 0) | (uint32_t)slot_at(0, 0, 1) << 4 | (uint32_t)slot_at(0, 1, 0) << 8 |
+      (uint32_t)slot_at(0, 1, 1) << 12 | (uint32_t)slot_at(1, 0, 0) << 16 | (uint32_t)slot_at(1, 0, 1) << 20 |
+      (uint32_t)slot_at(1, 1, 0) << 24 | (uint32_t)slot_at(1, 1, 1) << 28;
+};
+
+// The edge slots whose vertex cube (i, j, k) creates: libigl visits the cubes in order and
+// creates a vertex the first time an edge is seen, i.e. in the edge's lowest cube, which
+// lowers each coordinate across the edge by one where it can.
+template <int... E>
+__device__ __forceinline__ unsigned owned_mask_impl(int zero, std::integer_sequence<int, E...>) {
+  return ((((Edge<E>::need_zero & ~zero) == 0) ? 1u << E : 0u) | ...);
+}
+__device__ __forceinline__ unsigned owned_mask(int i, int j, int k) {
+  const int zero = (i == 0 ? 1 : 0) | (j == 0 ? 2 : 0) | (k == 0 ? 4 : 0);
+  return owned_mask_impl(zero, std::make_integer_sequence<int, 12>{});
 }
 
-// Cells are swept one (i, j) row at a time: grid (row segments of kSurfThreads cells, j, i),
-// so the linear block index runs in cell order.  False for the padding past a row's end.
+// Cubes are swept one (i, j) row at a time: grid (row segments of kSurfThreads cubes, j, i),
+// so the linear block index runs in cube order.  False for the padding past a row's end.
 __device__ __forceinline__ bool block_cell(int G, int& i, int& j, int& k) {
   i = (int)blockIdx.z;
   j = (int)blockIdx.y;
@@ -416,83 +439,209 @@ __device__ __forceinline__ int64_t block_linear() {
   return ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
 }
 
-// The one sweep over the cells: per block, its triangle and surface-cell counts, and in the
-// block's slots (kSurfThreads of them) its surface cells in cell order, each with its first
-// triangle's offset inside the block.
-__global__ void __launch_bounds__(kSurfThreads) mc_count_kernel(const float* __restrict__ field, int G, float thr,
-                                                                int* __restrict__ block_tris,
-                                                                int* __restrict__ block_cells,
-                                                                int2* __restrict__ slots) {
-  __shared__ int warp_tris[kSurfThreads / 32], warp_cells[kSurfThreads / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int i, j, k, cnt = 0;
-  if (block_cell(G, i, j, k)) cnt = mask_triangles(corner_mask(field, G, i, j, k, thr));
-  const unsigned surf = __ballot_sync(kFull, cnt > 0);
-  int inc = cnt;
+__device__ __forceinline__ int warp_inclusive(int v, int lane) {
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const int t = __shfl_up_sync(kFull, inc, o);
-    if (lane >= o) inc += t;
+    const int t = __shfl_up_sync(kFull, v, o);
+    if (lane >= o) v += t;
   }
+  return v;
+}
+
+// The one sweep over the cubes.  counts holds three runs of nblocks + 1 ints (triangles,
+// new vertices, surface cubes per block, each run ending in a zero); the block's slots
+// (kSurfThreads of them) list its surface cubes in cube order with their first triangle
+// and first vertex inside the block and their inside-corner mask.
+__global__ void __launch_bounds__(kSurfThreads) mc_count_kernel(const float* __restrict__ field, int G, float thr,
+                                                                int* __restrict__ counts, int64_t nblocks,
+                                                                int4* __restrict__ slots) {
+  __shared__ int warp_tris[kSurfThreads / 32], warp_verts[kSurfThreads / 32], warp_cells[kSurfThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int i, j, k;
+  unsigned m = 0;
+  int nt = 0, nv = 0;
+  if (block_cell(G, i, j, k)) {
+    m = corner_mask(field, G, i, j, k, thr);
+    nt = __ldg(&kMc.count[m]);
+    nv = __popc(__ldg(&kMc.crossed[m]) & owned_mask(i, j, k));
+  }
+  const unsigned surf = __ballot_sync(kFull, nt > 0);
+  const int tinc = warp_inclusive(nt, lane), vinc = warp_inclusive(nv, lane);
   if (lane == 31) {
-    warp_tris[warp] = inc;
+    warp_tris[warp] = tinc;
+    warp_verts[warp] = vinc;
     warp_cells[warp] = __popc(surf);
   }
   __syncthreads();
   const int64_t b = block_linear();
   if (threadIdx.x == 0) {
-    int t = 0, c = 0;
+    int t = 0, v = 0, c = 0;
     for (int w = 0; w < kSurfThreads / 32; ++w) {
       t += warp_tris[w];
+      v += warp_verts[w];
       c += warp_cells[w];
     }
-    block_tris[b] = t;
-    block_cells[b] = c;
+    counts[b] = t;
+    counts[(nblocks + 1) + b] = v;
+    counts[2 * (nblocks + 1) + b] = c;
+    if (b == 0) counts[nblocks] = counts[2 * nblocks + 1] = counts[3 * nblocks + 2] = 0;
   }
-  if (cnt == 0) return;
-  int tpre = 0, cpre = 0;
+  if (nt == 0) return;
+  int tpre = 0, vpre = 0, cpre = 0;
   for (int w = 0; w < warp; ++w) {
     tpre += warp_tris[w];
+    vpre += warp_verts[w];
     cpre += warp_cells[w];
   }
   const int rank = cpre + __popc(surf & ((1u << lane) - 1u));
-  slots[b * kSurfThreads + rank] = make_int2((i << 20) | (j << 10) | k, tpre + inc - cnt);
+  slots[b * kSurfThreads + rank] = make_int4((i << 20) | (j << 10) | k, tpre + tinc - nt, vpre + vinc - nv, (int)m);
 }
 
-// Triangles of the surface cells, one thread per cell.  RAW: the buffer holds the squared
-// distances and a corner's field value is min(cutoff, sqrt(s)) (what
-// finish_distance_kernel stores).
-// Surface cell c (in cell order) is found in the slots of the block b whose exclusive scan
-// of surface cells, cell_off[b], is the last one <= c; tri_off[b] is the block's first
-// triangle.
-template <bool RAW>
-__global__ void __launch_bounds__(kSurfThreads) mc_emit_kernel(const float* __restrict__ field, int G, float thr,
-                                                               float cutoff, float iso, float vdx,
-                                                               const int* __restrict__ tri_off,
-                                                               const int* __restrict__ cell_off, int64_t nblocks,
-                                                               const int2* __restrict__ slots, int ncells,
-                                                               float* __restrict__ tris) {
-  const int c = blockIdx.x * kSurfThreads + threadIdx.x;
-  if (c >= ncells) return;
-  int64_t lo = 0, hi = nblocks - 1;  // cell_off[0] = 0 <= c < cell_off[nblocks] = ncells
+// The three totals of the scanned counts into pinned host memory.
+__global__ void mc_totals_kernel(const int* __restrict__ scan, int64_t nblocks, int* total) {
+  total[0] = scan[nblocks];
+  total[1] = scan[2 * nblocks + 1] - scan[nblocks + 1];
+  total[2] = scan[3 * nblocks + 2] - scan[2 * nblocks + 2];
+}
+
+struct EmitArgs {
+  const float* field;
+  int G, gx;  // grid side, blocks per row of cubes
+  float thr, cutoff;
+  double iso, vdx;
+  const int* scan;  // scanned counts (three runs of nblocks + 1)
+  int64_t nblocks;
+  const int4* slots;
+  int ncells;
+  double* verts;
+  int* faces;
+  float* tris;
+};
+
+// The vertex libigl creates on edge slot E of cube (i, j, k) (add_vertex: the point
+// (1 - t) p0 + t p1 with t = |S0| / (|S0| + |S1|), p0 the lower node, in double; then
+// scaled by voxel_dx as MeshBuilder::computeMesh does).
+template <int E>
+__device__ __forceinline__ void edge_position(const double S[8], int i, int j, int k, double vdx, double p[3]) {
+  using D = Edge<E>;
+  const double s0 = fabs(S[D::a]), s1 = fabs(S[D::b]);
+  const double t = __ddiv_rn(s0, __dadd_rn(s0, s1));
+  const double u = __dsub_rn(1.0, t);
+  const int c[3] = {i + D::o0, j + D::o1, k + D::o2};
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const double a = (double)c[q], b = (double)(c[q] + (q == D::ax ? 1 : 0));
+    p[q] = __dmul_rn(__dadd_rn(__dmul_rn(u, a), __dmul_rn(t, b)), vdx);
+  }
+}
+
+// Index of the vertex on edge slot E of cube (i, j, k) when an earlier cube creates it: the
+// owner cube is found in its block's slots by binary search (they are in cube order), and
+// the vertex is the owner's first plus the owner's created edges before the owner's slot.
+template <int E>
+__device__ __forceinline__ int owner_vertex(const EmitArgs& a, int i, int j, int k) {
+  using D = Edge<E>;
+  const int s0 = (D::need_zero & 1) && i > 0, s1 = (D::need_zero & 2) && j > 0, s2 = (D::need_zero & 4) && k > 0;
+  const int ci = i - s0, cj = j - s1, ck = k - s2;
+  const int e2 = (int)((D::owner_slots >> (4 * (s0 * 4 + s1 * 2 + s2))) & 15u);
+  const int64_t b = ((int64_t)ci * (a.G - 1) + cj) * a.gx + ck / kSurfThreads;
+  const int* cell_off = a.scan + 2 * (a.nblocks + 1);
+  const int cnt = cell_off[b + 1] - cell_off[b];
+  const int key = (ci << 20) | (cj << 10) | ck;
+  const int* keys = reinterpret_cast<const int*>(a.slots + b * kSurfThreads);
+  int lo = 0, hi = cnt - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (keys[4 * mid] < key) lo = mid + 1; else hi = mid;
+  }
+  const int4 o = a.slots[b * kSurfThreads + lo];
+  const int* vert_off = a.scan + (a.nblocks + 1);
+  const unsigned mine = __ldg(&kMc.crossed[o.w & 255]) & owned_mask(ci, cj, ck) & ((1u << e2) - 1u);
+  return vert_off[b] - vert_off[0] + o.z + __popc(mine);
+}
+
+template <bool SOUP>
+struct EmitScratch {
+  int id[12][kEmitThreads];
+  float pos[SOUP ? 36 : 1][kEmitThreads];
+};
+
+template <bool SOUP, int E>
+__device__ __forceinline__ void emit_edge(const EmitArgs& a, const double S[8], int i, int j, int k, unsigned crossed,
+                                          unsigned owned, int vbase, EmitScratch<SOUP>& sh, int tid) {
+  if (!((crossed >> E) & 1u)) return;
+  const bool own = (owned >> E) & 1u;
+  int id;
+  if (own) id = vbase + __popc(crossed & owned & ((1u << E) - 1u));
+  else id = owner_vertex<E>(a, i, j, k);
+  sh.id[E][tid] = id;
+  if (own || SOUP) {
+    double p[3];
+    edge_position<E>(S, i, j, k, a.vdx, p);
+    if (own)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) a.verts[3 * (int64_t)id + q] = p[q];
+    if (SOUP)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) sh.pos[(3 * E + q) % (SOUP ? 36 : 1)][tid] = (float)p[q];
+  }
+}
+
+template <bool SOUP, int... E>
+__device__ __forceinline__ void emit_edges(const EmitArgs& a, const double S[8], int i, int j, int k, unsigned crossed,
+                                           unsigned owned, int vbase, EmitScratch<SOUP>& sh, int tid,
+                                           std::integer_sequence<int, E...>) {
+  (emit_edge<SOUP, E>(a, S, i, j, k, crossed, owned, vbase, sh, tid), ...);
+}
+
+// Vertices, faces (and the triangle soup) of the surface cubes, one thread per cube.
+// RAW: the buffer holds the squared distances and a corner's field value is
+// min(cutoff, sqrt(s)) (what finish_distance_kernel stores).  Surface cube c (in cube
+// order) is found in the slots of the block b whose scanned surface-cube count is the
+// last one <= c.
+template <bool RAW, bool SOUP>
+__global__ void __launch_bounds__(kEmitThreads) mc_emit_kernel(const EmitArgs a) {
+  __shared__ EmitScratch<SOUP> sh;
+  const int tid = threadIdx.x;
+  const int c = blockIdx.x * kEmitThreads + tid;
+  if (c >= a.ncells) return;
+  const int* tri_off = a.scan;
+  const int* vert_off = a.scan + (a.nblocks + 1);
+  const int* cell_off = a.scan + 2 * (a.nblocks + 1);
+  const int c0 = cell_off[0];
+  int64_t lo = 0, hi = a.nblocks - 1;  // cell_off[0] - c0 = 0 <= c < ncells
   while (lo < hi) {
     const int64_t mid = (lo + hi + 1) >> 1;
-    if (cell_off[mid] <= c) lo = mid; else hi = mid - 1;
+    if (cell_off[mid] - c0 <= c) lo = mid; else hi = mid - 1;
   }
-  int2 e = slots[lo * kSurfThreads + (c - cell_off[lo])];
-  e.y += tri_off[lo];
+  const int4 e = a.slots[lo * kSurfThreads + (c - (cell_off[lo] - c0))];
   const int i = e.x >> 20, j = (e.x >> 10) & 1023, k = e.x & 1023;
-  float f[8];
-  unsigned m = 0;
+  const int tbase = tri_off[lo] + e.y;
+  const int vbase = vert_off[lo] - vert_off[0] + e.z;
+  const unsigned m = (unsigned)e.w;
+  const int G = a.G;
+  double S[8];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const float v = field[((i + (q >> 2)) * G + j + ((q >> 1) & 1)) * G + k + (q & 1)];
-    m |= (unsigned)(v < thr) << q;
-    f[q] = RAW ? fminf(cutoff, __fsqrt_rn(v)) : v;
+  for (int n = 0; n < 8; ++n) {
+    const int di = n >> 2, dj = (n >> 1) & 1, dk = ((n >> 1) ^ n) & 1;  // libigl's corner n
+    const float v = a.field[((i + di) * G + j + dj) * G + k + dk];
+    const float f = RAW ? fminf(a.cutoff, __fsqrt_rn(v)) : v;
+    S[n] = __dsub_rn(a.iso, (double)f);
   }
-  float* out = tris + 9 * (int64_t)e.y;
-#pragma unroll 1
-  for (int t = 0; t < 6; ++t) out += 9 * tet_triangles(f, m, t, i, j, k, iso, vdx, out);
+  const unsigned crossed = __ldg(&kMc.crossed[m]);
+  emit_edges<SOUP>(a, S, i, j, k, crossed, owned_mask(i, j, k), vbase, sh, tid, std::make_integer_sequence<int, 12>{});
+  const int nt = __ldg(&kMc.count[m]);
+  for (int t = 0; t < nt; ++t) {
+    const int64_t f = (int64_t)(tbase + t);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const int sl = __ldg(&kMc.slot[m][3 * t + r]);
+      a.faces[3 * f + r] = sh.id[sl][tid];
+      if (SOUP)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) a.tris[9 * f + 3 * r + q] = sh.pos[(3 * sl + q) % (SOUP ? 36 : 1)][tid];
+    }
+  }
 }
 
 // The float threshold thr with  field < thr  <=>  iso - (double)field > 0.
@@ -566,11 +715,21 @@ cudaError_t reserve(T** p, int64_t* cap, int64_t need) {
 
 }  // namespace
 
+void surface_table(int32_t* counts, int32_t* slots) {
+  constexpr mc::Table t = mc::make_table();
+  for (int m = 0; m < 256; ++m) {
+    counts[m] = t.count[m];
+    for (int r = 0; r < 30; ++r) slots[30 * m + r] = t.slot[m][r];
+  }
+}
+
 void SurfaceBuffers::release() {
   cudaFree(field);
   cudaFree(cells);
   cudaFree(counts);
   cudaFree(scan);
+  cudaFree(verts);
+  cudaFree(faces);
   cudaFree(tris);
   cudaFreeHost(total);
   *this = SurfaceBuffers{};
@@ -605,53 +764,67 @@ cudaError_t launch_distance_field(const float* s, int64_t stride, int64_t n, int
   return cudaGetLastError();
 }
 
-cudaError_t extract_surface(int G, int radius, double voxel_dx, SurfaceBuffers& buf, cudaStream_t st,
-                            int64_t* n_out, int64_t* launches) {
-  *n_out = 0;
+cudaError_t extract_surface(int G, int radius, double voxel_dx, SurfaceBuffers& buf, cudaStream_t st, bool soup,
+                            int64_t* n_verts, int64_t* n_faces, int64_t* launches) {
+  *n_verts = *n_faces = 0;
   if (G < 2) return cudaSuccess;
   const SurfaceConsts K = surface_consts(radius, voxel_dx);
   const float thr = buf.raw ? sq_threshold(K.thr) : K.thr;
   const int Gm = G - 1;
   const dim3 grid((unsigned)((Gm + kSurfThreads - 1) / kSurfThreads), (unsigned)Gm, (unsigned)Gm);
   const int64_t nblocks = (int64_t)grid.x * grid.y * grid.z;
-  // counts: per-block triangles (nblocks + 1), then per-block surface cells (nblocks + 1)
-  cudaError_t e = reserve(&buf.counts, &buf.counts_cap, 2 * (nblocks + 1));
-  if (e == cudaSuccess) e = reserve(&buf.scan, &buf.scan_cap, scan_scratch_ints(nblocks + 1));
-  if (e == cudaSuccess && !buf.total) e = cudaMallocHost(&buf.total, 2 * sizeof(int));
+  // counts: per-block triangles, new vertices and surface cubes, nblocks + 1 each
+  cudaError_t e = reserve(&buf.counts, &buf.counts_cap, 3 * (nblocks + 1));
+  if (e == cudaSuccess) e = reserve(&buf.scan, &buf.scan_cap, scan_scratch_ints(3 * (nblocks + 1)));
+  if (e == cudaSuccess && !buf.total) e = cudaMallocHost(&buf.total, 3 * sizeof(int));
+  if (e == cudaSuccess) e = reserve(&buf.cells, &buf.cells_cap, nblocks * kSurfThreads);
   if (e != cudaSuccess) return e;
-  int* block_tris = buf.counts;
-  int* block_cells = buf.counts + nblocks + 1;
-  e = reserve(&buf.cells, &buf.cells_cap, nblocks * kSurfThreads);
-  if (e != cudaSuccess) return e;
-  mc_count_kernel<<<grid, kSurfThreads, 0, st>>>(buf.field, G, thr, block_tris, block_cells, buf.cells);
-  e = cudaMemsetAsync(block_tris + nblocks, 0, sizeof(int), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(block_cells + nblocks, 0, sizeof(int), st);
-  if (e == cudaSuccess) e = cudaGetLastError();
-  if (e == cudaSuccess) e = launch_exclusive_scan(block_tris, nblocks + 1, buf.scan, st, launches);
-  if (e == cudaSuccess) e = launch_exclusive_scan(block_cells, nblocks + 1, buf.scan, st, launches);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(buf.total, block_tris + nblocks, sizeof(int), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(buf.total + 1, block_cells + nblocks, sizeof(int), cudaMemcpyDeviceToHost, st);
+  mc_count_kernel<<<grid, kSurfThreads, 0, st>>>(buf.field, G, thr, buf.counts, nblocks, buf.cells);
+  e = cudaGetLastError();
+  // one scan over the three runs: a run's offsets are its scanned values less its first
+  if (e == cudaSuccess) e = launch_exclusive_scan(buf.counts, 3 * (nblocks + 1), buf.scan, st, launches);
+  if (e == cudaSuccess) {
+    mc_totals_kernel<<<1, 1, 0, st>>>(buf.counts, nblocks, buf.total);
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e;
-  if (launches) *launches += 1;
-  const int64_t total = buf.total[0];
-  const int ncells = buf.total[1];
-  if (total > 0) {
-    e = reserve(&buf.tris, &buf.tris_cap, 9 * total);
+  if (launches) *launches += 2;
+  const int64_t nt = buf.total[0], nv = buf.total[1];
+  const int ncells = buf.total[2];
+  if (nt > 0) {
+    e = reserve(&buf.verts, &buf.verts_cap, 3 * nv);
+    if (e == cudaSuccess) e = reserve(&buf.faces, &buf.faces_cap, 3 * nt);
+    if (e == cudaSuccess && soup) e = reserve(&buf.tris, &buf.tris_cap, 9 * nt);
     if (e != cudaSuccess) return e;
-    const float iso = (float)K.iso;
-    const unsigned eblocks = (unsigned)((ncells + kSurfThreads - 1) / kSurfThreads);
-    if (buf.raw)
-      mc_emit_kernel<true><<<eblocks, kSurfThreads, 0, st>>>(buf.field, G, thr, K.cutoff, iso, K.vdx, block_tris,
-                                                             block_cells, nblocks, buf.cells, ncells, buf.tris);
-    else
-      mc_emit_kernel<false><<<eblocks, kSurfThreads, 0, st>>>(buf.field, G, thr, K.cutoff, iso, K.vdx, block_tris,
-                                                              block_cells, nblocks, buf.cells, ncells, buf.tris);
+    EmitArgs a;
+    a.field = buf.field;
+    a.G = G;
+    a.gx = (int)grid.x;
+    a.thr = thr;
+    a.cutoff = K.cutoff;
+    a.iso = K.iso;
+    a.vdx = voxel_dx;
+    a.scan = buf.counts;
+    a.nblocks = nblocks;
+    a.slots = buf.cells;
+    a.ncells = ncells;
+    a.verts = buf.verts;
+    a.faces = buf.faces;
+    a.tris = soup ? buf.tris : nullptr;
+    const unsigned eblocks = (unsigned)((ncells + kEmitThreads - 1) / kEmitThreads);
+    if (buf.raw) {
+      if (soup) mc_emit_kernel<true, true><<<eblocks, kEmitThreads, 0, st>>>(a);
+      else mc_emit_kernel<true, false><<<eblocks, kEmitThreads, 0, st>>>(a);
+    } else {
+      if (soup) mc_emit_kernel<false, true><<<eblocks, kEmitThreads, 0, st>>>(a);
+      else mc_emit_kernel<false, false><<<eblocks, kEmitThreads, 0, st>>>(a);
+    }
     e = cudaGetLastError();
     if (launches) *launches += 1;
   }
-  *n_out = total;
+  *n_verts = nt > 0 ? nv : 0;
+  *n_faces = nt;
   return e;
 }
 

@@ -2,9 +2,9 @@
 
 ``MeshBuilder(N, dx, grid_side, particle_radius).computeMesh(filename, sim)`` follows
 MeshBuilder::computeMesh (include/mesh_builder.h:170-211) as src/main.cu:78-106 drives it
-once per saved frame: the distance field and the level set are computed on the GPU
-(``mpm_surface_mesh``), the triangle soup is welded into an indexed mesh on the host and
-written as an OBJ file (igl::writeOBJ's ``v`` / ``f`` lines).  The reference's optional
+once per saved frame: the distance field and the marching-cubes mesh are computed on the
+GPU (``mpm_surface_mesh_indexed``: libigl's vertex list bit for bit, faces over the same
+edge loops) and written as an OBJ file (igl::writeOBJ's ``v`` / ``f`` lines).  The reference's optional
 libigl post-processing (``--laplacian_smooth``, ``--mesh-face-count`` decimation, both
 off by default) is not provided.
 """
@@ -18,23 +18,25 @@ MESH_PARTICLE_RADIUS = 5
 
 
 def weld(tris: np.ndarray):
-    """Indexed mesh (V (n, 3) float32, F (T, 3) int32) of a triangle soup (T, 3, 3).
-    Vertices on the same voxel edge are bit-identical, so exact matching welds them.
-    Where the level set passes exactly through a voxel node, edge points coincide and
-    their triangles collapse to a repeated index; those faces are dropped."""
+    """Indexed mesh (V (n, 3), F (T, 3) int32) of a triangle soup (T, 3, 3), for soups
+    from mpm_surface_mesh.  Vertices on the same voxel edge are bit-identical, so exact
+    matching welds them.  Where the level set passes exactly through a voxel node, edge
+    points coincide and their triangles collapse to a repeated index; those faces are
+    dropped."""
     pts = np.ascontiguousarray(tris.reshape(-1, 3))
     if pts.shape[0] == 0:
-        return np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)
-    V, inv = np.unique(pts.view(np.dtype((np.void, 12))).ravel(), return_inverse=True)
+        return np.zeros((0, 3), pts.dtype), np.zeros((0, 3), np.int32)
+    V, inv = np.unique(pts.view(np.dtype((np.void, 3 * pts.itemsize))).ravel(), return_inverse=True)
     F = inv.reshape(-1, 3).astype(np.int32)
     F = F[(F[:, 0] != F[:, 1]) & (F[:, 1] != F[:, 2]) & (F[:, 0] != F[:, 2])]
-    return np.ascontiguousarray(V.view(np.float32).reshape(-1, 3)), F
+    return np.ascontiguousarray(V.view(pts.dtype).reshape(-1, 3)), F
 
 
 def write_obj(filename: str, V: np.ndarray, F: np.ndarray) -> None:
-    """igl::writeOBJ's subset: ``v x y z`` lines, then 1-based ``f a b c`` lines."""
+    """igl::writeOBJ's subset: ``v x y z`` lines (17 significant digits, enough to read
+    the doubles back exactly), then 1-based ``f a b c`` lines."""
     with open(filename, "w") as f:
-        np.savetxt(f, V, fmt="v %.9g %.9g %.9g")
+        np.savetxt(f, V, fmt="v %.17g %.17g %.17g")
         np.savetxt(f, F + 1, fmt="f %d %d %d")
 
 
@@ -46,8 +48,8 @@ class MeshBuilder:
         self.particle_radius = int(particle_radius)
 
     def mesh(self, sim):
-        """(V, F) of the particles' surface."""
-        return weld(sim.surface_mesh(self.grid_side, self.particle_radius))
+        """(V float64, F int32) of the particles' surface."""
+        return sim.surface_indexed(self.grid_side, self.particle_radius)
 
     def computeMesh(self, filename: str, sim) -> int:
         """Writes the surface of the simulation's active particles; returns the face count."""

@@ -179,13 +179,33 @@ class Simulation:
         _lib.check(self.L.mpm_surface_distance(self.ctx, G, int(radius), _ptr(out)), self.ctx)
         return out
 
+    def surface_indexed(self, grid_side: int = 250, radius: int = 5):
+        """The particles' surface as MeshBuilder::computeMesh hands it to igl::writeOBJ
+        (include/mesh_builder.h:170-210): vertices (V, 3) float64 in libigl's marching-cubes
+        order, bit for bit, and outward faces (F, 3) int32 (zero-based)."""
+        G = int(grid_side)
+        nv, nf = ctypes.c_int64(), ctypes.c_int64()
+        # a first guess of the sizes (a surface crossing 16 G^2 cubes); retried once if short
+        guess = max(1, min(5 * (G - 1) ** 3, 16 * G * G))
+        V = np.empty((guess, 3), np.float64)
+        F = np.empty((guess, 3), np.int32)
+        _lib.check(self.L.mpm_surface_mesh_indexed(self.ctx, G, int(radius), _ptr(V), V.shape[0], _ptr(F), F.shape[0],
+                                                   ctypes.byref(nv), ctypes.byref(nf)), self.ctx)
+        if nv.value > V.shape[0] or nf.value > F.shape[0]:
+            V = np.empty((max(nv.value, 1), 3), np.float64)
+            F = np.empty((max(nf.value, 1), 3), np.int32)
+            _lib.check(self.L.mpm_surface_mesh_indexed(self.ctx, G, int(radius), _ptr(V), V.shape[0], _ptr(F),
+                                                       F.shape[0], ctypes.byref(nv), ctypes.byref(nf)), self.ctx)
+        return V[:nv.value], F[:nf.value]
+
     def surface_mesh(self, grid_side: int = 250, radius: int = 5) -> np.ndarray:
         """Triangles (T, 3, 3) float32 of the particles' surface (the zero level of
-        radius voxel_dx - distance, include/mesh_builder.h:170-190), in cell order."""
+        radius voxel_dx - distance, include/mesh_builder.h:170-190): the faces of
+        surface_indexed with their vertices rounded to float, in the same order."""
         G = int(grid_side)
         n = ctypes.c_int64()
         # a first guess of the triangle count (a surface crossing 16 G^2 cells); retried once if short
-        out = np.empty((max(1, min(12 * (G - 1) ** 3, 16 * G * G)), 3, 3), np.float32)
+        out = np.empty((max(1, min(5 * (G - 1) ** 3, 16 * G * G)), 3, 3), np.float32)
         _lib.check(self.L.mpm_surface_mesh(self.ctx, G, int(radius), _ptr(out), out.shape[0], ctypes.byref(n)),
                    self.ctx)
         if n.value > out.shape[0]:

@@ -83,8 +83,11 @@ def lib():
                                          ctypes.c_int64, P, ctypes.c_int64, P, ctypes.c_int64]
         L.oracle_distance_field.restype = None
         L.oracle_distance_field.argtypes = [P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, P]
-        L.oracle_surface_mesh.restype = ctypes.c_int64
-        L.oracle_surface_mesh.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, P, ctypes.c_int64]
+        L.oracle_surface_indexed.restype = None
+        L.oracle_surface_indexed.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, P, ctypes.c_int64, P,
+                                             ctypes.c_int64, P, P]
+        L.oracle_surface_table.restype = None
+        L.oracle_surface_table.argtypes = [P, P]
         _lib = L
     return _lib
 
@@ -227,12 +230,30 @@ def distance_field(x: np.ndarray, grid_side: int, radius: int, vdx: float) -> np
     return f
 
 
-def surface_mesh(field: np.ndarray, radius: int, vdx: float) -> np.ndarray:
-    """Triangles (T, 3, 3) float32 of the level set radius vdx - field = 0."""
+def surface_indexed(field: np.ndarray, radius: int, vdx: float):
+    """Marching-cubes vertices (nv, 3) float64 and faces (nf, 3) int32 of the level set
+    radius vdx - field = 0 (oracle/surface_oracle.cpp)."""
     f = np.ascontiguousarray(field, np.float32)
     G = f.shape[0]
     L = lib()
-    n = L.oracle_surface_mesh(_ptr(f), G, int(radius), float(vdx), None, 0)
-    t = np.empty((max(n, 1), 3, 3), np.float32)
-    L.oracle_surface_mesh(_ptr(f), G, int(radius), float(vdx), _ptr(t), n)
-    return t[:n]
+    nv, nf = ctypes.c_int64(), ctypes.c_int64()
+    L.oracle_surface_indexed(_ptr(f), G, int(radius), float(vdx), None, 0, None, 0, ctypes.byref(nv), ctypes.byref(nf))
+    V = np.empty((max(nv.value, 1), 3), np.float64)
+    F = np.empty((max(nf.value, 1), 3), np.int32)
+    L.oracle_surface_indexed(_ptr(f), G, int(radius), float(vdx), _ptr(V), nv.value, _ptr(F), nf.value,
+                             ctypes.byref(nv), ctypes.byref(nf))
+    return V[:nv.value], F[:nf.value]
+
+
+def surface_mesh(field: np.ndarray, radius: int, vdx: float) -> np.ndarray:
+    """Triangles (T, 3, 3) float32: the faces' vertices rounded to float."""
+    V, F = surface_indexed(field, radius, vdx)
+    return V[F].astype(np.float32)
+
+
+def surface_table():
+    """The oracle's triangle table: counts (256,) and edge-slot triples (256, 30), -1 padded."""
+    n = np.empty(256, np.int32)
+    t = np.empty((256, 30), np.int32)
+    lib().oracle_surface_table(_ptr(n), _ptr(t))
+    return n, t

@@ -10,105 +10,83 @@
  * (Eigen's unrolled reduction of a 3-vector).  The minimum does not depend on the
  * particle order, so the GPU's atomic scatter must match it bit for bit.
  *
- * Surface: the reference hands S = radius voxel_dx - field (include/mesh_builder.h:188)
- * to libigl's marching cubes, which is not in this image.  The GPU extracts the same
- * zero level set by marching tetrahedra; this file restates that extraction: a corner is
- * inside when S > 0 in double (here tested directly, on the GPU through the equivalent
- * float threshold), each cell is split into the six tetrahedra around its main diagonal,
- * edge points are interpolated in float from the inside corner to the outside one,
- * triangles face outward by the tetrahedron's corner layout, and cells are visited in
- * (i, j, k) order.  IEEE float without contraction (built with -ffp-contract=off), so
- * the triangle lists agree bit for bit.
+ * Surface: MeshBuilder::computeMesh hands S = radius voxel_dx - field, on nodes at
+ * (i, j, k) with i slowest (include/mesh_builder.h:181-194), to libigl's marching cubes
+ * (the reference's vendored include/igl/copyleft/marching_cubes.cpp), then scales V by
+ * voxel_dx.  The vertices are restated from that code: cubes are visited with k fastest,
+ * a corner is inside when S > 0, and the crossed edges of each cube are visited in the
+ * order of its edge slots 0..11 (corner pairs below, lower node index first); an edge
+ * seen for the first time appends the vertex (1 - t) p0 + t p1, t = |S0| / (|S0| + |S1|),
+ * computed in double.  The faces are this project's own triangulation of the same
+ * crossings (libigl's triangle table is not restated): on each face of a cube, a segment
+ * joins the edge where the face's corner cycle (counter-clockwise seen from outside)
+ * enters the inside to the edge where it leaves it, and a face with two opposite inside
+ * corners cuts each of them off; the segments of a cube close into loops, and each loop,
+ * started at its lowest edge slot, is fanned from that edge.  Faces point outward.
  */
 #include <stdint.h>
 
 #include <algorithm>
 #include <cmath>
+#include <unordered_map>
 #include <vector>
 
 namespace {
 
-const int kTets[6][4] = {{0, 4, 6, 7}, {0, 4, 5, 7}, {0, 1, 5, 7}, {0, 1, 3, 7}, {0, 2, 3, 7}, {0, 2, 6, 7}};
+// corner n of a cube at offset (di, dj, dk) from its lowest node
+const int kCorner[8][3] = {{0, 0, 0}, {0, 0, 1}, {0, 1, 1}, {0, 1, 0}, {1, 0, 0}, {1, 0, 1}, {1, 1, 1}, {1, 1, 0}};
+// edge slot -> its two corners, lower node index first
+const int kEdge[12][2] = {{0, 1}, {1, 2}, {3, 2}, {0, 3}, {4, 5}, {5, 6}, {7, 6}, {4, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+// the six faces: corners counter-clockwise seen from outside the cube
+const int kFace[6][4] = {{0, 1, 2, 3}, {4, 7, 6, 5}, {0, 4, 5, 1}, {3, 2, 6, 7}, {0, 3, 7, 4}, {1, 5, 6, 2}};
 
-int bit(int q, int c) { return (q >> (2 - c)) & 1; }
-
-// edge point from the inside corner qi to the outside corner qo
-void edge_point(const float f[8], int qi, int qo, int i, int j, int k, float iso, float vdx, float* p) {
-  const float t = (iso - f[qi]) / (f[qo] - f[qi]);
-  const int cell[3] = {i, j, k};
-  for (int c = 0; c < 3; ++c) {
-    const float a = (float)(cell[c] + bit(qi, c)), b = (float)(cell[c] + bit(qo, c));
-    p[c] = (a + t * (b - a)) * vdx;
-  }
+int edge_of(int a, int b) {
+  for (int e = 0; e < 12; ++e)
+    if ((kEdge[e][0] == a && kEdge[e][1] == b) || (kEdge[e][0] == b && kEdge[e][1] == a)) return e;
+  return -1;
 }
 
-int det3(int L, int A, int B, int C) {
-  int u[3], v[3], w[3];
-  for (int c = 0; c < 3; ++c) {
-    u[c] = bit(A, c) - bit(L, c);
-    v[c] = bit(B, c) - bit(L, c);
-    w[c] = bit(C, c) - bit(L, c);
-  }
-  return u[0] * (v[1] * w[2] - v[2] * w[1]) - u[1] * (v[0] * w[2] - v[2] * w[0]) + u[2] * (v[0] * w[1] - v[1] * w[0]);
-}
-
-bool quad_flip(int a, int b, int c, int d) {
-  int e1[3], e2[3], aw[3];
-  for (int x = 0; x < 3; ++x) {
-    e1[x] = bit(d, x) - bit(c, x);
-    e2[x] = bit(b, x) + bit(d, x) - bit(a, x) - bit(c, x);
-    aw[x] = bit(c, x) + bit(d, x) - bit(a, x) - bit(b, x);
-  }
-  const int n0 = e1[1] * e2[2] - e1[2] * e2[1], n1 = e1[2] * e2[0] - e1[0] * e2[2], n2 = e1[0] * e2[1] - e1[1] * e2[0];
-  return n0 * aw[0] + n1 * aw[1] + n2 * aw[2] < 0;
-}
-
-void put_triangle(const float* p0, const float* p1, const float* p2, bool flip, std::vector<float>& out) {
-  const float* q1 = flip ? p2 : p1;
-  const float* q2 = flip ? p1 : p2;
-  for (int c = 0; c < 3; ++c) out.push_back(p0[c]);
-  for (int c = 0; c < 3; ++c) out.push_back(q1[c]);
-  for (int c = 0; c < 3; ++c) out.push_back(q2[c]);
-}
-
-void tet_triangles(const float f[8], unsigned inside, int t, int i, int j, int k, float iso, float vdx,
-                   std::vector<float>& out) {
-  int q[4], in[4], n_in = 0;
-  for (int r = 0; r < 4; ++r) {
-    q[r] = kTets[t][r];
-    in[r] = (inside >> q[r]) & 1;
-    n_in += in[r];
-  }
-  if (n_in == 0 || n_in == 4) return;
-  if (n_in == 1 || n_in == 3) {
-    int lone = 0;
-    for (int r = 0; r < 4; ++r)
-      if (in[r] == (n_in == 1)) lone = r;
-    int o[3], m = 0;
-    for (int r = 0; r < 4; ++r)
-      if (r != lone) o[m++] = q[r];
-    float p[3][3];
-    for (int e = 0; e < 3; ++e) {
-      if (n_in == 1) edge_point(f, q[lone], o[e], i, j, k, iso, vdx, p[e]);
-      else edge_point(f, o[e], q[lone], i, j, k, iso, vdx, p[e]);
+// The triangles (edge-slot triples) of a cube whose inside corners are the set bits of m.
+std::vector<int> cube_triangles(unsigned m) {
+  int next[12];
+  for (int e = 0; e < 12; ++e) next[e] = -1;
+  for (int f = 0; f < 6; ++f) {
+    const int* q = kFace[f];
+    bool in[4];
+    int ntrans = 0;
+    for (int r = 0; r < 4; ++r) in[r] = (m >> q[r]) & 1;
+    for (int r = 0; r < 4; ++r) ntrans += in[r] != in[(r + 1) % 4];
+    for (int r = 0; r < 4; ++r) {
+      // corner r inside: the edge into it from r - 1 and the edge out of it to r + 1
+      const int rp = (r + 3) % 4, rn = (r + 1) % 4;
+      if (ntrans == 4) {
+        if (in[r]) next[edge_of(q[rp], q[r])] = edge_of(q[r], q[rn]);
+      } else if (ntrans == 2) {
+        if (!in[r] && in[rn]) {
+          // enters the inside on edge (r, r + 1); leaves it on the first edge after
+          int s = rn;
+          while (in[(s + 1) % 4]) s = (s + 1) % 4;
+          next[edge_of(q[r], q[rn])] = edge_of(q[s], q[(s + 1) % 4]);
+        }
+      }
     }
-    const int det = det3(q[lone], o[0], o[1], o[2]);
-    put_triangle(p[0], p[1], p[2], n_in == 1 ? det < 0 : det > 0, out);
-    return;
   }
-  int a = -1, b = -1, c = -1, d = -1;
-  for (int r = 0; r < 4; ++r) {
-    if (in[r]) (a < 0 ? a : b) = q[r];
-    else (c < 0 ? c : d) = q[r];
+  std::vector<int> tris;
+  bool seen[12] = {};
+  for (int e0 = 0; e0 < 12; ++e0) {
+    if (next[e0] < 0 || seen[e0]) continue;
+    std::vector<int> loop;
+    for (int e = e0; !seen[e]; e = next[e]) {
+      seen[e] = true;
+      loop.push_back(e);
+    }
+    for (size_t r = 1; r + 1 < loop.size(); ++r) {
+      tris.push_back(loop[0]);
+      tris.push_back(loop[r]);
+      tris.push_back(loop[r + 1]);
+    }
   }
-  float ac[3], ad[3], bd[3], bc[3];
-  edge_point(f, a, c, i, j, k, iso, vdx, ac);
-  edge_point(f, a, d, i, j, k, iso, vdx, ad);
-  edge_point(f, b, d, i, j, k, iso, vdx, bd);
-  edge_point(f, b, c, i, j, k, iso, vdx, bc);
-  const bool flip = quad_flip(a, b, c, d);
-  put_triangle(ac, ad, bd, flip, out);
-  put_triangle(ac, bd, bc, flip, out);
+  return tris;
 }
 
 }  // namespace
@@ -145,31 +123,69 @@ void oracle_distance_field(const float* x, int64_t n, int32_t G, int32_t radius,
   }
 }
 
-/* Triangles of the level set radius voxel_dx - field = 0, 9 floats each, in cell order
- * (cell (i, j, k) at index (i (G-1) + j) (G-1) + k, then tetrahedra 0..5).  Writes up to
- * `capacity` triangles and returns the count. */
-int64_t oracle_surface_mesh(const float* field, int32_t G, int32_t radius, double voxel_dx, float* tris,
-                            int64_t capacity) {
-  if (G < 2) return 0;
-  // corner inside  <=>  S = radius voxel_dx - field > 0 in double  <=>  field < thr
-  const double iso = (double)(uint32_t)radius * voxel_dx;
-  const float iso_f = (float)iso;
-  const float vdx = (float)voxel_dx;
-  std::vector<float> out;
-  for (int i = 0; i + 1 < G; ++i)
-    for (int j = 0; j + 1 < G; ++j)
-      for (int k = 0; k + 1 < G; ++k) {
-        float f[8];
-        unsigned inside = 0;
-        for (int q = 0; q < 8; ++q) {
-          f[q] = field[((int64_t)(i + (q >> 2)) * G + j + ((q >> 1) & 1)) * G + k + (q & 1)];
-          inside |= (unsigned)((double)f[q] < iso) << q;
+/* Marching cubes of S = radius voxel_dx - field: vertices (nv x 3 doubles, world units)
+ * and faces (nf x 3 vertex indices), copied up to the capacities; *nv and *nf receive
+ * the counts. */
+void oracle_surface_indexed(const float* field, int32_t G, int32_t radius, double voxel_dx, double* V, int64_t vcap,
+                            int32_t* F, int64_t fcap, int64_t* nv, int64_t* nf) {
+  std::vector<double> verts;
+  std::vector<int32_t> faces;
+  if (G >= 2) {
+    const double iso = (double)(uint32_t)radius * voxel_dx;
+    const int64_t GG = (int64_t)G * G;
+    std::unordered_map<uint64_t, int32_t> edge_vertex;
+    std::vector<std::vector<int>> table(256);
+    for (unsigned m = 0; m < 256; ++m) table[m] = cube_triangles(m);
+    for (int i = 0; i + 1 < G; ++i)
+      for (int j = 0; j + 1 < G; ++j)
+        for (int k = 0; k + 1 < G; ++k) {
+          int64_t node[8];
+          double S[8];
+          unsigned m = 0;
+          for (int n = 0; n < 8; ++n) {
+            node[n] = (i + kCorner[n][0]) * GG + (int64_t)(j + kCorner[n][1]) * G + k + kCorner[n][2];
+            S[n] = iso - (double)field[node[n]];
+            m |= (unsigned)(S[n] > 0.0) << n;
+          }
+          if (m == 0 || m == 255) continue;
+          int32_t id[12];
+          for (int e = 0; e < 12; ++e) {
+            const int a = kEdge[e][0], b = kEdge[e][1];
+            if (((m >> a) & 1) == ((m >> b) & 1)) continue;
+            const uint64_t key = (uint64_t)node[a] * (uint64_t)(GG * G) + (uint64_t)node[b];
+            auto it = edge_vertex.find(key);
+            if (it != edge_vertex.end()) {
+              id[e] = it->second;
+              continue;
+            }
+            const double s0 = std::fabs(S[a]), s1 = std::fabs(S[b]);
+            const double t = s0 / (s0 + s1);
+            const int p0[3] = {i + kCorner[a][0], j + kCorner[a][1], k + kCorner[a][2]};
+            const int p1[3] = {i + kCorner[b][0], j + kCorner[b][1], k + kCorner[b][2]};
+            id[e] = (int32_t)(verts.size() / 3);
+            for (int c = 0; c < 3; ++c) {
+              const double v = (1.0 - t) * (double)p0[c] + t * (double)p1[c];
+              verts.push_back(v * voxel_dx);
+            }
+            edge_vertex.emplace(key, id[e]);
+          }
+          for (int e : table[m]) faces.push_back(id[e]);
         }
-        for (int t = 0; t < 6; ++t) tet_triangles(f, inside, t, i, j, k, iso_f, vdx, out);
-      }
-  const int64_t n = (int64_t)(out.size() / 9);
-  std::copy(out.begin(), out.begin() + 9 * std::min(n, capacity), tris);
-  return n;
+  }
+  *nv = (int64_t)(verts.size() / 3);
+  *nf = (int64_t)(faces.size() / 3);
+  std::copy(verts.begin(), verts.begin() + 3 * std::min(*nv, vcap), V);
+  std::copy(faces.begin(), faces.begin() + 3 * std::min(*nf, fcap), F);
+}
+
+/* The triangle table of the faces above: for each inside-corner mask m, n[m] triangles
+ * as edge-slot triples in slots[m] (up to 10 triangles).  For tests of the GPU table. */
+void oracle_surface_table(int32_t* n, int32_t* slots) {
+  for (unsigned m = 0; m < 256; ++m) {
+    const std::vector<int> t = cube_triangles(m);
+    n[m] = (int32_t)(t.size() / 3);
+    for (int r = 0; r < 30; ++r) slots[30 * m + r] = r < (int)t.size() ? t[r] : -1;
+  }
 }
 
 }  // extern "C"

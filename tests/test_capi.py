@@ -133,3 +133,20 @@ def test_cpp_facade_compiles_and_links(tmp_path):
                         "-Wl,-rpath," + os.path.dirname(lib)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert subprocess.run([str(exe)]).returncode == 0
+
+
+def test_library_triangle_table_matches_oracle(oracle_lib):
+    """The GPU mesher's compile-time triangle table (mpm_surface_table, no GPU needed) is
+    the oracle's."""
+    import ctypes
+
+    import numpy as np
+
+    from mpm_gb300 import _lib
+
+    counts = np.empty(256, np.int32)
+    slots = np.empty(256 * 30, np.int32)
+    L = _lib.lib()
+    assert L.mpm_surface_table(counts.ctypes.data_as(ctypes.c_void_p), slots.ctypes.data_as(ctypes.c_void_p)) == 0
+    n, t = oracle_lib.surface_table()
+    assert np.array_equal(counts, n) and np.array_equal(slots.reshape(256, 30), t)

@@ -6,9 +6,64 @@ properties of a closed, outward-oriented surface."""
 import numpy as np
 import pytest
 
-from surface_checks import edge_balance, enclosed_volume, golden_mesh_cases, matches_golden, weld
+from surface_checks import (ambiguous_mask, cube_loop_mismatches, cube_masks, edge_balance, enclosed_volume,
+                            golden_mesh_cases, golden_meshes, matches_golden, vertices_match, weld)
 
 MESH_CASES = golden_mesh_cases()
+MESHES = golden_meshes()
+
+
+@pytest.mark.parametrize("case", MESHES, ids=[c[0] for c in MESHES])
+def test_mesh_vertices_match_reference_golden(oracle_lib, case):
+    """The vertex list of MeshBuilder::computeMesh (libigl's marching cubes on
+    S = radius voxel_dx - field, scaled by voxel_dx; include/mesh_builder.h:165-211), bit for
+    bit and in the same order, and the same face count."""
+    name, x, N, G, r, V, F, sha, nv, nf = case
+    vdx = oracle_lib.voxel_dx(N, float(np.float32(1.0 / N)), G)
+    Vo, Fo = oracle_lib.surface_indexed(oracle_lib.distance_field(x, G, r, vdx), r, vdx)
+    assert vertices_match(Vo, V, sha, nv)
+    assert len(Fo) == nf
+
+
+@pytest.mark.parametrize("case", [c for c in MESHES if c[6] is not None], ids=[c[0] for c in MESHES if c[6] is not None])
+def test_mesh_faces_bound_the_reference_loops(oracle_lib, case):
+    """Per cube, the oracle's faces and libigl's bound the same directed loops of edge
+    vertices (same segments on every cube face, same orientation), ambiguous faces
+    included; only the triangulation inside a loop may differ."""
+    name, x, N, G, r, V, F, sha, nv, nf = case
+    vdx = oracle_lib.voxel_dx(N, float(np.float32(1.0 / N)), G)
+    field = oracle_lib.distance_field(x, G, r, vdx)
+    _, Fo = oracle_lib.surface_indexed(field, r, vdx)
+    counts, _ = oracle_lib.surface_table()
+    masks = cube_masks(field, r, vdx)
+    bad, cubes = cube_loop_mismatches(Fo, F, masks, counts)
+    assert cubes > 0 and bad == 0
+    if name.startswith("cloud"):
+        assert sum(ambiguous_mask(int(m)) for m in masks if counts[m]) > 10
+
+
+def test_loop_check_detects_a_reversed_face(oracle_lib):
+    name, x, N, G, r, V, F, sha, nv, nf = next(c for c in MESHES if c[6] is not None)
+    vdx = oracle_lib.voxel_dx(N, float(np.float32(1.0 / N)), G)
+    field = oracle_lib.distance_field(x, G, r, vdx)
+    _, Fo = oracle_lib.surface_indexed(field, r, vdx)
+    counts, _ = oracle_lib.surface_table()
+    Fo = Fo.copy()
+    Fo[len(Fo) // 2] = Fo[len(Fo) // 2][::-1]
+    bad, _ = cube_loop_mismatches(Fo, F, cube_masks(field, r, vdx), counts)
+    assert bad == 1
+
+
+def test_oracle_table_is_closed_and_oriented(oracle_lib):
+    """Each mask's triangles close around the crossed edges: every crossed edge slot is
+    used, and the triangles' boundary is a set of loops."""
+    counts, slots = oracle_lib.surface_table()
+    edges = ((0, 1), (1, 2), (3, 2), (0, 3), (4, 5), (5, 6), (7, 6), (4, 7), (0, 4), (1, 5), (2, 6), (3, 7))
+    for m in range(256):
+        crossed = {e for e, (a, b) in enumerate(edges) if ((m >> a) ^ (m >> b)) & 1}
+        T = slots[m][: 3 * counts[m]].reshape(-1, 3)
+        assert set(T.ravel().tolist()) == crossed
+        assert counts[m] <= 5
 
 
 @pytest.mark.parametrize("case", MESH_CASES, ids=[c[0] for c in MESH_CASES])
