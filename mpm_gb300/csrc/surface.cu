@@ -460,13 +460,19 @@ __global__ void __launch_bounds__(kSurfThreads) mc_count_kernel(const float* __r
   int i, j, k;
   unsigned m = 0;
   int nt = 0, nv = 0;
-  if (block_cell(G, i, j, k)) {
-    m = corner_mask(field, G, i, j, k, thr);
-    nt = __ldg(&kMc.count[m]);
-    nv = __popc(__ldg(&kMc.crossed[m]) & owned_mask(i, j, k));
+  if (block_cell(G, i, j, k)) m = corner_mask(field, G, i, j, k, thr);
+  // almost every cube lies wholly inside or outside: a warp without a surface cube skips
+  // the table and the scans
+  const unsigned surf = __ballot_sync(kFull, m != 0u && m != 0xffu);
+  int tinc = 0, vinc = 0;
+  if (surf) {
+    if (m != 0u && m != 0xffu) {
+      nt = __ldg(&kMc.count[m]);
+      nv = __popc(__ldg(&kMc.crossed[m]) & owned_mask(i, j, k));
+    }
+    tinc = warp_inclusive(nt, lane);
+    vinc = warp_inclusive(nv, lane);
   }
-  const unsigned surf = __ballot_sync(kFull, nt > 0);
-  const int tinc = warp_inclusive(nt, lane), vinc = warp_inclusive(nv, lane);
   if (lane == 31) {
     warp_tris[warp] = tinc;
     warp_verts[warp] = vinc;
