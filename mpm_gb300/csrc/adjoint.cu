@@ -576,8 +576,6 @@ mpm_status mpm_diff_forward(mpm_diff* d, const float* x0, const float* v0, const
   if (st != MPM_OK) return st;
   cur = 1;
   for (int32_t i = 0; i < nsteps; ++i) {
-    StepArgs dummy{};
-    (void)dummy;
     // fused: G2P of substep i from g[cur], P2G of i+1 into g[cur+1], clear g[cur+2]
     StepArgs a{};
     a.s = work;

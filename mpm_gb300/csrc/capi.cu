@@ -464,7 +464,6 @@ mpm_status mpm_create(const mpm_params* params, mpm_ctx** out) {
   mpm_ctx* c = new mpm_ctx();
   c->params = *params;
   derive_consts(c);
-  mpm_status st = MPM_OK;
   auto bail = [&](mpm_status s) {
     mpm_destroy(c);
     return s;
@@ -491,11 +490,10 @@ mpm_status mpm_create(const mpm_params* params, mpm_ctx** out) {
   if (cudaMalloc(&c->block_sums, sizeof(int) * std::max<int64_t>(nb, 1)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
   if (cudaMalloc(&c->status, sizeof(int)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
   if (cudaMalloc(&c->work, 4 * sizeof(int)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
-  if (cudaMemsetAsync(c->work, 0, 2 * sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
+  if (cudaMemsetAsync(c->work, 0, 4 * sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
 
   if (cudaMemsetAsync(c->status, 0, sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
-  (void)st;
   *out = c;
   return MPM_OK;
 }
