@@ -345,6 +345,8 @@ def test_argument_validation(gpu_lib, tmp_path):
     assert L.mpm_substep(None, 1) == INVALID
     assert L.mpm_sync(None) == INVALID
     assert L.mpm_surface_mesh(None, 16, 2, None, 0, None) == INVALID
+    assert L.mpm_surface_mesh_indexed(None, 16, 2, None, 0, None, 0, None, None) == INVALID
+    assert L.mpm_surface_table(None, None) == INVALID
     assert L.mpm_export_particles(None, 0, 0.1, None) == INVALID
     assert L.mpm_render_positions(None, None) == INVALID
     with Simulation(N=16) as sim:
@@ -362,8 +364,15 @@ def test_argument_validation(gpu_lib, tmp_path):
         rec, cnt = ctypes.c_void_p(), ctypes.c_int64()
         assert L.mpm_export_wait(sim.ctx, 1, ctypes.byref(rec), ctypes.byref(cnt)) == INVALID  # nothing exported
         tri = ctypes.c_int64()
+        nv = ctypes.c_int64()
         for G, r in ((1, 2), (513, 2), (16, -1), (16, 65)):
             assert L.mpm_surface_mesh(sim.ctx, G, r, None, 0, ctypes.byref(tri)) == INVALID, (G, r)
+            assert L.mpm_surface_mesh_indexed(sim.ctx, G, r, None, 0, None, 0, ctypes.byref(nv),
+                                              ctypes.byref(tri)) == INVALID, (G, r)
+        # a capacity without a buffer is refused; zero capacities only count
+        assert L.mpm_surface_mesh_indexed(sim.ctx, 16, 2, None, 4, None, 0, ctypes.byref(nv), ctypes.byref(tri)) == INVALID
+        assert L.mpm_surface_mesh_indexed(sim.ctx, 16, 2, None, 0, None, 0, ctypes.byref(nv), ctypes.byref(tri)) == 0
+        assert nv.value > 0 and tri.value > 0
         col = (ctypes.c_uint8 * 3)(1, 2, 3)
         img = np.empty(12, np.uint8)
         for w, h, ps in ((0, 10, 2.0), (10, 0, 2.0), (2, 2, 0.0), (2, 2, 100.0)):
