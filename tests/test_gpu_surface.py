@@ -90,10 +90,11 @@ def test_surface_triangles_match_oracle(gpu_lib, oracle_lib, G, radius):
     assert np.array_equal(tris.view(np.int32), ref.view(np.int32))
 
 
-@pytest.mark.parametrize("G,radius", [(48, 2), (33, 3), (300, 4), (2, 1)])
+@pytest.mark.parametrize("G,radius", [(48, 2), (33, 3), (300, 4), (512, 1), (2, 1)])
 def test_indexed_mesh_matches_oracle(gpu_lib, oracle_lib, G, radius):
-    """Vertices bit for bit and in order, faces index for index; G = 300 puts two blocks
-    of cubes on each row, so vertices are looked up across blocks."""
+    """Vertices bit for bit and in order, faces index for index; G = 300 and 512 put two
+    blocks of cubes on each row, so vertices are looked up across blocks, and 512 is the
+    largest grid (cube coordinates up to 510 in the packed 10-bit fields)."""
     N = 32
     x = np.concatenate([_ball(30000, (0.5, 0.45, 0.5), 0.22, 1), _ball(3000, (0.2, 0.8, 0.3), 0.08, 2),
                         np.random.default_rng(G).random((300, 3)).astype(np.float32)])
