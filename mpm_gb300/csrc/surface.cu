@@ -43,7 +43,8 @@ namespace mpm {
 
 namespace {
 
-constexpr int kSurfThreads = 256;
+constexpr int kSurfThreads = 128;
+constexpr int kRowCubes = 2 * kSurfThreads;  // cubes per block of the count sweep: two per thread
 constexpr int kDistThreads = 512;  // distance scatter: 16 warps share a chunk's tile
 constexpr int kDistChunk = 128;     // particles per CTA and chunk
 constexpr unsigned kInfBits = 0x7f800000u;
@@ -379,24 +380,6 @@ __device__ const mc::Table kMc = mc::make_table();
 
 constexpr int kEmitThreads = 128;
 
-// Bit n of the mask: corner n of cube (i, j, k) (libigl's numbering) is inside, i.e. its
-// value is below thr (the field against the float threshold of S > 0, or the raw squared
-// distance against the squared threshold).  Indices fit in int (G <= 512).
-__device__ __forceinline__ unsigned corner_mask(const float* field, int G, int i, int j, int k, float thr) {
-  const float* f = field + (i * G + j) * G + k;
-  const int sj = G, si = G * G;
-  unsigned m = 0;
-  m |= (unsigned)(f[0] < thr) << 0;
-  m |= (unsigned)(f[1] < thr) << 1;
-  m |= (unsigned)(f[sj + 1] < thr) << 2;
-  m |= (unsigned)(f[sj] < thr) << 3;
-  m |= (unsigned)(f[si] < thr) << 4;
-  m |= (unsigned)(f[si + 1] < thr) << 5;
-  m |= (unsigned)(f[si + sj + 1] < thr) << 6;
-  m |= (unsigned)(f[si + sj] < thr) << 7;
-  return m;
-}
-
 // Compile-time facts of edge slot E: its corners, axis and lower-corner offsets.
 template <int E>
 struct Edge {
@@ -426,15 +409,8 @@ __device__ __forceinline__ unsigned owned_mask(int i, int j, int k) {
   return owned_mask_impl(zero, std::make_integer_sequence<int, 12>{});
 }
 
-// Cubes are swept one (i, j) row at a time: grid (row segments of kSurfThreads cubes, j, i),
-// so the linear block index runs in cube order.  False for the padding past a row's end.
-__device__ __forceinline__ bool block_cell(int G, int& i, int& j, int& k) {
-  i = (int)blockIdx.z;
-  j = (int)blockIdx.y;
-  k = (int)blockIdx.x * kSurfThreads + (int)threadIdx.x;
-  return k < G - 1;
-}
-
+// Cubes are swept one (i, j) row at a time: grid (row segments of kRowCubes cubes, j, i), so
+// the linear block index runs in cube order (for G <= 513 a block holds a whole row).
 __device__ __forceinline__ int64_t block_linear() {
   return ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
 }
@@ -448,35 +424,63 @@ __device__ __forceinline__ int warp_inclusive(int v, int lane) {
   return v;
 }
 
-// The one sweep over the cubes.  counts holds three runs of nblocks + 1 ints (triangles,
-// new vertices, surface cubes per block, each run ending in a zero); the block's slots
-// (kSurfThreads of them) list its surface cubes in cube order with their first triangle
-// and first vertex inside the block and their inside-corner mask.
+// libigl's corner mask of a cube from its corners' inside bits on the four node rows
+// (i, j), (i, j + 1), (i + 1, j), (i + 1, j + 1), at the cube's k (lo) and k + 1 (hi).
+__device__ __forceinline__ unsigned mask_of(bool a00lo, bool a00hi, bool a01lo, bool a01hi, bool a10lo, bool a10hi,
+                                            bool a11lo, bool a11hi) {
+  return (unsigned)a00lo | (unsigned)a00hi << 1 | (unsigned)a01hi << 2 | (unsigned)a01lo << 3 | (unsigned)a10lo << 4 |
+         (unsigned)a10hi << 5 | (unsigned)a11hi << 6 | (unsigned)a11lo << 7;
+}
+
+// The one sweep over the cubes, two neighbouring cubes (k, k + 1) per thread, which share
+// the four corners at k + 1.  counts holds three runs of nblocks + 1 ints (triangles, new
+// vertices, surface cubes per block, each run ending in a zero); the block's slots
+// (kRowCubes of them) list its surface cubes in cube order with their first triangle and
+// first vertex inside the block and their inside-corner mask.
 __global__ void __launch_bounds__(kSurfThreads) mc_count_kernel(const float* __restrict__ field, int G, float thr,
                                                                 int* __restrict__ counts, int64_t nblocks,
                                                                 int4* __restrict__ slots) {
   __shared__ int warp_tris[kSurfThreads / 32], warp_verts[kSurfThreads / 32], warp_cells[kSurfThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int i, j, k;
-  unsigned m = 0;
-  int nt = 0, nv = 0;
-  if (block_cell(G, i, j, k)) m = corner_mask(field, G, i, j, k, thr);
+  const int i = (int)blockIdx.z, j = (int)blockIdx.y;
+  const int k = 2 * ((int)blockIdx.x * kSurfThreads + (int)threadIdx.x);
+  const bool v0 = k < G - 1, v1 = k + 1 < G - 1;
+  unsigned m0 = 0, m1 = 0;
+  if (v0) {
+    const float* f = field + (i * G + j) * G + k;
+    const int sj = G, si = G * G;
+    // k + 2 <= G - 1 whenever the second cube exists
+    const bool a00 = f[0] < thr, a00h = f[1] < thr, a01 = f[sj] < thr, a01h = f[sj + 1] < thr;
+    const bool a10 = f[si] < thr, a10h = f[si + 1] < thr, a11 = f[si + sj] < thr, a11h = f[si + sj + 1] < thr;
+    m0 = mask_of(a00, a00h, a01, a01h, a10, a10h, a11, a11h);
+    if (v1) {
+      const bool b00 = f[2] < thr, b01 = f[sj + 2] < thr, b10 = f[si + 2] < thr, b11 = f[si + sj + 2] < thr;
+      m1 = mask_of(a00h, b00, a01h, b01, a10h, b10, a11h, b11);
+    }
+  }
+  const bool s0 = m0 != 0u && m0 != 0xffu, s1 = m1 != 0u && m1 != 0xffu;
   // almost every cube lies wholly inside or outside: a warp without a surface cube skips
   // the table and the scans
-  const unsigned surf = __ballot_sync(kFull, m != 0u && m != 0xffu);
-  int tinc = 0, vinc = 0;
-  if (surf) {
-    if (m != 0u && m != 0xffu) {
-      nt = __ldg(&kMc.count[m]);
-      nv = __popc(__ldg(&kMc.crossed[m]) & owned_mask(i, j, k));
+  const bool any = __ballot_sync(kFull, s0 || s1) != 0u;
+  int nt0 = 0, nt1 = 0, nv0 = 0, nv1 = 0;
+  int tinc = 0, vinc = 0, cinc = 0;
+  if (any) {
+    if (s0) {
+      nt0 = __ldg(&kMc.count[m0]);
+      nv0 = __popc(__ldg(&kMc.crossed[m0]) & owned_mask(i, j, k));
     }
-    tinc = warp_inclusive(nt, lane);
-    vinc = warp_inclusive(nv, lane);
+    if (s1) {
+      nt1 = __ldg(&kMc.count[m1]);
+      nv1 = __popc(__ldg(&kMc.crossed[m1]) & owned_mask(i, j, k + 1));
+    }
+    tinc = warp_inclusive(nt0 + nt1, lane);
+    vinc = warp_inclusive(nv0 + nv1, lane);
+    cinc = warp_inclusive((int)s0 + (int)s1, lane);
   }
   if (lane == 31) {
     warp_tris[warp] = tinc;
     warp_verts[warp] = vinc;
-    warp_cells[warp] = __popc(surf);
+    warp_cells[warp] = cinc;
   }
   __syncthreads();
   const int64_t b = block_linear();
@@ -492,15 +496,18 @@ __global__ void __launch_bounds__(kSurfThreads) mc_count_kernel(const float* __r
     counts[2 * (nblocks + 1) + b] = c;
     if (b == 0) counts[nblocks] = counts[2 * nblocks + 1] = counts[3 * nblocks + 2] = 0;
   }
-  if (nt == 0) return;
+  if (!s0 && !s1) return;
   int tpre = 0, vpre = 0, cpre = 0;
   for (int w = 0; w < warp; ++w) {
     tpre += warp_tris[w];
     vpre += warp_verts[w];
     cpre += warp_cells[w];
   }
-  const int rank = cpre + __popc(surf & ((1u << lane) - 1u));
-  slots[b * kSurfThreads + rank] = make_int4((i << 20) | (j << 10) | k, tpre + tinc - nt, vpre + vinc - nv, (int)m);
+  int rank = cpre + cinc - (int)s0 - (int)s1;
+  const int t0 = tpre + tinc - nt0 - nt1, vv0 = vpre + vinc - nv0 - nv1;
+  int4* out = slots + b * kRowCubes;
+  if (s0) out[rank++] = make_int4((i << 20) | (j << 10) | k, t0, vv0, (int)m0);
+  if (s1) out[rank] = make_int4((i << 20) | (j << 10) | (k + 1), t0 + nt0, vv0 + nv0, (int)m1);
 }
 
 // The three totals of the scanned counts into pinned host memory.
@@ -550,17 +557,17 @@ __device__ __forceinline__ int owner_vertex(const EmitArgs& a, int i, int j, int
   const int s0 = (D::need_zero & 1) && i > 0, s1 = (D::need_zero & 2) && j > 0, s2 = (D::need_zero & 4) && k > 0;
   const int ci = i - s0, cj = j - s1, ck = k - s2;
   const int e2 = (int)((D::owner_slots >> (4 * (s0 * 4 + s1 * 2 + s2))) & 15u);
-  const int64_t b = ((int64_t)ci * (a.G - 1) + cj) * a.gx + ck / kSurfThreads;
+  const int64_t b = ((int64_t)ci * (a.G - 1) + cj) * a.gx + ck / kRowCubes;
   const int* cell_off = a.scan + 2 * (a.nblocks + 1);
   const int cnt = cell_off[b + 1] - cell_off[b];
   const int key = (ci << 20) | (cj << 10) | ck;
-  const int* keys = reinterpret_cast<const int*>(a.slots + b * kSurfThreads);
+  const int* keys = reinterpret_cast<const int*>(a.slots + b * kRowCubes);
   int lo = 0, hi = cnt - 1;
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
     if (keys[4 * mid] < key) lo = mid + 1; else hi = mid;
   }
-  const int4 o = a.slots[b * kSurfThreads + lo];
+  const int4 o = a.slots[b * kRowCubes + lo];
   const int* vert_off = a.scan + (a.nblocks + 1);
   const unsigned mine = __ldg(&kMc.crossed[o.w & 255]) & owned_mask(ci, cj, ck) & ((1u << e2) - 1u);
   return vert_off[b] - vert_off[0] + o.z + __popc(mine);
@@ -620,7 +627,7 @@ __global__ void __launch_bounds__(kEmitThreads) mc_emit_kernel(const EmitArgs a)
     const int64_t mid = (lo + hi + 1) >> 1;
     if (cell_off[mid] - c0 <= c) lo = mid; else hi = mid - 1;
   }
-  const int4 e = a.slots[lo * kSurfThreads + (c - (cell_off[lo] - c0))];
+  const int4 e = a.slots[lo * kRowCubes + (c - (cell_off[lo] - c0))];
   const int i = e.x >> 20, j = (e.x >> 10) & 1023, k = e.x & 1023;
   const int tbase = tri_off[lo] + e.y;
   const int vbase = vert_off[lo] - vert_off[0] + e.z;
@@ -777,13 +784,13 @@ cudaError_t extract_surface(int G, int radius, double voxel_dx, SurfaceBuffers& 
   const SurfaceConsts K = surface_consts(radius, voxel_dx);
   const float thr = buf.raw ? sq_threshold(K.thr) : K.thr;
   const int Gm = G - 1;
-  const dim3 grid((unsigned)((Gm + kSurfThreads - 1) / kSurfThreads), (unsigned)Gm, (unsigned)Gm);
+  const dim3 grid((unsigned)((Gm + kRowCubes - 1) / kRowCubes), (unsigned)Gm, (unsigned)Gm);
   const int64_t nblocks = (int64_t)grid.x * grid.y * grid.z;
   // counts: per-block triangles, new vertices and surface cubes, nblocks + 1 each
   cudaError_t e = reserve(&buf.counts, &buf.counts_cap, 3 * (nblocks + 1));
   if (e == cudaSuccess) e = reserve(&buf.scan, &buf.scan_cap, scan_scratch_ints(3 * (nblocks + 1)));
   if (e == cudaSuccess && !buf.total) e = cudaMallocHost(&buf.total, 3 * sizeof(int));
-  if (e == cudaSuccess) e = reserve(&buf.cells, &buf.cells_cap, nblocks * kSurfThreads);
+  if (e == cudaSuccess) e = reserve(&buf.cells, &buf.cells_cap, nblocks * kRowCubes);
   if (e != cudaSuccess) return e;
   mc_count_kernel<<<grid, kSurfThreads, 0, st>>>(buf.field, G, thr, buf.counts, nblocks, buf.cells);
   e = cudaGetLastError();
