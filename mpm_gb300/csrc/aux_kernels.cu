@@ -11,16 +11,21 @@ namespace mpm {
 // histogram (warp-aggregated atomics) -> exclusive scan -> scatter.  Order inside
 // a cell is not stable; the substep does not depend on it.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t cell_key(const float* s, int64_t st, int64_t p, float dx_inv, int N) {
+__device__ __forceinline__ uint32_t cell_key_of(const float x[3], float dx_inv, int N) {
   int b[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    int v = QuadraticInterpolationKernel::base_cell(s[(kX + d) * st + p], dx_inv);
+    int v = QuadraticInterpolationKernel::base_cell(x[d], dx_inv);
     b[d] = min(max(v, 0), N - 1);
   }
   const uint32_t nb = (uint32_t)(N + 3) >> 2;
   const uint32_t brick = ((uint32_t)(b[0] >> 2) * nb + (uint32_t)(b[1] >> 2)) * nb + (uint32_t)(b[2] >> 2);
   return brick * 64u + (uint32_t)(((b[0] & 3) << 4) | ((b[1] & 3) << 2) | (b[2] & 3));
+}
+
+__device__ __forceinline__ uint32_t cell_key(const float* s, int64_t st, int64_t p, float dx_inv, int N) {
+  const float x[3] = {s[(kX + 0) * st + p], s[(kX + 1) * st + p], s[(kX + 2) * st + p]};
+  return cell_key_of(x, dx_inv, N);
 }
 
 // Scene of particle p in a batch (binary search over the scene offsets).
@@ -262,23 +267,52 @@ __global__ void __launch_bounds__(kScanThreads) scan_small(int* counts, int64_t 
   }
 }
 
+// Exclusive scan of the cell counts; returns the number of launches.
+int scan_cell_counts(const SortArgs& a, cudaStream_t st) {
+  if (a.cells <= kSmallScan && a.cells % 4 == 0) {
+    scan_small<<<1, kScanThreads, 0, st>>>(a.counts, a.cells);
+    return 1;
+  }
+  const int per = kThreads * kScanItems;
+  const int nb = (int)((a.cells + per - 1) / per);
+  scan_blocks<<<nb, kThreads, 0, st>>>(a.counts, a.cells, a.block_sums);
+  scan_block_sums<<<1, kThreads, 0, st>>>(a.block_sums, nb);
+  scan_add<<<nb, kThreads, 0, st>>>(a.counts, a.cells, a.block_sums);
+  return 3;
+}
+
+// Cell keys and their histogram of positions given as x, y, z per particle (host-visible
+// or device memory), with a copy of the positions to xcopy (when not null) and *bad = 1
+// for a position that is not finite.
+__global__ void presort_keys_kernel(const float* __restrict__ x, float* __restrict__ xcopy, SortArgs a, int* bad) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < a.n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = base + threadIdx.x;
+    const bool valid = p < a.n;
+    uint32_t key = 0xffffffffu;
+    if (valid) {
+      const float xp[3] = {x[3 * p], x[3 * p + 1], x[3 * p + 2]};
+      if (!isfinite(xp[0]) || !isfinite(xp[1]) || !isfinite(xp[2])) *bad = 1;
+      if (xcopy) {
+        xcopy[3 * p] = xp[0];
+        xcopy[3 * p + 1] = xp[1];
+        xcopy[3 * p + 2] = xp[2];
+      }
+      key = cell_key_of(xp, a.dx_inv, a.N);
+      a.keys[p] = key;
+    }
+    const unsigned same = __match_any_sync(kFull, key);
+    if (valid && lane == __ffs(same) - 1) atomicAdd(a.counts + key, __popc(same));
+  }
+}
+
 cudaError_t launch_sort(const SortArgs& a, int num_sms, cudaStream_t st, int64_t* launches) {
   if (a.n == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(a.counts, 0, sizeof(int) * a.cells, st);
   if (e != cudaSuccess) return e;
   int blocks = (int)std::min<int64_t>((a.n + kThreads - 1) / kThreads, (int64_t)num_sms * 8);
   sort_histogram<<<blocks, kThreads, 0, st>>>(a);
-  int n_launch = 3;
-  if (a.cells <= kSmallScan && a.cells % 4 == 0) {
-    scan_small<<<1, kScanThreads, 0, st>>>(a.counts, a.cells);
-  } else {
-    const int per = kThreads * kScanItems;
-    const int nb = (int)((a.cells + per - 1) / per);
-    scan_blocks<<<nb, kThreads, 0, st>>>(a.counts, a.cells, a.block_sums);
-    scan_block_sums<<<1, kThreads, 0, st>>>(a.block_sums, nb);
-    scan_add<<<nb, kThreads, 0, st>>>(a.counts, a.cells, a.block_sums);
-    n_launch = 5;
-  }
+  int n_launch = 2 + scan_cell_counts(a, st);
   if (a.perm) {
     sort_rank<<<blocks, kThreads, 0, st>>>(a);
     if (a.ncomp == kLiquidComps)
@@ -408,12 +442,15 @@ constexpr int kRowsPerBlock = 256;
 // particle arrays; *bad = 1 when a position is not finite.  One block per 256 particles,
 // each array moved through shared memory in contiguous 16-byte pieces.
 __global__ void __launch_bounds__(kRowsPerBlock) deinterleave_arrays_kernel(HostArrays a, float* __restrict__ s,
-                                                                            int64_t st, int64_t n, int* bad) {
+                                                                            int64_t st, int64_t n,
+                                                                            const uint32_t* __restrict__ dest, int* bad) {
   __shared__ __align__(16) float tile[9 * kRowsPerBlock];
   const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
   const int cnt = (int)(n - r0 < kRowsPerBlock ? n - r0 : kRowsPerBlock);
   const int t = threadIdx.x;
   const int64_t p = r0 + t;
+  // row p's device slot: its own, or its place in cell order (dest, from launch_presort)
+  const int64_t q = t < cnt ? (dest ? (int64_t)dest[p] : p) : 0;
   auto field = [&](const float* src, int W, int comp0, auto def) {
     if (src) {
       if (W == 1) load_rows<1>(src, r0, cnt, tile);
@@ -425,7 +462,7 @@ __global__ void __launch_bounds__(kRowsPerBlock) deinterleave_arrays_kernel(Host
       for (int d = 0; d < W; ++d) {
         const float v = src ? tile[W * t + d] : def(d);
         if (comp0 == kX && !isfinite(v)) *bad = 1;
-        s[(int64_t)(comp0 + d) * st + p] = v;
+        s[(int64_t)(comp0 + d) * st + q] = v;
       }
     __syncthreads();
   };
@@ -468,11 +505,12 @@ __global__ void __launch_bounds__(kRowsPerBlock) interleave_arrays_kernel(const 
 
 }  // namespace
 
-cudaError_t launch_deinterleave_arrays(HostArrays a, float* s, int64_t stride, int64_t n, int* bad, cudaStream_t st) {
+cudaError_t launch_deinterleave_arrays(HostArrays a, float* s, int64_t stride, int64_t n, int* bad, cudaStream_t st,
+                                       const uint32_t* dest) {
   cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), st);
   if (e != cudaSuccess || n == 0) return e;
-  deinterleave_arrays_kernel<<<(unsigned)((n + kRowsPerBlock - 1) / kRowsPerBlock), kRowsPerBlock, 0, st>>>(a, s, stride,
-                                                                                                        n, bad);
+  deinterleave_arrays_kernel<<<(unsigned)((n + kRowsPerBlock - 1) / kRowsPerBlock), kRowsPerBlock, 0, st>>>(
+      a, s, stride, n, dest, bad);
   return cudaGetLastError();
 }
 
@@ -487,6 +525,21 @@ cudaError_t launch_interleave_arrays(const float* s, int64_t stride, const uint3
 cudaError_t launch_inverse(const uint32_t* id, int64_t n, uint32_t* inv, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   inverse_kernel<<<grid_for(n), 256, 0, st>>>(id, n, inv);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_presort(const float* x, float* xcopy, const SortArgs& a, uint32_t* dest, int* bad, int num_sms,
+                           cudaStream_t st, int64_t* launches) {
+  if (a.n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.counts, 0, sizeof(int) * a.cells, st);
+  if (e != cudaSuccess) return e;
+  const int blocks = (int)std::min<int64_t>((a.n + kThreads - 1) / kThreads, (int64_t)num_sms * 8);
+  presort_keys_kernel<<<blocks, kThreads, 0, st>>>(x, xcopy, a, bad);
+  int n_launch = 3 + scan_cell_counts(a, st);
+  sort_rank<<<blocks, kThreads, 0, st>>>(a);
+  inverse_kernel<<<grid_for(a.n), 256, 0, st>>>(a.perm, a.n, dest);
+  if (launches) *launches += n_launch;
   return cudaGetLastError();
 }
 

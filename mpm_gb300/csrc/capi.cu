@@ -580,6 +580,13 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   // buffer with copies.  When the particle arrays keep their size, the conversion writes
   // the spare copy, which replaces the current one after the check.
   const bool grow = n > c->capacity || !c->sA;
+  // a per-particle material array keeps the upload order (its bytes are copied as given),
+  // so only uploads without one are put in cell order on the way in
+  bool mixed = !c->liquid_layout && c->n_materials > 1;
+  if (mat)
+    for (int64_t p = 0; p < n && !mixed; ++p) mixed = mat[p] != 0;
+  const bool presort = n > 0 && !grow && !mixed;
+  bool presorted = false;
   HostArrays arr{};
   bool direct = false;
   if (n > 0 && !grow) {
@@ -617,6 +624,38 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
       st = ensure_particles(c, n);
       if (st != MPM_OK) return st;
       MPM_CUDA(c, launch_deinterleave_arrays(arr, c->sA, c->stride, n, c->work + 2, c->stream));
+    } else if (presort) {
+      if (direct) MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // earlier work may read the stage
+      // Cell order from the positions first, then each particle goes straight to its slot:
+      // the sort the first substep would run (a gather of every array) is not needed.
+      // Host positions are copied to the stage on the way, so the host link carries them once.
+      float* xcopy = nullptr;
+      if (direct) {
+        st = ensure_stage(c, 3 * sizeof(float) * (size_t)n);
+        if (st != MPM_OK) return st;
+        xcopy = c->stage;
+      }
+      SortArgs so{};
+      so.n = n;
+      so.keys = c->keys;
+      so.perm = c->keys + c->capacity;
+      so.counts = c->counts;
+      so.block_sums = c->block_sums;
+      so.cells = c->sort_keys;
+      so.N = (int)c->params.N;
+      so.dx_inv = c->K.g.dx_inv;
+      MPM_CUDA(c, launch_presort(arr.x, xcopy, so, c->idB, c->work + 2, c->num_sms, c->stream, &c->launches));
+      MPM_CUDA(c, cudaMemcpyAsync(&bad, c->work + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (bad) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
+      HostArrays sorted_arr = arr;
+      if (xcopy) sorted_arr.x = xcopy;
+      MPM_CUDA(c, launch_deinterleave_arrays(sorted_arr, c->sB, c->stride, n, c->work + 2, c->stream, c->idB));
+      // slot q holds particle perm[q]: that is the id array
+      MPM_CUDA(c, cudaMemcpyAsync(c->idA, so.perm, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
+      MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // the caller may reuse the host arrays on return
+      std::swap(c->sA, c->sB);
+      presorted = true;
     } else {
       if (direct) MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // earlier work may read the spare copy
       MPM_CUDA(c, launch_deinterleave_arrays(arr, c->sB, c->stride, n, c->work + 2, c->stream));
@@ -635,13 +674,15 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   c->pending = false;
   c->prev = -1;
   c->substeps = 0;
-  c->since_sort = c->params.sort_interval;  // sort before the first substep
-  c->unsorted = true;
+  c->since_sort = presorted ? 0 : c->params.sort_interval;  // otherwise sort before the first substep
+  c->unsorted = !presorted;
   c->t = 0.0;
   free_objects(c);
   if (n == 0) return MPM_OK;
-  MPM_CUDA(c, launch_iota(c->idA, n, c->stream));
-  c->launches += 1;
+  if (!presorted) {
+    MPM_CUDA(c, launch_iota(c->idA, n, c->stream));
+    c->launches += 1;
+  }
   c->have_mat = !c->liquid_layout && c->n_materials > 1;
   if (c->have_mat) {
     if (mat) {

@@ -139,7 +139,15 @@ struct OutArrays {
 };
 // Arrays -> component-major particle arrays in one pass (missing fields take their rest
 // values); *bad = 1 when a position is not finite.
-cudaError_t launch_deinterleave_arrays(HostArrays a, float* s, int64_t stride, int64_t n, int* bad, cudaStream_t st);
+cudaError_t launch_deinterleave_arrays(HostArrays a, float* s, int64_t stride, int64_t n, int* bad, cudaStream_t st,
+                                       const uint32_t* dest = nullptr);
+// Cell order of positions before they are uploaded (x: x, y, z per particle, host-visible
+// or device memory): keys and counts of a (keys, counts, block_sums, cells, N, dx_inv, n),
+// the permutation into a.perm (slot q holds particle perm[q]) and its inverse into dest
+// (particle p goes to slot dest[p]); a copy of the positions into xcopy when not null;
+// *bad = 1 when a position is not finite.
+cudaError_t launch_presort(const float* x, float* xcopy, const SortArgs& a, uint32_t* dest, int* bad, int num_sms,
+                           cudaStream_t st, int64_t* launches);
 // Component-major particle arrays -> the non-null arrays in upload order (inv as from
 // launch_inverse, null for the identity).
 cudaError_t launch_interleave_arrays(const float* s, int64_t stride, const uint32_t* inv, int64_t n, OutArrays o,
