@@ -644,16 +644,18 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
       so.cells = c->sort_keys;
       so.N = (int)c->params.N;
       so.dx_inv = c->K.g.dx_inv;
-      MPM_CUDA(c, launch_presort(arr.x, xcopy, so, c->idB, c->work + 2, c->num_sms, c->stream, &c->launches));
-      MPM_CUDA(c, cudaMemcpyAsync(&bad, c->work + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-      MPM_CUDA(c, cudaStreamSynchronize(c->stream));
-      if (bad) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
+      // the check flag is read once, at the end: until then only the spare copy, the stage
+      // and sort scratch have been written, so a rejected upload leaves the context as it was
+      MPM_CUDA(c, launch_presort(arr.x, xcopy, so, c->idB, c->work + 3, c->num_sms, c->stream, &c->launches));
       HostArrays sorted_arr = arr;
       if (xcopy) sorted_arr.x = xcopy;
       MPM_CUDA(c, launch_deinterleave_arrays(sorted_arr, c->sB, c->stride, n, c->work + 2, c->stream, c->idB));
+      int flags[2] = {0, 0};
+      MPM_CUDA(c, cudaMemcpyAsync(flags, c->work + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // also: the caller may reuse the host arrays on return
+      if (flags[0] || flags[1]) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
       // slot q holds particle perm[q]: that is the id array
       MPM_CUDA(c, cudaMemcpyAsync(c->idA, so.perm, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
-      MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // the caller may reuse the host arrays on return
       std::swap(c->sA, c->sB);
       presorted = true;
     } else {
