@@ -59,6 +59,11 @@ struct mpm_ctx {
   int64_t cells = 0;
   int64_t sort_keys = 0;  // key space of the bricked cell sort (>= cells)
   int cur = 0;            // slot holding the P2G grid of the next substep (when pending)
+  // Calls that are followed by an upload (copies every substep) would throw away the P2G
+  // the fused step prefetches for the next substep: once that is seen, such calls end with
+  // a G2P-only step, until a call follows one of them without an upload in between.
+  bool tail_g2p = false;
+  bool ended_g2p = false;  // the last call ended with a G2P-only step
   int prev = -1;          // slot the last completed substep's G2P read
   bool pending = false;
 
@@ -353,9 +358,9 @@ mpm_status run_step(mpm_ctx* c, StepKind kind) {
   a.grid_out = c->grid[(r + 1) % 3];
   a.grid_zero = c->grid[(r + 2) % 3];
   MPM_CUDA(c, launch_step(a, kind, c->liquid_layout, guard, blocks, c->stream, &c->launches));
-  if (kind == kStepFused) c->prev = r;
+  if (kind != kStepP2GOnly) c->prev = r;
   c->cur = (r + 1) % 3;
-  c->pending = true;
+  c->pending = kind != kStepG2POnly;
   return MPM_OK;
 }
 
@@ -673,6 +678,9 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
     if (st != MPM_OK) return st;
   }
   c->n = n;
+  // a prefetched P2G is thrown away here: end later calls with a G2P-only step
+  if (c->pending || c->ended_g2p) c->tail_g2p = true;
+  c->ended_g2p = false;
   c->pending = false;
   c->prev = -1;
   c->substeps = 0;
@@ -736,6 +744,10 @@ mpm_status mpm_substep(mpm_ctx* c, int32_t nsteps) {
   mpm_status st = check_ready(c);
   if (st != MPM_OK) return st;
   if (nsteps < 0) return fail(c, MPM_ERR_INVALID, "nsteps must be >= 0");
+  // the last call ended without the prefetched P2G and the state was not replaced since:
+  // that P2G is needed after all, so calls end with the fused step again
+  if (nsteps > 0 && c->ended_g2p) c->tail_g2p = false;
+  if (nsteps > 0) c->ended_g2p = false;
   for (int32_t i = 0; i < nsteps; ++i) {
     if (!c->objects.empty()) {
       st = update_objects(c);
@@ -750,8 +762,10 @@ mpm_status mpm_substep(mpm_ctx* c, int32_t nsteps) {
         st = run_step(c, kStepP2GOnly);
         if (st != MPM_OK) return st;
       }
-      st = run_step(c, kStepFused);
+      const bool g2p_only = c->tail_g2p && i == nsteps - 1 && c->objects.empty();
+      st = run_step(c, g2p_only ? kStepG2POnly : kStepFused);
       if (st != MPM_OK) return st;
+      c->ended_g2p = g2p_only;
     }
     c->substeps += 1;
     c->since_sort += 1;

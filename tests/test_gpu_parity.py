@@ -359,6 +359,39 @@ def test_reupload_in_cell_order_matches_a_fresh_upload(gpu_lib, liquid):
             assert np.array_equal(ra["mat"], rb["mat"])
 
 
+def test_upload_loop_ending_without_prefetch_matches_plain_substeps(gpu_lib):
+    """Calls that an upload follows end with a G2P-only step (the prefetched P2G would be
+    thrown away). When a call then follows without an upload, the skipped P2G is redone:
+    the trajectory and the grid readback match a context that never re-uploaded."""
+    from mpm_gb300 import scenes
+    from mpm_gb300.simulation import Simulation
+
+    cfg = scenes.config_elastic(n=5000, seed=12)
+    st = cfg["state"]
+    with Simulation.from_config(cfg) as a, Simulation.from_config(cfg) as b:
+        a.upload(st)
+        a.advance(2)
+        a.upload(st)  # throws a prefetched P2G away: calls now end with G2P only
+        a.advance(1)
+        a.upload(st)
+        a.advance(1)  # ends with G2P only
+        ga = a.get_grid(0)
+        a.advance(3)  # no upload in between: the skipped P2G is redone
+        b.upload(st)
+        b.advance(1)
+        gb = b.get_grid(0)
+        b.advance(3)
+        ra, rb = a.download(), b.download()
+        p = cfg["params"]
+        vmax = max(float(np.abs(rb["v"]).max()), abs(p["dt"] * p["gravity"]))
+        scale = {"x": 1.0, "v": vmax, "C": 4.0 * p["N"] * vmax, "F": 1.0, "Jp": 1.0}
+        for k in scale:
+            if k in ra:
+                assert np.abs(ra[k] - rb[k]).max() <= 1e-5 * scale[k], k
+        assert np.abs(ga - gb).max() <= 1e-5 * max(float(np.abs(gb).max()), 1e-6)
+        assert a.substeps == b.substeps == 4
+
+
 def test_argument_validation(gpu_lib, tmp_path):
     """Every entry point rejects bad arguments with its status code (no device work)."""
     import ctypes
