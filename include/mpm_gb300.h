@@ -343,19 +343,23 @@ mpm_status mpm_diff_backward(mpm_diff* diff, const float* gx_final, const float*
                              float* gC0, float* gF0, double* gmu_glambda);
 
 /* Substep entry point that allocates nothing.  It has no counterpart in the reference.
- * For callers that cannot call cudaMalloc: code running while someone else captures a CUDA
- * graph, plugins whose host owns all device memory, and callers that forbid allocation after
- * start-up.  It runs `nsteps` substeps on the caller's device state in place, on `stream`
- * (NULL: the legacy default stream), asynchronously:
+ * For callers that cannot call cudaMalloc: plugins whose host application owns all device
+ * memory through its own pool, and embedded or real-time callers that forbid allocation after
+ * start-up (an allocation may block, fail or fragment memory at a time they do not choose).
+ * It runs `nsteps` substeps on the caller's device state in place, on `stream` (NULL: the
+ * legacy default stream), asynchronously:
  *   - state: caller-owned device memory in the library's component-major layout, component k
  *     of particle p at state[k * stride + p]: x 0-2, v 3-5, C 6-14 and F 15-23 (row-major),
  *     Jp 24 (J for a single-liquid table, whose F components are not touched);
- *   - mat: device array of material indices, or NULL for material 0;
- *   - the scratch (three P2G grids, the padded velocity grid and two counters) is a static
- *     device array of 2.3 MiB that every GPU loading the library holds until exit, so N is
- *     limited to 32
- *     (MPM_ERR_UNSUPPORTED above); g2p_guard and check_finite are not supported here.
+ *   - mat: device array of material indices (each < n_materials; a larger index is flagged
+ *     in the status word and the particle takes material 0), or NULL for material 0;
+ *   - the scratch (three P2G grids, the padded velocity grid and the device status word) is a
+ *     static device array of 2.3 MiB that every GPU loading the library holds until exit, so N
+ *     is limited to 32 (MPM_ERR_UNSUPPORTED above); g2p_guard is not supported here.
  * Particles are processed in the caller's order (no cell sort; sorted input runs faster).
+ * Device-side faults (an expired bounded wait, a non-finite position with check_finite, a
+ * material index past the table) set the status word; it is kept across calls until
+ * mpm_noalloc_status reads and clears it.
  * The first call on a device looks up the scratch's device address (cudaGetSymbolAddress), so
  * make that first call before any stream capture.  All calls share the scratch, which keeps
  * the last call's contents (each call clears what must start at zero): calls that overlap on
@@ -363,6 +367,17 @@ mpm_status mpm_diff_backward(mpm_diff* diff, const float* gx_final, const float*
 mpm_status mpm_substep_noalloc(const mpm_params* params, const mpm_material* materials, int32_t n_materials,
                                float* state, int64_t stride, const uint8_t* mat, int64_t n, int32_t nsteps,
                                void* stream);
+/* Status of the no-allocation substeps on the current device (no counterpart in the
+ * reference): waits for `stream`, reads the status word in the static scratch and clears it.
+ * Returns MPM_ERR_TIMEOUT when a bounded device wait expired (the substep that saw it may
+ * have gathered from a grid tile that never arrived), MPM_ERR_STATE for a non-finite particle
+ * or a material index past the table, MPM_OK otherwise.  Allocates nothing. */
+mpm_status mpm_noalloc_status(void* stream);
+/* Self-check of that status path (no counterpart in the reference): one warp on `stream`
+ * waits on an mbarrier nothing completes, gives up after `polls` polls (1..2^20) and sets the
+ * timeout bit of the no-allocation status word, as the substep does when a tile copy never
+ * lands; mpm_noalloc_status then returns MPM_ERR_TIMEOUT.  Allocates nothing. */
+mpm_status mpm_noalloc_check_wait_timeout(int32_t polls, void* stream);
 
 #ifdef __cplusplus
 }

@@ -129,6 +129,8 @@ SIGNATURES = [
     ("mpm_diff_backward", I32, [P, P, P, P, P, P, P, P]),
     ("mpm_substep_noalloc", I32, [ctypes.POINTER(MpmParams), ctypes.POINTER(MpmMaterial), I32, P, I64, P, I64, I32,
                                   P]),
+    ("mpm_noalloc_status", I32, [P]),
+    ("mpm_noalloc_check_wait_timeout", I32, [I32, P]),
 ]
 
 _lib = None

@@ -425,9 +425,7 @@ struct mpm_diff {
   double* pgrad = nullptr;
   float* stage = nullptr;
   uint32_t* id = nullptr;
-  int* work = nullptr;
   int* status = nullptr;
-  int parity = 0;
   int64_t cells = 0;
   std::string last_error;
 };
@@ -451,14 +449,11 @@ mpm_status dlaunch(mpm_diff* d, StepKind kind, float* state, const float4* gin, 
   a.grid_cells = d->cells;
   set_vgrid(a, d->vel);
   a.status = d->status;
-  a.work = d->work + d->parity;
-  a.work_next = d->work + (d->parity ^ 1);
   a.K = d->K;
   int chunk = 0, blocks = 0;
   step_launch_shape(d->num_sms, d->n, false, false, kind, 2, chunk, blocks);
   a.chunk = chunk;
   if (launch_step(a, kind, false, false, blocks, d->stream) != cudaSuccess) return MPM_ERR_CUDA;
-  d->parity ^= 1;
   return MPM_OK;
 }
 
@@ -503,8 +498,8 @@ mpm_status mpm_diff_create(const mpm_params* params, const mpm_material* materia
       cudaMalloc(&d->grid3, sizeof(float4) * d->cells * 3) || cudaMalloc(&d->vgrid, sizeof(float4) * d->cells) ||
       cudaMalloc(&d->gadj, sizeof(float4) * d->cells) || cudaMalloc(&d->adj, sf) ||
       cudaMalloc(&d->pgrad, 2 * sizeof(double)) || cudaMalloc(&d->stage, sf) ||
-      cudaMalloc(&d->id, sizeof(uint32_t) * d->stride) || cudaMalloc(&d->work, 2 * sizeof(int)) ||
-      cudaMalloc(&d->status, sizeof(int)) || cudaMemset(d->work, 0, 2 * sizeof(int)) ||
+      cudaMalloc(&d->id, sizeof(uint32_t) * d->stride) ||
+      cudaMalloc(&d->status, sizeof(int)) ||
       cudaMemset(d->status, 0, sizeof(int)) || cudaMemset(d->ckpt, 0, sf * nck) || cudaMemset(d->seg, 0, sf) ||
       cudaMemset(d->adj, 0, sf) ||
       cudaMalloc(&d->step_vgrid, sizeof(float4) * vgrid_nodes((int)params->N))) {
@@ -527,7 +522,7 @@ mpm_status mpm_diff_destroy(mpm_diff* d) {
   if (!d) return MPM_ERR_INVALID;
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (void* p : {(void*)d->ckpt, (void*)d->seg, (void*)d->seg_grid, (void*)d->grid3, (void*)d->vgrid,
-                  (void*)d->step_vgrid, (void*)d->gadj, (void*)d->adj, (void*)d->pgrad, (void*)d->stage, (void*)d->id, (void*)d->work,
+                  (void*)d->step_vgrid, (void*)d->gadj, (void*)d->adj, (void*)d->pgrad, (void*)d->stage, (void*)d->id,
                   (void*)d->status})
     cudaFree(p);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -588,14 +583,11 @@ mpm_status mpm_diff_forward(mpm_diff* d, const float* x0, const float* v0, const
     a.grid_cells = d->cells;
     set_vgrid(a, d->vel);
     a.status = d->status;
-    a.work = d->work + d->parity;
-    a.work_next = d->work + (d->parity ^ 1);
     a.K = d->K;
     int chunk = 0, blocks = 0;
     step_launch_shape(d->num_sms, n, false, false, kStepFused, 2, chunk, blocks);
     a.chunk = chunk;
     if (launch_step(a, kStepFused, false, false, blocks, s) != cudaSuccess) return MPM_ERR_CUDA;
-    d->parity ^= 1;
     cur = (cur + 1) % 3;
     if ((i + 1) % d->ckpt_every == 0 && i + 1 < nsteps)
       if (cudaMemcpyAsync(d->ckpt + state_floats(d) * ((i + 1) / d->ckpt_every), work, sb, cudaMemcpyDeviceToDevice,

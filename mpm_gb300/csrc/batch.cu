@@ -54,14 +54,12 @@ struct mpm_batch {
   int4* d_ranges = nullptr;
   int nranges = 0;
   int* boxes = nullptr;
-  int* work = nullptr;
   int* status = nullptr;
   float* stage = nullptr;
 
   int cur = 0;
   bool pending = false;
   int64_t launch_index = 0;  // fused/P2G launches since upload (selects the box slots)
-  int parity = 0;
   int64_t since_sort = 0;
   int64_t launches = 0;
   struct Graph {
@@ -121,12 +119,9 @@ mpm_status launch(mpm_batch* b, StepKind kind) {
   }
   a.grid_out = b->grid[(r + 1) % 3];
   a.grid_zero = b->grid[(r + 2) % 3];
-  a.work = b->work + b->parity;
-  a.work_next = b->work + (b->parity ^ 1);
   a.chunk = 32 * b->steps_per_warp;
   const int blocks = (kind == kStepP2GOnly) ? b->blocks_p2g : b->blocks_fused;
   BCUDA(b, launch_step(a, kind, false, false, blocks, b->stream, &b->launches));
-  b->parity ^= 1;
   b->cur = (r + 1) % 3;
   b->launch_index += 1;
   b->pending = true;
@@ -263,7 +258,7 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
   if (cudaMalloc(&b->counts, 4 * keys) || cudaMalloc(&b->block_sums, 4 * std::max<int64_t>(nbs, 1)) ||
       cudaMalloc(&b->d_scenes, sizeof(SceneDev) * nscenes) || cudaMalloc(&b->d_start, 8 * (nscenes + 1)) ||
       cudaMalloc(&b->d_key_base, 4 * nscenes) || cudaMalloc(&b->d_ranges, sizeof(int4) * std::max(b->nranges, 1)) ||
-      cudaMalloc(&b->boxes, sizeof(int) * 6 * kBoxSlots * nscenes) || cudaMalloc(&b->work, 2 * sizeof(int)) ||
+      cudaMalloc(&b->boxes, sizeof(int) * 6 * kBoxSlots * nscenes) ||
       cudaMalloc(&b->status, sizeof(int)))
     return bail(MPM_ERR_NOMEM);
   std::vector<int> boxes(6 * kBoxSlots * nscenes);
@@ -273,7 +268,7 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
       cudaMemcpy(b->d_key_base, key_base.data(), 4 * nscenes, cudaMemcpyHostToDevice) ||
       (b->nranges && cudaMemcpy(b->d_ranges, ranges.data(), sizeof(int4) * b->nranges, cudaMemcpyHostToDevice)) ||
       cudaMemcpy(b->boxes, boxes.data(), sizeof(int) * boxes.size(), cudaMemcpyHostToDevice) ||
-      cudaMemset(b->work, 0, 2 * sizeof(int)) || cudaMemset(b->status, 0, sizeof(int)) ||
+      cudaMemset(b->status, 0, sizeof(int)) ||
       cudaStreamSynchronize(b->stream))
     return bail(MPM_ERR_CUDA);
   *out = b;
@@ -287,7 +282,7 @@ mpm_status mpm_batch_destroy(mpm_batch* b) {
   for (void* p : {(void*)b->sA, (void*)b->sB, (void*)b->matA, (void*)b->matB, (void*)b->idA, (void*)b->idB,
                   (void*)b->keys, (void*)b->stage, (void*)b->grid[0], (void*)b->grid[1], (void*)b->grid[2], (void*)b->vgrid,
                   (void*)b->counts, (void*)b->block_sums, (void*)b->d_scenes, (void*)b->d_start, (void*)b->d_key_base,
-                  (void*)b->d_ranges, (void*)b->boxes, (void*)b->work, (void*)b->status})
+                  (void*)b->d_ranges, (void*)b->boxes, (void*)b->status})
     cudaFree(p);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
@@ -350,7 +345,7 @@ mpm_status mpm_batch_substep_graph(mpm_batch* b, int32_t nsteps) {
     if (st != MPM_OK) return st;
   }
   // A captured run is: one cell sort (when sorting is on), then nsteps fused launches.
-  // The graph bakes in the particle-buffer roles and the grid, counter and box-slot
+  // The graph bakes in the particle-buffer roles and the grid and box-slot
   // indices (launch index mod 6), so one graph is kept per (nsteps, phase, buffer role).
   const bool sorting = b->sort_interval > 0;
   const int role = (b->sA < b->sB) ? 0 : 1;
@@ -358,7 +353,7 @@ mpm_status mpm_batch_substep_graph(mpm_batch* b, int32_t nsteps) {
   const std::pair<int, int> key(nsteps, key_phase);
   auto it = b->graphs.find(key);
   if (it == b->graphs.end()) {
-    const int cur = b->cur, parity = b->parity;
+    const int cur = b->cur;
     const int64_t li = b->launch_index, ss = b->since_sort, lc = b->launches;
     float* sA = b->sA;
     float* sB = b->sB;
@@ -374,7 +369,6 @@ mpm_status mpm_batch_substep_graph(mpm_batch* b, int32_t nsteps) {
     const int64_t captured = b->launches - lc;
     // capturing recorded the work without running it: restore the host-side state
     b->cur = cur;
-    b->parity = parity;
     b->launch_index = li;
     b->since_sort = ss;
     b->launches = lc;
@@ -404,7 +398,6 @@ mpm_status mpm_batch_substep_graph(mpm_batch* b, int32_t nsteps) {
     std::swap(b->idA, b->idB);
   }
   b->cur = (int)((b->cur + nsteps) % 3);
-  b->parity ^= (nsteps & 1);
   b->launch_index += nsteps;
   b->since_sort = nsteps;
   return MPM_OK;

@@ -75,8 +75,7 @@ struct mpm_ctx {
   float* stage = nullptr;
   size_t stage_bytes = 0;
   int* status = nullptr;
-  int* work = nullptr;  // two range counters, alternating between substep launches; [2]: upload check
-  int launch_parity = 0;
+  int* work = nullptr;  // [2]: upload position check, [3]: cell-order position check
   bool unsorted = true;  // particle order unrelated to cells (upload, append): the next sort gathers
 
   int64_t substeps = 0;
@@ -350,9 +349,6 @@ mpm_status run_step(mpm_ctx* c, StepKind kind) {
   int chunk, blocks;
   launch_shape(c, kind, guard, chunk, blocks);
   a.chunk = chunk;
-  a.work = c->work + (c->launch_parity & 1);
-  a.work_next = c->work + ((c->launch_parity + 1) & 1);
-  c->launch_parity ^= 1;
   const int r = c->cur;
   a.grid_in = (kind == kStepP2GOnly) ? nullptr : c->grid[r];
   a.grid_out = c->grid[(r + 1) % 3];

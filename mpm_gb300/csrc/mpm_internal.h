@@ -37,8 +37,6 @@ struct StepArgs {
   int64_t guard_limit;    // G2P only for id <= guard_limit when the guard is on
   int check_finite;
   int* status;
-  int* work;              // range counter of this launch, starts at 0
-  int* work_next;         // range counter of the next launch, cleared by this one
   // batch mode (nscenes > 0): ranges never straddle scenes; grids are cleared sparsely
   int nscenes;
   const int4* ranges;     // (scene, begin, end, 0)

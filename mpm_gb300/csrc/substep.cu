@@ -245,7 +245,15 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
         if (!LIQ) {
 #pragma unroll
           for (int i = 0; i < 9; ++i) F[i / 3][i % 3] = s[(kF + i) * st + p];
-          if (A.mat) mi = A.mat[p];
+          if (A.mat) {
+            mi = A.mat[p];
+            // an index past the table (caller-owned material arrays are not checked on
+            // the host) is flagged and the particle takes material 0
+            if (mi >= A.K.n_materials) {
+              atomicOr(A.status, kStatusIndex);
+              mi = 0;
+            }
+          }
         }
         if (frozen && P2G) {
 #pragma unroll

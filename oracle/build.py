@@ -5,8 +5,10 @@
 * ``_ref/libref_svd.so`` — the reference's own ``include/svd3_cuda.h`` compiled
   for the host from where it lies in the reference checkout, through
   ``ref_shim/`` (host definitions of the three CUDA rounding intrinsics it uses).
-  Built only when the reference checkout is present (this container); nothing
-  from the reference is copied into the repository.
+  Built only when the reference checkout is given: the ``ref_root`` argument of
+  :func:`build_ref`, else the ``MPM_REFERENCE_ROOT`` environment variable; without
+  either it is skipped with a message.  Nothing from the reference is copied into
+  the repository.
 * ``_ref/libref_substep.so`` — the reference's own policy headers
   (TransferScheme.h, MaterialModel.cuh, InterpolationKernel.cuh, types.h,
   svd3_cuda.h) compiled for the host against the project-written Eigen subset in
@@ -22,7 +24,6 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("MPM_REFERENCE_ROOT", "/root/reference")
 
 
 def _run(cmd):
@@ -44,14 +45,22 @@ def build_oracle(force: bool = False) -> str:
     return out
 
 
-def reference_available() -> bool:
-    return os.path.isfile(os.path.join(REF_ROOT, "include", "svd3_cuda.h"))
+def reference_root(ref_root=None):
+    """The reference checkout: the argument, else MPM_REFERENCE_ROOT; None when neither
+    names a checkout (a directory holding include/svd3_cuda.h)."""
+    root = ref_root or os.environ.get("MPM_REFERENCE_ROOT")
+    if root and os.path.isfile(os.path.join(root, "include", "svd3_cuda.h")):
+        return root
+    return None
 
 
-def build_ref(force: bool = False) -> list:
-    """Compile the reference-derived host libraries into oracle/_ref (only when the
-    reference checkout exists). Returns the list of built paths."""
-    if not reference_available():
+def build_ref(ref_root=None, force: bool = False) -> list:
+    """Compile the reference-derived host libraries into oracle/_ref from the reference
+    checkout (``ref_root`` or MPM_REFERENCE_ROOT). Returns the list of built paths;
+    empty, with a message, when no checkout is given."""
+    REF_ROOT = reference_root(ref_root)
+    if REF_ROOT is None:
+        print("oracle/_ref not built: no reference checkout given (pass ref_root or set MPM_REFERENCE_ROOT)")
         return []
     outdir = os.path.join(HERE, "_ref")
     os.makedirs(outdir, exist_ok=True)
@@ -77,5 +86,7 @@ def build_ref(force: bool = False) -> list:
 
 
 if __name__ == "__main__":
+    import sys
+
     print(build_oracle(force=True))
-    print(build_ref(force=True))
+    print(build_ref(sys.argv[1] if len(sys.argv) > 1 else None, force=True))

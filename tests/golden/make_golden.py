@@ -1,7 +1,8 @@
 """Generate the golden fixtures under tests/golden from the reference checkout.
 
-Run here, where the reference is present (it is not on the GPU machines):
-    python tests/golden/make_golden.py
+Run where the reference checkout is present (it is not on the GPU machines):
+    python tests/golden/make_golden.py <reference checkout>
+or with MPM_REFERENCE_ROOT naming the checkout.
 Writes:
   ref_linalg.json  — the matrices and tolerances of the reference's own tests
                      (tests/test_linalg.cu: TestPolar.*, TestDevicePolar.Basic,
@@ -27,7 +28,7 @@ sys.path.insert(0, ROOT)
 
 from oracle import build as obuild  # noqa: E402
 
-REF = obuild.REF_ROOT
+REF = None  # the reference checkout, set by main() from argv[1] or MPM_REFERENCE_ROOT
 
 
 def linalg_vectors():
@@ -62,10 +63,14 @@ def svd_vectors():
 
 
 def main():
+    global REF
+    REF = obuild.reference_root(sys.argv[1] if len(sys.argv) > 1 else None)
+    if REF is None:
+        raise SystemExit("reference checkout not given (argv[1] or MPM_REFERENCE_ROOT); fixtures unchanged")
     obuild.build_oracle()
-    built = obuild.build_ref()
+    built = obuild.build_ref(REF)
     if not built:
-        raise SystemExit("reference checkout not found; fixtures unchanged")
+        raise SystemExit("reference libraries not built; fixtures unchanged")
     with open(os.path.join(HERE, "ref_linalg.json"), "w") as f:
         json.dump(linalg_vectors(), f, indent=1)
     np.savez_compressed(os.path.join(HERE, "ref_svd.npz"), **svd_vectors())

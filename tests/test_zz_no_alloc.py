@@ -1,10 +1,11 @@
 """GPU test of mpm_substep_noalloc, the substep entry point that allocates nothing.
 
-Callers that cannot call cudaMalloc use this entry point: code that runs while
-another component captures a CUDA graph, plugins whose host application owns all
-device memory, and callers that forbid allocation after start-up.  They pass their
-own device buffers for the particle state; the substep's scratch (the rotating P2G
-grids) is a static device array inside the library, limited to N <= 32.
+Callers that cannot call cudaMalloc use this entry point: plugins whose host
+application owns all device memory through its own pool, and embedded or real-time
+callers that forbid allocation after start-up.  They pass their own device buffers for
+the particle state; the substep's scratch (the rotating P2G grids, the velocity grid
+and the device status word) is a static device array inside the library, limited to
+N <= 32.  mpm_noalloc_status reads and clears that status word.
 
 The file is named so that pytest collects it last: a run that stops at the first
 failure has already run every other test.  Each check compares the entry point with
@@ -94,11 +95,13 @@ def test_noalloc_matches_context_path(gpu_lib, name):
     fields = ("x", "v", "C", "Jp") if liquid else ("x", "v", "C", "F", "Jp")
 
     assert call_noalloc(gpu_lib, cfg, dev, stride, dev_mat, n, 2) == 0
+    assert gpu_lib.mpm_noalloc_status(None) == 0
     out1 = from_component_major(dev.cpu().numpy(), n)
     errs = compare_states(out1, ref1, cfg["params"], st)
     assert max(errs[k] for k in fields) < 1e-5, errs
 
     assert call_noalloc(gpu_lib, cfg, dev, stride, dev_mat, n, 3) == 0
+    assert gpu_lib.mpm_noalloc_status(None) == 0
     out2 = from_component_major(dev.cpu().numpy(), n)
     errs = compare_states(out2, ref2, cfg["params"], st)
     assert max(errs[k] for k in fields) < 1e-5, errs
@@ -116,3 +119,52 @@ def test_noalloc_rejects_grid_beyond_scratch(gpu_lib):
     before = dev.clone()
     assert call_noalloc(gpu_lib, cfg, dev, 2048, None, 2_000, 1) == 6
     assert torch.equal(dev, before)
+
+
+def test_noalloc_status_reports_an_expired_wait(gpu_lib):
+    """A bounded device wait that runs out sets the no-allocation status word: a warp
+    waits on an mbarrier that nothing completes and gives up after 64 polls, as the
+    substep does when a tile copy never lands.  The bit survives a following substep
+    call (which does not clear it), mpm_noalloc_status returns MPM_ERR_TIMEOUT once and
+    clears it, and the substeps keep working afterwards."""
+    import torch
+
+    from mpm_gb300 import scenes
+
+    assert gpu_lib.mpm_noalloc_status(None) == 0
+    assert gpu_lib.mpm_noalloc_check_wait_timeout(0, None) == 1  # polls out of range
+    assert gpu_lib.mpm_noalloc_check_wait_timeout(64, None) == 0
+    cfg = scenes.config_elastic(n=4_000, seed=26)
+    st = cfg["state"]
+    dev = torch.from_numpy(to_component_major(st, 4032)).cuda()
+    assert call_noalloc(gpu_lib, cfg, dev, 4032, None, 4_000, 1) == 0
+    assert gpu_lib.mpm_noalloc_status(None) == 4  # MPM_ERR_TIMEOUT
+    assert gpu_lib.mpm_noalloc_status(None) == 0  # cleared by the read
+    assert call_noalloc(gpu_lib, cfg, dev, 4032, None, 4_000, 1) == 0
+    assert gpu_lib.mpm_noalloc_status(None) == 0
+    assert torch.isfinite(dev).all()
+
+
+def test_noalloc_flags_material_index_past_the_table(gpu_lib):
+    """A material index the table does not hold is flagged (MPM_ERR_STATE) and the
+    particle takes material 0, so the result equals that of an all-zero material array
+    (to the rounding of the grid's float atomics, whose order varies between runs)."""
+    import torch
+
+    from mpm_gb300 import scenes
+
+    cfg = scenes.mixed_scene(n=6_000, seed=27)
+    st = cfg["state"]
+    n = st["x"].shape[0]
+    stride = (n + 63) // 64 * 64
+    zero = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    bad = zero.clone()
+    bad[n // 2] = 200
+    a = torch.from_numpy(to_component_major(st, stride)).cuda()
+    b = a.clone()
+    assert gpu_lib.mpm_noalloc_status(None) == 0
+    assert call_noalloc(gpu_lib, cfg, a, stride, zero, n, 2) == 0
+    assert gpu_lib.mpm_noalloc_status(None) == 0
+    assert call_noalloc(gpu_lib, cfg, b, stride, bad, n, 2) == 0
+    assert gpu_lib.mpm_noalloc_status(None) == 3  # MPM_ERR_STATE
+    assert torch.allclose(a, b, rtol=1e-5, atol=1e-6)
