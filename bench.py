@@ -55,6 +55,8 @@ def parse():
                              "render"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="headline workload only (no snow, batched and differentiable sections)")
     ap.add_argument("--e2e-steps", type=int, default=5)
     return ap.parse_args()
 
@@ -152,14 +154,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(workload):
-    """DRAM bytes of one substep (velocity pass + fused kernel) from the committed ncu summary."""
+def profile_summary(workload):
+    """Figures of one substep (velocity pass + fused kernel) from the committed ncu summary
+    of the workload: DRAM bytes and warp instructions per substep, the SM clock of the
+    capture."""
     p = os.path.join(ROOT, "profiles", f"scene_step_{workload}.json")
     if os.path.exists(p):
         with open(p) as f:
-            d = json.load(f)
-        return d.get("dram_bytes_per_substep")
-    return None
+            return json.load(f)
+    return {}
 
 
 def cpu_baseline(cfg, budget_s=12.0, max_particles=None):
@@ -221,6 +224,67 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def time_substeps(sim, steps, warmup, stream, flush):
+    """Device time of `steps` single substeps (CUDA events on the library's stream), the L2
+    flushed by a 512 MiB write before each (outside the events).  Returns the per-step
+    times (ms), whether each step ran only the two substep kernels (no sort), the kernel
+    launches and the wall time of the timed loop."""
+    import torch
+
+    for _ in range(warmup):
+        flush.fill_(1.0)
+        sim.advance(1)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    pure = []
+    launches0 = sim.launches
+    wall0 = time.perf_counter()
+    for k in range(steps):
+        flush.fill_(float(k))
+        l0 = sim.launches
+        starts[k].record(stream)
+        sim.advance(1)
+        ends[k].record(stream)
+        pure.append(sim.launches - l0 == 2)  # velocity pass + fused kernel, no sort
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    return ms, pure, sim.launches - launches0, wall
+
+
+def substep_roofline(cfg, n, ms, pure, workload):
+    """HBM roofline of one substep (velocity pass + fused kernel): algorithmic bytes
+    (B_ALG per particle + 32 B per grid node) over the mean time of the steps that ran no
+    sort, against the measured copy bandwidth."""
+    N = cfg["params"]["N"]
+    fused_ms = [m for m, p in zip(ms, pure) if p]
+    kernel_ms = statistics.mean(fused_ms) if fused_ms else statistics.mean(ms)
+    peak, peak_kind = measured_peaks()
+    name = cfg["materials"][0].name
+    bytes_per_launch = B_ALG[name if name in B_ALG else "liquid"] * n + GRID_BYTES_PER_NODE * N ** 3
+    achieved = bytes_per_launch / (kernel_ms * 1e-3) / 1e9
+    prof = profile_summary(workload)
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": prof.get("dram_bytes_per_substep"),
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "kernel": "mpm::grid_velocity_kernel + mpm::scene_step_kernel (one substep)", "kernel_ms": kernel_ms,
+            "bytes_per_launch": bytes_per_launch}
+
+
+def issue_fraction(roofline, workload, clocks, num_sms):
+    """Share of the SMs' issue slots the substep kernels used: their warp instructions per
+    substep (from the committed ncu summary of the same workload) over kernel time x SMs x
+    4 schedulers x the median SM clock sampled during the timed region."""
+    prof = profile_summary(workload)
+    inst = prof.get("warp_instructions_per_substep")
+    mhz = (clocks or {}).get("sm_mhz") or prof.get("sm_mhz")
+    if not inst or not mhz:
+        return None
+    slots = roofline["kernel_ms"] * 1e-3 * num_sms * 4 * mhz * 1e6
+    return inst / slots
+
+
 def run_ours(args):
     import torch
 
@@ -245,52 +309,31 @@ def run_ours(args):
     sim.set_stream(stream.cuda_stream)
     sim.upload(cfg["state"])
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    num_sms = torch.cuda.get_device_properties(0).multi_processor_count
 
+    torch.cuda.synchronize()
+    D.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
     for _ in range(args.warmup):
         flush.fill_(1.0)
         sim.advance(1)
     torch.cuda.synchronize()
     D.barrier()
     torch.cuda.synchronize()
-
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    pure = []
-    sampler = ClockSampler(local)
-    sampler.start()
-    time.sleep(0.3)
-    launches0 = sim.launches
     wall0_abs = time.time()
-    wall0 = time.perf_counter()
-    for k in range(args.steps):
-        flush.fill_(float(k))
-        l0 = sim.launches
-        starts[k].record(stream)
-        sim.advance(1)
-        ends[k].record(stream)
-        pure.append(sim.launches - l0 == 2)  # velocity pass + fused kernel, no sort
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
-    launches = sim.launches - launches0
+    ms, pure, launches, wall = time_substeps(sim, args.steps, 0, stream, flush)
     clocks = sampler.stop(wall0_abs, wall0_abs + wall)
-    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     sim.sync()
     torch.cuda.synchronize()
     D.barrier()
     dev_ms = D.max_over_ranks(sum(ms))  # the slowest replica
     ms_per_step = dev_ms / args.steps
     value = D.job_rate(world * n * args.steps, dev_ms * 1e-3)
-
-    fused_ms = [m for m, p in zip(ms, pure) if p]
-    kernel_ms = statistics.mean(fused_ms) if fused_ms else ms_per_step
-    peak, peak_kind = measured_peaks()
-    bytes_per_launch = B_ALG[cfg["materials"][0].name if cfg["materials"][0].name in B_ALG else "liquid"] * n \
-        + GRID_BYTES_PER_NODE * N ** 3
-    achieved = bytes_per_launch / (kernel_ms * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": profile_traffic(workload), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": "mpm::grid_velocity_kernel + mpm::scene_step_kernel (one substep)", "kernel_ms": kernel_ms,
-                "bytes_per_launch": bytes_per_launch}
+    roofline = substep_roofline(cfg, n, ms, pure, workload)
+    roofline["issue_frac"] = issue_fraction(roofline, workload, clocks, num_sms)
 
     e2e = None
     if not args.no_e2e:
@@ -299,6 +342,13 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(cfg, max_particles=None if args.config != "liquid" else 1_000_000)
     sim.close()
+    extra = {}
+    if world == 1 and args.config == "liquid" and not args.no_extra:
+        del flush
+        torch.cuda.empty_cache()
+        extra["snow"] = snow_section(args, stream, num_sms)
+        extra["batched"] = batched_section(args, stream)
+        extra["differentiable"] = differentiable_section(args)
     if rank == 0:
         line = {
             "metric": "particle-substeps/s", "value": value, "unit": "particle-substeps/s", "n_gpus": world,
@@ -311,9 +361,41 @@ def run_ours(args):
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
             "wall_s_timed_region": wall,
         }
+        if extra:
+            line["snow"] = extra["snow"]
+            line["batched"] = extra["batched"]
+            line["differentiable"] = extra["differentiable"]
+            line["snow_value"] = extra["snow"]["value"]
+            line["snow_roofline_frac"] = extra["snow"]["roofline"]["frac"]
+            line["batched_vs_looped"] = extra["batched"]["batched_vs_looped"]
+            line["bwd_fwd_ratio"] = extra["differentiable"]["bwd_fwd_ratio"]
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def snow_section(args, stream, num_sms):
+    """The snow workload (500,000 particles in two spheres, N = 64, SVD plasticity),
+    timed like the headline: single substeps, L2 flushed between them."""
+    import torch
+
+    from mpm_gb300.simulation import Simulation
+
+    cfg, workload = make_cfg("snow")
+    n = cfg["state"]["x"].shape[0]
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    with Simulation.from_config(cfg) as sim:
+        sim.set_stream(stream.cuda_stream)
+        sim.upload(cfg["state"])
+        ms, pure, launches, _ = time_substeps(sim, args.steps, max(args.warmup, 3), stream, flush)
+        sim.sync()
+    del flush
+    roof = substep_roofline(cfg, n, ms, pure, workload)
+    roof["issue_frac"] = issue_fraction(roof, workload, None, num_sms)
+    return {"value": n * len(ms) / (sum(ms) * 1e-3), "unit": "particle-substeps/s", "ms_per_step": sum(ms) / len(ms),
+            "steps": len(ms), "roofline": roof, "gpu_launches": launches,
+            "config": {"workload": workload, "particles": n, "N": cfg["params"]["N"], "material": "snow",
+                       "sort_interval": cfg["params"]["sort_interval"], "l2": "flushed between steps"}}
 
 
 def run_e2e(sim, cfg, steps, world):
@@ -355,9 +437,110 @@ def run_e2e(sim, cfg, steps, world):
             "path": "mpm_upload_soa + mpm_substep(1) + mpm_download_soa, pinned host buffers"}
 
 
+def batched_section(args, stream, scs=None, rank=0, world=1):
+    """The batched workload (256 scenes): one replayed CUDA graph of 50 substeps per step,
+    against looping plain single-scene launches over the same scenes, measured two ways
+    with no Python per-call dispatch: (a) a compiled host loop (mpm_substep_many) that
+    enqueues substep by substep over one context per scene, and (b) that loop captured
+    into one CUDA graph and replayed.  The ratio is taken against the faster looped arm."""
+    import torch
+
+    from mpm_gb300 import distributed as D
+    from mpm_gb300 import scenes
+    from mpm_gb300.batch import Batch
+    from mpm_gb300.simulation import Simulation, advance_many
+
+    all_scenes = scenes.config_batched(nscenes=256, seed=0)
+    n_all = sum(s["state"]["x"].shape[0] for s in all_scenes)
+    # scenes are independent: rank r takes scenes r, r + world, ... (no collective on the data path)
+    scs = D.shard(all_scenes, rank, world)
+    n = sum(s["state"]["x"].shape[0] for s in scs)
+    sub = 50
+    b = Batch(scs, sort_interval=16)
+    b.set_stream(stream.cuda_stream)
+    b.upload([s["state"] for s in scs])
+    for _ in range(max(args.warmup, 3)):
+        b.advance(sub, graph=True)
+    torch.cuda.synchronize()
+    D.barrier()
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 10))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    l0 = b.launches
+    for a, e in ev:
+        a.record(stream)
+        b.advance(sub, graph=True)
+        e.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = sum(a.elapsed_time(e) for a, e in ev)
+    local_rate = n * sub * steps / (batched_ms * 1e-3)
+    batched_ms_max = D.max_over_ranks(batched_ms)  # the slowest rank's share
+    launches = b.launches - l0
+    b.sync()
+    b.close()
+    value = D.job_rate(n_all * sub * steps, batched_ms_max * 1e-3)
+
+    # looped plain launches: one context per scene, all on one stream
+    sims = []
+    for sc in scs:
+        sim = Simulation(materials=[sc["material"]], sort_interval=16, **sc["params"])
+        sim.set_stream(stream.cuda_stream)
+        sim.upload(sc["state"])
+        sims.append(sim)
+    advance_many(sims, 3)
+    torch.cuda.synchronize()
+    # (a) the compiled loop, 10 substeps of every scene: device time by events, wall time
+    # of the enqueueing loop; the slower of the two is what the loop delivers
+    loop_sub = 10
+    a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    a.record(stream)
+    advance_many(sims, loop_sub)
+    e.record(stream)
+    t_enq = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    loop_wall = time.perf_counter() - t0
+    loop_ms = a.elapsed_time(e)
+    c_loop = n * loop_sub / max(loop_ms * 1e-3, loop_wall)
+    # (b) the same loop over `sub` substeps captured once into a CUDA graph, replayed once
+    # (a replay runs exactly the captured substeps, so the contexts stay consistent)
+    graph_rate, graph_ms, nodes = None, None, None
+    try:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream, capture_error_mode="thread_local"):
+            advance_many(sims, sub)
+        a.record(stream)
+        g.replay()
+        e.record(stream)
+        torch.cuda.synchronize()
+        graph_ms = a.elapsed_time(e)
+        graph_rate = n * sub / (graph_ms * 1e-3)
+        nodes = int(sum(s.launches for s in sims))
+        del g
+    except Exception as exc:  # report, do not hide: the compiled loop still stands
+        graph_rate = None
+        graph_ms = f"capture failed: {exc}"
+    for sim in sims:
+        sim.close()
+    looped = max(c_loop, graph_rate or 0.0)
+    return {"value": value, "unit": "particle-substeps/s", "ms_per_step": batched_ms_max / steps, "steps": steps,
+            "substeps_per_step": sub, "gpu_launches": launches,
+            "config": {"workload": "batched_256_scenes", "particles": n_all, "scenes": 256, "graph": True,
+                       "parallelism": f"scenes split over {world} ranks" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (state ~1 GB)"},
+            "looped_c_loop": {"value": c_loop, "unit": "particle-substeps/s", "device_ms": loop_ms,
+                              "wall_ms": 1e3 * loop_wall, "enqueue_ms": 1e3 * t_enq, "substeps": loop_sub,
+                              "how": "mpm_substep_many: one compiled host loop, mpm_substep(ctx, 1) per scene per "
+                                     "substep, one context per scene, one stream"},
+            "looped_graph": {"value": graph_rate, "unit": "particle-substeps/s", "device_ms": graph_ms,
+                             "substeps": sub,
+                             "how": "the same compiled loop over 50 substeps captured into one CUDA graph, replayed "
+                                    "once (device time by events)"},
+            "batched_vs_looped": local_rate / looped,
+            "looped_baseline": "the faster of looped_c_loop and looped_graph"}
+
+
 def run_batched(args):
-    """256 independent scenes (config_batched): one CUDA graph of 50 substeps per step,
-    against looping plain launches scene by scene (one context per scene)."""
     import torch
 
     from mpm_gb300 import distributed as D
@@ -368,89 +551,26 @@ def run_batched(args):
     if rank == 0 or world == 1:
         build.build()
     D.barrier()
-    from mpm_gb300 import scenes
-    from mpm_gb300.batch import Batch
-    from mpm_gb300.simulation import Simulation
-
-    all_scenes = scenes.config_batched(nscenes=256, seed=0)
-    n_all = sum(s["state"]["x"].shape[0] for s in all_scenes)
-    # scenes are independent: rank r takes scenes r, r + world, ... (no collective on the data path)
-    scs = D.shard(all_scenes, rank, world)
-    n = sum(s["state"]["x"].shape[0] for s in scs)
-    sub = 50
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    b = Batch(scs, sort_interval=16)
-    b.set_stream(stream.cuda_stream)
-    b.upload([s["state"] for s in scs])
-    for _ in range(max(args.warmup, 3)):
-        b.advance(sub, graph=True)
-    torch.cuda.synchronize()
-    D.barrier()
-    torch.cuda.synchronize()
-    steps = max(1, min(args.steps, 20))
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    l0 = b.launches
-    for a, e in ev:
-        a.record(stream)
-        b.advance(sub, graph=True)
-        e.record(stream)
-    torch.cuda.synchronize()
-    batched_ms = sum(a.elapsed_time(e) for a, e in ev)
-    local_rate = n * sub * steps / (batched_ms * 1e-3)
-    batched_ms = D.max_over_ranks(batched_ms)  # the slowest rank's share
-    launches = b.launches - l0
-    b.sync()
-    b.close()
-    value = D.job_rate(n_all * sub * steps, batched_ms * 1e-3)
-
-    # looped plain launches: one context per scene, substep by substep over the scenes
-    sims = []
-    for sc in scs:
-        sim = Simulation(materials=[sc["material"]], sort_interval=16, **sc["params"])
-        sim.set_stream(stream.cuda_stream)
-        sim.upload(sc["state"])
-        sims.append(sim)
-    for sim in sims:
-        sim.advance(3)
-    torch.cuda.synchronize()
-    loop_sub = 10
-    a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t0 = time.perf_counter()
-    a.record(stream)
-    for _ in range(loop_sub):
-        for sim in sims:
-            sim.advance(1)
-    e.record(stream)
-    torch.cuda.synchronize()
-    loop_wall = time.perf_counter() - t0
-    loop_ms = a.elapsed_time(e)
-    looped = n * loop_sub / (max(loop_ms * 1e-3, loop_wall))
-    for sim in sims:
-        sim.close()
+    sec = batched_section(args, stream, rank=rank, world=world)
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     if rank != 0:
         return
-    line = {"metric": "particle-substeps/s", "value": value, "unit": "particle-substeps/s", "n_gpus": world,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": batched_ms / steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batched_256_scenes", "particles": n_all, "scenes": 256,
-                       "parallelism": f"scenes split over {world} ranks" if world > 1 else "single",
-                       "substeps_per_step": sub, "graph": True, "l2": "inputs larger than L2 (state ~1 GB)"},
-            "looped_plain": {"value": looped, "unit": "particle-substeps/s",
-                             "how": "one context per scene of rank 0, mpm_substep(1) per scene per substep, 10 substeps"},
-            "batched_vs_looped": local_rate / looped, "gpu_launches": launches}
+    line = {"metric": "particle-substeps/s", "value": sec["value"], "unit": "particle-substeps/s", "n_gpus": world,
+            "steps": sec["steps"], "warmup": args.warmup, "ms_per_step": sec["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic"}
+    line.update({k: v for k, v in sec.items() if k not in line})
     print(json.dumps(line), flush=True)
 
 
-def run_differentiable(args):
-    """Config 5: 100k fixed-corotated particles, N=64, 256 substeps, checkpoint every 16;
-    forward (checkpointed) and backward (recompute + adjoint kernels) wall times."""
-    from mpm_gb300 import build
-
-    build.build()
+def differentiable_section(args):
+    """The differentiable workload (100,000 fixed-corotated particles, N = 64, 256
+    substeps, a checkpoint every 16): the checkpointed forward and the backward
+    (recompute of each segment + adjoint kernels), wall clock around the blocking
+    mpm_diff_forward / mpm_diff_backward calls."""
     import torch
 
     from mpm_gb300 import scenes
@@ -476,16 +596,25 @@ def run_differentiable(args):
             fw.append(t1 - t0)
             bw.append(t3 - t2)
     sim.close()
-    f, b = statistics.median(fw), statistics.median(bw)
     torch.cuda.synchronize()
-    line = {"metric": "particle-substeps/s", "value": n * nsteps / f, "unit": "particle-substeps/s", "n_gpus": 1,
-            "steps": len(fw), "warmup": args.warmup, "ms_per_step": 1e3 * f / nsteps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+    f, b = statistics.median(fw), statistics.median(bw)
+    return {"value": n * nsteps / f, "unit": "particle-substeps/s", "forward_s": f, "backward_s": b,
+            "bwd_fwd_ratio": b / f, "steps": len(fw),
             "config": {"workload": "differentiable_100k_N64_256", "particles": n, "N": 64, "substeps": nsteps,
                        "checkpoint_every": 16},
-            "forward_s": f, "backward_s": b, "bwd_fwd_ratio": b / f,
-            "timing": "wall clock around the blocking mpm_diff_forward / mpm_diff_backward calls (host copies of the "
-                      "initial state and of the gradients included)"}
+            "timing": "wall clock around the blocking mpm_diff_forward / mpm_diff_backward calls (host copies of "
+                      "the initial state and of the gradients included)"}
+
+
+def run_differentiable(args):
+    from mpm_gb300 import build
+
+    build.build()
+    sec = differentiable_section(args)
+    line = {"metric": "particle-substeps/s", "value": sec["value"], "unit": "particle-substeps/s", "n_gpus": 1,
+            "steps": sec["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * sec["forward_s"] / 256,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic"}
+    line.update({k: v for k, v in sec.items() if k not in line})
     print(json.dumps(line), flush=True)
 
 

@@ -134,6 +134,12 @@ mpm_status mpm_get_grid(mpm_ctx* ctx, int32_t which, float* out);
 /* Re-sort particles by cell now (also done every sort_interval substeps). */
 mpm_status mpm_sort(mpm_ctx* ctx);
 
+/* Simulation::advance over several independent scenes: nsteps substeps of each of the
+ * `count` contexts, interleaved substep by substep, from one compiled host loop (the loop a
+ * C++ caller of the reference writes over its Simulation objects, src/mpm.cu:323-329).
+ * Asynchronous like mpm_substep; stops at the first failing context and returns its status. */
+mpm_status mpm_substep_many(mpm_ctx* const* ctxs, int32_t count, int32_t nsteps);
+
 /* Simulation::getFullParticleCount (src/mpm.cu:253-259). */
 int64_t mpm_particle_count(const mpm_ctx* ctx);
 /* Number of substeps advanced since the last upload. */

@@ -110,6 +110,7 @@ SIGNATURES = [
     ("mpm_last_error", I32, [P, ctypes.c_char_p, ctypes.c_size_t]),
     ("mpm_launch_count", I64, [P]),
     ("mpm_set_tuning", I32, [P, I32, I32, I32]),
+    ("mpm_substep_many", I32, [ctypes.POINTER(P), I32, I32]),
     ("mpm_batch_create", I32, [ctypes.POINTER(MpmScene), I32, I32, ctypes.POINTER(P)]),
     ("mpm_batch_destroy", I32, [P]),
     ("mpm_batch_set_stream", I32, [P, P]),

@@ -1162,6 +1162,18 @@ mpm_status mpm_sort(mpm_ctx* c) {
   return run_sort(c);
 }
 
+mpm_status mpm_substep_many(mpm_ctx* const* ctxs, int32_t count, int32_t nsteps) {
+  if (!ctxs || count < 0 || nsteps < 0) return MPM_ERR_INVALID;
+  for (int32_t i = 0; i < count; ++i)
+    if (!ctxs[i]) return MPM_ERR_INVALID;
+  for (int32_t s = 0; s < nsteps; ++s)
+    for (int32_t i = 0; i < count; ++i) {
+      const mpm_status st = mpm_substep(ctxs[i], 1);
+      if (st != MPM_OK) return st;
+    }
+  return MPM_OK;
+}
+
 int64_t mpm_particle_count(const mpm_ctx* c) { return c ? c->n : -1; }
 int64_t mpm_substep_count(const mpm_ctx* c) { return c ? c->substeps : -1; }
 int64_t mpm_launch_count(const mpm_ctx* c) { return c ? c->launches : -1; }

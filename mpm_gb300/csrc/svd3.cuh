@@ -23,10 +23,19 @@ struct Mat3 {
   __device__ __forceinline__ float operator()(int r, int c) const { return m[3 * r + c]; }
 };
 
+// Hardware reciprocal square root refined by one Newton step in residual form:
+// y1 = y + (y / 2) e with e = 1 - x y^2 evaluated by an FMA, so the correction is carried
+// in a small number at full relative precision.  The product form y (1.5 - x y^2 / 2)
+// rounds its factor near 1.0, where the float grid is coarse; that left a systematic
+// error in the quaternion and Givens normalisations, so U and V came out slightly
+// non-orthonormal in one direction.  Through det(U clamp(S) V^T) it drifted snow's Jp by
+// 3e-7 per substep (1.7e-4 over 500 substeps against the FP64 oracle) and biased F - R
+// in the elastic stress (2.3e-3 in dL/dE over 256 substeps).  With the residual form the
+// drift is the FP32 oracle's (1.6e-5 over 500 substeps) at the same speed.
 __device__ __forceinline__ float rsqrt_nr(float x) {
-  // hardware reciprocal square root refined by one Newton step
-  float y = rsqrtf(x);
-  return y * fmaf(-0.5f * x * y, y, 1.5f);
+  const float y = rsqrtf(x);
+  const float e = fmaf(-(x * y), y, 1.0f);
+  return fmaf(0.5f * y, e, y);
 }
 
 __device__ __forceinline__ void jacobi_half_angle(float app, float apq, float aqq, float& ch, float& sh) {

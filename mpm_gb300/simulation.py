@@ -241,3 +241,21 @@ class Simulation:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def advance_many(sims, nsteps: int = 1):
+    """Simulation::advance over several independent scenes: nsteps substeps of every
+    simulation, interleaved substep by substep, in one compiled loop (mpm_substep_many)."""
+    sims = list(sims)
+    if not sims:
+        return
+    L = sims[0].L
+    arr = (ctypes.c_void_p * len(sims))(*[s.ctx.value for s in sims])
+    code = L.mpm_substep_many(arr, len(sims), int(nsteps))
+    if code != 0:
+        for s in sims:  # report the context that failed, when it recorded a message
+            buf = ctypes.create_string_buffer(512)
+            L.mpm_last_error(s.ctx, buf, 512)
+            if buf.value:
+                raise _lib.MpmError(code, buf.value.decode(errors="replace"))
+        raise _lib.MpmError(code, "mpm_substep_many failed")

@@ -1,5 +1,9 @@
-"""GPU tests of the hand-written adjoint (mpm_diff_*): gradients of
-L = ||COM(x_final) - target||^2 w.r.t. the initial velocities and positions and E, nu,
+"""GPU tests of the hand-written adjoint (mpm_diff_*): gradients w.r.t. the initial
+velocities and positions and E, nu of two losses of the final positions,
+  L  = ||COM(x_final) - target||^2   (the differentiable workload's loss), and
+  L2 = mean ||x_final - COM||^2      (the spread, which depends on E and nu: the COM of a
+                                      body clear of the walls does not, since P2G and G2P
+                                      conserve momentum, so dL/dE = dL/dnu = 0),
 against (1) autograd through the dense float64 torch substep (tests/dense_mpm.py) and
 (2) central finite differences of the FP64 CPU oracle.  Bar: 1e-3 relative."""
 import numpy as np
@@ -20,25 +24,40 @@ def small_case(n=300, seed=5, N=16):
     return cfg
 
 
-def loss_grad_x(x):
-    com = x.astype(np.float64).mean(0)
+def loss_grad_x(x, loss="com"):
+    """dL/dx_final and L for the COM loss or the spread."""
+    x = x.astype(np.float64)
+    com = x.mean(0)
+    if loss == "spread":
+        return 2.0 * (x - com) / x.shape[0], float(((x - com) ** 2).sum(1).mean())
     return np.tile(2.0 * (com - TARGET) / x.shape[0], (x.shape[0], 1)), float(((com - TARGET) ** 2).sum())
 
 
-def gpu_grads(cfg, nsteps, ckpt):
+def sheared_case(n=300, seed=5, N=16):
+    """The small case with a coherent initial velocity (a shear plus a compression of the
+    body, ~2/s): strains reach ~1e-2 within the run, so the elastic constants move the
+    spread well above FP32 rounding."""
+    cfg = small_case(n, seed, N)
+    x = cfg["state"]["x"].astype(np.float64)
+    G = np.array([[-1.0, 2.0, 0.0], [0.5, -1.5, 0.0], [0.0, 1.0, -2.0]])
+    cfg["state"]["v"] = (cfg["state"]["v"] + (x - x.mean(0)) @ G.T).astype(np.float32)
+    return cfg
+
+
+def gpu_grads(cfg, nsteps, ckpt, loss="com"):
     from mpm_gb300.autograd import DiffSim, lame_grad
 
     m = cfg["materials"][0]
     sim = DiffSim(cfg["params"], m, cfg["state"]["x"].shape[0], nsteps, ckpt)
     xo, _ = sim.forward(cfg["state"], nsteps)
-    gx, L = loss_grad_x(xo)
+    gx, L = loss_grad_x(xo, loss)
     g = sim.backward(gx)
     g["E"], g["nu"] = lame_grad(m.E, m.nu, g["mu0"], g["lambda0"])
     sim.close()
     return g, L
 
 
-def dense_grads(cfg, nsteps):
+def dense_grads(cfg, nsteps, loss="com"):
     st = cfg["state"]
     m = cfg["materials"][0]
     d = m.derived()
@@ -50,7 +69,10 @@ def dense_grads(cfg, nsteps):
     E = torch.tensor(float(m.E), dtype=torch.float64, requires_grad=True)
     nu = torch.tensor(float(m.nu), dtype=torch.float64, requires_grad=True)
     x, _, _, _ = dense_mpm.rollout(x0, v0, t(st["C"]), t(st["F"]), t(st["Jp"]), E, nu, P, nsteps)
-    L = ((x.mean(0) - torch.tensor(TARGET)) ** 2).sum()
+    if loss == "spread":
+        L = ((x - x.mean(0)) ** 2).sum(1).mean()
+    else:
+        L = ((x.mean(0) - torch.tensor(TARGET)) ** 2).sum()
     gx, gv, gE, gnu = torch.autograd.grad(L, (x0, v0, E, nu))
     return {"x": gx.numpy(), "v": gv.numpy(), "E": float(gE), "nu": float(gnu)}, float(L)
 
@@ -69,29 +91,46 @@ def test_adjoint_matches_dense_autograd(gpu_lib, nsteps, ckpt):
     assert abs(L - Lr) < 1e-5 * Lr
     assert rel(g["v"], r["v"]) < 1e-3, rel(g["v"], r["v"])
     assert rel(g["x"], r["x"]) < 1e-3, rel(g["x"], r["x"])
-    assert abs(g["E"] - r["E"]) < 1e-3 * abs(r["E"]) + 1e-12, (g["E"], r["E"])
-    assert abs(g["nu"] - r["nu"]) < 1e-3 * abs(r["nu"]) + 1e-12, (g["nu"], r["nu"])
+    # the COM loss does not depend on E or nu: both sides vanish
+    assert abs(g["E"]) < 1e-9 * abs(Lr) and abs(r["E"]) < 1e-9 * abs(Lr), (g["E"], r["E"])
+
+
+@pytest.mark.parametrize("nsteps,ckpt", [(8, 3), (24, 8)])
+def test_elastic_constant_gradients_match_dense_autograd(gpu_lib, nsteps, ckpt):
+    """dL2/dE and dL2/dnu of the spread of a sheared body, and its dL2/dx0, dL2/dv0, against
+    autograd through the dense float64 substep; the gradients are far from zero."""
+    cfg = sheared_case()
+    g, L = gpu_grads(cfg, nsteps, ckpt, "spread")
+    r, Lr = dense_grads(cfg, nsteps, "spread")
+    assert abs(L - Lr) < 1e-5 * Lr
+    m = cfg["materials"][0]
+    # the constants matter: a 1% change of E moves the spread by more than 1e-7 of itself
+    assert abs(r["E"]) * 0.01 * m.E > 1e-7 * Lr, (r["E"], Lr)
+    assert abs(g["E"] - r["E"]) < 1e-3 * abs(r["E"]), (g["E"], r["E"])
+    assert abs(g["nu"] - r["nu"]) < 1e-3 * abs(r["nu"]), (g["nu"], r["nu"])
+    assert rel(g["v"], r["v"]) < 1e-3, rel(g["v"], r["v"])
+    assert rel(g["x"], r["x"]) < 1e-3, rel(g["x"], r["x"])
 
 
 def test_adjoint_matches_fp64_finite_differences(gpu_lib, oracle_lib):
-    """Directional derivatives along random velocity perturbations, and dL/dE, dL/dnu,
-    against central differences of the FP64 oracle."""
+    """Directional derivatives of the COM loss along random velocity perturbations, and
+    dL2/dE, dL2/dnu of the spread of a sheared body, against central differences of the
+    FP64 oracle."""
     cfg = small_case(n=2000, seed=6)
     nsteps = 12
     g, _ = gpu_grads(cfg, nsteps, 4)
     st = cfg["state"]
     m = cfg["materials"][0]
 
-    def L_of(v0=None, E=None, nu=None):
+    def L_of(v0=None, E=None, nu=None, state=None, loss="com"):
         from mpm_gb300 import materials as M
 
         mm = M.fixed_corotated(m.particle_volume, m.density, E if E is not None else m.E, nu if nu is not None else m.nu)
-        s = dict(st)
+        s = dict(state if state is not None else st)
         if v0 is not None:
             s["v"] = v0
         out, _, _ = oracle_lib.substep(s, cfg["params"], [mm.derived()], nsteps, np.float64)
-        com = out["x"].mean(0)
-        return float(((com - TARGET) ** 2).sum())
+        return loss_grad_x(out["x"], loss)[1]
 
     rng = np.random.default_rng(0)
     v0 = st["v"].astype(np.float64)
@@ -101,10 +140,13 @@ def test_adjoint_matches_fp64_finite_differences(gpu_lib, oracle_lib):
         fd = (L_of(v0=v0 + eps * u) - L_of(v0=v0 - eps * u)) / (2 * eps)
         ad = float((g["v"].astype(np.float64) * u).sum())
         assert abs(ad - fd) < 1e-3 * abs(fd) + 1e-12, (ad, fd)
+    sh = sheared_case(n=2000, seed=6)
+    g2, _ = gpu_grads(sh, nsteps, 4, "spread")
     for name, val in (("E", m.E), ("nu", m.nu)):
         h = 1e-3 * val
-        fd = (L_of(**{name: val + h}) - L_of(**{name: val - h})) / (2 * h)
-        assert abs(g[name] - fd) < 1e-3 * abs(fd) + 1e-12, (name, g[name], fd)
+        fd = (L_of(**{name: val + h}, state=sh["state"], loss="spread") -
+              L_of(**{name: val - h}, state=sh["state"], loss="spread")) / (2 * h)
+        assert abs(g2[name] - fd) < 1e-3 * abs(fd), (name, g2[name], fd)
 
 
 def test_autograd_function(gpu_lib):
@@ -127,33 +169,66 @@ def test_autograd_function(gpu_lib):
     sim.close()
 
 
-def test_full_size_differentiable_config(gpu_lib):
-    """100k particles, N=64, 256 substeps, checkpoint every 16: the gradient is finite
-    and its directional derivative matches the GPU forward's central difference."""
+def test_full_size_differentiable_config(gpu_lib, oracle_lib):
+    """The differentiable workload in full: 100,000 fixed-corotated particles, N = 64, 256
+    substeps, a checkpoint every 16.  The GPU adjoint (FP32 forward, hand-written adjoint
+    kernels) against central differences of the FP64 oracle, bar 1e-3 relative:
+      * dL/dv0 of the workload's loss L = ||COM(x_final) - (0.6, 0.3, 0.5)||^2 along two
+        seeded directions (a common drift plus noise, and pure noise);
+      * dL2/dE and dL2/dnu of the spread L2 = mean ||x_final - COM||^2.  The COM loss does
+        not depend on E or nu while the body flies clear of the walls (P2G and G2P conserve
+        momentum, so the COM follows the initial mean velocity and gravity): its dL/dE and
+        dL/dnu vanish up to rounding.  Both the adjoint's and the finite difference's are
+        checked to be negligible: relative to L, below 1e-3 of the spread's relative
+        sensitivity (dL2/dE) / L2."""
+    from mpm_gb300 import materials as M
     from mpm_gb300 import scenes
-    from mpm_gb300.autograd import DiffSim
+    from mpm_gb300.autograd import DiffSim, lame_grad
 
     cfg = scenes.config_differentiable()
     st = cfg["state"]
     n = st["x"].shape[0]
-    sim = DiffSim(cfg["params"], cfg["materials"][0], n, 256, 16)
-    xo, _ = sim.forward(st, 256)
+    nsteps = 256
+    assert n == 100_000 and cfg["params"]["N"] == 64 and cfg["checkpoint_every"] == 16
+    m = cfg["materials"][0]
+    sim = DiffSim(cfg["params"], m, n, nsteps, 16)
+    xo, _ = sim.forward(st, nsteps)
     gx, L = loss_grad_x(xo)
     g = sim.backward(gx)
     assert np.isfinite(g["v"]).all() and np.isfinite(g["x"]).all()
-    rng = np.random.default_rng(1)
-    # a common drift plus noise: the loss sees the centre of mass, so the common part
-    # gives a finite difference well above FP32 rounding
-    u = (np.array([1.0, 0.5, -0.3]) + 0.1 * rng.standard_normal(st["v"].shape)).astype(np.float32)
-    eps = 2e-2
-
-    def L_of(v):
-        s = dict(st)
-        s["v"] = v
-        x, _ = sim.forward(s, 256)
-        return loss_grad_x(x)[1]
-
-    fd = (L_of(st["v"] + eps * u) - L_of(st["v"] - eps * u)) / (2 * eps)
-    ad = float((g["v"].astype(np.float64) * u).sum())
-    assert abs(ad - fd) < 2e-2 * abs(fd), (ad, fd)
+    gE, gnu = lame_grad(m.E, m.nu, g["mu0"], g["lambda0"])
+    x64 = xo.astype(np.float64)
+    com = x64.mean(0)
+    g2 = sim.backward(2.0 * (x64 - com) / n)
+    g2E, g2nu = lame_grad(m.E, m.nu, g2["mu0"], g2["lambda0"])
     sim.close()
+
+    def run(v0=None, E=None, nu=None):
+        mm = M.fixed_corotated(m.particle_volume, m.density, E if E is not None else m.E,
+                               nu if nu is not None else m.nu)
+        s = dict(st)
+        if v0 is not None:
+            s["v"] = v0
+        out, _, _ = oracle_lib.substep(s, cfg["params"], [mm.derived()], nsteps, np.float64)
+        x = out["x"]
+        c = x.mean(0)
+        return float(((c - TARGET) ** 2).sum()), float(((x - c) ** 2).sum(1).mean())
+
+    rng = np.random.default_rng(1)
+    v0 = st["v"].astype(np.float64)
+    dirs = [np.array([1.0, 0.5, -0.3]) + 0.1 * rng.standard_normal(v0.shape), rng.standard_normal(v0.shape)]
+    for u in dirs:
+        eps = 1e-3
+        fd = (run(v0=v0 + eps * u)[0] - run(v0=v0 - eps * u)[0]) / (2 * eps)
+        ad = float((g["v"].astype(np.float64) * u).sum())
+        assert abs(ad - fd) < 1e-3 * abs(fd), (ad, fd)
+    L2 = float(((x64 - com) ** 2).sum(1).mean())
+    for name, val, ad2, ad1 in (("E", m.E, g2E, gE), ("nu", m.nu, g2nu, gnu)):
+        h = 1e-3 * val
+        lp, lm = run(**{name: val + h}), run(**{name: val - h})
+        fd2 = (lp[1] - lm[1]) / (2 * h)
+        print(f"{name}: spread adjoint {ad2:.6e} fd {fd2:.6e}; COM adjoint {ad1:.3e} fd {(lp[0] - lm[0]) / (2 * h):.3e}")
+        assert abs(ad2 - fd2) < 1e-3 * abs(fd2), (name, ad2, fd2)
+        fd1 = (lp[0] - lm[0]) / (2 * h)
+        negligible = 1e-3 * abs(fd2) / L2 * L
+        assert abs(fd1) < negligible and abs(ad1) < negligible, (name, ad1, fd1, negligible)
