@@ -288,12 +288,56 @@ mpm_status mpm_last_error(const mpm_ctx* ctx, char* buf, size_t len);
 /* Kernel launches issued by this context since creation (for accounting). */
 int64_t mpm_launch_count(const mpm_ctx* ctx);
 
-/* Tuning knob of the fused substep kernel: steps_per_warp, the largest number of
- * 32-particle steps in each range a warp claims (1..256, default 2; 0 keeps the current
- * value); it is halved while each warp would get fewer than 6 ranges.
- * reserved1, reserved2: must be >= 0; ignored (the grid tile is a fixed TMA box and
- * the launch is sized by occupancy). */
-mpm_status mpm_set_tuning(mpm_ctx* ctx, int32_t steps_per_warp, int32_t reserved1, int32_t reserved2);
+/* G2P tile boxes of the fused substep kernel (grid nodes along i x j x k): a box covers
+ * the steps whose 32 particles' base cells span at most (box - 2) cells per dimension;
+ * other steps gather straight from the velocity grid. */
+enum {
+  MPM_TILE_4x4x6 = 1, /* the default: one cell, or two neighbours along a sort-brick row */
+  MPM_TILE_4x4x4 = 2, /* a third fewer bytes per copy, for steps within 2 x 2 x 2 cells */
+  MPM_TILE_4x6x6 = 3  /* also steps across a brick's rows, for sparse scenes (12 warps) */
+};
+/* Tuning knobs of the fused substep kernel (the reference launches a fixed 64-thread
+ * block per 64 particles, src/mpm.cu:217-222):
+ *   steps_per_warp: the largest number of 32-particle steps in each range a warp claims
+ *     (1..256, default 2); it is halved while each warp would get fewer than 6 ranges;
+ *   warps_per_cta: CTA size of the fused kernel, 4, 6 or 12 warps (3, 2 or 1 CTAs per SM,
+ *     12 warps resident either way; default 12);
+ *   tile_box: MPM_TILE_* (the 4x4x4 and 4x6x6 boxes need 12 warps per CTA).
+ * 0 keeps a knob's current value.  Results do not depend on the knobs beyond rounding
+ * (the order of the grid's float additions). */
+mpm_status mpm_set_tuning(mpm_ctx* ctx, int32_t steps_per_warp, int32_t warps_per_cta, int32_t tile_box);
+
+/* A launch shape of the fused substep kernel (and the sort interval it was measured with). */
+typedef struct mpm_tuning {
+  int32_t steps_per_warp;
+  int32_t warps_per_cta;
+  int32_t tile_box;       /* MPM_TILE_* */
+  int32_t sort_interval;
+  double us_per_substep;  /* measured device time of one substep with this shape (0: not measured) */
+  int32_t from_cache;     /* 1: taken from the cache file without measuring */
+  int32_t candidates;     /* shapes timed by the search */
+} mpm_tuning;
+
+enum {
+  MPM_TUNE_SORT_INTERVAL = 1, /* also choose the sort interval (it then replaces params.sort_interval) */
+  MPM_TUNE_IGNORE_CACHE = 2   /* measure even when the cache holds an entry (and replace it) */
+};
+
+/* Autotuner (no counterpart in the reference, whose launch shape is fixed,
+ * src/mpm.cu:217-222): chooses the fused substep's steps per warp, CTA size and tile box
+ * (and, with MPM_TUNE_SORT_INTERVAL, the sort interval) for the context's current scene and
+ * applies them.  The search is a coordinate descent over those knobs; each candidate is timed
+ * with CUDA events over budget_substeps substeps (0: 48; sort intervals over at least two of
+ * their periods) on a temporary copy of the context's particles, so the context's own state
+ * does not change.  With a cache_path (a JSON file; NULL: no cache), a shape found for the
+ * same device, library build and workload class (particle layout, N, particle count to the
+ * nearest power of two, material kinds) is reused without measuring, and a new one is
+ * stored.  *out (may be NULL) receives the chosen shape.  Synchronises; allocates a copy of
+ * the particle arrays while it runs. */
+mpm_status mpm_autotune(mpm_ctx* ctx, const char* cache_path, int32_t flags, int32_t budget_substeps,
+                        mpm_tuning* out);
+/* The context's current launch shape (us_per_substep, from_cache and candidates are 0). */
+mpm_status mpm_get_tuning(const mpm_ctx* ctx, mpm_tuning* out);
 
 /* ---------------------------------------------------------------------------
  * Batched scenes.  The reference runs one scene per Simulation; a batch advances many

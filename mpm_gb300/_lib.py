@@ -68,6 +68,22 @@ class MpmObject(ctypes.Structure):
     ]
 
 
+TILE_4x4x6, TILE_4x4x4, TILE_4x6x6 = 1, 2, 3
+TUNE_SORT_INTERVAL, TUNE_IGNORE_CACHE = 1, 2
+
+
+class MpmTuning(ctypes.Structure):
+    _fields_ = [
+        ("steps_per_warp", ctypes.c_int32),
+        ("warps_per_cta", ctypes.c_int32),
+        ("tile_box", ctypes.c_int32),
+        ("sort_interval", ctypes.c_int32),
+        ("us_per_substep", ctypes.c_double),
+        ("from_cache", ctypes.c_int32),
+        ("candidates", ctypes.c_int32),
+    ]
+
+
 # (name, restype, argtypes) for every entry point of include/mpm_gb300.h
 P = ctypes.c_void_p
 I32, I64 = ctypes.c_int32, ctypes.c_int64
@@ -111,6 +127,8 @@ SIGNATURES = [
     ("mpm_launch_count", I64, [P]),
     ("mpm_set_tuning", I32, [P, I32, I32, I32]),
     ("mpm_substep_many", I32, [ctypes.POINTER(P), I32, I32]),
+    ("mpm_autotune", I32, [P, ctypes.c_char_p, I32, I32, ctypes.POINTER(MpmTuning)]),
+    ("mpm_get_tuning", I32, [P, ctypes.POINTER(MpmTuning)]),
     ("mpm_batch_create", I32, [ctypes.POINTER(MpmScene), I32, I32, ctypes.POINTER(P)]),
     ("mpm_batch_destroy", I32, [P]),
     ("mpm_batch_set_stream", I32, [P, P]),

@@ -453,7 +453,8 @@ mpm_status dlaunch(mpm_diff* d, StepKind kind, float* state, const float4* gin, 
   int chunk = 0, blocks = 0;
   step_launch_shape(d->num_sms, d->n, false, false, kind, 2, chunk, blocks);
   a.chunk = chunk;
-  if (launch_step(a, kind, false, false, blocks, d->stream) != cudaSuccess) return MPM_ERR_CUDA;
+  if (launch_step(a, kind, false, false, blocks, d->stream, nullptr, StepTuning{kStepWarps, 0}, &d->vel) != cudaSuccess)
+    return MPM_ERR_CUDA;
   return MPM_OK;
 }
 
@@ -587,7 +588,8 @@ mpm_status mpm_diff_forward(mpm_diff* d, const float* x0, const float* v0, const
     int chunk = 0, blocks = 0;
     step_launch_shape(d->num_sms, n, false, false, kStepFused, 2, chunk, blocks);
     a.chunk = chunk;
-    if (launch_step(a, kStepFused, false, false, blocks, s) != cudaSuccess) return MPM_ERR_CUDA;
+    if (launch_step(a, kStepFused, false, false, blocks, s, nullptr, StepTuning{kStepWarps, 0}, &d->vel) != cudaSuccess)
+      return MPM_ERR_CUDA;
     cur = (cur + 1) % 3;
     if ((i + 1) % d->ckpt_every == 0 && i + 1 < nsteps)
       if (cudaMemcpyAsync(d->ckpt + state_floats(d) * ((i + 1) / d->ckpt_every), work, sb, cudaMemcpyDeviceToDevice,

@@ -16,6 +16,7 @@
 #include "seeding.h"
 #include "surface.h"
 #include "export.h"
+#include "tuning_cache.h"
 
 using namespace mpm;
 
@@ -82,6 +83,7 @@ struct mpm_ctx {
   int64_t since_sort = 0;
   int64_t launches = 0;
   int steps_per_warp = 2;
+  StepTuning tuning{kStepWarps, 0};  // launch shape of the fused substep kernel
   std::string last_error;
 
   double t = 0.0;  // simulated time (Simulation::t)
@@ -340,7 +342,7 @@ StepArgs make_step_args(mpm_ctx* c) {
 }
 
 void launch_shape(mpm_ctx* c, StepKind kind, bool guard, int& chunk, int& blocks) {
-  mpm::step_launch_shape(c->num_sms, c->n, c->liquid_layout, guard, kind, c->steps_per_warp, chunk, blocks);
+  mpm::step_launch_shape(c->num_sms, c->n, c->liquid_layout, guard, kind, c->steps_per_warp, chunk, blocks, c->tuning);
 }
 
 mpm_status run_step(mpm_ctx* c, StepKind kind) {
@@ -353,7 +355,7 @@ mpm_status run_step(mpm_ctx* c, StepKind kind) {
   a.grid_in = (kind == kStepP2GOnly) ? nullptr : c->grid[r];
   a.grid_out = c->grid[(r + 1) % 3];
   a.grid_zero = c->grid[(r + 2) % 3];
-  MPM_CUDA(c, launch_step(a, kind, c->liquid_layout, guard, blocks, c->stream, &c->launches));
+  MPM_CUDA(c, launch_step(a, kind, c->liquid_layout, guard, blocks, c->stream, &c->launches, c->tuning, &c->vel));
   if (kind != kStepP2GOnly) c->prev = r;
   c->cur = (r + 1) % 3;
   c->pending = kind != kStepG2POnly;
@@ -441,16 +443,17 @@ void make_dev_material(const mpm_material& m, DevMaterial& d) {
 // fewer, coarser ranges the warps finish unevenly (a 500k-particle snow substep ran 6%
 // faster with 1-step than with 2-step ranges).
 void step_launch_shape(int num_sms, int64_t n, bool liquid, bool guard, StepKind kind, int steps_per_warp,
-                       int& chunk, int& blocks) {
-  const size_t smem = step_smem_bytes(kind, false);
-  const int bps = step_blocks_per_sm(kind, liquid, guard, smem);
-  const int64_t resident_warps = (int64_t)num_sms * bps * kStepWarps;
+                       int& chunk, int& blocks, StepTuning want) {
+  const StepTuning t = step_tuning(kind, guard, false, want);
+  const int warps = t.warps;
+  const size_t smem = step_smem_bytes(kind, false, t);
+  const int bps = step_blocks_per_sm(kind, liquid, guard, smem, false, t);
+  const int64_t resident_warps = (int64_t)num_sms * bps * warps;
   int64_t steps = steps_per_warp;
   while (steps > 1 && n < resident_warps * 32 * steps * 6) steps /= 2;
   chunk = (int)(steps * 32);
   const int64_t nranges = (n + chunk - 1) / chunk;
-  blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nranges + kStepWarps - 1) / kStepWarps,
-                                                       (int64_t)num_sms * bps));
+  blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nranges + warps - 1) / warps, (int64_t)num_sms * bps));
 }
 
 }  // namespace mpm
@@ -1184,11 +1187,261 @@ mpm_status mpm_last_error(const mpm_ctx* c, char* buf, size_t len) {
   return MPM_OK;
 }
 
-mpm_status mpm_set_tuning(mpm_ctx* c, int32_t steps_per_warp, int32_t reserved1, int32_t reserved2) {
+mpm_status mpm_set_tuning(mpm_ctx* c, int32_t steps_per_warp, int32_t warps_per_cta, int32_t tile_box) {
   if (!c) return MPM_ERR_INVALID;
   if (steps_per_warp < 0 || steps_per_warp > 256) return fail(c, MPM_ERR_INVALID, "steps_per_warp out of range");
-  if (reserved1 < 0 || reserved2 < 0) return fail(c, MPM_ERR_INVALID, "reserved arguments must be >= 0");
+  if (warps_per_cta != 0 && warps_per_cta != 4 && warps_per_cta != 6 && warps_per_cta != 12)
+    return fail(c, MPM_ERR_INVALID, "warps_per_cta must be 4, 6 or 12 (0 keeps the current value)");
+  if (tile_box < 0 || tile_box > MPM_TILE_4x6x6)
+    return fail(c, MPM_ERR_INVALID, "tile_box must be one of MPM_TILE_* (0 keeps the default box)");
+  StepTuning t = c->tuning;
+  if (warps_per_cta) t.warps = warps_per_cta;
+  if (tile_box) t.tile = tile_box - 1;
+  if (t.tile != 0 && t.warps != kStepWarps)
+    return fail(c, MPM_ERR_INVALID, "the 4x4x4 and 4x6x6 tile boxes run with 12 warps per CTA");
   if (steps_per_warp) c->steps_per_warp = steps_per_warp;
+  c->tuning = t;
+  return MPM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner.  The reference launches a fixed 64-thread block per 64 particles
+// (src/mpm.cu:217-222); here the fused kernel's launch shape is searched per workload
+// class on a clone of the caller's scene, so the caller's state is not touched.
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+struct TuneCandidate {
+  int spw, warps, tile_box, sort;  // tile_box: MPM_TILE_*
+};
+
+std::string device_key(int dev) {
+  cudaDeviceProp p{};
+  if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return "unknown device";
+  char b[320];
+  std::snprintf(b, sizeof(b), "%s (%d SMs, cc %d.%d)", p.name, p.multiProcessorCount, p.major, p.minor);
+  return b;
+}
+
+// Changes with every build of this file, so a rebuilt library measures again.
+const char* build_key() { return "mpm_gb300 " __DATE__ " " __TIME__; }
+
+// Workload class: particle layout, grid size, particle count to the nearest power of two,
+// and the material kinds present.
+std::string class_key(const mpm_ctx* c) {
+  unsigned kinds = 0;
+  for (int i = 0; i < c->n_materials; ++i) kinds |= 1u << c->mats[i].kind;
+  const int lg = c->n > 0 ? (int)std::lround(std::log2((double)c->n)) : 0;
+  char b[160];
+  std::snprintf(b, sizeof(b), "%s N=%u n~2^%d kinds=0x%x", c->liquid_layout ? "liquid" : "general", c->params.N, lg,
+                kinds);
+  return b;
+}
+
+// A context with the caller's parameters, materials and particle arrays (copied on the
+// device), for timing launch shapes.
+mpm_status tuning_clone(mpm_ctx* c, mpm_ctx** out) {
+  mpm_ctx* t = nullptr;
+  mpm_status st = mpm_create(&c->params, &t);
+  if (st != MPM_OK) return st;
+  st = mpm_set_materials(t, c->mats, c->n_materials);
+  if (st == MPM_OK) st = ensure_particles(t, c->n);
+  if (st != MPM_OK) {
+    mpm_destroy(t);
+    return st;
+  }
+  *out = t;
+  return MPM_OK;
+}
+
+// Resets the clone to the caller's current particles.
+mpm_status tuning_restore(mpm_ctx* c, mpm_ctx* t) {
+  MPM_CUDA(c, cudaMemcpy2DAsync(t->sA, sizeof(float) * t->stride, c->sA, sizeof(float) * c->stride,
+                                sizeof(float) * c->n, kNumComps, cudaMemcpyDeviceToDevice, t->stream));
+  if (c->have_mat) MPM_CUDA(c, cudaMemcpyAsync(t->matA, c->matA, c->n, cudaMemcpyDeviceToDevice, t->stream));
+  MPM_CUDA(c, cudaMemcpyAsync(t->idA, c->idA, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToDevice, t->stream));
+  t->n = c->n;
+  t->have_mat = c->have_mat;
+  t->unsorted = c->unsorted;
+  t->pending = false;
+  t->tail_g2p = t->ended_g2p = false;
+  t->prev = -1;
+  t->substeps = 0;
+  t->t = 0.0;
+  return MPM_OK;
+}
+
+// Mean device time of one substep (microseconds) with candidate k: `warm` substeps (the
+// run's first P2G and, with sorting, a sort), then `steps` timed substeps.
+mpm_status time_candidate(mpm_ctx* c, mpm_ctx* t, const TuneCandidate& k, int warm, int steps, cudaEvent_t e0,
+                          cudaEvent_t e1, double* us) {
+  mpm_status st = tuning_restore(c, t);
+  if (st != MPM_OK) return st;
+  t->steps_per_warp = k.spw;
+  t->tuning = StepTuning{k.warps, k.tile_box - 1};
+  t->params.sort_interval = k.sort;
+  t->since_sort = k.sort;  // sort first, as after an upload
+  st = mpm_substep(t, warm);
+  if (st != MPM_OK) return fail(c, st, "tuning: " + t->last_error);
+  MPM_CUDA(c, cudaEventRecord(e0, t->stream));
+  st = mpm_substep(t, steps);
+  if (st != MPM_OK) return fail(c, st, "tuning: " + t->last_error);
+  MPM_CUDA(c, cudaEventRecord(e1, t->stream));
+  st = mpm_sync(t);
+  if (st != MPM_OK) return fail(c, st, "tuning: " + t->last_error);
+  float ms = 0.f;
+  MPM_CUDA(c, cudaEventElapsedTime(&ms, e0, e1));
+  *us = 1e3 * (double)ms / steps;
+  return MPM_OK;
+}
+
+void apply_tuning(mpm_ctx* c, const TuneCandidate& k, bool with_sort) {
+  c->steps_per_warp = k.spw;
+  c->tuning = StepTuning{k.warps, k.tile_box - 1};
+  if (with_sort) c->params.sort_interval = k.sort;
+}
+
+}  // namespace
+
+extern "C" {
+
+mpm_status mpm_autotune(mpm_ctx* c, const char* cache_path, int32_t flags, int32_t budget_substeps,
+                        mpm_tuning* out) {
+  mpm_status st = check_ready(c);
+  if (st != MPM_OK) return st;
+  if (c->n <= 0) return fail(c, MPM_ERR_INVALID, "autotune needs uploaded particles");
+  if (budget_substeps < 0 || budget_substeps > 4096) return fail(c, MPM_ERR_INVALID, "budget_substeps out of range");
+  if (flags & ~(MPM_TUNE_SORT_INTERVAL | MPM_TUNE_IGNORE_CACHE)) return fail(c, MPM_ERR_INVALID, "unknown flags");
+  const bool with_sort = (flags & MPM_TUNE_SORT_INTERVAL) != 0;
+  const std::string dkey = device_key(c->device), bkey = build_key();
+  const std::string ckey = class_key(c) + (with_sort ? " +sort" : "");
+  TuneCandidate best{c->steps_per_warp, c->tuning.warps, c->tuning.tile + 1, c->params.sort_interval};
+  mpm_tuning res{};
+  if (cache_path && !(flags & MPM_TUNE_IGNORE_CACHE)) {
+    TuningEntry e;
+    if (find_tuning(read_tuning_cache(cache_path), dkey, bkey, ckey, &e) && e.steps_per_warp >= 1 &&
+        e.steps_per_warp <= 256 && (e.warps_per_cta == 4 || e.warps_per_cta == 6 || e.warps_per_cta == 12) &&
+        e.tile_box >= MPM_TILE_4x4x6 && e.tile_box <= MPM_TILE_4x6x6 && e.sort_interval >= 0 &&
+        (e.tile_box == MPM_TILE_4x4x6 || e.warps_per_cta == kStepWarps)) {
+      best = TuneCandidate{e.steps_per_warp, e.warps_per_cta, e.tile_box, with_sort ? e.sort_interval : best.sort};
+      apply_tuning(c, best, with_sort);
+      res = mpm_tuning{best.spw, best.warps, best.tile_box, c->params.sort_interval, e.us_per_substep, 1, 0};
+      if (out) *out = res;
+      return MPM_OK;
+    }
+  }
+  MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // the clone copies the current particles
+  mpm_ctx* t = nullptr;
+  st = tuning_clone(c, &t);
+  if (st != MPM_OK) return fail(c, st, "tuning: cannot create the trial context");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    mpm_destroy(t);
+    return fail(c, MPM_ERR_CUDA, "tuning: cannot create events");
+  }
+  const int steps = budget_substeps > 0 ? budget_substeps : 48;
+  const int warm = 4;
+  int timed = 0;
+  double best_us = 0.0;
+  auto run = [&](TuneCandidate k, int n_steps, double* us) -> mpm_status {
+    ++timed;
+    return time_candidate(c, t, k, warm, n_steps, e0, e1, us);
+  };
+  // Coordinate descent from the current shape: steps per warp, CTA size, tile box and,
+  // when asked for, the sort interval; a knob moves only for a gain above 1 %, so timing
+  // noise does not flip it.
+  st = run(best, steps, &best_us);
+  auto consider = [&](TuneCandidate k, int n_steps, double base_us, TuneCandidate& cur, double& cur_us) {
+    double us = 0.0;
+    if (st != MPM_OK) return;
+    st = run(k, n_steps, &us);
+    if (st == MPM_OK && us < 0.99 * cur_us && us < 0.99 * base_us) {
+      cur = k;
+      cur_us = us;
+    }
+  };
+  for (int spw : {1, 2, 4, 8})
+    if (spw != best.spw) {
+      TuneCandidate k = best;
+      k.spw = spw;
+      TuneCandidate cur = best;
+      double cur_us = best_us;
+      consider(k, steps, best_us, cur, cur_us);
+      best = cur;
+      best_us = cur_us;
+    }
+  for (int warps : {4, 6, 12})
+    if (warps != best.warps) {
+      TuneCandidate k = best;
+      k.warps = warps;
+      k.tile_box = MPM_TILE_4x4x6;
+      TuneCandidate cur = best;
+      double cur_us = best_us;
+      consider(k, steps, best_us, cur, cur_us);
+      best = cur;
+      best_us = cur_us;
+    }
+  for (int box : {MPM_TILE_4x4x6, MPM_TILE_4x4x4, MPM_TILE_4x6x6})
+    if (box != best.tile_box) {
+      TuneCandidate k = best;
+      k.tile_box = box;
+      if (box != MPM_TILE_4x4x6) k.warps = kStepWarps;
+      TuneCandidate cur = best;
+      double cur_us = best_us;
+      consider(k, steps, best_us, cur, cur_us);
+      best = cur;
+      best_us = cur_us;
+    }
+  if (with_sort && st == MPM_OK) {
+    // a sort interval is timed over at least two of its periods; the current shape is
+    // re-timed over the same length so the comparison is even
+    for (int si : {4, 8, 16, 32, 64})
+      if (si != best.sort) {
+        const int n_steps = std::max(steps, 2 * std::max(si, best.sort));
+        double base_us = 0.0;
+        if (st == MPM_OK) st = run(best, n_steps, &base_us);
+        TuneCandidate k = best;
+        k.sort = si;
+        TuneCandidate cur = best;
+        double cur_us = base_us;
+        consider(k, n_steps, base_us, cur, cur_us);
+        if (st == MPM_OK && cur.sort != best.sort) {
+          best = cur;
+          best_us = cur_us;
+        }
+      }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  mpm_destroy(t);
+  if (st != MPM_OK) return st;
+  apply_tuning(c, best, with_sort);
+  res = mpm_tuning{best.spw, best.warps, best.tile_box, c->params.sort_interval, best_us, 0, timed};
+  if (cache_path) {
+    TuningEntry e;
+    e.device = dkey;
+    e.build = bkey;
+    e.klass = ckey;
+    e.steps_per_warp = best.spw;
+    e.warps_per_cta = best.warps;
+    e.tile_box = best.tile_box;
+    e.sort_interval = c->params.sort_interval;
+    e.us_per_substep = best_us;
+    if (!store_tuning(cache_path, e)) {
+      if (out) *out = res;
+      return fail(c, MPM_ERR_IO, std::string("tuning: cannot write the cache file ") + cache_path);
+    }
+  }
+  if (out) *out = res;
+  return MPM_OK;
+}
+
+mpm_status mpm_get_tuning(const mpm_ctx* c, mpm_tuning* out) {
+  if (!c || !out) return MPM_ERR_INVALID;
+  *out = mpm_tuning{c->steps_per_warp, c->tuning.warps, c->tuning.tile + 1, c->params.sort_interval, 0.0, 0, 0};
   return MPM_OK;
 }
 

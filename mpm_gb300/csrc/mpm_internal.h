@@ -54,17 +54,26 @@ struct StepArgs {
 // Velocity grid of a single-scene substep: the grid operation applied to a P2G grid,
 // padded by 3 nodes below and 2 above in each dimension ((N + 5)^3 float4 nodes, zero
 // in the padding), so the G2P stencil of every particle that is not completely
-// outside the domain reads inside it; plus the TMA tensor map of its tiles.
+// outside the domain reads inside it; plus the TMA tensor maps of its tiles, one per
+// tile box.
+constexpr int kTileShapes = 3;
 struct VelocityGrid {
-  CUtensorMap map;
+  CUtensorMap map[kTileShapes];
   float4* ptr = nullptr;
   int N = 0;
 };
 int64_t vgrid_nodes(int N);
 // Describes caller-owned memory of vgrid_nodes(N) float4 (16-byte aligned) as a velocity grid.
 cudaError_t vgrid_bind(VelocityGrid& v, float4* ptr, int N);
-// Points a launch's arguments at a velocity grid.
-void set_vgrid(StepArgs& a, const VelocityGrid& v);
+// Points a launch's arguments at a velocity grid and the tensor map of tile box `tile`.
+void set_vgrid(StepArgs& a, const VelocityGrid& v, int tile = 0);
+
+// Launch shape knobs of the fused single-scene substep: warps per CTA (4, 6 or 12) and
+// the G2P tile box (0: 4x4x6, 1: 4x4x4, 2: 4x6x6; boxes 1 and 2 with 12 warps).
+struct StepTuning {
+  int warps;
+  int tile;
+};
 // One warp waiting `polls` times on an mbarrier nothing arrives on; sets kStatusTimeout.
 cudaError_t launch_wait_timeout_probe(int* status, int polls, cudaStream_t st);
 // Velocity pass of a batch: for every scene, the grid op over the nodes of the P2G box
@@ -77,12 +86,19 @@ enum StepKind { kStepP2GOnly = 0, kStepFused = 1, kStepG2POnly = 2 };
 // Launches one substep (a.nscenes > 0: a batch). liquid = liquid-only layout.  A
 // single-scene launch with G2P is two kernels: the velocity pass (grid_in -> a.vgrid)
 // and the substep kernel.  *launches (may be null) counts the kernels.
+// want: launch shape asked for (StepTuning; launches other than the single-scene fused
+// substep use 12 warps and box 0).  vel: the velocity grid, required by single-scene
+// launches with G2P (the launch reads it through the tensor map of its box).
 cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guard, int grid_blocks,
-                        cudaStream_t st, int64_t* launches = nullptr);
+                        cudaStream_t st, int64_t* launches = nullptr, StepTuning want = StepTuning{kStepWarps, 0},
+                        const VelocityGrid* vel = nullptr);
+// The launch shape a launch of this kind uses when `want` is asked for.
+StepTuning step_tuning(StepKind kind, bool guard, bool batch, StepTuning want);
 // Dynamic shared memory of a variant: G2P tiles + per-warp P2G reduction buffers.
-size_t step_smem_bytes(StepKind kind, bool batch);
+size_t step_smem_bytes(StepKind kind, bool batch, StepTuning want = StepTuning{kStepWarps, 0});
 // Max resident CTAs per SM for the variant at the given dynamic shared memory.
-int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem, bool batch = false);
+int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem, bool batch = false,
+                       StepTuning want = StepTuning{kStepWarps, 0});
 
 }  // namespace mpm
 
@@ -96,7 +112,7 @@ void make_dev_material(const mpm_material& m, DevMaterial& d);
 void make_sim_consts(const mpm_params& p, const mpm_material* mats, int n_materials, SimConsts& K);
 // Range size (chunk, particles) and grid size of a substep launch.
 void step_launch_shape(int num_sms, int64_t n, bool liquid, bool guard, StepKind kind, int steps_per_warp,
-                       int& chunk, int& blocks);
+                       int& chunk, int& blocks, StepTuning want = StepTuning{kStepWarps, 0});
 
 // Cell sort (counting sort by the linear index of the base cell).
 struct SortArgs {

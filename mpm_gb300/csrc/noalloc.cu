@@ -110,7 +110,8 @@ extern "C" mpm_status mpm_substep_noalloc(const mpm_params* params, const mpm_ma
     a.grid_in = (kind == kStepP2GOnly) ? nullptr : grid[cur];
     a.grid_out = grid[(cur + 1) % 3];
     a.grid_zero = grid[(cur + 2) % 3];
-    if (launch_step(a, kind, liquid, false, blocks, s) != cudaSuccess) return MPM_ERR_CUDA;
+    if (launch_step(a, kind, liquid, false, blocks, s, nullptr, StepTuning{kStepWarps, 0}, &vel) != cudaSuccess)
+      return MPM_ERR_CUDA;
     cur = (cur + 1) % 3;
   }
   return MPM_OK;

@@ -59,7 +59,7 @@ __device__ __forceinline__ void p2g_scatter_step(float4* wbuf, int lane, int key
                                                  float4* grid, int N) {
   if (__ballot_sync(kFull, key >= 0) == 0u) return;
   if (key >= 0) p2g_write_column_f<UNIT_MASS>(wbuf, lane, w, q0, E, m);
-  warp_scatter_runs(wbuf, lane, key, grid, N, UNIT_MASS ? run_mass : 1.f);
+  warp_scatter_runs<UNIT_MASS>(wbuf, lane, key, grid, N, UNIT_MASS ? run_mass : 1.f);
 }
 
 // ===========================================================================
@@ -67,11 +67,22 @@ __device__ __forceinline__ void p2g_scatter_step(float4* wbuf, int lane, int key
 // ===========================================================================
 
 // Velocity grid padding (nodes below / above the grid in each dimension) and the TMA
-// tile box (x = slowest grid index i, z = fastest index k).
+// tile boxes (X along the slowest grid index i, Z along the fastest index k).  A box of
+// X x Y x Z nodes covers every step whose base cells span at most (X-2) x (Y-2) x (Z-2)
+// cells.  Box 0 (4 x 4 x 6) covers one cell, or two neighbours along a row of a 4x4x4
+// sort brick, including the wrap to the next row; box 1 (4 x 4 x 4) copies a third less
+// for steps inside 2 x 2 x 2 cells; box 2 (4 x 6 x 6) also covers steps across a
+// brick's rows, for sparser scenes.  The autotuner picks one per workload.
 constexpr int kPadLo = 3, kPadHi = 2;
-constexpr int kTileX = 4, kTileY = 4, kTileZ = 6;
-constexpr int kTileNodes = kTileX * kTileY * kTileZ;
-constexpr uint32_t kTileBytes = kTileNodes * sizeof(float4);
+template <int TILE>
+struct TileBox {
+  static constexpr int X = 4, Y = (TILE == 2) ? 6 : 4, Z = (TILE == 1) ? 4 : 6;
+  static constexpr int kNodes = X * Y * Z;
+  static constexpr uint32_t kBytes = kNodes * sizeof(float4);
+};
+constexpr int tile_nodes(int tile) {
+  return tile == 1 ? TileBox<1>::kNodes : (tile == 2 ? TileBox<2>::kNodes : TileBox<0>::kNodes);
+}
 enum TileState { kTileNone = 0, kTileSmem = 1, kTileGlobal = 2 };
 
 // gridOpKernel (src/mpm.cu:76-107) for every node, into the padded velocity grid;
@@ -135,9 +146,11 @@ __device__ __forceinline__ void load_step_head(const StepArgs& A, const float* s
 }
 
 // Box of the base cells of a step's G2P particles (warp-collective).  When it fits the
-// tile, lane 0 starts the TMA copy of the tile into `tile`, completing on `bar`.
+// tile box, lane 0 starts the TMA copy of the tile into `tile`, completing on `bar`.
+template <int TILE>
 __device__ __forceinline__ int plan_tile(const float x[3], bool active, const GridConsts& K, int lane,
                                          const CUtensorMap* map, float4* tile, uint64_t* bar, int lo[3]) {
+  using TB = TileBox<TILE>;
   int b[3], hi[3];
 #pragma unroll
   for (int dd = 0; dd < 3; ++dd) b[dd] = QuadraticInterpolationKernel::base_cell(x[dd], K.dx_inv);
@@ -148,10 +161,10 @@ __device__ __forceinline__ int plan_tile(const float x[3], bool active, const Gr
     hi[dd] = __reduce_max_sync(kFull, active ? b[dd] : INT_MIN);
   }
   if (hi[0] < lo[0]) return kTileNone;
-  if (hi[0] - lo[0] > kTileX - 3 || hi[1] - lo[1] > kTileY - 3 || hi[2] - lo[2] > kTileZ - 3) return kTileGlobal;
+  if (hi[0] - lo[0] > TB::X - 3 || hi[1] - lo[1] > TB::Y - 3 || hi[2] - lo[2] > TB::Z - 3) return kTileGlobal;
   if (lane == 0) {
     // x coordinate in floats: 4 (lo + pad) is a multiple of 4 floats = 16 bytes
-    mbar_arrive_expect_tx(bar, kTileBytes);
+    mbar_arrive_expect_tx(bar, TB::kBytes);
     tma_load_3d(tile, map, 4 * (lo[2] + kPadLo), lo[1] + kPadLo, lo[0] + kPadLo, bar);
   }
   return kTileSmem;
@@ -162,8 +175,14 @@ __device__ __forceinline__ float4* align_smem128(float4* p) {
   return reinterpret_cast<float4*>(reinterpret_cast<char*>(p) + ((128u - (a & 127u)) & 127u));
 }
 
-template <bool LIQ, bool G2P, bool P2G, bool GUARD>
-__global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __grid_constant__ StepArgs A) {
+// WARPS warps per CTA: 4, 6 or 12, so that 3, 2 or 1 CTAs (12 warps) are resident per SM
+// at <= 168 registers; shared memory per warp is two TMA tiles (1.5 KB each for box 0)
+// plus the 14.3 KB P2G transpose buffer, 17.3 KB (12 warps: 207 KB of the SM's 228 KB).
+// TILE: the tile box (TileBox).
+template <bool LIQ, bool G2P, bool P2G, bool GUARD, int WARPS, int TILE>
+__global__ void __launch_bounds__(WARPS * 32, kStepWarps / WARPS) scene_step_kernel(const __grid_constant__ StepArgs A) {
+  using TB = TileBox<TILE>;
+  constexpr int kTileNodes = TB::kNodes, kTileY = TB::Y, kTileZ = TB::Z;
   extern __shared__ float4 smem_dyn[];
   __shared__ int cta_next;  // next CTA-local range index to hand out
   float4* smem = align_smem128(smem_dyn);
@@ -171,9 +190,9 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
   const int lane = tid & 31, warp = tid >> 5;
   // per-warp regions: two TMA tiles (G2P), the P2G transpose buffer, two mbarriers
   float4* tiles = smem + warp * (2 * kTileNodes);
-  float4* wbuf = smem + (G2P ? kStepWarps * 2 * kTileNodes : 0) + warp * kRedFloat4;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (G2P ? kStepWarps * 2 * kTileNodes : 0) +
-                                               (P2G ? kStepWarps * kRedFloat4 : 0)) +
+  float4* wbuf = smem + (G2P ? WARPS * 2 * kTileNodes : 0) + warp * kRedFloat4;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (G2P ? WARPS * 2 * kTileNodes : 0) +
+                                               (P2G ? WARPS * kRedFloat4 : 0)) +
                    2 * warp;
   const GridConsts& K = A.K.g;  // read from the parameter space, not copied to registers
   const int N = K.N;
@@ -184,7 +203,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
   const int64_t st = A.stride;
   const int64_t n = A.n, chunk = A.chunk;
 
-  if (tid == 0) cta_next = kStepWarps;
+  if (tid == 0) cta_next = WARPS;
   __syncthreads();
   if (G2P) {
     if (lane == 0) {
@@ -216,7 +235,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
     uint32_t parity = 0u;  // bit b: phase parity of bars[b]
     // the velocity pass (this launch's programmatic prerequisite) has completed past here
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    if (G2P) tstate = plan_tile(cx, pb + lane < re && !cfz, K, lane, &A.vmap, tiles, bars, tlo);
+    if (G2P) tstate = plan_tile<TILE>(cx, pb + lane < re && !cfz, K, lane, &A.vmap, tiles, bars, tlo);
 
     while (true) {
       const bool last = pb + 32 >= re;
@@ -296,7 +315,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
         // The next step's tile goes to the other buffer, whose last reader was the
         // previous step (every lane has passed that step's P2G warp syncs).
         if (more)
-          tstate = plan_tile(nx, nvalid && !nfz, K, lane, &A.vmap, tiles + (buf ^ 1) * kTileNodes, bars + (buf ^ 1),
+          tstate = plan_tile<TILE>(nx, nvalid && !nfz, K, lane, &A.vmap, tiles + (buf ^ 1) * kTileNodes, bars + (buf ^ 1),
                              tlo);
       }
       if (g2p_on) {
@@ -336,7 +355,8 @@ __global__ void __launch_bounds__(kStepThreads, 1) scene_step_kernel(const __gri
   // ---- clear the grid buffer the previous substep read (used by the launch after next)
   if (A.grid_zero) {
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int64_t i = (int64_t)blockIdx.x * kStepThreads + tid; i < A.grid_cells; i += (int64_t)gridDim.x * kStepThreads)
+    for (int64_t i = (int64_t)blockIdx.x * (WARPS * 32) + tid; i < A.grid_cells;
+         i += (int64_t)gridDim.x * (WARPS * 32))
       A.grid_zero[i] = z;
   }
 }
@@ -578,20 +598,24 @@ cudaError_t vgrid_bind(VelocityGrid& v, float4* ptr, int N) {
   const cuuint64_t P = (cuuint64_t)N + kPadLo + kPadHi;
   const cuuint64_t dims[3] = {4 * P, P, P};
   const cuuint64_t strides[2] = {16 * P, 16 * P * P};  // bytes, dimensions 1 and 2
-  const cuuint32_t box[3] = {4 * kTileZ, kTileY, kTileX};
   const cuuint32_t estr[3] = {1, 1, 1};
-  const CUresult r = encode(&v.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, ptr, dims, strides, box, estr,
-                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+  const cuuint32_t boxes[kTileShapes][3] = {{4 * TileBox<0>::Z, TileBox<0>::Y, TileBox<0>::X},
+                                            {4 * TileBox<1>::Z, TileBox<1>::Y, TileBox<1>::X},
+                                            {4 * TileBox<2>::Z, TileBox<2>::Y, TileBox<2>::X}};
+  for (int t = 0; t < kTileShapes; ++t) {
+    const CUresult r = encode(&v.map[t], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, ptr, dims, strides, boxes[t], estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+  }
   v.ptr = ptr;
   v.N = N;
   return cudaSuccess;
 }
 
-void set_vgrid(StepArgs& a, const VelocityGrid& v) {
+void set_vgrid(StepArgs& a, const VelocityGrid& v, int tile) {
   a.vgrid = v.ptr;
-  a.vmap = v.map;
+  a.vmap = v.map[(tile >= 0 && tile < kTileShapes) ? tile : 0];
 }
 
 cudaError_t launch_batch_velocity(const float4* grid, float4* vgrid, const SceneDev* scenes, int nscenes,
@@ -619,21 +643,46 @@ cudaError_t launch_wait_timeout_probe(int* status, int polls, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <bool LIQ, bool G2P, bool P2G, bool GUARD>
+template <bool LIQ, bool G2P, bool P2G, bool GUARD, int WARPS, int TILE = 0>
 static void* scene_kernel() {
-  return (void*)scene_step_kernel<LIQ, G2P, P2G, GUARD>;
+  return (void*)scene_step_kernel<LIQ, G2P, P2G, GUARD, WARPS, TILE>;
 }
 
-static void* select_kernel(StepKind kind, bool liquid, bool guard, bool batch) {
+StepTuning step_tuning(StepKind kind, bool guard, bool batch, StepTuning want) {
+  // The fused substep of the plain layouts comes in every CTA size with tile box 0, and
+  // with boxes 1 and 2 at 12 warps; the launches that start or end a run, the G2P-guard
+  // variants and batches use 12 warps and box 0.
+  StepTuning t{kStepWarps, 0};
+  if (batch || guard || kind != kStepFused) return t;
+  if (want.tile == 1 || want.tile == 2) {
+    t.tile = want.tile;
+    return t;
+  }
+  if (want.warps == 4 || want.warps == 6) t.warps = want.warps;
+  return t;
+}
+
+static void* select_kernel(StepKind kind, bool liquid, bool guard, bool batch, StepTuning want) {
   if (batch) {  // batches use the general layout, no guard
     if (kind == kStepP2GOnly) return (void*)batch_step_kernel<false, true>;
     return (void*)batch_step_kernel<true, true>;
   }
-#define MPM_SEL(L, G)                                                    \
-  if (liquid == L && guard == G) {                                       \
-    if (kind == kStepP2GOnly) return scene_kernel<L, false, true, G>();  \
-    if (kind == kStepFused) return scene_kernel<L, true, true, G>();     \
-    return scene_kernel<L, true, false, G>();                            \
+  const StepTuning t = step_tuning(kind, guard, batch, want);
+  if (kind == kStepFused && !guard) {
+    if (t.warps == 4) return liquid ? scene_kernel<true, true, true, false, 4>() : scene_kernel<false, true, true, false, 4>();
+    if (t.warps == 6) return liquid ? scene_kernel<true, true, true, false, 6>() : scene_kernel<false, true, true, false, 6>();
+    if (t.tile == 1)
+      return liquid ? scene_kernel<true, true, true, false, kStepWarps, 1>()
+                    : scene_kernel<false, true, true, false, kStepWarps, 1>();
+    if (t.tile == 2)
+      return liquid ? scene_kernel<true, true, true, false, kStepWarps, 2>()
+                    : scene_kernel<false, true, true, false, kStepWarps, 2>();
+  }
+#define MPM_SEL(L, G)                                                                \
+  if (liquid == L && guard == G) {                                                   \
+    if (kind == kStepP2GOnly) return scene_kernel<L, false, true, G, kStepWarps>();  \
+    if (kind == kStepFused) return scene_kernel<L, true, true, G, kStepWarps>();     \
+    return scene_kernel<L, true, false, G, kStepWarps>();                            \
   }
   MPM_SEL(true, false)
   MPM_SEL(true, true)
@@ -643,11 +692,12 @@ static void* select_kernel(StepKind kind, bool liquid, bool guard, bool batch) {
   return nullptr;
 }
 
-size_t step_smem_bytes(StepKind kind, bool batch) {
+size_t step_smem_bytes(StepKind kind, bool batch, StepTuning want) {
   size_t b = 0;
   if (batch) return (kind != kStepG2POnly) ? (size_t)kStepWarps * kRedFloat4 * sizeof(float4) : 16;
-  if (kind != kStepP2GOnly) b += (size_t)kStepWarps * 2 * (kTileBytes + sizeof(uint64_t));
-  if (kind != kStepG2POnly) b += (size_t)kStepWarps * kRedFloat4 * sizeof(float4);
+  const StepTuning t = step_tuning(kind, false, batch, want);
+  if (kind != kStepP2GOnly) b += (size_t)t.warps * 2 * (tile_nodes(t.tile) * sizeof(float4) + sizeof(uint64_t));
+  if (kind != kStepG2POnly) b += (size_t)t.warps * kRedFloat4 * sizeof(float4);
   return b + 128;  // alignment of the TMA tiles
 }
 
@@ -667,25 +717,31 @@ cudaError_t prepare_step_kernel(void* fn, size_t smem) {
 }
 
 cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guard, int grid_blocks, cudaStream_t st,
-                        int64_t* launches) {
+                        int64_t* launches, StepTuning want, const VelocityGrid* vel) {
   const bool batch = a.nscenes > 0;
-  void* fn = select_kernel(kind, liquid, guard, batch);
-  const size_t smem = step_smem_bytes(kind, batch);
+  // a single-scene G2P launch reads its tiles with the tensor map of the kernel's box:
+  // the map is taken here, from the velocity grid, for the box the launch uses
+  if (!batch && kind != kStepP2GOnly && !vel) return cudaErrorInvalidValue;
+  void* fn = select_kernel(kind, liquid, guard, batch, want);
+  const StepTuning t = step_tuning(kind, guard, batch, want);
+  const int warps = t.warps;
+  const size_t smem = step_smem_bytes(kind, batch, t);
   cudaError_t e = prepare_step_kernel(fn, smem);
   if (e != cudaSuccess) return e;
   if (!batch && kind != kStepP2GOnly) {
-    if (!a.vgrid || !a.grid_in) return cudaErrorInvalidValue;
+    if (!vel->ptr || !a.grid_in) return cudaErrorInvalidValue;
     const int P = a.K.g.N + kPadLo + kPadHi;
     const int tx = P <= 64 ? 64 : 128;
-    grid_velocity_kernel<<<dim3((unsigned)((P + tx - 1) / tx), (unsigned)P, (unsigned)P), tx, 0, st>>>(a.grid_in, a.vgrid,
+    grid_velocity_kernel<<<dim3((unsigned)((P + tx - 1) / tx), (unsigned)P, (unsigned)P), tx, 0, st>>>(a.grid_in, vel->ptr,
                                                                                                    a.K.g);
     if (launches) *launches += 1;
   }
   StepArgs copy = a;
+  if (!batch && kind != kStepP2GOnly) set_vgrid(copy, *vel, t.tile);
   void* args[] = {&copy};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid_blocks);
-  cfg.blockDim = dim3(kStepThreads);
+  cfg.blockDim = dim3(batch ? kStepThreads : warps * 32);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   // programmatic dependent launch after the velocity pass (see grid_velocity_kernel)
@@ -699,8 +755,9 @@ cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guar
   return e;
 }
 
-int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem, bool batch) {
-  void* fn = select_kernel(kind, liquid, guard, batch);
+int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem, bool batch, StepTuning want) {
+  void* fn = select_kernel(kind, liquid, guard, batch, want);
+  const int warps = step_tuning(kind, guard, batch, want).warps;
   if (prepare_step_kernel(fn, smem) != cudaSuccess) return 1;
   // the answer depends on the kernel, its shared memory and the device only: ask once
   int dev = 0;
@@ -711,7 +768,9 @@ int step_blocks_per_sm(StepKind kind, bool liquid, bool guard, size_t smem, bool
   for (const auto& k : known)
     if (std::get<0>(k) == fn && std::get<1>(k) == smem && std::get<2>(k) == dev) return std::get<3>(k);
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kStepThreads, smem) != cudaSuccess || nb < 1) nb = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, batch ? kStepThreads : warps * 32, smem) != cudaSuccess ||
+      nb < 1)
+    nb = 1;
   known.emplace_back(fn, smem, dev, nb);
   return nb;
 }

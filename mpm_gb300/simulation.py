@@ -77,9 +77,11 @@ class Simulation:
         """Enqueue all further work on the cudaStream_t `handle` (an int; 0 = the context's own)."""
         _lib.check(self.L.mpm_set_stream(self.ctx, ctypes.c_void_p(int(handle)) if handle else None), self.ctx)
 
-    def set_tuning(self, steps_per_warp=0):
-        """Fused-kernel knob: 32-particle steps per range a warp claims (0 keeps the current value)."""
-        _lib.check(self.L.mpm_set_tuning(self.ctx, int(steps_per_warp), 0, 0), self.ctx)
+    def set_tuning(self, steps_per_warp=0, warps_per_cta=0, tile_box=0):
+        """Fused-kernel knobs (0 keeps the current value): 32-particle steps per range a warp
+        claims, warps per CTA (4, 6 or 12) and the G2P tile box (_lib.TILE_*)."""
+        _lib.check(self.L.mpm_set_tuning(self.ctx, int(steps_per_warp), int(warps_per_cta), int(tile_box)),
+                   self.ctx)
 
     def upload(self, state: dict):
         """particlesToDevice (src/mpm.cu:278-286): x, v, C, F, Jp, mat host arrays."""
