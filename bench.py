@@ -584,30 +584,40 @@ def differentiable_section(args):
     from mpm_gb300 import scenes
     from mpm_gb300.autograd import DiffSim
 
+    from mpm_gb300 import materials as M
+
     cfg = scenes.config_differentiable()
     st = cfg["state"]
     n = st["x"].shape[0]
     nsteps = 256
-    sim = DiffSim(cfg["params"], cfg["materials"][0], n, nsteps, 16)
     target = np.array([0.6, 0.3, 0.5])
-    fw, bw = [], []
-    for k in range(max(args.warmup, 1) + max(1, min(args.steps, 5))):
-        t0 = time.perf_counter()
-        xo, _ = sim.forward(st, nsteps)
-        t1 = time.perf_counter()
-        com = xo.astype(np.float64).mean(0)
-        gx = np.tile(2.0 * (com - target) / n, (n, 1))
-        t2 = time.perf_counter()
-        sim.backward(gx)
-        t3 = time.perf_counter()
-        if k >= max(args.warmup, 1):
-            fw.append(t1 - t0)
-            bw.append(t3 - t2)
-    sim.close()
-    torch.cuda.synchronize()
-    f, b = statistics.median(fw), statistics.median(bw)
+
+    def time_fwd_bwd(material):
+        sim = DiffSim(cfg["params"], material, n, nsteps, 16)
+        fw, bw = [], []
+        for k in range(max(args.warmup, 1) + max(1, min(args.steps, 5))):
+            t0 = time.perf_counter()
+            xo, _ = sim.forward(st, nsteps)
+            t1 = time.perf_counter()
+            com = xo.astype(np.float64).mean(0)
+            gx = np.tile(2.0 * (com - target) / n, (n, 1))
+            t2 = time.perf_counter()
+            sim.backward(gx)
+            t3 = time.perf_counter()
+            if k >= max(args.warmup, 1):
+                fw.append(t1 - t0)
+                bw.append(t3 - t2)
+        sim.close()
+        torch.cuda.synchronize()
+        return statistics.median(fw), statistics.median(bw), len(fw)
+
+    f, b, k = time_fwd_bwd(cfg["materials"][0])
+    # the same body as snow (plasticity and hardening in the adjoint)
+    sf, sb, _ = time_fwd_bwd(M.snow(cfg["materials"][0].particle_volume))
     return {"value": n * nsteps / f, "unit": "particle-substeps/s", "forward_s": f, "backward_s": b,
-            "bwd_fwd_ratio": b / f, "steps": len(fw),
+            "bwd_fwd_ratio": b / f, "steps": k,
+            "snow": {"forward_s": sf, "backward_s": sb, "bwd_fwd_ratio": sb / sf,
+                     "material": "snow (E 1.4e5, nu 0.2, hardening 10, clamps [0.975, 1.0075])"},
             "config": {"workload": "differentiable_100k_N64_256", "particles": n, "N": 64, "substeps": nsteps,
                        "checkpoint_every": 16},
             "timing": "wall clock around the blocking mpm_diff_forward / mpm_diff_backward calls (host copies of "

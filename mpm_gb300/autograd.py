@@ -16,7 +16,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .materials import FIXED_COROTATED, Material
+from .materials import FIXED_COROTATED, SNOW, Material
 
 
 def _ptr(a):
@@ -29,8 +29,8 @@ def _f32(a, shape):
 
 class DiffSim:
     def __init__(self, params: dict, material: Material, n: int, max_steps: int, checkpoint_every: int = 16):
-        if material.kind != FIXED_COROTATED:
-            raise ValueError("the adjoint covers the fixed-corotated material")
+        if material.kind not in (FIXED_COROTATED, SNOW):
+            raise ValueError("the adjoint covers the fixed-corotated and snow materials")
         self.L = _lib.lib()
         self.params = _lib.MpmParams(float(params["dt"]), int(params["N"]), float(params.get("gravity", -9.81)),
                                      int(params.get("boundary_mode", 0)), int(params.get("boundary_cells", 3)), 0, 0, 0)

@@ -1,19 +1,25 @@
 // Differentiable substep: checkpointed forward and hand-written adjoint kernels.
 //
 // The reference has no gradients.  This file differentiates the substep of
-// src/mpm.cu:14-178 for the fixed-corotated material (MMFixedCorotated,
-// include/MaterialModel.cuh:40-62: P F^T = 2 mu (F - R) F^T + lambda (Jp - 1) Jp I,
-// no plasticity, Jp constant).  One substep n maps state_n = (x, v, C, F) to state_{n+1};
-// its adjoint runs three kernels:
-//   adj_g2p    per particle: back through advection, the F update and the G2P gather;
+// src/mpm.cu:14-178 for two materials:
+//   MMFixedCorotated (include/MaterialModel.cuh:40-62): P F^T = 2 mu (F - R) F^T +
+//     lambda (Jp - 1) Jp I, no plasticity;
+//   MMSnow (include/MaterialModel.cuh:67-116): the same stress with mu, lambda scaled by
+//     e = exp(h (1 - Jp)) (computePF, :85-93), and the plasticity of endOfStepMutation
+//     (:95-115): F^ = (I + dt C') F = U S V^T, F' = U clamp(S, lo, hi) V^T,
+//     Jp' = clamp(Jp det F^ / det F', 0.6, 20).
+// One substep n maps state_n = (x, v, C, F, Jp) to state_{n+1}; its adjoint runs three
+// kernels:
+//   adj_g2p    per particle: back through advection, the plasticity (the SVD and clamp
+//              adjoint below, and the Jp update), the F update and the G2P gather;
 //              gathers the grid velocity and SCATTERS the grid-velocity adjoint (the
 //              G2P adjoint is a cell-sorted scatter, reduced per warp like P2G);
 //   adj_gridop per node: back through the grid operation (division by the mass,
 //              gravity, walls) to adjoints of the P2G momentum and mass;
 //   adj_p2g    per particle: GATHERS the momentum/mass adjoints (the P2G adjoint is a
 //              gather) and goes back through the affine term, the stress (with the
-//              polar decomposition's adjoint) and the weights; accumulates dL/dmu and
-//              dL/dlambda.
+//              polar decomposition's adjoint and the hardening factor's dependence on
+//              Jp) and the weights; accumulates dL/dmu0 and dL/dlambda0.
 // The forward run stores the state every `checkpoint_every` substeps; the backward
 // pass recomputes each segment forward (keeping every state and P2G grid of the
 // segment) and then runs the adjoint substeps in reverse.
@@ -68,7 +74,83 @@ __global__ void adj_velocity_kernel(const float4* grid, float4* vgrid, float4* g
   }
 }
 
-// Back through x' = x + dt v', F' = (I + dt C') F and the G2P gather (src/mpm.cu:136-176).
+// Adjoint of the snow plasticity at F^ (MMSnow::endOfStepMutation,
+// include/MaterialModel.cuh:95-115).  With F^ = U S V^T (U, V rotations, S = diag(s)) and
+// g = clamp(., lo, hi) applied to each singular value, F' = U g(S) V^T is an isotropic
+// function of F^.  In the SVD frame, B = U^T dF^ V maps to U^T dF' V = M(B):
+//   M_ii = g'(s_i) B_ii;
+//   for i != j, with sym = (B_ij + B_ji) / 2 and skw = (B_ij - B_ji) / 2,
+//   M_ij = a_ij sym + b_ij skw, M_ji = a_ij sym - b_ij skw,
+//   a_ij = (g_i - g_j) / (s_i - s_j)  (1 when both are inside the band, 0 when both are
+//          clamped to the same bound, the mean of g' when s_i = s_j),
+//   b_ij = (g_i + g_j) / (s_i + s_j).
+// M is symmetric in the Frobenius inner product, so the adjoint is F^bar = U M(U^T F'bar V) V^T.
+// The Jp update Jp' = Jp r, r = det F^ / det F' = prod s_i / prod g_i (U, V rotations), has,
+// when Jp' is not clamped to [0.6, 20], dJp'/dJp = r and dJp'/dF^ = Jp' U diag(1/s_i - g'_i/g_i) V^T.
+// Returns the F^ adjoint in Fhb (from F'bar = Fb and Jp'bar = jb) and r; *unclamped tells
+// whether Jp' was inside [0.6, 20].
+__device__ __forceinline__ void snow_plasticity_adjoint(const float Fh[3][3], float Jp, float lo, float hi,
+                                                        const float Fb[3][3], float jb, float Fhb[3][3], float& r,
+                                                        bool& unclamped) {
+  float U[3][3], V[3][3], s[3];
+  svd3(Fh, U, s, V);
+  float g[3], gp[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    g[i] = clampf(s[i], lo, hi);
+    gp[i] = (s[i] > lo && s[i] < hi) ? 1.f : 0.f;
+  }
+  r = (s[0] / g[0]) * (s[1] / g[1]) * (s[2] / g[2]);
+  const float jn = Jp * r;
+  unclamped = jn > 0.6f && jn < 20.f;
+  // B = U^T Fb V
+  float T[3][3], B[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) T[i][j] = Fb[i][0] * V[0][j] + Fb[i][1] * V[1][j] + Fb[i][2] * V[2][j];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) B[i][j] = U[0][i] * T[0][j] + U[1][i] * T[1][j] + U[2][i] * T[2][j];
+  float Mm[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    Mm[i][i] = gp[i] * B[i][i];
+    if (unclamped) Mm[i][i] += jb * jn * (1.f / s[i] - gp[i] / g[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 3; ++j) {
+      float a;
+      if (gp[i] != 0.f && gp[j] != 0.f) {
+        a = 1.f;
+      } else if (gp[i] == 0.f && gp[j] == 0.f && g[i] == g[j]) {
+        a = 0.f;
+      } else {
+        const float d = s[i] - s[j];
+        a = (fabsf(d) > 1e-12f) ? (g[i] - g[j]) / d : 0.5f * (gp[i] + gp[j]);
+      }
+      const float den = s[i] + s[j];
+      const float b = (fabsf(den) > 1e-12f) ? (g[i] + g[j]) / den : 0.f;
+      const float sym = 0.5f * (B[i][j] + B[j][i]), skw = 0.5f * (B[i][j] - B[j][i]);
+      Mm[i][j] = a * sym + b * skw;
+      Mm[j][i] = a * sym - b * skw;
+    }
+  // Fhb = U Mm V^T
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) T[i][j] = Mm[i][0] * V[j][0] + Mm[i][1] * V[j][1] + Mm[i][2] * V[j][2];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Fhb[i][j] = U[i][0] * T[0][j] + U[i][1] * T[1][j] + U[i][2] * T[2][j];
+}
+
+// Back through x' = x + dt v', the snow plasticity (above), F^ = (I + dt C') F and the G2P
+// gather (src/mpm.cu:136-176).
 __global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(const AdjArgs A) {
   extern __shared__ float4 smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -101,6 +183,26 @@ __global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(const AdjArgs A) {
       stencil(x, K, b, w, d);
       if (!outside_domain(b[0], b[1], b[2], N)) {
         key = pack_key(b[0], b[1], b[2]);
+        if (A.M.kind == kSnow) {
+          // aF holds the adjoint of F' = U clamp(S) V^T: take it back to F^ = (I + dt C') F,
+          // and the Jp' adjoint back to Jp
+          float Fh[3][3];
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+              Fh[r][c] = F[r][c] + K.dt * (C1[r][0] * F[0][c] + C1[r][1] * F[1][c] + C1[r][2] * F[2][c]);
+          const float Jp = ld(A.s, st, kJp, p);
+          const float jb = ld(A.a, st, kJp, p);
+          float Fhb[3][3], ratio;
+          bool unclamped;
+          snow_plasticity_adjoint(Fh, Jp, A.M.clamp_lo, A.M.clamp_hi, aF, jb, Fhb, ratio, unclamped);
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) aF[r][c] = Fhb[r][c];
+          A.a[kJp * st + p] = unclamped ? jb * ratio : 0.f;
+        }
         // v' total adjoint, C' total adjoint
 #pragma unroll
         for (int q = 0; q < 3; ++q) vt[q] = av[q] + K.dt * ax[q];
@@ -288,21 +390,29 @@ __global__ void __launch_bounds__(kAdjThreads) adj_p2g_kernel(const AdjArgs A) {
     for (int r = 0; r < 3; ++r)
 #pragma unroll
       for (int c = 0; c < 3; ++c) PFb[r][c] = sc * Ab[r][c];
-    float mu = M.mu0;
-    // dL/dmu = <PFb, 2 (F - R) F^T>, dL/dlambda = tr(PFb) (Jp - 1) Jp
+    // PF = e (2 mu0 G + lambda0 (Jp - 1) Jp I), G = (F - R) F^T, e = exp(h (1 - Jp)) for snow
+    // and jelly with h != 0 (compute_PF), else 1
+    const bool hardens = (M.kind == kSnow || M.kind == kJelly) && M.hardening != 0.f;
+    const float e = hardens ? expf(M.hardening * (1.f - Jp)) : 1.f;
+    const float mu = M.mu0 * e;
     float G[3][3];
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
       for (int c = 0; c < 3; ++c)
         G[r][c] = (F[r][0] - R[r][0]) * F[c][0] + (F[r][1] - R[r][1]) * F[c][1] + (F[r][2] - R[r][2]) * F[c][2];
-    float dmu = 0.f;
+    float pg = 0.f;  // <PFb, G>
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) dmu += 2.f * PFb[r][c] * G[r][c];
-    mubar += dmu;
-    lambar += (double)(PFb[0][0] + PFb[1][1] + PFb[2][2]) * ((Jp - 1.f) * Jp);
+      for (int c = 0; c < 3; ++c) pg += PFb[r][c] * G[r][c];
+    const float trb = PFb[0][0] + PFb[1][1] + PFb[2][2];
+    // dL/dmu0 = e <PFb, 2 G>, dL/dlambda0 = e tr(PFb) (Jp - 1) Jp
+    mubar += (double)(2.f * e * pg);
+    lambar += (double)(e * trb * ((Jp - 1.f) * Jp));
+    // dL/dJp: de/dJp = -h e on both terms, and d((Jp - 1) Jp)/dJp = 2 Jp - 1
+    const float jbar = (hardens ? -M.hardening * e * (2.f * M.mu0 * pg + M.lambda0 * ((Jp - 1.f) * Jp) * trb) : 0.f) +
+                       M.lambda0 * e * (2.f * Jp - 1.f) * trb;
     // F adjoint of G(F) = (F - R) F^T with Gbar = 2 mu PFb
     float Gb[3][3];
 #pragma unroll
@@ -377,6 +487,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_p2g_kernel(const AdjArgs A) {
       A.a[(kC + q) * st + p] = m * Ab[q / 3][q % 3];
       A.a[(kF + q) * st + p] += Fb[q / 3][q % 3];
     }
+    A.a[kJp * st + p] += jbar;
   }
   // block reduction of the parameter gradients
   __shared__ double red[2][kAdjWarps];
@@ -477,7 +588,7 @@ extern "C" {
 mpm_status mpm_diff_create(const mpm_params* params, const mpm_material* material, int64_t n, int32_t max_steps,
                            int32_t checkpoint_every, mpm_diff** out) {
   if (!params || !material || !out || n <= 0 || max_steps <= 0 || checkpoint_every <= 0) return MPM_ERR_INVALID;
-  if (material->kind != MPM_MAT_FIXED_COROTATED) return MPM_ERR_UNSUPPORTED;
+  if (material->kind != MPM_MAT_FIXED_COROTATED && material->kind != MPM_MAT_SNOW) return MPM_ERR_UNSUPPORTED;
   if (params->N < 4 || params->N > 1000 || !(params->dt > 0.f) || params->g2p_guard) return MPM_ERR_INVALID;
   *out = nullptr;
   mpm_diff* d = new mpm_diff();
@@ -533,7 +644,8 @@ mpm_status mpm_diff_destroy(mpm_diff* d) {
 
 mpm_status mpm_diff_set_material(mpm_diff* d, const mpm_material* material) {
   if (!d || !material) return MPM_ERR_INVALID;
-  if (material->kind != MPM_MAT_FIXED_COROTATED) return MPM_ERR_UNSUPPORTED;
+  if (material->kind != MPM_MAT_FIXED_COROTATED && material->kind != MPM_MAT_SNOW) return MPM_ERR_UNSUPPORTED;
+  if (material->kind != d->material.kind) return MPM_ERR_INVALID;  // the recompute needs the same model
   d->material = *material;
   make_sim_consts(d->params, material, 1, d->K);
   return MPM_OK;

@@ -115,22 +115,23 @@ def test_elastic_constant_gradients_match_dense_autograd(gpu_lib, nsteps, ckpt):
 
 def test_adjoint_matches_fp64_finite_differences(gpu_lib, oracle_lib):
     """Directional derivatives of the COM loss along random velocity perturbations, and
-    dL2/dE, dL2/dnu of the spread of a sheared body, against central differences of the
-    FP64 oracle."""
+    dL2/dmu0, dL2/dlambda0 of the spread of a sheared body, against central differences of
+    the FP64 oracle (steps of mu0 and lambda0 exactly representable in float32)."""
     cfg = small_case(n=2000, seed=6)
     nsteps = 12
     g, _ = gpu_grads(cfg, nsteps, 4)
     st = cfg["state"]
     m = cfg["materials"][0]
 
-    def L_of(v0=None, E=None, nu=None, state=None, loss="com", nsteps=nsteps):
-        from mpm_gb300 import materials as M
+    base = m.derived()
 
-        mm = M.fixed_corotated(m.particle_volume, m.density, E if E is not None else m.E, nu if nu is not None else m.nu)
+    def L_of(v0=None, state=None, loss="com", nsteps=nsteps, **consts):
+        d = dict(base)
+        d.update(consts)
         s = dict(state if state is not None else st)
         if v0 is not None:
             s["v"] = v0
-        out, _, _ = oracle_lib.substep(s, cfg["params"], [mm.derived()], nsteps, np.float64)
+        out, _, _ = oracle_lib.substep(s, cfg["params"], [d], nsteps, np.float64)
         return loss_grad_x(out["x"], loss)[1]
 
     rng = np.random.default_rng(0)
@@ -143,10 +144,11 @@ def test_adjoint_matches_fp64_finite_differences(gpu_lib, oracle_lib):
         assert abs(ad - fd) < 1e-3 * abs(fd) + 1e-12, (ad, fd)
     sh = sheared_case(n=2000, seed=6)
     g2, _ = gpu_grads(sh, 48, 16, "spread")
-    for name, val in (("E", m.E), ("nu", m.nu)):
-        h = 1e-3 * val
-        fd = (L_of(**{name: val + h}, state=sh["state"], loss="spread", nsteps=48) -
-              L_of(**{name: val - h}, state=sh["state"], loss="spread", nsteps=48)) / (2 * h)
+    for name in ("mu0", "lambda0"):
+        val = np.float32(base[name])
+        hp, hm = float(np.float32(val * 1.001)), float(np.float32(val * 0.999))
+        fd = (L_of(state=sh["state"], loss="spread", nsteps=48, **{name: hp}) -
+              L_of(state=sh["state"], loss="spread", nsteps=48, **{name: hm})) / (hp - hm)
         assert abs(g2[name] - fd) < 1e-3 * abs(fd), (name, g2[name], fd)
 
 
@@ -176,12 +178,15 @@ def test_full_size_differentiable_config(gpu_lib, oracle_lib):
     kernels) against central differences of the FP64 oracle, bar 1e-3 relative:
       * dL/dv0 of the workload's loss L = ||COM(x_final) - (0.6, 0.3, 0.5)||^2 along two
         seeded directions (a common drift plus noise, and pure noise);
-      * dL2/dE and dL2/dnu of the spread L2 = mean ||x_final - COM||^2.  The COM loss does
+      * dL2/dmu0 and dL2/dlambda0 of the spread L2 = mean ||x_final - COM||^2, against
+        differences of mu0 and lambda0 by steps exactly representable in float32 (the
+        reference derives them in float, so steps of E or nu would be rounded there); dL/dE
+        and dL/dnu follow by the exact chain rule of lame_grad.  The COM loss does
         not depend on E or nu while the body flies clear of the walls (P2G and G2P conserve
         momentum, so the COM follows the initial mean velocity and gravity): its dL/dE and
         dL/dnu vanish up to rounding.  Both the adjoint's and the finite difference's are
         checked to be negligible: relative to L, below 1e-3 of the spread's relative
-        sensitivity (dL2/dE) / L2."""
+        sensitivity (dL2/dmu0) / L2."""
     from mpm_gb300 import materials as M
     from mpm_gb300 import scenes
     from mpm_gb300.autograd import DiffSim, lame_grad
@@ -204,13 +209,15 @@ def test_full_size_differentiable_config(gpu_lib, oracle_lib):
     g2E, g2nu = lame_grad(m.E, m.nu, g2["mu0"], g2["lambda0"])
     sim.close()
 
-    def run(v0=None, E=None, nu=None):
-        mm = M.fixed_corotated(m.particle_volume, m.density, E if E is not None else m.E,
-                               nu if nu is not None else m.nu)
+    base = m.derived()
+
+    def run(v0=None, **consts):
+        d = dict(base)
+        d.update(consts)
         s = dict(st)
         if v0 is not None:
             s["v"] = v0
-        out, _, _ = oracle_lib.substep(s, cfg["params"], [mm.derived()], nsteps, np.float64)
+        out, _, _ = oracle_lib.substep(s, cfg["params"], [d], nsteps, np.float64)
         x = out["x"]
         c = x.mean(0)
         return float(((c - TARGET) ** 2).sum()), float(((x - c) ** 2).sum(1).mean())
@@ -224,12 +231,14 @@ def test_full_size_differentiable_config(gpu_lib, oracle_lib):
         ad = float((g["v"].astype(np.float64) * u).sum())
         assert abs(ad - fd) < 1e-3 * abs(fd), (ad, fd)
     L2 = float(((x64 - com) ** 2).sum(1).mean())
-    for name, val, ad2, ad1 in (("E", m.E, g2E, gE), ("nu", m.nu, g2nu, gnu)):
-        h = 1e-3 * val
-        lp, lm = run(**{name: val + h}), run(**{name: val - h})
-        fd2 = (lp[1] - lm[1]) / (2 * h)
-        print(f"{name}: spread adjoint {ad2:.6e} fd {fd2:.6e}; COM adjoint {ad1:.3e} fd {(lp[0] - lm[0]) / (2 * h):.3e}")
-        assert abs(ad2 - fd2) < 1e-3 * abs(fd2), (name, ad2, fd2)
-        fd1 = (lp[0] - lm[0]) / (2 * h)
+    for name in ("mu0", "lambda0"):
+        val = np.float32(base[name])
+        hp, hm = float(np.float32(val * 1.001)), float(np.float32(val * 0.999))
+        lp, lm = run(**{name: hp}), run(**{name: hm})
+        fd2 = (lp[1] - lm[1]) / (hp - hm)
+        fd1 = (lp[0] - lm[0]) / (hp - hm)
+        print(f"{name}: spread adjoint {g2[name]:.6e} fd {fd2:.6e}; COM adjoint {g[name]:.3e} fd {fd1:.3e}")
+        assert abs(g2[name] - fd2) < 1e-3 * abs(fd2), (name, g2[name], fd2)
         negligible = 1e-3 * abs(fd2) / L2 * L
-        assert abs(fd1) < negligible and abs(ad1) < negligible, (name, ad1, fd1, negligible)
+        assert abs(fd1) < negligible and abs(g[name]) < negligible, (name, g[name], fd1, negligible)
+    assert np.isfinite([gE, gnu, g2E, g2nu]).all()
