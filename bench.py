@@ -55,6 +55,11 @@ def parse():
                              "render"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--shape", default="auto",
+                    help="launch shape of the fused kernel: 'auto' (the autotuner picks it) or "
+                         "steps_per_warp,warps_per_cta,tile_box (e.g. 2,12,1) to fix it, as the profiles do")
+    ap.add_argument("--diff-material", default="both", choices=["both", "fixed_corotated", "snow"],
+                    help="materials timed by the differentiable workload")
     ap.add_argument("--no-extra", action="store_true",
                     help="headline workload only (no snow, batched and differentiable sections)")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -224,6 +229,17 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def choose_shape(sim, shape):
+    """The fused kernel's launch shape: the autotuner's pick, or a fixed one."""
+    from mpm_gb300 import autotune
+
+    if shape == "auto":
+        return autotune.tune(sim, None, tune_sort_interval=False, budget_substeps=32)
+    spw, warps, box = (int(t) for t in shape.split(","))
+    sim.set_tuning(spw, warps, box)
+    return dict(autotune.current(sim), fixed=True)
+
+
 def time_substeps(sim, steps, warmup, stream, flush):
     """Device time of `steps` single substeps (CUDA events on the library's stream), the L2
     flushed by a 512 MiB write before each (outside the events).  Returns the per-step
@@ -308,11 +324,9 @@ def run_ours(args):
     sim = Simulation.from_config(cfg)
     sim.set_stream(stream.cuda_stream)
     sim.upload(cfg["state"])
-    # the launch shape comes from the autotuner (measured here, on a copy of the scene);
-    # the workload fixes the sort interval
-    from mpm_gb300 import autotune
-
-    tuning = autotune.tune(sim, None, tune_sort_interval=False, budget_substeps=32)
+    # the launch shape comes from the autotuner (measured here, on a copy of the scene) unless
+    # --shape fixes it; the workload fixes the sort interval
+    tuning = choose_shape(sim, args.shape)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     num_sms = torch.cuda.get_device_properties(0).multi_processor_count
 
@@ -389,12 +403,10 @@ def snow_section(args, stream, num_sms):
     cfg, workload = make_cfg("snow")
     n = cfg["state"]["x"].shape[0]
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    from mpm_gb300 import autotune
-
     with Simulation.from_config(cfg) as sim:
         sim.set_stream(stream.cuda_stream)
         sim.upload(cfg["state"])
-        tuning = autotune.tune(sim, None, tune_sort_interval=False, budget_substeps=32)
+        tuning = choose_shape(sim, args.shape)
         ms, pure, launches, _ = time_substeps(sim, args.steps, max(args.warmup, 3), stream, flush)
         sim.sync()
     del flush
@@ -611,13 +623,20 @@ def differentiable_section(args):
         torch.cuda.synchronize()
         return statistics.median(fw), statistics.median(bw), len(fw)
 
-    f, b, k = time_fwd_bwd(cfg["materials"][0])
-    # the same body as snow (plasticity and hardening in the adjoint)
-    sf, sb, _ = time_fwd_bwd(M.snow(cfg["materials"][0].particle_volume))
+    which = getattr(args, "diff_material", "both")
+    f = b = k = None
+    if which in ("both", "fixed_corotated"):
+        f, b, k = time_fwd_bwd(cfg["materials"][0])
+    snow = None
+    if which in ("both", "snow"):
+        # the same body as snow (plasticity and hardening in the adjoint)
+        sf, sb, k2 = time_fwd_bwd(M.snow(cfg["materials"][0].particle_volume))
+        snow = {"forward_s": sf, "backward_s": sb, "bwd_fwd_ratio": sb / sf,
+                "material": "snow (E 1.4e5, nu 0.2, hardening 10, clamps [0.975, 1.0075])"}
+        if f is None:
+            f, b, k = sf, sb, k2
     return {"value": n * nsteps / f, "unit": "particle-substeps/s", "forward_s": f, "backward_s": b,
-            "bwd_fwd_ratio": b / f, "steps": k,
-            "snow": {"forward_s": sf, "backward_s": sb, "bwd_fwd_ratio": sb / sf,
-                     "material": "snow (E 1.4e5, nu 0.2, hardening 10, clamps [0.975, 1.0075])"},
+            "bwd_fwd_ratio": b / f, "steps": k, "snow": snow,
             "config": {"workload": "differentiable_100k_N64_256", "particles": n, "N": 64, "substeps": nsteps,
                        "checkpoint_every": 16},
             "timing": "wall clock around the blocking mpm_diff_forward / mpm_diff_backward calls (host copies of "

@@ -149,6 +149,11 @@ def test_adjoint_matches_fp64_finite_differences(gpu_lib, oracle_lib):
         hp, hm = float(np.float32(val * 1.001)), float(np.float32(val * 0.999))
         fd = (L_of(state=sh["state"], loss="spread", nsteps=48, **{name: hp}) -
               L_of(state=sh["state"], loss="spread", nsteps=48, **{name: hm})) / (hp - hm)
+        if name == "lambda0":
+            # the stress's lambda term is lambda0 (Jp - 1) Jp with the stored Jp, which stays 1
+            # for this material (the reference's stress uses Jp, not det F): no dependence
+            assert fd == 0.0 and g2[name] == 0.0, (g2[name], fd)
+            continue
         assert abs(g2[name] - fd) < 1e-3 * abs(fd), (name, g2[name], fd)
 
 
@@ -238,6 +243,10 @@ def test_full_size_differentiable_config(gpu_lib, oracle_lib):
         fd2 = (lp[1] - lm[1]) / (hp - hm)
         fd1 = (lp[0] - lm[0]) / (hp - hm)
         print(f"{name}: spread adjoint {g2[name]:.6e} fd {fd2:.6e}; COM adjoint {g[name]:.3e} fd {fd1:.3e}")
+        if name == "lambda0":
+            # lambda0 (Jp - 1) Jp with Jp = 1 throughout: the spread does not depend on lambda0
+            assert fd2 == 0.0 and g2[name] == 0.0 and fd1 == 0.0 and g[name] == 0.0, (g2[name], fd2)
+            continue
         assert abs(g2[name] - fd2) < 1e-3 * abs(fd2), (name, g2[name], fd2)
         negligible = 1e-3 * abs(fd2) / L2 * L
         assert abs(fd1) < negligible and abs(g[name]) < negligible, (name, g[name], fd1, negligible)
