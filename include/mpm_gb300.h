@@ -47,8 +47,13 @@ enum {
   MPM_MAT_SNOW = 0,            /* MMSnow            include/MaterialModel.cuh:67-116 */
   MPM_MAT_FIXED_COROTATED = 1, /* MMFixedCorotated  include/MaterialModel.cuh:40-62 */
   MPM_MAT_JELLY = 2,           /* MMJelly           include/MaterialModel.cuh:119-150 */
-  MPM_MAT_LIQUID = 3           /* weakly compressible liquid, P F^T = K (J-1) J I,
+  MPM_MAT_LIQUID = 3,          /* weakly compressible liquid, P F^T = K (J-1) J I,
                                   J <- J det(I + dt C), F = J^(1/3) I (not in the reference) */
+  MPM_MAT_USER_BASE = 16,      /* kinds 16..63: material models compiled into a build of the
+                                  library through include/mpm_gb300_policies.cuh (the
+                                  reference's MaterialModel alias, include/mpm.cuh:25); a table
+                                  holding one holds that kind only */
+  MPM_MAT_USER_END = 64
 };
 
 /* Boundary rule of the grid operation. */
@@ -105,6 +110,10 @@ mpm_status mpm_set_params(mpm_ctx* ctx, const mpm_params* params);
 /* The material table the reference copies to the device in initCuda
  * (src/mpm.cu:199-201); particles index it with their material byte. */
 mpm_status mpm_set_materials(mpm_ctx* ctx, const mpm_material* materials, int32_t count);
+/* 1 when this build can run material kind `kind`: the built-in kinds, and kinds compiled in
+ * through include/mpm_gb300_policies.cuh (no counterpart in the reference, whose model is
+ * fixed by a compile-time alias, include/mpm.cuh:25); 0 otherwise.  Needs no GPU. */
+int32_t mpm_material_kind_available(int32_t kind);
 
 /* Simulation::particlesToDevice (src/mpm.cu:278-286), SoA host arrays.  mat may be
  * NULL (all particles use material 0).  Replaces all particles. */

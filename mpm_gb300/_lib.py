@@ -129,6 +129,7 @@ SIGNATURES = [
     ("mpm_substep_many", I32, [ctypes.POINTER(P), I32, I32]),
     ("mpm_autotune", I32, [P, ctypes.c_char_p, I32, I32, ctypes.POINTER(MpmTuning)]),
     ("mpm_get_tuning", I32, [P, ctypes.POINTER(MpmTuning)]),
+    ("mpm_material_kind_available", I32, [I32]),
     ("mpm_batch_create", I32, [ctypes.POINTER(MpmScene), I32, I32, ctypes.POINTER(P)]),
     ("mpm_batch_destroy", I32, [P]),
     ("mpm_batch_set_stream", I32, [P, P]),
@@ -161,19 +162,38 @@ class MpmError(RuntimeError):
         self.code = code
 
 
+def load_library(path: str) -> ctypes.CDLL:
+    """A build of the library at `path` (e.g. one with compiled-in material models from
+    build.build_with_materials) with the entry points' signatures set."""
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing; run mpm_gb300.build.build() (needs nvcc)")
+    L = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
 def lib() -> ctypes.CDLL:
     """Load the CUDA library (raises if it is missing: there is no CPU fallback)."""
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise ImportError(f"{LIB_PATH} is missing; run mpm_gb300.build.build() (needs nvcc)")
-        L = ctypes.CDLL(LIB_PATH)
-        for name, res, args in SIGNATURES:
-            fn = getattr(L, name)
-            fn.restype = res
-            fn.argtypes = args
-        _lib = L
+        _lib = load_library(LIB_PATH)
     return _lib
+
+
+# the library each live context was created by (contexts of a build with compiled-in
+# materials report their errors through that build)
+_owner = {}
+
+
+def register_context(ctx, L) -> None:
+    _owner[ctx.value] = L
+
+
+def forget_context(ctx) -> None:
+    _owner.pop(ctx.value, None)
 
 
 def check(code: int, ctx=None) -> None:
@@ -181,6 +201,6 @@ def check(code: int, ctx=None) -> None:
         msg = ""
         if ctx:
             buf = ctypes.create_string_buffer(512)
-            lib().mpm_last_error(ctx, buf, 512)
+            (_owner.get(getattr(ctx, "value", None)) or lib()).mpm_last_error(ctx, buf, 512)
             msg = buf.value.decode(errors="replace")
         raise MpmError(code, msg)

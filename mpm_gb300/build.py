@@ -24,7 +24,7 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", 
 
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    files.append(os.path.join(ROOT, "include", "mpm_gb300.h"))
+    files += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     return max(os.path.getmtime(f) for f in files)
 
 
@@ -55,6 +55,36 @@ def build(force: bool = False, verbose: bool = False) -> str:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
     return LIB
+
+
+def build_with_materials(sources, out: str, force: bool = False) -> str:
+    """A build of the library at `out` with material models compiled in: `sources` are .cu
+    files that include mpm_gb300_policies.cuh and register their policies with
+    MPM_GB300_REGISTER_MATERIAL (the reference's way of choosing a MaterialModel is to edit
+    its compile-time alias and rebuild, include/mpm.cuh:25).  The library's own objects
+    come from build(); only the given files are compiled here."""
+    build()
+    sources = [os.path.abspath(s) for s in sources]
+    objs = [os.path.join(BUILD, os.path.splitext(s)[0] + ".o") for s in SOURCES]
+    newest = max([os.path.getmtime(s) for s in sources] + [os.path.getmtime(o) for o in objs] + [_deps()])
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
+        return out
+    outdir = os.path.dirname(os.path.abspath(out))
+    os.makedirs(outdir, exist_ok=True)
+    plugin_objs = []
+    for src in sources:
+        obj = os.path.join(outdir, os.path.splitext(os.path.basename(src))[0] + ".plugin.o")
+        cmd = [NVCC, *ARCH, *FLAGS, "-I", CSRC, "-c", src, "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
+        plugin_objs.append(obj)
+    tmp = out + ".tmp"
+    r = subprocess.run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, *plugin_objs, "-lcudart"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.replace(tmp, out)
+    return out
 
 
 if __name__ == "__main__":

@@ -341,13 +341,22 @@ StepArgs make_step_args(mpm_ctx* c) {
   return a;
 }
 
+// A compiled-in material (include/mpm_gb300_policies.cuh) runs its kernels in the default
+// launch shape; the steps per warp still apply.
+bool compiled_in_material(const mpm_ctx* c) { return c->n_materials > 0 && c->mats[0].kind >= MPM_MAT_USER_BASE; }
+
+StepTuning ctx_tuning(const mpm_ctx* c) { return compiled_in_material(c) ? StepTuning{kStepWarps, 0} : c->tuning; }
+
 void launch_shape(mpm_ctx* c, StepKind kind, bool guard, int& chunk, int& blocks) {
-  mpm::step_launch_shape(c->num_sms, c->n, c->liquid_layout, guard, kind, c->steps_per_warp, chunk, blocks, c->tuning);
+  mpm::step_launch_shape(c->num_sms, c->n, c->liquid_layout, guard, kind, c->steps_per_warp, chunk, blocks,
+                         ctx_tuning(c));
 }
 
 mpm_status run_step(mpm_ctx* c, StepKind kind) {
   StepArgs a = make_step_args(c);
   const bool guard = c->params.g2p_guard != 0;
+  if (guard && compiled_in_material(c))
+    return fail(c, MPM_ERR_UNSUPPORTED, "the G2P guard is not available with a compiled-in material");
   int chunk, blocks;
   launch_shape(c, kind, guard, chunk, blocks);
   a.chunk = chunk;
@@ -355,7 +364,7 @@ mpm_status run_step(mpm_ctx* c, StepKind kind) {
   a.grid_in = (kind == kStepP2GOnly) ? nullptr : c->grid[r];
   a.grid_out = c->grid[(r + 1) % 3];
   a.grid_zero = c->grid[(r + 2) % 3];
-  MPM_CUDA(c, launch_step(a, kind, c->liquid_layout, guard, blocks, c->stream, &c->launches, c->tuning, &c->vel));
+  MPM_CUDA(c, launch_step(a, kind, c->liquid_layout, guard, blocks, c->stream, &c->launches, ctx_tuning(c), &c->vel));
   if (kind != kStepP2GOnly) c->prev = r;
   c->cur = (r + 1) % 3;
   c->pending = kind != kStepG2POnly;
@@ -552,8 +561,14 @@ mpm_status mpm_set_params(mpm_ctx* c, const mpm_params* p) {
 mpm_status mpm_set_materials(mpm_ctx* c, const mpm_material* m, int32_t count) {
   if (!c) return MPM_ERR_INVALID;
   if (!m || count <= 0 || count > MPM_MAX_MATERIALS) return fail(c, MPM_ERR_INVALID, "material count out of range");
+  const bool user = m[0].kind >= MPM_MAT_USER_BASE;
   for (int i = 0; i < count; ++i) {
-    if (m[i].kind < 0 || m[i].kind > MPM_MAT_LIQUID) return fail(c, MPM_ERR_INVALID, "unknown material kind");
+    const bool known = (m[i].kind >= 0 && m[i].kind <= MPM_MAT_LIQUID) || find_material_kernels(m[i].kind, nullptr);
+    if (!known) return fail(c, MPM_ERR_INVALID, "unknown material kind (not built in and not compiled in)");
+    if (user && m[i].kind != m[0].kind)
+      return fail(c, MPM_ERR_INVALID, "a table with a compiled-in material kind holds that kind only");
+    if (!user && m[i].kind >= MPM_MAT_USER_BASE)
+      return fail(c, MPM_ERR_INVALID, "a table with a compiled-in material kind holds that kind only");
     if (!(m[i].particle_volume > 0.f) || !(m[i].density > 0.f))
       return fail(c, MPM_ERR_INVALID, "particle_volume and density must be positive");
   }
@@ -1437,6 +1452,11 @@ mpm_status mpm_autotune(mpm_ctx* c, const char* cache_path, int32_t flags, int32
   }
   if (out) *out = res;
   return MPM_OK;
+}
+
+int32_t mpm_material_kind_available(int32_t kind) {
+  if (kind >= 0 && kind <= MPM_MAT_LIQUID) return 1;
+  return find_material_kernels(kind, nullptr) ? 1 : 0;
 }
 
 mpm_status mpm_get_tuning(const mpm_ctx* c, mpm_tuning* out) {

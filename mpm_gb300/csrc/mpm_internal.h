@@ -83,6 +83,21 @@ cudaError_t launch_batch_velocity(const float4* grid, float4* vgrid, const Scene
 
 enum StepKind { kStepP2GOnly = 0, kStepFused = 1, kStepG2POnly = 2 };
 
+// Material kinds of policies compiled in through include/mpm_gb300_policies.cuh
+// (MPM_MAT_USER_BASE ... in the C ABI) and their kernels: the fused substep, the
+// P2G-only launch that starts a run and the G2P-only launch that may end one.
+constexpr int kUserKindBase = 16, kUserKindEnd = 64;
+struct MaterialKernels {
+  void* fused;
+  void* p2g_only;
+  void* g2p_only;
+};
+// Registers the kernels of material kind `kind` (once per kind; false if the kind is out
+// of range or taken).
+bool register_material_kernels(int kind, const MaterialKernels& k);
+// The kernels of a registered kind.
+bool find_material_kernels(int kind, MaterialKernels* out);
+
 // Launches one substep (a.nscenes > 0: a batch). liquid = liquid-only layout.  A
 // single-scene launch with G2P is two kernels: the velocity pass (grid_in -> a.vgrid)
 // and the substep kernel.  *launches (may be null) counts the kernels.

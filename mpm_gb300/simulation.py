@@ -34,8 +34,10 @@ class Simulation:
     sort interval of the cell-sorted layout."""
 
     def __init__(self, dt=1e-4, N=60, gravity=-9.81, boundary_mode=0, boundary_cells=3, g2p_guard=False,
-                 sort_interval=16, check_finite=False, materials=None):
-        self.L = _lib.lib()
+                 sort_interval=16, check_finite=False, materials=None, library=None):
+        # library: a build with compiled-in material models (_lib.load_library); default:
+        # the library of this package
+        self.L = library if library is not None else _lib.lib()
         self.params = _lib.MpmParams(float(dt), int(N), float(gravity), int(boundary_mode), int(boundary_cells),
                                      int(bool(g2p_guard)), int(sort_interval), int(bool(check_finite)))
         ctx = ctypes.c_void_p()
@@ -43,6 +45,7 @@ class Simulation:
         if code != 0:
             raise _lib.MpmError(code, "mpm_create failed")
         self.ctx = ctx
+        _lib.register_context(ctx, self.L)
         self.N = int(N)
         self.materials = []
         if materials is not None:
@@ -229,6 +232,7 @@ class Simulation:
 
     def close(self):
         if getattr(self, "ctx", None):
+            _lib.forget_context(self.ctx)
             self.L.mpm_destroy(self.ctx)
             self.ctx = None
 
