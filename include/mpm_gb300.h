@@ -170,6 +170,13 @@ int64_t mpm_substep_count(const mpm_ctx* ctx);
  * uploaded particles first, then active objects in activation order.
  * ------------------------------------------------------------------------- */
 enum { MPM_SHAPE_BOX = 0, MPM_SHAPE_SPHERE = 1, MPM_SHAPE_MESH = 2 };
+/* Inside test of MESH objects. */
+enum {
+  MPM_INSIDE_RAY_PARITY = 0, /* odd number of +x ray crossings: exact for closed meshes (default) */
+  MPM_INSIDE_WINDING = 1     /* generalized winding number > 1/2 (libigl's winding_number, which the
+                                reference calls, src/mpm.cu:383): also open or self-overlapping
+                                meshes; sums every triangle for every candidate */
+};
 
 typedef struct mpm_object {
   int32_t shape;             /* MPM_SHAPE_* */
@@ -183,8 +190,9 @@ typedef struct mpm_object {
   uint64_t seed;             /* seeding stream */
   const float* vertices;     /* MESH: 3 floats per vertex, any scale (host memory) */
   int64_t n_vertices;
-  const int32_t* triangles;  /* MESH: 3 vertex indices per triangle of a closed mesh */
+  const int32_t* triangles;  /* MESH: 3 vertex indices per triangle (closed for ray parity) */
   int64_t n_triangles;
+  int32_t inside_test;       /* MESH: MPM_INSIDE_* */
 } mpm_object;
 
 /* Seed an object's particles on the GPU and add it to the scene; *n_particles (may be

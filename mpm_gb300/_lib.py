@@ -48,6 +48,7 @@ class MpmScene(ctypes.Structure):
 
 
 SHAPE_BOX, SHAPE_SPHERE, SHAPE_MESH = 0, 1, 2
+INSIDE_RAY_PARITY, INSIDE_WINDING = 0, 1
 
 
 class MpmObject(ctypes.Structure):
@@ -65,6 +66,7 @@ class MpmObject(ctypes.Structure):
         ("n_vertices", ctypes.c_int64),
         ("triangles", ctypes.c_void_p),
         ("n_triangles", ctypes.c_int64),
+        ("inside_test", ctypes.c_int32),
     ]
 
 

@@ -57,6 +57,81 @@ __device__ bool inside_mesh(const SeedShape& sh, const float p[3]) {
   return (crossings & 1) != 0;
 }
 
+// The generalized winding number of the mesh at p (Jacobson, Kavan, Sorkine-Hornung,
+// "Robust inside-outside segmentation using generalized winding numbers", SIGGRAPH 2013):
+// the sum over triangles of their signed solid angles over 4 pi, each
+// atan2(det, |a||b||c| + (b.c)|a| + (c.a)|b| + (a.b)|c|) / (2 pi) with a, b, c the corners
+// relative to p, in the order of libigl's solid_angle (include/igl/solid_angle.cpp of the
+// reference's vendored libigl), the reference's inside test.  FP64.
+__device__ double winding_number_d(const SeedShape& sh, const float p[3]) {
+  const double inv2pi = 0.15915494309189535;
+  double w = 0.0;
+  for (int t = 0; t < sh.n_tris; ++t) {
+    const float* A = sh.verts + 3 * sh.tris[3 * t + 0];
+    const float* B = sh.verts + 3 * sh.tris[3 * t + 1];
+    const float* C = sh.verts + 3 * sh.tris[3 * t + 2];
+    double v[3][3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      v[0][d] = (double)A[d] - (double)p[d];
+      v[1][d] = (double)B[d] - (double)p[d];
+      v[2][d] = (double)C[d] - (double)p[d];
+    }
+    const double la = sqrt(v[0][0] * v[0][0] + v[0][1] * v[0][1] + v[0][2] * v[0][2]);
+    const double lb = sqrt(v[1][0] * v[1][0] + v[1][1] * v[1][1] + v[1][2] * v[1][2]);
+    const double lc = sqrt(v[2][0] * v[2][0] + v[2][1] * v[2][1] + v[2][2] * v[2][2]);
+    const double det = v[0][0] * v[1][1] * v[2][2] + v[1][0] * v[2][1] * v[0][2] + v[2][0] * v[0][1] * v[1][2] -
+                       v[2][0] * v[1][1] * v[0][2] - v[1][0] * v[0][1] * v[2][2] - v[0][0] * v[2][1] * v[1][2];
+    const double d0 = v[1][0] * v[2][0] + v[1][1] * v[2][1] + v[1][2] * v[2][2];
+    const double d1 = v[2][0] * v[0][0] + v[2][1] * v[0][1] + v[2][2] * v[0][2];
+    const double d2 = v[0][0] * v[1][0] + v[0][1] * v[1][1] + v[0][2] * v[1][2];
+    w += atan2(det, la * lb * lc + d0 * la + d1 * lb + d2 * lc) * inv2pi;
+  }
+  return w;
+}
+
+// Inside test by the winding number: w > 1/2.  The sum is first taken in FP32 with a
+// bound on its rounding error (per triangle: the float corner vectors, determinant and
+// denominator are within 24 u |a||b||c| of exact, u = 2^-24, which moves atan2 by at most
+// (|den| e + |det| e) / (det^2 + den^2); plus atan2f's and the summation's own error).  A
+// point whose FP32 sum is farther from 1/2 than twice the bound is decided by it; the rest
+// (points at the surface, or in the mouth of an open mesh's hole) take the FP64 sum, so the
+// decision is the FP64 one.
+__device__ bool inside_winding(const SeedShape& sh, const float p[3]) {
+  const float u = 5.9604645e-8f;
+  float w = 0.f, bound = 0.f;
+  for (int t = 0; t < sh.n_tris; ++t) {
+    const float* A = sh.verts + 3 * sh.tris[3 * t + 0];
+    const float* B = sh.verts + 3 * sh.tris[3 * t + 1];
+    const float* C = sh.verts + 3 * sh.tris[3 * t + 2];
+    float v[3][3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      v[0][d] = A[d] - p[d];
+      v[1][d] = B[d] - p[d];
+      v[2][d] = C[d] - p[d];
+    }
+    const float la = sqrtf(v[0][0] * v[0][0] + v[0][1] * v[0][1] + v[0][2] * v[0][2]);
+    const float lb = sqrtf(v[1][0] * v[1][0] + v[1][1] * v[1][1] + v[1][2] * v[1][2]);
+    const float lc = sqrtf(v[2][0] * v[2][0] + v[2][1] * v[2][1] + v[2][2] * v[2][2]);
+    const float det = v[0][0] * v[1][1] * v[2][2] + v[1][0] * v[2][1] * v[0][2] + v[2][0] * v[0][1] * v[1][2] -
+                      v[2][0] * v[1][1] * v[0][2] - v[1][0] * v[0][1] * v[2][2] - v[0][0] * v[2][1] * v[1][2];
+    const float d0 = v[1][0] * v[2][0] + v[1][1] * v[2][1] + v[1][2] * v[2][2];
+    const float d1 = v[2][0] * v[0][0] + v[2][1] * v[0][1] + v[2][2] * v[0][2];
+    const float d2 = v[0][0] * v[1][0] + v[0][1] * v[1][1] + v[0][2] * v[1][2];
+    const float lll = la * lb * lc;
+    const float den = lll + d0 * la + d1 * lb + d2 * lc;
+    w += atan2f(det, den) * 0.15915494f;
+    const float e = 24.f * u * lll;
+    const float r2 = det * det + den * den;
+    // atan2f: within a few ulps of its result (at most pi; 8 ulps allowed); the sum rounds
+    // once per term
+    bound += ((fabsf(den) + fabsf(det)) * e / r2 + 8.f * u * 3.1415927f) * 0.15915494f + u * fabsf(w);
+  }
+  if (fabsf(w - 0.5f) > 2.f * bound + 1e-6f) return w > 0.5f;  // also false for NaN bounds: FP64
+  return winding_number_d(sh, p) > 0.5;
+}
+
 __device__ __forceinline__ bool inside(const SeedShape& sh, const float p[3]) {
   if (sh.kind == kSeedBox) return true;
   if (sh.kind == kSeedSphere) {
@@ -65,7 +140,7 @@ __device__ __forceinline__ bool inside(const SeedShape& sh, const float p[3]) {
     const double dz = dsub((double)p[2], sh.center[2]);
     return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)) < sh.r2;
   }
-  return inside_mesh(sh, p);
+  return sh.winding ? inside_winding(sh, p) : inside_mesh(sh, p);
 }
 
 // Pass 1: kept candidates per block, and per thread the mask of its kept candidates (the
@@ -150,6 +225,7 @@ mpm_status build_seed_shape(const mpm_object& o, uint32_t density, SeedShapeOwne
   sh = SeedShape{};
   sh.seed = o.seed;
   if (!(o.size > 0.f) || !std::isfinite(o.size)) return MPM_ERR_INVALID;
+  if (o.inside_test != MPM_INSIDE_RAY_PARITY && o.inside_test != MPM_INSIDE_WINDING) return MPM_ERR_INVALID;
   for (int c = 0; c < 3; ++c)
     if (!std::isfinite(o.position[c])) return MPM_ERR_INVALID;
   if (o.shape == MPM_SHAPE_BOX) {
@@ -202,6 +278,8 @@ mpm_status build_seed_shape(const mpm_object& o, uint32_t density, SeedShapeOwne
         hi[c] = std::max(hi[c], V[3 * v + c]);
       }
     sh.kind = kSeedMesh;
+    sh.winding = o.inside_test == MPM_INSIDE_WINDING ? 1 : 0;
+    sh.n_tris = (int)o.n_triangles;
     for (int c = 0; c < 3; ++c) {
       sh.lo[c] = lo[c];
       sh.range[c] = (double)hi[c] - (double)lo[c];

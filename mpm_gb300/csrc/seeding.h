@@ -24,6 +24,8 @@ struct SeedShape {
   const int* bin_tris;
   int bins_y, bins_z;
   double bin_y0, bin_z0, bin_inv_dy, bin_inv_dz;
+  int winding;  // mesh: 1 = generalized winding number > 1/2 instead of ray parity
+  int n_tris;
 };
 
 // SplitMix64 (Steele, Lea, Flood, OOPSLA 2014): a bijective 64-bit mix of a counter.

@@ -56,6 +56,7 @@ class SceneObject:
     seed: int = 0
     vertices: np.ndarray | None = None   # (V, 3) float32, MESH only
     triangles: np.ndarray | None = None  # (T, 3) int32, MESH only
+    inside_test: int = _lib.INSIDE_RAY_PARITY  # MESH: _lib.INSIDE_WINDING for open meshes
     name: str = field(default="", compare=False)
 
     def to_c(self):
@@ -70,6 +71,7 @@ class SceneObject:
         o.lifetime_begin = float(self.lifetime_begin)
         o.lifetime_end = float(self.lifetime_end)
         o.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
+        o.inside_test = int(self.inside_test)
         keep = []
         if self.shape == _lib.SHAPE_MESH:
             V = np.ascontiguousarray(np.asarray(self.vertices, np.float32).reshape(-1, 3))
@@ -144,8 +146,27 @@ def load_scene(path: str, particle_count: int = CLI_DEFAULTS["particle_count"], 
         else:
             o.shape = _lib.SHAPE_MESH
             o.vertices, o.triangles = read_obj(os.path.join(meshes, mesh))
+            # ray parity is exact for closed meshes; others take the winding number, the
+            # reference's inside test (src/mpm.cu:383)
+            if not is_closed(o.triangles):
+                o.inside_test = _lib.INSIDE_WINDING
         objs.append(o)
     return mats, objs
+
+
+def is_closed(triangles) -> bool:
+    """Whether every edge of the triangle mesh is shared by exactly two triangles, in
+    opposite directions (a closed, consistently oriented surface)."""
+    T = np.asarray(triangles, np.int64).reshape(-1, 3)
+    if T.size == 0:
+        return False
+    e = np.concatenate([T[:, [0, 1]], T[:, [1, 2]], T[:, [2, 0]]])
+    key = lambda a, b: a * (int(T.max()) + 1) + b  # noqa: E731
+    fwd, cnt = np.unique(key(e[:, 0], e[:, 1]), return_counts=True)
+    if np.any(cnt != 1):
+        return False
+    rev = np.unique(key(e[:, 1], e[:, 0]))
+    return len(fwd) == len(rev) and bool(np.all(fwd == rev))
 
 
 def build_simulation(path: str, N: int = CLI_DEFAULTS["N"], dt: float = CLI_DEFAULTS["dt"],

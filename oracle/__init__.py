@@ -80,7 +80,7 @@ def lib():
         L.oracle_max_threads.restype = ctypes.c_int
         L.oracle_seed_object.restype = ctypes.c_int64
         L.oracle_seed_object.argtypes = [ctypes.c_int, ctypes.c_float, P, P, ctypes.c_uint64, ctypes.c_uint32, P,
-                                         ctypes.c_int64, P, ctypes.c_int64, P, ctypes.c_int64]
+                                         ctypes.c_int64, P, ctypes.c_int64, ctypes.c_int32, P, ctypes.c_int64]
         L.oracle_distance_field.restype = None
         L.oracle_distance_field.argtypes = [P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, P]
         L.oracle_surface_indexed.restype = None
@@ -196,7 +196,7 @@ def max_threads() -> int:
 
 
 def seed_object(shape: int, size: float, position, box_extent=(1.0, 1.0, 1.0), seed: int = 0, density: int = 1000,
-                vertices=None, triangles=None) -> np.ndarray:
+                vertices=None, triangles=None, inside_test: int = 0) -> np.ndarray:
     """Positions (n, 3) float32 of the restated rejection sampler (oracle/seed_oracle.cpp)."""
     L = lib()
     pos = np.ascontiguousarray(np.asarray(position, np.float32).reshape(3))
@@ -208,7 +208,7 @@ def seed_object(shape: int, size: float, position, box_extent=(1.0, 1.0, 1.0), s
         T = np.ascontiguousarray(np.asarray(triangles, np.int32).reshape(-1, 3))
         nv, nt = V.shape[0], T.shape[0]
     args = (int(shape), float(size), _ptr(pos), _ptr(ext), int(seed) & 0xFFFFFFFFFFFFFFFF, int(density), _ptr(V),
-            nv, _ptr(T), nt)
+            nv, _ptr(T), nt, int(inside_test))
     n = L.oracle_seed_object(*args, None, 0)
     if n < 0:
         raise ValueError("invalid object")

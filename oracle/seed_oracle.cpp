@@ -8,7 +8,15 @@
  * volume) (src/mpm.cu:369-371).  The reference draws with rand() and tests meshes with
  * libigl's winding number (igl::winding_number); this restatement draws candidate i
  * from SplitMix64 (Steele, Lea, Flood, OOPSLA 2014) of seed + 3 i + axis and tests
- * closed meshes by the parity of +x ray crossings, the rules the GPU seeder documents.
+ * meshes by the parity of +x ray crossings or, with inside_test = 1, by the generalized
+ * winding number in double (libigl's solid_angle summed over the triangles, inside when
+ * above 1/2), the rules the GPU seeder documents.
+ *
+ * The reference stores libigl's float winding number in an integer matrix and keeps a
+ * candidate when that integer is 1 (src/mpm.cu:352, 383-385), so an interior point whose
+ * float sum rounds to just below 1 is dropped: about half of them (a float32 sum over a
+ * 1,280-triangle sphere puts 50 % of interior points below 1).  Neither the oracle nor the
+ * GPU seeder reproduces that; both keep every point inside.
  * Every operation is an IEEE double (or float where the placement is float) with no
  * contraction (built with -ffp-contract=off), so GPU and oracle agree bit for bit.
  */
@@ -47,16 +55,37 @@ bool crosses(const float* a, const float* b, const float* c, double px, double p
   return xs / s > px;
 }
 
+// A triangle's share of the winding number at p, as libigl's solid_angle computes it
+// (include/igl/solid_angle.cpp of the reference's vendored libigl): atan2(det, |a||b||c| + (b.c)|a| + (c.a)|b| + (a.b)|c|) / (2 pi).
+double winding_term(const float* A, const float* B, const float* C, const float p[3]) {
+  double v[3][3];
+  for (int d = 0; d < 3; ++d) {
+    v[0][d] = (double)A[d] - (double)p[d];
+    v[1][d] = (double)B[d] - (double)p[d];
+    v[2][d] = (double)C[d] - (double)p[d];
+  }
+  const double la = std::sqrt(v[0][0] * v[0][0] + v[0][1] * v[0][1] + v[0][2] * v[0][2]);
+  const double lb = std::sqrt(v[1][0] * v[1][0] + v[1][1] * v[1][1] + v[1][2] * v[1][2]);
+  const double lc = std::sqrt(v[2][0] * v[2][0] + v[2][1] * v[2][1] + v[2][2] * v[2][2]);
+  const double det = v[0][0] * v[1][1] * v[2][2] + v[1][0] * v[2][1] * v[0][2] + v[2][0] * v[0][1] * v[1][2] -
+                     v[2][0] * v[1][1] * v[0][2] - v[1][0] * v[0][1] * v[2][2] - v[0][0] * v[2][1] * v[1][2];
+  const double d0 = v[1][0] * v[2][0] + v[1][1] * v[2][1] + v[1][2] * v[2][2];
+  const double d1 = v[2][0] * v[0][0] + v[2][1] * v[0][1] + v[2][2] * v[0][2];
+  const double d2 = v[0][0] * v[1][0] + v[0][1] * v[1][1] + v[0][2] * v[1][2];
+  return std::atan2(det, la * lb * lc + d0 * la + d1 * lb + d2 * lc) * 0.15915494309189535;
+}
+
 }  // namespace
 
 extern "C" {
 
-/* shape: 0 box (box_extent relative edges), 1 sphere, 2 mesh (vertices, triangles).
- * Writes up to `capacity` particles (3 floats each, candidate order) to x and returns
- * the number kept, or -1 for an invalid object. */
+/* shape: 0 box (box_extent relative edges), 1 sphere, 2 mesh (vertices, triangles;
+ * inside_test 0: ray parity, 1: winding number > 1/2).  Writes up to `capacity`
+ * particles (3 floats each, candidate order) to x and returns the number kept, or -1 for
+ * an invalid object. */
 int64_t oracle_seed_object(int shape, float size, const float* position, const float* box_extent, uint64_t seed,
                            uint32_t density, const float* vertices, int64_t n_vertices, const int32_t* triangles,
-                           int64_t n_triangles, float* x, int64_t capacity) {
+                           int64_t n_triangles, int32_t inside_test, float* x, int64_t capacity) {
   double lo[3], range[3], center[3] = {0, 0, 0}, r2 = 0.0;
   std::vector<float> V;
   if (!(size > 0.f)) return -1;
@@ -118,6 +147,11 @@ int64_t oracle_seed_object(int shape, float size, const float* position, const f
     if (shape == 1) {
       const double dx = (double)p[0] - center[0], dy = (double)p[1] - center[1], dz = (double)p[2] - center[2];
       in = ((dx * dx + dy * dy) + dz * dz) < r2;
+    } else if (shape == 2 && inside_test == 1) {
+      double w = 0.0;
+      for (int64_t t = 0; t < n_triangles; ++t)
+        w += winding_term(&V[3 * triangles[3 * t]], &V[3 * triangles[3 * t + 1]], &V[3 * triangles[3 * t + 2]], p);
+      in = w > 0.5;
     } else if (shape == 2) {
       int crossings = 0;
       for (int64_t t = 0; t < n_triangles; ++t)

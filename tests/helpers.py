@@ -87,3 +87,18 @@ def write_obj(path, V, F, quads=False):
             f.write(f"v {v[0]:.7f} {v[1]:.7f} {v[2]:.7f}\n")
         for tri in F:
             f.write("f " + " ".join(f"{i + 1}/{i + 1}" for i in tri) + "\n")
+
+
+def open_icosphere(subdivisions=3, cut=0.6):
+    """The icosphere with the triangles of its cap y > cut removed: a mesh with a hole."""
+    V, F = icosphere(subdivisions)
+    keep = V[F].max(axis=1)[:, 1] <= cut
+    return V, F[keep]
+
+
+def two_spheres(subdivisions=2):
+    """Two overlapping closed icospheres in one mesh (centres 0.6 apart, radius 1): ray parity
+    calls their overlap outside (two crossings), the winding number 2."""
+    V, F = icosphere(subdivisions)
+    V2 = V + np.array([0.6, 0.0, 0.0], np.float32)
+    return np.concatenate([V, V2]).astype(np.float32), np.concatenate([F, F + V.shape[0]]).astype(np.int32)

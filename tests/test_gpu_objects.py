@@ -5,7 +5,7 @@ a scene built from objects."""
 import numpy as np
 import pytest
 
-from helpers import compare_states, icosphere
+from helpers import compare_states, icosphere, open_icosphere, two_spheres
 
 pytestmark = pytest.mark.gpu
 
@@ -34,6 +34,29 @@ def test_gpu_seeding_matches_oracle(gpu_lib, oracle_lib, name):
     assert len(g) > 1000
     assert g.shape == r.shape
     assert np.array_equal(g, r)
+
+
+@pytest.mark.parametrize("mesh", ["closed", "open", "overlapping"])
+def test_gpu_winding_number_seeding_matches_oracle(gpu_lib, oracle_lib, mesh):
+    """The winding-number inside test (MPM_INSIDE_WINDING): bit-exact positions in the same
+    order as the oracle's FP64 restatement on a closed icosphere, an icosphere with a hole
+    and two overlapping spheres (inside where the winding number is 2).  Near-surface points
+    go through the FP64 path on the GPU."""
+    from mpm_gb300 import _lib
+    from mpm_gb300.scene_file import SceneObject, seed_object
+
+    V, F = {"closed": icosphere(3), "open": open_icosphere(3), "overlapping": two_spheres(2)}[mesh]
+    o = SceneObject(shape=_lib.SHAPE_MESH, size=0.3, position=(0.2, 0.25, 0.3), seed=31, vertices=V, triangles=F,
+                    inside_test=_lib.INSIDE_WINDING)
+    dens = 400000
+    g = seed_object(o, dens)
+    r = oracle_lib.seed_object(o.shape, o.size, o.position, o.box_extent, o.seed, dens, V, F, inside_test=1)
+    assert len(g) > 1000
+    assert g.shape == r.shape
+    assert np.array_equal(g, r)
+    if mesh == "closed":
+        ray = oracle_lib.seed_object(o.shape, o.size, o.position, o.box_extent, o.seed, dens, V, F)
+        assert np.array_equal(g, ray)
 
 
 def test_objects_join_and_leave_at_their_lifetimes(gpu_lib):

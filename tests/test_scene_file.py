@@ -117,3 +117,74 @@ def test_oracle_mesh_parity_matches_the_mesh_volume(oracle_lib):
     cand = int(dens * np.prod(Vs.max(0) - Vs.min(0)))
     p = mesh_volume(Vs, F) / np.prod(Vs.max(0) - Vs.min(0))
     assert abs(len(xm) - cand * p) < 5 * np.sqrt(cand * p * (1 - p)), (len(xm), cand * p)
+
+
+def _winding_numbers(Vs, F, P):
+    """Generalized winding numbers of points P, as numpy float64 solid angles."""
+    a, b, c = (Vs[F[:, k]][None, :, :] - P[:, None, :] for k in range(3))
+    la, lb, lc = (np.linalg.norm(x, axis=2) for x in (a, b, c))
+    det = np.einsum("ptj,ptj->pt", a, np.cross(b, c))
+    den = la * lb * lc + np.einsum("ptj,ptj->pt", b, c) * la + np.einsum("ptj,ptj->pt", c, a) * lb + \
+        np.einsum("ptj,ptj->pt", a, b) * lc
+    return (np.arctan2(det, den) / (2 * np.pi)).sum(1)
+
+
+def _splitmix64(z):
+    with np.errstate(over="ignore"):
+        z = z + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def _candidates(seed, lo, rng, n):
+    """Candidates 0..n-1 of the rejection sampler: float(lo + u range), u from SplitMix64 of
+    seed + 3 i + axis with 53 bits."""
+    i = np.arange(n, dtype=np.uint64)
+    out = np.empty((n, 3), np.float32)
+    for c in range(3):
+        u = (_splitmix64(np.uint64(seed) + np.uint64(3) * i + np.uint64(c)) >> np.uint64(11)).astype(np.float64) \
+            * (1.0 / 9007199254740992.0)
+        out[:, c] = (lo[c] + u * rng[c]).astype(np.float32)
+    return out
+
+
+def _placed(V, size, pos):
+    Vd = V.astype(np.float32)
+    lo, hi = Vd.min(0), Vd.max(0)
+    scale = np.float32(size) / (hi - lo).max()
+    return (Vd * scale + (np.asarray(pos, np.float32) - scale * lo)).astype(np.float32)
+
+
+def test_oracle_winding_number_inside_test(oracle_lib):
+    """The oracle's winding-number test (inside_test = 1): on a closed mesh it keeps the same
+    particles as ray parity; on a mesh with a hole and on two overlapping spheres its kept
+    points are those of an independent numpy winding number above 1/2, among the candidates of
+    ray parity's run (kept or not)."""
+    from helpers import icosphere, open_icosphere, two_spheres
+
+    dens, size, pos = 60000, 0.3, (0.2, 0.2, 0.2)
+    V, F = icosphere(2)
+    ray = oracle_lib.seed_object(2, size, pos, seed=7, density=dens, vertices=V, triangles=F)
+    wind = oracle_lib.seed_object(2, size, pos, seed=7, density=dens, vertices=V, triangles=F, inside_test=1)
+    assert len(ray) > 300 and np.array_equal(ray, wind)
+    for V, F in (open_icosphere(2), two_spheres(2)):
+        Vs = _placed(V, size, pos)
+        lo, hi = Vs.min(0).astype(np.float64), Vs.max(0).astype(np.float64)
+        cand = _candidates(7, lo, hi - lo, int(dens * np.prod(hi - lo)))
+        w = _winding_numbers(Vs.astype(np.float64), F, cand.astype(np.float64))
+        wind = oracle_lib.seed_object(2, size, pos, seed=7, density=dens, vertices=V, triangles=F, inside_test=1)
+        assert np.array_equal(wind, cand[w > 0.5])
+    ray = oracle_lib.seed_object(2, size, pos, seed=7, density=dens, vertices=V, triangles=F)
+    assert len(wind) > len(ray) * 1.2  # the overlap of the two spheres is inside only by the winding number
+
+
+def test_open_meshes_use_the_winding_number():
+    from helpers import icosphere, open_icosphere, two_spheres
+
+    from mpm_gb300.scene_file import is_closed
+
+    assert is_closed(icosphere(2)[1]) and is_closed(two_spheres(2)[1])
+    assert not is_closed(open_icosphere(2)[1])
+    F = icosphere(1)[1]
+    assert not is_closed(F[:, [0, 2, 1]][:1].tolist() + F[1:].tolist())  # one flipped triangle
