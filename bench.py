@@ -833,7 +833,61 @@ def run_mesh(args):
             "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "meshes/s", "cores": 1, "kind": "port",
                              "sample": f"the same {n} particles on the same grid (oracle distance field and "
                                        f"marching cubes, 1 thread, {cpu_s:.1f} s)"}}
+    line["smooth"] = smooth_section(sim, Vh, Fh, nvert, ntri, timed, steps)
     print(json.dumps(line), flush=True)
+
+
+def smooth_section(sim, Vh, Fh, nv, nf, timed, steps):
+    """MeshBuilder::smoothMesh (include/mesh_builder.h:212-245, the reference's
+    --laplacian_smooth) on the mesh just extracted: device time of mpm_surface_smooth_device
+    on a copy of the vertices in HBM (CUDA events on the context's stream, L2 flushed
+    before), the conjugate-gradient iteration count, the wall time of mpm_surface_smooth on
+    host arrays, and the oracle's direct sparse solve of the same system on the host
+    (scipy's SuperLU) with the largest difference between the two."""
+    import ctypes
+
+    import torch
+
+    from mpm_gb300 import _lib
+    from oracle import smooth_oracle
+
+    V0 = Vh[:nv].clone().numpy()
+    F0 = Fh[:nf].clone().numpy()
+    V0d = torch.from_numpy(V0).cuda()
+    Fd = torch.from_numpy(F0).cuda()
+    Vd = torch.empty_like(V0d)
+    it = ctypes.c_int32()
+
+    def call_device():
+        _lib.check(sim.L.mpm_surface_smooth_device(sim.ctx, ctypes.c_void_p(Vd.data_ptr()), nv,
+                                                   ctypes.c_void_p(Fd.data_ptr()), nf, ctypes.byref(it)), sim.ctx)
+
+    Vh2 = V0.copy()
+
+    def call_host():
+        Vh2[:] = V0
+        _lib.check(sim.L.mpm_surface_smooth(sim.ctx, Vh2.ctypes.data_as(ctypes.c_void_p), nv,
+                                            F0.ctypes.data_as(ctypes.c_void_p), nf, ctypes.byref(it)), sim.ctx)
+
+    Vd.copy_(V0d)
+    call_device()
+    dev, launches = [], []
+    for _ in range(steps):
+        Vd.copy_(V0d)
+        l0 = sim.launches
+        dev.append(timed(call_device)[0])
+        launches.append(sim.launches - l0)
+    wall = [timed(call_host)[1] for _ in range(min(steps, 5))]
+    c0 = time.perf_counter()
+    ref = smooth_oracle.smooth_mesh(V0, F0)
+    cpu_s = time.perf_counter() - c0
+    U = Vd.cpu().numpy()
+    d_s = statistics.median(dev)
+    return {"ms": 1e3 * d_s, "iterations": int(it.value), "us_per_iteration": 1e6 * d_s / max(it.value, 1),
+            "gpu_launches": int(statistics.median(launches)), "e2e_ms": 1e3 * statistics.median(wall),
+            "max_rel_diff_vs_oracle": float(np.abs(U - ref).max() / np.abs(ref).max()),
+            "cpu_baseline": {"ms": 1e3 * cpu_s, "cores": 1, "kind": "port",
+                             "sample": f"scipy SuperLU direct solve of the same {nv}-vertex system"}}
 
 
 def _liquid_sim(stream):

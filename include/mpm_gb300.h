@@ -252,6 +252,24 @@ mpm_status mpm_surface_mesh_device(mpm_ctx* ctx, int32_t grid_side, int32_t radi
  * after the call returns (the call itself waits once, for the counts). */
 mpm_status mpm_surface_mesh_indexed_device(mpm_ctx* ctx, int32_t grid_side, int32_t radius, const double** vertices,
                                            const int32_t** faces, int64_t* n_vertices, int64_t* n_faces);
+/* Laplacian smoothing of a triangle mesh (MeshBuilder::smoothMesh,
+ * include/mesh_builder.h:212-245, the --laplacian_smooth step of computeMesh): one implicit
+ * step U = (M - 0.001 L)^-1 M V with libigl's cotangent Laplacian L and barycentric lumped
+ * mass matrix M of the input mesh, then U divided by the square root of its area (the
+ * reference's rescale to unit area).  vertices (3 doubles each) are replaced by U; faces are 3
+ * zero-based vertex indices each.  Solved in double on the GPU by conjugate gradients
+ * preconditioned by the diagonal, to a relative residual of 1e-12 per coordinate (the
+ * reference factors M - 0.001 L by a sparse Cholesky).  A vertex that no face uses keeps
+ * its position (rescaled).  MPM_ERR_INVALID for a face index outside [0, n_vertices), a face
+ * of zero area (the reference's cotangent weights are not finite there) or vertices without
+ * faces; MPM_ERR_STATE if the solver did not converge (vertices unchanged then).
+ * *iterations (may be NULL) receives the solver's iteration count.  Synchronises. */
+mpm_status mpm_surface_smooth(mpm_ctx* ctx, double* vertices, int64_t n_vertices, const int32_t* faces,
+                              int64_t n_faces, int32_t* iterations);
+/* The same on device arrays (e.g. those of mpm_surface_mesh_indexed_device), in place, on the
+ * context's stream; synchronises. */
+mpm_status mpm_surface_smooth_device(mpm_ctx* ctx, double* vertices, int64_t n_vertices, const int32_t* faces,
+                                     int64_t n_faces, int32_t* iterations);
 
 /* ---------------------------------------------------------------------------
  * Particle export (ParticleWriter::writeParticles, include/particle_writer.h:19-43).  The

@@ -108,11 +108,13 @@ class Simulation {
 /* MeshBuilder(params, flags, grid_size) / computeMesh (include/mesh_builder.h:19-34,
  * 165-211): the surface of the simulation's particles on a grid_side^3 voxel grid with the
  * given particle radius (in voxels), written as an OBJ file: libigl's marching-cubes
- * vertex list (bit for bit, in its order) and outward faces over the same edge loops. */
+ * vertex list (bit for bit, in its order) and outward faces over the same edge loops.
+ * laplacian_smooth (the reference's --laplacian_smooth) smooths the vertices as
+ * MeshBuilder::smoothMesh does (mpm_surface_smooth). */
 class MeshBuilder {
  public:
-  explicit MeshBuilder(int32_t grid_side = 250, int32_t particle_radius = 5)
-      : grid_side_(grid_side), radius_(particle_radius) {}
+  explicit MeshBuilder(int32_t grid_side = 250, int32_t particle_radius = 5, bool laplacian_smooth = false)
+      : grid_side_(grid_side), radius_(particle_radius), smooth_(laplacian_smooth) {}
 
   /* The triangle soup, 9 floats per triangle (the faces of mesh(), in order). */
   std::vector<float> triangles(Simulation& sim) const {
@@ -141,6 +143,8 @@ class MeshBuilder {
     }
     V.resize(3 * (size_t)nv);
     F.resize(3 * (size_t)nf);
+    /* --laplacian_smooth: MeshBuilder::smoothMesh (include/mesh_builder.h:212-245) */
+    if (smooth_ && nf > 0) status(sim, mpm_surface_smooth(sim.handle(), V.data(), nv, F.data(), nf, nullptr));
   }
 
   /* Writes the OBJ file (igl::writeOBJ's v / f lines); returns the number of faces. */
@@ -164,6 +168,7 @@ class MeshBuilder {
     throw Error(st, std::string("surface: ") + msg);
   }
   int32_t grid_side_, radius_;
+  bool smooth_;
 };
 
 /* ParticleWriter::writeParticles (include/particle_writer.h:19-43): the active particles

@@ -114,6 +114,8 @@ SIGNATURES = [
     ("mpm_surface_mesh_indexed_device", I32, [P, I32, I32, ctypes.POINTER(P), ctypes.POINTER(P),
                                                ctypes.POINTER(I64), ctypes.POINTER(I64)]),
     ("mpm_surface_table", I32, [P, P]),
+    ("mpm_surface_smooth", I32, [P, P, I64, P, I64, ctypes.POINTER(I32)]),
+    ("mpm_surface_smooth_device", I32, [P, P, I64, P, I64, ctypes.POINTER(I32)]),
     ("mpm_surface_distance_device", I32, [P, I32, I32, ctypes.POINTER(P)]),
     ("mpm_export_particles", I32, [P, I32, ctypes.c_float, ctypes.POINTER(I64)]),
     ("mpm_export_wait", I32, [P, I32, ctypes.POINTER(P), ctypes.POINTER(I64)]),

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmpm_gb300.so")
 SOURCES = ["substep.cu", "aux_kernels.cu", "capi.cu", "noalloc.cu", "batch.cu", "adjoint.cu", "seeding.cu", "surface.cu",
-           "export.cu", "tuning_cache.cpp"]
+           "smooth.cu", "export.cu", "tuning_cache.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",

@@ -89,6 +89,7 @@ struct mpm_ctx {
   double t = 0.0;  // simulated time (Simulation::t)
   std::vector<ObjectRec> objects;
   SurfaceBuffers surf;
+  SmoothBuffers smooth;
   struct ExportSlot {
     void* dev = nullptr;   // packed records on the device
     void* host = nullptr;  // pinned copy
@@ -519,6 +520,7 @@ mpm_status mpm_destroy(mpm_ctx* c) {
   for (auto& g : c->grid) cudaFree(g);
   cudaFree(c->vgrid_mem);
   c->surf.release();
+  c->smooth.release();
   if (c->copy_stream) {
     cudaStreamSynchronize(c->copy_stream);
     cudaStreamDestroy(c->copy_stream);
@@ -1050,6 +1052,66 @@ mpm_status mpm_surface_mesh_indexed_device(mpm_ctx* c, int32_t G, int32_t radius
   *n_vertices = nv;
   *n_faces = nf;
   return MPM_OK;
+}
+
+namespace {
+
+// smooth_mesh on device arrays and its outcome as a status.
+mpm_status smooth_device(mpm_ctx* c, double* V, int64_t nv, const int32_t* F, int64_t nf, int32_t* iterations) {
+  if (nv > 0 && nf == 0) return fail(c, MPM_ERR_INVALID, "smooth: vertices without faces (the system is singular)");
+  SmoothResult r;
+  cudaError_t e = smooth_mesh(V, F, nv, nf, c->smooth, c->stream, &c->launches, &r);
+  if (e != cudaSuccess)
+    return fail(c, e == cudaErrorMemoryAllocation ? MPM_ERR_NOMEM : MPM_ERR_CUDA,
+                std::string("smooth: ") + cudaGetErrorString(e));
+  if (iterations) *iterations = r.iterations;
+  if (r.bad_index) return fail(c, MPM_ERR_INVALID, "smooth: a face index is outside [0, n_vertices)");
+  if (r.bad_area) return fail(c, MPM_ERR_INVALID, "smooth: a face has zero area (its cotangent weights are not finite)");
+  if (!r.converged)
+    return fail(c, MPM_ERR_STATE, "smooth: conjugate gradients did not converge (relative residual " +
+                                      std::to_string(r.relative_residual) + " after " +
+                                      std::to_string(r.iterations) + " iterations)");
+  MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+}  // namespace
+
+mpm_status mpm_surface_smooth(mpm_ctx* c, double* vertices, int64_t nv, const int32_t* faces, int64_t nf,
+                              int32_t* iterations) {
+  if (!c || nv < 0 || nf < 0 || (nv > 0 && !vertices) || (nf > 0 && !faces) || nv > INT32_MAX ||
+      nf > INT32_MAX / 3)
+    return MPM_ERR_INVALID;
+  SmoothBuffers& sb = c->smooth;
+  auto grow = [](auto*& p, int64_t& cap, int64_t need) {
+    if (p && cap >= need) return cudaSuccess;
+    cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const cudaError_t e = cudaMalloc(&p, sizeof(*p) * (size_t)std::max<int64_t>(need, 1));
+    if (e == cudaSuccess) cap = need;
+    return e;
+  };
+  MPM_CUDA(c, grow(sb.V, sb.V_cap, 3 * nv));
+  MPM_CUDA(c, grow(sb.F, sb.F_cap, 3 * nf));
+  if (nv > 0)
+    MPM_CUDA(c, cudaMemcpyAsync(sb.V, vertices, sizeof(double) * 3 * (size_t)nv, cudaMemcpyHostToDevice, c->stream));
+  if (nf > 0)
+    MPM_CUDA(c, cudaMemcpyAsync(sb.F, faces, sizeof(int32_t) * 3 * (size_t)nf, cudaMemcpyHostToDevice, c->stream));
+  const mpm_status st = smooth_device(c, sb.V, nv, sb.F, nf, iterations);
+  if (st != MPM_OK) return st;
+  if (nv > 0)
+    MPM_CUDA(c, cudaMemcpyAsync(vertices, sb.V, sizeof(double) * 3 * (size_t)nv, cudaMemcpyDeviceToHost, c->stream));
+  MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+mpm_status mpm_surface_smooth_device(mpm_ctx* c, double* vertices, int64_t nv, const int32_t* faces, int64_t nf,
+                                     int32_t* iterations) {
+  if (!c || nv < 0 || nf < 0 || (nv > 0 && !vertices) || (nf > 0 && !faces) || nv > INT32_MAX ||
+      nf > INT32_MAX / 3)
+    return MPM_ERR_INVALID;
+  return smooth_device(c, vertices, nv, faces, nf, iterations);
 }
 
 mpm_status mpm_export_particles(mpm_ctx* c, int32_t slot, float radius, int64_t* n) {

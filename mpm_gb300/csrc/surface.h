@@ -41,6 +41,48 @@ cudaError_t extract_surface(int G, int radius, double voxel_dx, SurfaceBuffers& 
 // The triangle table: counts[256] and slots[256 * 30] (edge slots, -1 past the count).
 void surface_table(int32_t* counts, int32_t* slots);
 
+// Device buffers of the Laplacian smoother (smooth.cu), kept by the context between calls
+// (grown, never shrunk).
+struct SmoothBuffers {
+  double* C = nullptr;     // per face: the three cotangent entries and the double area
+  int64_t C_cap = 0;
+  double* vec = nullptr;   // per vertex: M, D = -L(i, i), 1 / S(i, i); then Y, r, p, q (3 each)
+  int64_t vec_cap = 0;
+  double* part = nullptr;  // per-block partial sums
+  int64_t part_cap = 0;
+  int* ints = nullptr;     // row offsets, fill counters, scan scratch, corners, row lengths, neighbours
+  int64_t ints_cap = 0;
+  double* w = nullptr;     // the entries L(i, j) of the rows' neighbours
+  int64_t w_cap = 0;
+  double* scal = nullptr;  // the solver's scalars
+  int* flags = nullptr;    // check bits and the last-block ticket
+  double* V = nullptr;     // staging of host vertices
+  int64_t V_cap = 0;
+  int* F = nullptr;        // staging of host faces
+  int64_t F_cap = 0;
+  double* host = nullptr;  // pinned words read back by the solver
+  void release();
+};
+
+constexpr double kSmoothTolerance = 1e-12;  // relative residual per coordinate
+constexpr int kSmoothMaxIterations = 20000;
+constexpr int kSmoothCheckEvery = 16;       // iterations between residual read-backs
+
+struct SmoothResult {
+  int iterations = 0;
+  double relative_residual = 0.0;  // largest over the coordinates
+  bool converged = false;
+  bool bad_index = false;  // a face index outside [0, n_vertices)
+  bool bad_area = false;   // a face of zero area
+};
+
+// One implicit Laplacian smoothing step of the mesh (V: 3 doubles per vertex, F: 3 indices
+// per face, both on the device), written over V, and the rescale to unit area
+// (MeshBuilder::smoothMesh, include/mesh_builder.h:212-245).  V is left unchanged when the
+// result reports a bad index, a degenerate face or no convergence.  Synchronises the stream.
+cudaError_t smooth_mesh(double* V, const int* F, int64_t nv, int64_t nf, SmoothBuffers& sb, cudaStream_t st,
+                        int64_t* launches, SmoothResult* res);
+
 // Marching cubes in libigl's cube layout, on nodes (i, j, k) with k fastest as
 // MeshBuilder::computeMesh lays them out (include/mesh_builder.h:181-193).  Corner n of a
 // cube sits at offset kCorner[n] (di, dj, dk) from its lowest node; edge slot e joins

@@ -4,9 +4,12 @@
 MeshBuilder::computeMesh (include/mesh_builder.h:170-211) as src/main.cu:78-106 drives it
 once per saved frame: the distance field and the marching-cubes mesh are computed on the
 GPU (``mpm_surface_mesh_indexed``: libigl's vertex list bit for bit, faces over the same
-edge loops) and written as an OBJ file (igl::writeOBJ's ``v`` / ``f`` lines).  The reference's optional
-libigl post-processing (``--laplacian_smooth``, ``--mesh-face-count`` decimation, both
-off by default) is not provided.
+edge loops) and written as an OBJ file (igl::writeOBJ's ``v`` / ``f`` lines).  ``laplacian_smooth``
+(the reference's ``--laplacian_smooth``, off by default) applies MeshBuilder::smoothMesh
+(include/mesh_builder.h:212-245) on the GPU (``mpm_surface_smooth``): one implicit
+cotangent-Laplacian step and the rescale to unit area.  The reference's other optional
+post-processing step, ``--mesh-face-count`` decimation by igl::decimate (off by default),
+is not provided.
 """
 from __future__ import annotations
 
@@ -43,13 +46,19 @@ def write_obj(filename: str, V: np.ndarray, F: np.ndarray) -> None:
 class MeshBuilder:
     """MeshBuilder(params, flags, grid_size) (include/mesh_builder.h:19-34)."""
 
-    def __init__(self, grid_side: int = MESH_GRID, particle_radius: int = MESH_PARTICLE_RADIUS):
+    def __init__(self, grid_side: int = MESH_GRID, particle_radius: int = MESH_PARTICLE_RADIUS,
+                 laplacian_smooth: bool = False):
         self.grid_side = int(grid_side)
         self.particle_radius = int(particle_radius)
+        self.laplacian_smooth = bool(laplacian_smooth)
 
     def mesh(self, sim):
-        """(V float64, F int32) of the particles' surface."""
-        return sim.surface_indexed(self.grid_side, self.particle_radius)
+        """(V float64, F int32) of the particles' surface, smoothed when laplacian_smooth
+        is set (include/mesh_builder.h:195-199)."""
+        V, F = sim.surface_indexed(self.grid_side, self.particle_radius)
+        if self.laplacian_smooth and F.shape[0] > 0:
+            V = sim.smooth_mesh(V, F)
+        return V, F
 
     def computeMesh(self, filename: str, sim) -> int:
         """Writes the surface of the simulation's active particles; returns the face count."""

@@ -203,6 +203,18 @@ class Simulation:
                                                        F.shape[0], ctypes.byref(nv), ctypes.byref(nf)), self.ctx)
         return V[:nv.value], F[:nf.value]
 
+    def smooth_mesh(self, V: np.ndarray, F: np.ndarray) -> np.ndarray:
+        """MeshBuilder::smoothMesh (include/mesh_builder.h:212-245) on the GPU: one implicit
+        cotangent-Laplacian smoothing step (M - 0.001 L) U = M V, rescaled to unit area
+        (mpm_surface_smooth); returns U (V, 3) float64."""
+        U = np.ascontiguousarray(np.asarray(V, np.float64).reshape(-1, 3)).copy()
+        Fi = np.ascontiguousarray(np.asarray(F, np.int32).reshape(-1, 3))
+        it = ctypes.c_int32()
+        _lib.check(self.L.mpm_surface_smooth(self.ctx, _ptr(U), U.shape[0], _ptr(Fi), Fi.shape[0], ctypes.byref(it)),
+                   self.ctx)
+        self.smooth_iterations = it.value
+        return U
+
     def surface_mesh(self, grid_side: int = 250, radius: int = 5) -> np.ndarray:
         """Triangles (T, 3, 3) float32 of the particles' surface (the zero level of
         radius voxel_dx - distance, include/mesh_builder.h:170-190): the faces of
