@@ -57,21 +57,23 @@ namespace mpm {
 // The substep kernel is launched as its programmatic dependent: it may start (claim
 // ranges, load its first positions) while this pass runs, and waits for the pass
 // with griddepcontrol.wait before it reads the velocity grid.
-// One thread per padded node: grid (rows of the padded k extent, P, P), so the indices
-// need no division (padded grids stay far below 2^31 nodes).
+// One thread per padded node, in the padded grid's order (consecutive threads take
+// consecutive k), so every warp is full: a block per padded row left most of each block's
+// threads idle (69 of 128 at N = 64).  Padded grids stay below 2^31 nodes (N <= 1000).
 __global__ void grid_velocity_kernel(const float4* __restrict__ grid, float4* __restrict__ vgrid, GridConsts K) {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   const int N = K.N, P = N + kPadLo + kPadHi;
-  const int pk = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (pk >= P) return;
-  const int pj = (int)blockIdx.y, pi = (int)blockIdx.z;
+  const int q = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (q >= P * P * P) return;
+  const int pi = q / (P * P), rem = q - pi * (P * P);
+  const int pj = rem / P, pk = rem - pj * P;
   const int i = pi - kPadLo, j = pj - kPadLo, k = pk - kPadLo;
   float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
   if ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N) {
     const float3 v = grid_node_velocity(grid[(i * N + j) * N + k], i, j, k, K);
     out = make_float4(v.x, v.y, v.z, 0.f);
   }
-  vgrid[(pi * P + pj) * P + pk] = out;
+  vgrid[q] = out;
 }
 
 // ===========================================================================
@@ -479,9 +481,8 @@ cudaError_t launch_step(const StepArgs& a, StepKind kind, bool liquid, bool guar
   if (!batch && kind != kStepP2GOnly) {
     if (!vel->ptr || !a.grid_in) return cudaErrorInvalidValue;
     const int P = a.K.g.N + kPadLo + kPadHi;
-    const int tx = P <= 64 ? 64 : 128;
-    grid_velocity_kernel<<<dim3((unsigned)((P + tx - 1) / tx), (unsigned)P, (unsigned)P), tx, 0, st>>>(a.grid_in, vel->ptr,
-                                                                                                   a.K.g);
+    const int64_t nodes = (int64_t)P * P * P;
+    grid_velocity_kernel<<<(unsigned)((nodes + 255) / 256), 256, 0, st>>>(a.grid_in, vel->ptr, a.K.g);
     if (launches) *launches += 1;
   }
   StepArgs copy = a;
