@@ -40,7 +40,15 @@ def configs():
         "snow_500k_N64": lambda: scenes.config_snow(),
         "mixed_20k_N32": lambda: scenes.mixed_scene(),
         "fixed_corotated_100k_N64": lambda: scenes.config_differentiable(),
+        # grid sides whose padded extents (N + 5) are not powers of two, and a tiny grid
+        "elastic_20k_N37": lambda: scenes.config_elastic(n=20_000, seed=5, N=37),
+        "elastic_2k_N5": lambda: _with_params(scenes.config_elastic(n=2_000, seed=6, N=5), boundary_cells=2),
     }
+
+
+def _with_params(cfg, **params):
+    cfg["params"].update(params)
+    return cfg
 
 
 @pytest.mark.parametrize("name", list(configs().keys()))
