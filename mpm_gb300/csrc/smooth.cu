@@ -198,14 +198,14 @@ __global__ void smooth_expand_kernel(const int* __restrict__ F, const double* __
         corner[b + 1] = key;
       }
     double m = 0.0, d = 0.0;
-    const int base = 2 * lo;
+    const int64_t base = 2 * (int64_t)lo;  // 2 pairs per corner: up to 6 x (faces) entries
     for (int e = lo; e < hi; ++e) {
       const int id = corner[e];
       const int f = id / 3, k = id - 3 * f;
       const int k1 = k == 2 ? 0 : k + 1, k2 = k == 0 ? 2 : k - 1;
       // the edge to corner k1 is opposite corner k2, the edge to corner k2 opposite k1
       const double w1 = C[4 * (int64_t)f + k2], w2 = C[4 * (int64_t)f + k1];
-      const int o = base + 2 * (e - lo);
+      const int64_t o = base + 2 * (int64_t)(e - lo);
       nbr[o] = F[3 * (int64_t)f + k1];
       w[o] = w1;
       nbr[o + 1] = F[3 * (int64_t)f + k2];
@@ -215,10 +215,10 @@ __global__ void smooth_expand_kernel(const int* __restrict__ F, const double* __
     }
     int n = 2 * (hi - lo);
     if (sorted && n > 1) {
-      for (int a = base + 1; a < base + n; ++a) {  // stable insertion sort by neighbour
+      for (int64_t a = base + 1; a < base + n; ++a) {  // stable insertion sort by neighbour
         const int kn = nbr[a];
         const double kw = w[a];
-        int b = a - 1;
+        int64_t b = a - 1;
         while (b >= base && nbr[b] > kn) {
           nbr[b + 1] = nbr[b];
           w[b + 1] = w[b];
@@ -228,7 +228,7 @@ __global__ void smooth_expand_kernel(const int* __restrict__ F, const double* __
         w[b + 1] = kw;
       }
       int u = 1;
-      for (int a = base + 1; a < base + n; ++a) {
+      for (int64_t a = base + 1; a < base + n; ++a) {
         if (nbr[a] == nbr[base + u - 1]) {
           w[base + u - 1] += w[a];
         } else {
@@ -272,8 +272,9 @@ __global__ void smooth_init_kernel(Solver s, const double* __restrict__ V) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < s.nv; i += (int64_t)gridDim.x * blockDim.x) {
     const double vi[3] = {V[3 * i], V[3 * i + 1], V[3 * i + 2]};
     double lv[3] = {0.0, 0.0, 0.0};
-    const int o = 2 * s.rowptr[i], n = s.len[i];
-    for (int e = o; e < o + n; ++e) {
+    const int64_t o = 2 * (int64_t)s.rowptr[i];
+    const int n = s.len[i];
+    for (int64_t e = o; e < o + n; ++e) {
       const int j = s.nbr[e];
       const double we = s.w[e];
 #pragma unroll
@@ -310,8 +311,9 @@ __global__ void smooth_apply_kernel(Solver s) {
     const double pi[3] = {s.p[3 * i], s.p[3 * i + 1], s.p[3 * i + 2]};
     const double d = s.D[i], m = s.M[i];
     double lp[3] = {-d * pi[0], -d * pi[1], -d * pi[2]};
-    const int o = 2 * s.rowptr[i], n = s.len[i];
-    for (int e = o; e < o + n; ++e) {
+    const int64_t o = 2 * (int64_t)s.rowptr[i];
+    const int n = s.len[i];
+    for (int64_t e = o; e < o + n; ++e) {
       const int j = s.nbr[e];
       const double we = s.w[e];
 #pragma unroll
