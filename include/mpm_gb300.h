@@ -367,8 +367,10 @@ enum {
  * does not change.  With a cache_path (a JSON file; NULL: no cache), a shape found for the
  * same device, library build and workload class (particle layout, N, particle count to the
  * nearest power of two, material kinds) is reused without measuring, and a new one is
- * stored.  *out (may be NULL) receives the chosen shape.  Synchronises; allocates a copy of
- * the particle arrays while it runs. */
+ * stored (MPM_ERR_IO, with the shape applied, when the file cannot be written or is not a
+ * tuning cache: another file at that path is never overwritten).  *out (may be NULL)
+ * receives the chosen shape.  Synchronises; allocates a copy of the particle arrays while it
+ * runs. */
 mpm_status mpm_autotune(mpm_ctx* ctx, const char* cache_path, int32_t flags, int32_t budget_substeps,
                         mpm_tuning* out);
 /* The context's current launch shape (us_per_substep, from_cache and candidates are 0). */

@@ -4,6 +4,7 @@
 #include "tuning_cache.h"
 
 #include <cctype>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -84,7 +85,28 @@ bool get_num(const std::map<std::string, std::string>& kv, const char* k, double
   char* end = nullptr;
   const std::string t = it->second.substr(1);
   out = std::strtod(t.c_str(), &end);
-  return end && *end == '\0';
+  return end && *end == '\0' && std::isfinite(out);
+}
+
+// A number field that is a 32-bit integer (anything else skips the entry).
+bool get_int(const std::map<std::string, std::string>& kv, const char* k, int& out) {
+  double v = 0.0;
+  if (!get_num(kv, k, v) || v < -2147483648.0 || v > 2147483647.0 || v != std::floor(v)) return false;
+  out = (int)v;
+  return true;
+}
+
+// Whether `path` holds a file that is not a cache of this format (so it is not ours to
+// replace).
+bool foreign_file(const std::string& path) {
+  std::ifstream f(path);
+  if (!f) return false;
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string s = ss.str();
+  bool blank = true;
+  for (char c : s) blank = blank && std::isspace((unsigned char)c);
+  return !blank && s.find(kFormat) == std::string::npos;
 }
 
 std::string quote(const std::string& s) {
@@ -129,17 +151,11 @@ std::vector<TuningEntry> read_tuning_cache(const std::string& path, bool* ok) {
       break;
     }
     TuningEntry t;
-    double spw, w, tb, si, us;
     if (get_str(kv, "device", t.device) && get_str(kv, "build", t.build) && get_str(kv, "class", t.klass) &&
-        get_num(kv, "steps_per_warp", spw) && get_num(kv, "warps_per_cta", w) && get_num(kv, "tile_box", tb) &&
-        get_num(kv, "sort_interval", si) && get_num(kv, "us_per_substep", us)) {
-      t.steps_per_warp = (int)spw;
-      t.warps_per_cta = (int)w;
-      t.tile_box = (int)tb;
-      t.sort_interval = (int)si;
-      t.us_per_substep = us;
+        get_int(kv, "steps_per_warp", t.steps_per_warp) && get_int(kv, "warps_per_cta", t.warps_per_cta) &&
+        get_int(kv, "tile_box", t.tile_box) && get_int(kv, "sort_interval", t.sort_interval) &&
+        get_num(kv, "us_per_substep", t.us_per_substep))
       out.push_back(t);
-    }
   }
   return out;
 }
@@ -155,6 +171,7 @@ bool find_tuning(const std::vector<TuningEntry>& entries, const std::string& dev
 }
 
 bool store_tuning(const std::string& path, const TuningEntry& e) {
+  if (foreign_file(path)) return false;  // not a cache file: leave it alone
   bool ok = true;
   std::vector<TuningEntry> entries = read_tuning_cache(path, &ok);
   bool replaced = false;

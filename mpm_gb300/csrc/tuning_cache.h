@@ -24,14 +24,16 @@ struct TuningEntry {
 };
 
 // Entries of the cache file at `path` (empty when it is missing or holds none).  Entries
-// with a missing or malformed field are skipped; *ok (may be null) is false when the file
+// with a missing or malformed field (a count that is not a 32-bit integer, a number that
+// is not finite) are skipped; *ok (may be null) is false when the file
 // exists but is not a cache file of this format.
 std::vector<TuningEntry> read_tuning_cache(const std::string& path, bool* ok = nullptr);
 // The entry with this device, build and class, if any.
 bool find_tuning(const std::vector<TuningEntry>& entries, const std::string& device, const std::string& build,
                  const std::string& klass, TuningEntry* out);
 // Writes the entries, replacing one with the same (device, build, class) as `e` or adding
-// it; the file is written to a temporary name and renamed into place.  False on I/O error.
+// it; the file is written to a temporary name and renamed into place.  False on I/O error,
+// and when `path` holds a file that is not a cache of this format (it is left unchanged).
 bool store_tuning(const std::string& path, const TuningEntry& e);
 
 }  // namespace mpm

@@ -94,3 +94,21 @@ def test_foreign_and_damaged_files(tool, tmp_path):
          "sort_interval": 0, "us_per_substep": 2.0}]}))
     assert run(tool, mixed, "find", "a", "b", "c")[0] == "miss"
     assert run(tool, mixed, "find", "a", "b", "d")[0] == "hit"
+    # counts out of the int range or not integral, and non-finite times, skip the entry
+    odd = tmp_path / "odd.json"
+    odd.write_text('{"format": "mpm_gb300 tuning cache 1", "entries": ['
+                   '{"device": "a", "build": "b", "class": "c", "steps_per_warp": 1e300, "warps_per_cta": 12, '
+                   '"tile_box": 1, "sort_interval": 0, "us_per_substep": 1.0},'
+                   '{"device": "a", "build": "b", "class": "d", "steps_per_warp": 2.5, "warps_per_cta": 12, '
+                   '"tile_box": 1, "sort_interval": 0, "us_per_substep": 1.0},'
+                   '{"device": "a", "build": "b", "class": "e", "steps_per_warp": 2, "warps_per_cta": 12, '
+                   '"tile_box": 1, "sort_interval": 0, "us_per_substep": 1e999}]}')
+    for k in "cde":
+        assert run(tool, odd, "find", "a", "b", k)[0] == "miss"
+    # a file that is not a cache is never overwritten by a store
+    r = subprocess.run([tool, str(foreign), "store", "a", "b", "c", "2", "12", "1", "0", "1.0"], capture_output=True)
+    assert r.returncode == 3
+    assert foreign.read_text() == '{"something": "else"}'
+    # a damaged cache of this format is ours: a store rewrites it with its readable entries
+    run(tool, damaged, "store", "a", "b", "z", 2, 12, 1, 0, 1.0)
+    assert run(tool, damaged, "find", "a", "b", "z")[0] == "hit"
