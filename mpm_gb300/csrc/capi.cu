@@ -1059,6 +1059,7 @@ namespace {
 // smooth_mesh on device arrays and its outcome as a status.
 mpm_status smooth_device(mpm_ctx* c, double* V, int64_t nv, const int32_t* F, int64_t nf, int32_t* iterations) {
   if (nv > 0 && nf == 0) return fail(c, MPM_ERR_INVALID, "smooth: vertices without faces (the system is singular)");
+  if (nv == 0 && nf > 0) return fail(c, MPM_ERR_INVALID, "smooth: a face index is outside [0, n_vertices)");
   SmoothResult r;
   cudaError_t e = smooth_mesh(V, F, nv, nf, c->smooth, c->stream, &c->launches, &r);
   if (e != cudaSuccess)

@@ -142,6 +142,9 @@ def test_smooth_errors_and_empty(gpu_lib):
     # vertices without faces: singular
     with pytest.raises(_lib.MpmError):
         sim.smooth_mesh(V, np.zeros((0, 3), np.int32))
+    # faces without vertices: every index is out of range
+    with pytest.raises(_lib.MpmError):
+        sim.smooth_mesh(np.zeros((0, 3)), F)
     # nothing to smooth
     assert sim.smooth_mesh(np.zeros((0, 3)), np.zeros((0, 3), np.int32)).shape == (0, 3)
     # the input is unchanged by a refused call, and the context still works
