@@ -259,7 +259,12 @@ __global__ void __launch_bounds__(kStepThreads, 1) batch_step_kernel(const __gri
             p2g_prepare_f<false>(M, K, F, Jp, Cm, v, pc, f, E, q0, m);
           }
         }
-        p2g_scatter_step<false>(wbuf, lane, key, w, q0, E, m, 1.f, gout, N);
+        // every particle of a scene has the scene's mass: unit-mass columns, each run's
+        // summed weight scaled by it (the single-run walk made this larger kernel slower)
+        if (__ballot_sync(kFull, key >= 0) != 0u) {
+          if (key >= 0) p2g_write_column_f<true>(wbuf, lane, w, q0, E, m);
+          warp_scatter_runs<false>(wbuf, lane, key, gout, N, M.mass);
+        }
       }
     }
     if (P2G) {
