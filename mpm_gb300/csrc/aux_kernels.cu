@@ -11,21 +11,24 @@ namespace mpm {
 // histogram (warp-aggregated atomics) -> exclusive scan -> scatter.  Order inside
 // a cell is not stable; the substep does not depend on it.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t cell_key_of(const float x[3], float dx_inv, int N) {
+// *outside (when given): the particle lies completely outside the domain, by the test
+// and the base cells the substep uses (so the two always agree).
+__device__ __forceinline__ uint32_t cell_key_of(const float x[3], float dx_inv, int N, bool* outside = nullptr) {
   int b[3];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    int v = QuadraticInterpolationKernel::base_cell(x[d], dx_inv);
-    b[d] = min(max(v, 0), N - 1);
-  }
+  for (int d = 0; d < 3; ++d) b[d] = QuadraticInterpolationKernel::base_cell(x[d], dx_inv);
+  if (outside) *outside = outside_domain(b[0], b[1], b[2], N);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) b[d] = min(max(b[d], 0), N - 1);
   const uint32_t nb = (uint32_t)(N + 3) >> 2;
   const uint32_t brick = ((uint32_t)(b[0] >> 2) * nb + (uint32_t)(b[1] >> 2)) * nb + (uint32_t)(b[2] >> 2);
   return brick * 64u + (uint32_t)(((b[0] & 3) << 4) | ((b[1] & 3) << 2) | (b[2] & 3));
 }
 
-__device__ __forceinline__ uint32_t cell_key(const float* s, int64_t st, int64_t p, float dx_inv, int N) {
+__device__ __forceinline__ uint32_t cell_key(const float* s, int64_t st, int64_t p, float dx_inv, int N,
+                                             bool* outside = nullptr) {
   const float x[3] = {s[(kX + 0) * st + p], s[(kX + 1) * st + p], s[(kX + 2) * st + p]};
-  return cell_key_of(x, dx_inv, N);
+  return cell_key_of(x, dx_inv, N, outside);
 }
 
 // Scene of particle p in a batch (binary search over the scene offsets).
@@ -38,13 +41,19 @@ __device__ __forceinline__ int scene_of(const int64_t* start, int nscenes, int64
   return lo;
 }
 
+// The stored sort key of particle p: its bricked cell key, with kKeyOutside set in a
+// partial sort when the particle lies completely outside the domain.
 __device__ __forceinline__ uint32_t sort_key(const SortArgs& a, int64_t p) {
+  bool outside = false;
+  uint32_t key;
   if (a.nscenes > 0) {
     const int sc = scene_of(a.scene_start, a.nscenes, p);
     const GridConsts& g = a.scenes[sc].g;
-    return a.scene_key_base[sc] + cell_key(a.sA, a.stride, p, g.dx_inv, g.N);
+    key = a.scene_key_base[sc] + cell_key(a.sA, a.stride, p, g.dx_inv, g.N, &outside);
+  } else {
+    key = cell_key(a.sA, a.stride, p, a.dx_inv, a.N, &outside);
   }
-  return cell_key(a.sA, a.stride, p, a.dx_inv, a.N);
+  return (a.partial && outside) ? (key | kKeyOutside) : key;
 }
 
 __global__ void sort_histogram(SortArgs a) {
@@ -55,7 +64,7 @@ __global__ void sort_histogram(SortArgs a) {
     uint32_t key = valid ? sort_key(a, p) : 0xffffffffu;
     if (valid) a.keys[p] = key;
     const unsigned same = __match_any_sync(kFull, key);
-    if (valid && lane == __ffs(same) - 1) atomicAdd(a.counts + key, __popc(same));
+    if (valid && lane == __ffs(same) - 1) atomicAdd(a.counts + (key & ~kKeyOutside), __popc(same));
   }
 }
 
@@ -139,11 +148,34 @@ __device__ __forceinline__ int moved_comp(int c) {
   return LIQ ? (c < kLiquidComps - 1 ? c : kJp) : c;
 }
 
+// Component k of the c-th component the substep reads back from memory when the
+// particle's G2P runs: x and J (liquid layout); x, F and Jp (general layout).  v and C
+// are G2P outputs, rewritten before they are read again.
+template <bool LIQ>
+__device__ __forceinline__ int carried_comp(int c) {
+  return c < 3 ? kX + c : ((LIQ || c == 12) ? kJp : kF + (c - 3));
+}
+
+template <bool LIQ, bool PARTIAL>
+__device__ __forceinline__ void move_particle(const float* __restrict__ sA, float* __restrict__ sB, int64_t st,
+                                              int64_t p, int64_t q) {
+  constexpr int NC = PARTIAL ? (LIQ ? 4 : 13) : (LIQ ? kLiquidComps : kNumComps);
+  float vals[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) vals[c] = __ldg(sA + (PARTIAL ? carried_comp<LIQ>(c) : moved_comp<LIQ>(c)) * st + p);
+#pragma unroll
+  for (int c = 0; c < NC; ++c) sB[(PARTIAL ? carried_comp<LIQ>(c) : moved_comp<LIQ>(c)) * st + q] = vals[c];
+}
+
 // Scatter every particle to its sorted slot.  All components of a particle are
 // loaded before any is stored, so a thread keeps 16 or 25 loads in flight.
-template <bool LIQ>
+// PARTIAL: the launch after the sort runs G2P on every particle inside the domain
+// (the P2G of the next substep is already on the grid), which rewrites v and C
+// without reading them, so those particles move only their carried components; a
+// particle flagged outside the domain keeps its whole state through the substep and
+// moves all of it.
+template <bool LIQ, bool PARTIAL>
 __global__ void sort_scatter(SortArgs a) {
-  constexpr int NC = LIQ ? kLiquidComps : kNumComps;
   const int lane = threadIdx.x & 31;
   const float* __restrict__ sA = a.sA;
   float* __restrict__ sB = a.sB;
@@ -155,15 +187,14 @@ __global__ void sort_scatter(SortArgs a) {
     const unsigned same = __match_any_sync(kFull, key);
     const int leader = __ffs(same) - 1;
     int start = 0;
-    if (valid && lane == leader) start = atomicAdd(a.counts + key, __popc(same));
+    if (valid && lane == leader) start = atomicAdd(a.counts + (key & ~kKeyOutside), __popc(same));
     start = __shfl_sync(kFull, start, leader);
     if (!valid) continue;
     const int64_t q = (int64_t)start + __popc(same & ((1u << lane) - 1u));
-    float vals[NC];
-#pragma unroll
-    for (int c = 0; c < NC; ++c) vals[c] = __ldg(sA + moved_comp<LIQ>(c) * st + p);
-#pragma unroll
-    for (int c = 0; c < NC; ++c) sB[moved_comp<LIQ>(c) * st + q] = vals[c];
+    if (PARTIAL && !(key & kKeyOutside))
+      move_particle<LIQ, true>(sA, sB, st, p, q);
+    else
+      move_particle<LIQ, false>(sA, sB, st, p, q);
     if (a.matA) a.matB[q] = a.matA[p];
     a.idB[q] = a.idA[p];
   }
@@ -181,7 +212,7 @@ __global__ void sort_rank(SortArgs a) {
     const unsigned same = __match_any_sync(kFull, key);
     const int leader = __ffs(same) - 1;
     int start = 0;
-    if (valid && lane == leader) start = atomicAdd(a.counts + key, __popc(same));
+    if (valid && lane == leader) start = atomicAdd(a.counts + (key & ~kKeyOutside), __popc(same));
     start = __shfl_sync(kFull, start, leader);
     if (valid) a.perm[(int64_t)start + __popc(same & ((1u << lane) - 1u))] = (uint32_t)p;
   }
@@ -321,9 +352,14 @@ cudaError_t launch_sort(const SortArgs& a, int num_sms, cudaStream_t st, int64_t
       sort_gather<false><<<blocks, kThreads, 0, st>>>(a);
     n_launch += 1;
   } else if (a.ncomp == kLiquidComps) {
-    sort_scatter<true><<<blocks, kThreads, 0, st>>>(a);
+    if (a.partial)
+      sort_scatter<true, true><<<blocks, kThreads, 0, st>>>(a);
+    else
+      sort_scatter<true, false><<<blocks, kThreads, 0, st>>>(a);
+  } else if (a.partial) {
+    sort_scatter<false, true><<<blocks, kThreads, 0, st>>>(a);
   } else {
-    sort_scatter<false><<<blocks, kThreads, 0, st>>>(a);
+    sort_scatter<false, false><<<blocks, kThreads, 0, st>>>(a);
   }
   if (launches) *launches += n_launch;
   return cudaGetLastError();

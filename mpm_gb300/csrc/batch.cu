@@ -128,7 +128,8 @@ mpm_status launch(mpm_batch* b, StepKind kind) {
   return MPM_OK;
 }
 
-mpm_status sort(mpm_batch* b) {
+// g2p_next: as run_sort in capi.cu (the launch after the sort is a fused launch)
+mpm_status sort(mpm_batch* b, bool g2p_next) {
   SortArgs s{};
   s.sA = b->sA;
   s.sB = b->sB;
@@ -147,6 +148,7 @@ mpm_status sort(mpm_batch* b) {
   s.scene_start = b->d_start;
   s.scene_key_base = b->d_key_base;
   s.scenes = b->d_scenes;
+  s.partial = g2p_next && b->key_space <= (int64_t)kKeyOutside;
   BCUDA(b, launch_sort(s, b->num_sms, b->stream, &b->launches));
   std::swap(b->sA, b->sB);
   std::swap(b->matA, b->matB);
@@ -158,7 +160,7 @@ mpm_status sort(mpm_batch* b) {
 mpm_status advance(mpm_batch* b, int32_t nsteps) {
   for (int32_t i = 0; i < nsteps; ++i) {
     if (b->sort_interval > 0 && b->since_sort >= b->sort_interval) {
-      mpm_status st = sort(b);
+      mpm_status st = sort(b, b->pending);
       if (st != MPM_OK) return st;
     }
     if (!b->pending) {
@@ -362,7 +364,7 @@ mpm_status mpm_batch_substep_graph(mpm_batch* b, int32_t nsteps) {
     uint32_t* iA = b->idA;
     uint32_t* iB = b->idB;
     BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    mpm_status st = sorting ? sort(b) : MPM_OK;
+    mpm_status st = sorting ? sort(b, true) : MPM_OK;  // the P2G of the run ran before the capture
     for (int32_t i = 0; i < nsteps && st == MPM_OK; ++i) st = launch(b, kStepFused);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);

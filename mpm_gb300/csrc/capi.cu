@@ -372,7 +372,10 @@ mpm_status run_step(mpm_ctx* c, StepKind kind) {
   return MPM_OK;
 }
 
-mpm_status run_sort(mpm_ctx* c) {
+// g2p_next: the launch after this sort is a G2P launch over the sorted particles (the
+// P2G of its substep is already on the grid), so the sort may move only what that
+// launch reads back (SortArgs::partial).
+mpm_status run_sort(mpm_ctx* c, bool g2p_next) {
   if (c->n == 0) return MPM_OK;
   SortArgs s{};
   s.sA = c->sA;
@@ -393,6 +396,8 @@ mpm_status run_sort(mpm_ctx* c) {
   s.dx_inv = c->K.g.dx_inv;
   // liquid layout: x, v, C, J (16 components); general: all 25
   s.ncomp = c->liquid_layout ? kLiquidComps : kNumComps;
+  // guarded particles skip G2P and scatter their stored v and C, so they keep the full move
+  s.partial = g2p_next && !c->unsorted && c->params.g2p_guard == 0 && c->sort_keys <= (int64_t)kKeyOutside;
   MPM_CUDA(c, launch_sort(s, c->num_sms, c->stream, &c->launches));
   std::swap(c->sA, c->sB);
   std::swap(c->matA, c->matB);
@@ -771,7 +776,7 @@ mpm_status mpm_substep(mpm_ctx* c, int32_t nsteps) {
     }
     if (c->n > 0) {
       if (c->params.sort_interval > 0 && c->since_sort >= c->params.sort_interval) {
-        st = run_sort(c);
+        st = run_sort(c, c->pending);
         if (st != MPM_OK) return st;
       }
       if (!c->pending) {
@@ -1240,7 +1245,7 @@ mpm_status mpm_check_wait_timeout(mpm_ctx* c, int32_t polls) {
 
 mpm_status mpm_sort(mpm_ctx* c) {
   if (!c) return MPM_ERR_INVALID;
-  return run_sort(c);
+  return run_sort(c, false);
 }
 
 mpm_status mpm_substep_many(mpm_ctx* const* ctxs, int32_t count, int32_t nsteps) {

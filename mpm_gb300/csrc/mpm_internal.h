@@ -147,12 +147,18 @@ struct SortArgs {
   int N;
   float dx_inv;
   int ncomp;            // kLiquidComps (x, v, C, J) or kNumComps (all)
+  // nonzero: the next launch runs G2P on the sorted particles (its P2G grid is already
+  // built), so particles inside the domain move only x, J (and F); a scatter sort only,
+  // key space at most kKeyOutside
+  int partial;
   // batch mode (nscenes > 0): keys are scene_key_base[scene] + the bricked key in the scene's grid
   int nscenes;
   const int64_t* scene_start;      // nscenes + 1 particle offsets
   const uint32_t* scene_key_base;  // nscenes
   const SceneDev* scenes;
 };
+// Bit of a stored sort key that flags a particle completely outside the domain (partial sorts).
+constexpr uint32_t kKeyOutside = 0x80000000u;
 cudaError_t launch_sort(const SortArgs& a, int num_sms, cudaStream_t st, int64_t* launches);
 
 // Host-interleaved <-> component-major conversion.

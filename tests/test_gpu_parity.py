@@ -111,6 +111,35 @@ def test_sort_does_not_change_results(gpu_lib, oracle_lib, sort_interval):
     assert max(errs.values()) < 2e-5, errs
 
 
+@pytest.mark.parametrize("kind", ["liquid", "snow"])
+def test_sort_keeps_particles_outside_the_domain(gpu_lib, oracle_lib, kind):
+    """A sort between substeps moves only what the next G2P reads back (x and J, or x, F
+    and Jp) for particles inside the domain: their v and C are rewritten by that G2P.
+    Particles completely outside the domain skip G2P and keep their whole state, so the
+    sort moves all of it; here they carry random v, C (and F) that must come back intact
+    after sorts between every substep."""
+    from helpers import FIELDS
+    from mpm_gb300 import scenes
+
+    cfg = scenes.config_liquid(n=60_000, seed=7) if kind == "liquid" else scenes.config_snow(n=60_000, seed=7, N=32)
+    st = cfg["state"]
+    rng = np.random.default_rng(8)
+    idx = rng.choice(st["x"].shape[0], 500, replace=False)
+    st["x"][idx] = rng.uniform(-0.9, -0.3, (500, 3)).astype(np.float32)  # base cells below -3
+    st["v"][idx] = rng.standard_normal((500, 3)).astype(np.float32)
+    st["C"][idx] = rng.standard_normal((500, 3, 3)).astype(np.float32)
+    if kind == "snow":
+        st["F"][idx] += (0.01 * rng.standard_normal((500, 3, 3))).astype(np.float32)
+        st["Jp"][idx] = rng.uniform(0.9, 1.1, 500).astype(np.float32)
+    out, _ = run_gpu(cfg, 5, sort_interval=1)
+    kept = ("x", "v", "C", "Jp") if kind == "liquid" else FIELDS  # the liquid layout stores no F
+    for k in kept:
+        assert np.array_equal(out[k][idx], st[k][idx]), k
+    o32, _, _ = run_oracle(oracle_lib, cfg, 5, np.float32)
+    errs = compare_states(out, o32, cfg["params"], cfg["state"])
+    assert max(errs.values()) < 2e-5, errs
+
+
 @pytest.mark.parametrize("tuning", [(1,), (4,), (16,), (8,)])
 def test_tuning_variants(gpu_lib, oracle_lib, tuning):
     """Range sizes (steps per warp) give the same result."""
