@@ -542,8 +542,8 @@ __global__ void __launch_bounds__(kRowsPerBlock) interleave_arrays_kernel(const 
 }  // namespace
 
 cudaError_t launch_deinterleave_arrays(HostArrays a, float* s, int64_t stride, int64_t n, int* bad, cudaStream_t st,
-                                       const uint32_t* dest) {
-  cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), st);
+                                       const uint32_t* dest, bool bad_zeroed) {
+  cudaError_t e = bad_zeroed ? cudaSuccess : cudaMemsetAsync(bad, 0, sizeof(int), st);
   if (e != cudaSuccess || n == 0) return e;
   deinterleave_arrays_kernel<<<(unsigned)((n + kRowsPerBlock - 1) / kRowsPerBlock), kRowsPerBlock, 0, st>>>(
       a, s, stride, n, dest, bad);
@@ -565,9 +565,9 @@ cudaError_t launch_inverse(const uint32_t* id, int64_t n, uint32_t* inv, cudaStr
 }
 
 cudaError_t launch_presort(const float* x, float* xcopy, const SortArgs& a, uint32_t* dest, int* bad, int num_sms,
-                           cudaStream_t st, int64_t* launches) {
+                           cudaStream_t st, int64_t* launches, bool bad_zeroed) {
   if (a.n == 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), st);
+  cudaError_t e = bad_zeroed ? cudaSuccess : cudaMemsetAsync(bad, 0, sizeof(int), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(a.counts, 0, sizeof(int) * a.cells, st);
   if (e != cudaSuccess) return e;
   const int blocks = (int)std::min<int64_t>((a.n + kThreads - 1) / kThreads, (int64_t)num_sms * 8);

@@ -77,6 +77,10 @@ struct mpm_ctx {
   size_t stage_bytes = 0;
   int* status = nullptr;
   int* work = nullptr;  // [2]: upload position check, [3]: cell-order position check
+  // the two position checks of an upload in cell order, in mapped pinned memory: the
+  // kernels write them and the host reads them after its synchronisation (no copy)
+  int* host_flags = nullptr;
+  int* host_flags_dev = nullptr;
   bool unsorted = true;  // particle order unrelated to cells (upload, append): the next sort gathers
 
   int64_t substeps = 0;
@@ -510,6 +514,8 @@ mpm_status mpm_create(const mpm_params* params, mpm_ctx** out) {
   if (cudaMalloc(&c->status, sizeof(int)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
   if (cudaMalloc(&c->work, 4 * sizeof(int)) != cudaSuccess) return bail(MPM_ERR_NOMEM);
   if (cudaMemsetAsync(c->work, 0, 4 * sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
+  if (cudaHostAlloc(&c->host_flags, 4 * sizeof(int), cudaHostAllocMapped) != cudaSuccess) return bail(MPM_ERR_NOMEM);
+  if (cudaHostGetDevicePointer(&c->host_flags_dev, c->host_flags, 0) != cudaSuccess) return bail(MPM_ERR_CUDA);
 
   if (cudaMemsetAsync(c->status, 0, sizeof(int), c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(MPM_ERR_CUDA);
@@ -543,6 +549,7 @@ mpm_status mpm_destroy(mpm_ctx* c) {
   cudaFree(c->stage);
   cudaFree(c->status);
   cudaFree(c->work);
+  cudaFreeHost(c->host_flags);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return MPM_OK;
@@ -670,14 +677,17 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
       so.cells = c->sort_keys;
       so.N = (int)c->params.N;
       so.dx_inv = c->K.g.dx_inv;
-      // the check flag is read once, at the end: until then only the spare copy, the stage
-      // and sort scratch have been written, so a rejected upload leaves the context as it was
-      MPM_CUDA(c, launch_presort(arr.x, xcopy, so, c->idB, c->work + 3, c->num_sms, c->stream, &c->launches));
+      // the check flags are read once, at the end: until then only the spare copy, the stage
+      // and sort scratch have been written, so a rejected upload leaves the context as it was.
+      // No kernel still writes the flags: both paths synchronised the stream above.
+      volatile int* flags = c->host_flags;
+      flags[0] = 0;
+      flags[1] = 0;
+      MPM_CUDA(c, launch_presort(arr.x, xcopy, so, c->idB, c->host_flags_dev + 1, c->num_sms, c->stream, &c->launches,
+                                 true));
       HostArrays sorted_arr = arr;
       if (xcopy) sorted_arr.x = xcopy;
-      MPM_CUDA(c, launch_deinterleave_arrays(sorted_arr, c->sB, c->stride, n, c->work + 2, c->stream, c->idB));
-      int flags[2] = {0, 0};
-      MPM_CUDA(c, cudaMemcpyAsync(flags, c->work + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      MPM_CUDA(c, launch_deinterleave_arrays(sorted_arr, c->sB, c->stride, n, c->host_flags_dev, c->stream, c->idB, true));
       MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // also: the caller may reuse the host arrays on return
       if (flags[0] || flags[1]) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
       // slot q holds particle perm[q]: that is the id array

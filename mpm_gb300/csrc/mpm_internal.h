@@ -173,16 +173,17 @@ struct OutArrays {
   float *x, *v, *C, *F, *J;
 };
 // Arrays -> component-major particle arrays in one pass (missing fields take their rest
-// values); *bad = 1 when a position is not finite.
+// values); *bad = 1 when a position is not finite (*bad is zeroed first on the stream
+// unless bad_zeroed: a flag the caller cleared, e.g. in mapped host memory).
 cudaError_t launch_deinterleave_arrays(HostArrays a, float* s, int64_t stride, int64_t n, int* bad, cudaStream_t st,
-                                       const uint32_t* dest = nullptr);
+                                       const uint32_t* dest = nullptr, bool bad_zeroed = false);
 // Cell order of positions before they are uploaded (x: x, y, z per particle, host-visible
 // or device memory): keys and counts of a (keys, counts, block_sums, cells, N, dx_inv, n),
 // the permutation into a.perm (slot q holds particle perm[q]) and its inverse into dest
 // (particle p goes to slot dest[p]); a copy of the positions into xcopy when not null;
-// *bad = 1 when a position is not finite.
+// *bad = 1 when a position is not finite (zeroed first unless bad_zeroed, as above).
 cudaError_t launch_presort(const float* x, float* xcopy, const SortArgs& a, uint32_t* dest, int* bad, int num_sms,
-                           cudaStream_t st, int64_t* launches);
+                           cudaStream_t st, int64_t* launches, bool bad_zeroed = false);
 // Component-major particle arrays -> the non-null arrays in upload order (inv as from
 // launch_inverse, null for the identity).
 cudaError_t launch_interleave_arrays(const float* s, int64_t stride, const uint32_t* inv, int64_t n, OutArrays o,

@@ -140,6 +140,26 @@ def test_sort_keeps_particles_outside_the_domain(gpu_lib, oracle_lib, kind):
     assert max(errs.values()) < 2e-5, errs
 
 
+@pytest.mark.parametrize("kind", ["liquid", "snow"])
+def test_explicit_sort_moves_the_whole_state(gpu_lib, kind):
+    """mpm_sort between calls is followed by no G2P of its own, so it moves every
+    component: a download after it returns exactly what the download before it did."""
+    from mpm_gb300 import scenes
+    from mpm_gb300.simulation import Simulation
+
+    cfg = scenes.config_liquid(n=40_000, seed=3) if kind == "liquid" else scenes.config_snow(n=40_000, seed=3, N=32)
+    with Simulation.from_config(cfg, sort_interval=2) as sim:
+        sim.upload(cfg["state"])
+        sim.advance(5)
+        before = sim.download()
+        sim.sort()
+        after = sim.download()
+        for k in before:
+            assert np.array_equal(before[k], after[k]), k
+        sim.advance(3)  # and the run goes on from the sorted state
+        assert np.isfinite(sim.download()["x"]).all()
+
+
 @pytest.mark.parametrize("tuning", [(1,), (4,), (16,), (8,)])
 def test_tuning_variants(gpu_lib, oracle_lib, tuning):
     """Range sizes (steps per warp) give the same result."""
@@ -275,6 +295,12 @@ def test_check_finite_flags_non_finite_state(gpu_lib):
             with pytest.raises(_lib.MpmError) as ei:
                 sim.upload(bad)
             assert ei.value.code == 1
+        # the same count: the upload that puts particles in cell order checks them too
+        same = {k: v.copy() for k, v in good.items()}
+        same["x"][5] = [0.5, 0.5, np.nan]
+        with pytest.raises(_lib.MpmError) as ei:
+            sim.upload(same)
+        assert ei.value.code == 1
         assert sim.n == len(good["x"]) and sim.substeps == 2
         after = sim.download()
         for k in before:
