@@ -41,6 +41,12 @@ __device__ __forceinline__ int scene_of(const int64_t* start, int nscenes, int64
   return lo;
 }
 
+// The counter of a stored key: partial sorts (key spaces of at most 2^31) flag keys in bit
+// 31; other sorts use every bit (batches may have key spaces up to 2^32).
+__device__ __forceinline__ uint32_t key_slot(const SortArgs& a, uint32_t key) {
+  return a.partial ? (key & ~kKeyOutside) : key;
+}
+
 // The stored sort key of particle p: its bricked cell key, with kKeyOutside set in a
 // partial sort when the particle lies completely outside the domain.
 __device__ __forceinline__ uint32_t sort_key(const SortArgs& a, int64_t p) {
@@ -64,7 +70,7 @@ __global__ void sort_histogram(SortArgs a) {
     uint32_t key = valid ? sort_key(a, p) : 0xffffffffu;
     if (valid) a.keys[p] = key;
     const unsigned same = __match_any_sync(kFull, key);
-    if (valid && lane == __ffs(same) - 1) atomicAdd(a.counts + (key & ~kKeyOutside), __popc(same));
+    if (valid && lane == __ffs(same) - 1) atomicAdd(a.counts + key_slot(a, key), __popc(same));
   }
 }
 
@@ -187,7 +193,7 @@ __global__ void sort_scatter(SortArgs a) {
     const unsigned same = __match_any_sync(kFull, key);
     const int leader = __ffs(same) - 1;
     int start = 0;
-    if (valid && lane == leader) start = atomicAdd(a.counts + (key & ~kKeyOutside), __popc(same));
+    if (valid && lane == leader) start = atomicAdd(a.counts + key_slot(a, key), __popc(same));
     start = __shfl_sync(kFull, start, leader);
     if (!valid) continue;
     const int64_t q = (int64_t)start + __popc(same & ((1u << lane) - 1u));
@@ -212,7 +218,7 @@ __global__ void sort_rank(SortArgs a) {
     const unsigned same = __match_any_sync(kFull, key);
     const int leader = __ffs(same) - 1;
     int start = 0;
-    if (valid && lane == leader) start = atomicAdd(a.counts + (key & ~kKeyOutside), __popc(same));
+    if (valid && lane == leader) start = atomicAdd(a.counts + key_slot(a, key), __popc(same));
     start = __shfl_sync(kFull, start, leader);
     if (valid) a.perm[(int64_t)start + __popc(same & ((1u << lane) - 1u))] = (uint32_t)p;
   }
