@@ -82,6 +82,10 @@ struct mpm_ctx {
   int* host_flags = nullptr;
   int* host_flags_dev = nullptr;
   bool unsorted = true;  // particle order unrelated to cells (upload, append): the next sort gathers
+  // the inverse of the id permutation while the ids are unchanged: the one a cell-ordered
+  // upload leaves in the sort scratch, or the last one computed into the spare id copy;
+  // null when it has to be computed (inverse_ids)
+  const uint32_t* inv = nullptr;
 
   int64_t substeps = 0;
   int64_t since_sort = 0;
@@ -205,6 +209,7 @@ void free_particles(mpm_ctx* c) {
 
 mpm_status ensure_particles(mpm_ctx* c, int64_t n) {
   if (n <= c->capacity && c->sA) return MPM_OK;
+  c->inv = nullptr;
   free_particles(c);
   const int64_t cap = std::max<int64_t>(64, (n + 63) / 64 * 64);
   const size_t fbytes = sizeof(float) * (size_t)kNumComps * cap;
@@ -243,6 +248,7 @@ mpm_status grow_particles(mpm_ctx* c, int64_t need) {
   MPM_CUDA(c, cudaMemcpyAsync(mA, c->matA, c->n, cudaMemcpyDeviceToDevice, c->stream));
   MPM_CUDA(c, cudaMemcpyAsync(iA, c->idA, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToDevice, c->stream));
   MPM_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->inv = nullptr;
   free_particles(c);
   c->sA = sA;
   c->sB = sB;
@@ -262,6 +268,7 @@ void free_objects(mpm_ctx* c) {
 
 // The particle set changed: the next substep re-sorts and restarts with a P2G launch.
 void particles_changed(mpm_ctx* c) {
+  c->inv = nullptr;
   c->pending = false;
   c->since_sort = c->params.sort_interval;
 }
@@ -402,6 +409,7 @@ mpm_status run_sort(mpm_ctx* c, bool g2p_next) {
   s.ncomp = c->liquid_layout ? kLiquidComps : kNumComps;
   // guarded particles skip G2P and scatter their stored v and C, so they keep the full move
   s.partial = g2p_next && !c->unsorted && c->params.g2p_guard == 0 && c->sort_keys <= (int64_t)kKeyOutside;
+  c->inv = nullptr;
   MPM_CUDA(c, launch_sort(s, c->num_sms, c->stream, &c->launches));
   std::swap(c->sA, c->sB);
   std::swap(c->matA, c->matB);
@@ -613,6 +621,7 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   // buffer with copies.  When the particle arrays keep their size, the conversion writes
   // the spare copy, which replaces the current one after the check.
   const bool grow = n > c->capacity || !c->sA;
+  c->inv = nullptr;  // every path below writes the spare id copy or the sort scratch
   // a per-particle material array keeps the upload order (its bytes are copied as given),
   // so only uploads without one are put in cell order on the way in
   bool mixed = !c->liquid_layout && c->n_materials > 1;
@@ -671,28 +680,31 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
       SortArgs so{};
       so.n = n;
       so.keys = c->keys;
-      so.perm = c->keys + c->capacity;
+      // slot q holds particle perm[q]: the new id array, written into the spare id copy
+      so.perm = c->idB;
+      uint32_t* dest = c->keys + c->capacity;  // particle p goes to slot dest[p]
       so.counts = c->counts;
       so.block_sums = c->block_sums;
       so.cells = c->sort_keys;
       so.N = (int)c->params.N;
       so.dx_inv = c->K.g.dx_inv;
-      // the check flags are read once, at the end: until then only the spare copy, the stage
-      // and sort scratch have been written, so a rejected upload leaves the context as it was.
+      // the check flags are read once, at the end: until then only the spare particle and id
+      // copies, the stage and sort scratch have been written, so a rejected upload leaves the
+      // context as it was.
       // No kernel still writes the flags: both paths synchronised the stream above.
       volatile int* flags = c->host_flags;
       flags[0] = 0;
       flags[1] = 0;
-      MPM_CUDA(c, launch_presort(arr.x, xcopy, so, c->idB, c->host_flags_dev + 1, c->num_sms, c->stream, &c->launches,
+      MPM_CUDA(c, launch_presort(arr.x, xcopy, so, dest, c->host_flags_dev + 1, c->num_sms, c->stream, &c->launches,
                                  true));
       HostArrays sorted_arr = arr;
       if (xcopy) sorted_arr.x = xcopy;
-      MPM_CUDA(c, launch_deinterleave_arrays(sorted_arr, c->sB, c->stride, n, c->host_flags_dev, c->stream, c->idB, true));
+      MPM_CUDA(c, launch_deinterleave_arrays(sorted_arr, c->sB, c->stride, n, c->host_flags_dev, c->stream, dest, true));
       MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // also: the caller may reuse the host arrays on return
       if (flags[0] || flags[1]) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
-      // slot q holds particle perm[q]: that is the id array
-      MPM_CUDA(c, cudaMemcpyAsync(c->idA, so.perm, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
       std::swap(c->sA, c->sB);
+      std::swap(c->idA, c->idB);
+      c->inv = dest;
       presorted = true;
     } else {
       if (direct) MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // earlier work may read the spare copy
@@ -865,14 +877,27 @@ mpm_status mpm_sync(mpm_ctx* c) {
   return MPM_OK;
 }
 
+// The inverse of the id permutation (the slot of each particle in upload order): the
+// cached one while the ids are unchanged, else computed into the spare id copy.
+cudaError_t inverse_ids(mpm_ctx* c, const uint32_t** inv) {
+  if (!c->inv) {
+    const cudaError_t e = launch_inverse(c->idA, c->n, c->idB, c->stream);
+    if (e != cudaSuccess) return e;
+    c->launches += c->n > 0;
+    c->inv = c->idB;
+  }
+  *inv = c->inv;
+  return cudaSuccess;
+}
+
 mpm_status mpm_download_soa(mpm_ctx* c, float* x, float* v, float* C, float* F, float* Jp, uint8_t* mat) {
   if (!c) return MPM_ERR_INVALID;
   const int64_t n = c->n;
   if (n == 0) return MPM_OK;
-  // the particles sit in cell order: invert the id array into the other id copy (free
-  // outside sorts and object updates) and gather in upload order
-  MPM_CUDA(c, launch_inverse(c->idA, n, c->idB, c->stream));
-  c->launches += 1;
+  // the particles sit in cell order: gather them in upload order through the inverse of
+  // the id array
+  const uint32_t* inv = nullptr;
+  MPM_CUDA(c, inverse_ids(c, &inv));
   {
     // pinned host arrays are written by the conversion kernel itself over the host link
     const void *dx = nullptr, *dv = nullptr, *dC = nullptr, *dF = nullptr, *dJ = nullptr;
@@ -881,7 +906,7 @@ mpm_status mpm_download_soa(mpm_ctx* c, float* x, float* v, float* C, float* F, 
                         (!F || device_view(F, 36 * n, &dF)) && (!Jp || device_view(Jp, 4 * n, &dJ));
     if (direct) {
       const OutArrays o{(float*)dx, (float*)dv, (float*)dC, (float*)dF, (float*)dJ};
-      MPM_CUDA(c, launch_interleave_arrays(c->sA, c->stride, c->idB, n, o, c->liquid_layout, c->stream));
+      MPM_CUDA(c, launch_interleave_arrays(c->sA, c->stride, inv, n, o, c->liquid_layout, c->stream));
       c->launches += 1;
       x = v = C = F = Jp = nullptr;  // written
     }
@@ -890,7 +915,7 @@ mpm_status mpm_download_soa(mpm_ctx* c, float* x, float* v, float* C, float* F, 
   if (st != MPM_OK) return st;
   const unsigned fields = (x ? kFieldX : 0) | (v ? kFieldV : 0) | (C ? kFieldC : 0) | (F ? kFieldF : 0) |
                           (Jp ? kFieldJ : 0);
-  MPM_CUDA(c, launch_interleave(c->sA, c->stride, c->idB, n, c->stage, c->liquid_layout, fields, c->stream));
+  MPM_CUDA(c, launch_interleave(c->sA, c->stride, inv, n, c->stage, c->liquid_layout, fields, c->stream));
   c->launches += fields != 0;
   float* xs = c->stage;
   float* vs = xs + 3 * n;
@@ -1156,15 +1181,16 @@ mpm_status mpm_export_particles(mpm_ctx* c, int32_t slot, float radius, int64_t*
     if (cudaMallocHost(&x.host, bytes) != cudaSuccess) return fail(c, MPM_ERR_NOMEM, "export: pinned buffer");
     x.cap = cnt;
   }
-  MPM_CUDA(c, launch_inverse(c->idA, cnt, c->idB, c->stream));
-  MPM_CUDA(c, launch_bgeo_pack(c->sA, c->stride, c->idB, cnt, radius, x.dev, c->stream));
+  const uint32_t* inv = nullptr;
+  MPM_CUDA(c, inverse_ids(c, &inv));
+  MPM_CUDA(c, launch_bgeo_pack(c->sA, c->stride, inv, cnt, radius, x.dev, c->stream));
   MPM_CUDA(c, cudaEventRecord(x.packed, c->stream));
   MPM_CUDA(c, cudaStreamWaitEvent(c->copy_stream, x.packed, 0));
   if (cnt > 0)
     MPM_CUDA(c, cudaMemcpyAsync(x.host, x.dev, (size_t)kBgeoRecordBytes * (size_t)cnt, cudaMemcpyDeviceToHost,
                                 c->copy_stream));
   MPM_CUDA(c, cudaEventRecord(x.copied, c->copy_stream));
-  c->launches += 2 * (cnt > 0);
+  c->launches += cnt > 0;
   x.n = cnt;
   x.pending = true;
   *n = cnt;
@@ -1207,9 +1233,10 @@ mpm_status mpm_render_positions_device(mpm_ctx* c, const float** positions) {
       return fail(c, MPM_ERR_NOMEM, "render: positions");
     c->positions_cap = c->n;
   }
-  MPM_CUDA(c, launch_inverse(c->idA, c->n, c->idB, c->stream));
-  MPM_CUDA(c, launch_project(c->sA, c->stride, c->idB, c->n, c->positions, c->stream));
-  c->launches += 2 * (c->n > 0);
+  const uint32_t* inv = nullptr;
+  MPM_CUDA(c, inverse_ids(c, &inv));
+  MPM_CUDA(c, launch_project(c->sA, c->stride, inv, c->n, c->positions, c->stream));
+  c->launches += c->n > 0;
   *positions = c->positions;
   return MPM_OK;
 }
@@ -1356,6 +1383,7 @@ mpm_status tuning_restore(mpm_ctx* c, mpm_ctx* t) {
   if (c->have_mat) MPM_CUDA(c, cudaMemcpyAsync(t->matA, c->matA, c->n, cudaMemcpyDeviceToDevice, t->stream));
   MPM_CUDA(c, cudaMemcpyAsync(t->idA, c->idA, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToDevice, t->stream));
   t->n = c->n;
+  t->inv = nullptr;
   t->have_mat = c->have_mat;
   t->unsorted = c->unsorted;
   t->pending = false;
