@@ -36,6 +36,39 @@ def test_batch_matches_oracle_per_scene(gpu_lib, oracle_lib):
         assert max(errs.values()) < 2e-5, (sc["params"]["N"], sc["material"].name, errs)
 
 
+def test_batch_sorts_keep_particles_outside_the_domain(gpu_lib, oracle_lib):
+    """The batch's sorts move only what the next fused launch reads back for particles
+    inside their scene's domain; particles completely outside it (each scene with its own
+    N) keep their whole state through sorts before every substep, in the launched and the
+    replayed-graph runs."""
+    from helpers import FIELDS
+    from mpm_gb300.batch import Batch
+
+    scs = small_batch(seed=4, nscenes=6)
+    rng = np.random.default_rng(5)
+    idx = []
+    for sc in scs:
+        st = sc["state"]
+        k = rng.choice(st["x"].shape[0], 50, replace=False)
+        st["x"][k] = rng.uniform(1.3, 1.9, (50, 3)).astype(np.float32)  # base cells past N
+        st["v"][k] = rng.standard_normal((50, 3)).astype(np.float32)
+        st["C"][k] = rng.standard_normal((50, 3, 3)).astype(np.float32)
+        st["F"][k] += (0.01 * rng.standard_normal((50, 3, 3))).astype(np.float32)
+        idx.append(k)
+    for graph in (False, True):
+        with Batch(scs, sort_interval=1) as b:
+            b.upload([s["state"] for s in scs])
+            b.advance(4, graph=graph)
+            outs = b.split(b.download())
+        for sc, out, k in zip(scs, outs, idx):
+            for f in FIELDS:
+                assert np.array_equal(out[f][k], sc["state"][f][k]), (graph, f)
+            if not graph:
+                ref = oracle_scene(oracle_lib, sc, 4)
+                errs = compare_states(out, ref, sc["params"], sc["state"])
+                assert max(errs.values()) < 2e-5, (sc["params"]["N"], sc["material"].name, errs)
+
+
 def test_batch_matches_single_scene_contexts(gpu_lib):
     from mpm_gb300.batch import Batch
     from mpm_gb300.simulation import Simulation
