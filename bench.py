@@ -479,6 +479,10 @@ def batched_section(args, stream, scs=None, rank=0, world=1):
     b = Batch(scs, sort_interval=16)
     b.set_stream(stream.cuda_stream)
     b.upload([s["state"] for s in scs])
+    # the range size of the batched kernel, chosen by the batch autotuner on a copy of the batch
+    from mpm_gb300 import autotune
+
+    tuning = autotune.tune_batch(b, autotune.default_cache_path(), budget_substeps=24)
     for _ in range(max(args.warmup, 3)):
         b.advance(sub, graph=True)
     torch.cuda.synchronize()
@@ -544,7 +548,7 @@ def batched_section(args, stream, scs=None, rank=0, world=1):
         sim.close()
     looped = max(c_loop, graph_rate or 0.0)
     return {"value": value, "unit": "particle-substeps/s", "ms_per_step": batched_ms_max / steps, "steps": steps,
-            "substeps_per_step": sub, "gpu_launches": launches,
+            "substeps_per_step": sub, "gpu_launches": launches, "tuning": tuning,
             "config": {"workload": "batched_256_scenes", "particles": n_all, "scenes": 256, "graph": True,
                        "parallelism": f"scenes split over {world} ranks" if world > 1 else "single",
                        "l2": "inputs larger than L2 (state ~1 GB)"},

@@ -45,3 +45,25 @@ def current(sim) -> dict:
     t = _lib.MpmTuning()
     _lib.check(sim.L.mpm_get_tuning(sim.ctx, ctypes.byref(t)), sim.ctx)
     return _as_dict(t)
+
+
+def _batch_dict(t: _lib.MpmTuning) -> dict:
+    return {"steps_per_warp": t.steps_per_warp, "warps_per_cta": t.warps_per_cta, "sort_interval": t.sort_interval,
+            "us_per_substep": t.us_per_substep, "from_cache": bool(t.from_cache), "candidates": t.candidates}
+
+
+def tune_batch(batch, cache_path: str | None = None, budget_substeps: int = 0, ignore_cache: bool = False) -> dict:
+    """Chooses and applies the range size (steps per warp) of a Batch with particles, timed
+    as replayed graphs on a copy of the batch (mpm_batch_autotune).  Returns the choice."""
+    t = _lib.MpmTuning()
+    flags = _lib.TUNE_IGNORE_CACHE if ignore_cache else 0
+    path = cache_path.encode() if cache_path else None
+    batch._check(batch.L.mpm_batch_autotune(batch.h, path, flags, int(budget_substeps), ctypes.byref(t)))
+    return _batch_dict(t)
+
+
+def current_batch(batch) -> dict:
+    """The batch's current launch shape."""
+    t = _lib.MpmTuning()
+    batch._check(batch.L.mpm_batch_get_tuning(batch.h, ctypes.byref(t)))
+    return _batch_dict(t)

@@ -55,6 +55,10 @@ class Batch:
     def set_stream(self, handle: int):
         self._check(self.L.mpm_batch_set_stream(self.h, ctypes.c_void_p(int(handle))))
 
+    def set_steps_per_warp(self, steps_per_warp: int):
+        """Range size of the batched kernel in 32-particle steps (1..256)."""
+        self._check(self.L.mpm_batch_set_steps_per_warp(self.h, int(steps_per_warp)))
+
     def upload(self, states):
         """states: one state dict per scene (or one concatenated dict)."""
         if isinstance(states, dict):

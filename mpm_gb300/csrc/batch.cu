@@ -11,12 +11,15 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
+#include <set>
 #include <string>
 #include <vector>
 
 #include "mpm_internal.h"
+#include "tuning_cache.h"
 
 using namespace mpm;
 
@@ -93,6 +96,32 @@ void free_graphs(mpm_batch* b) {
   b->graphs.clear();
 }
 
+// The range table for the batch's steps_per_warp (ranges of 32 * steps_per_warp
+// particles that never cross a scene) and the launch grids sized by its length.  The
+// caller makes sure no launch still reads the old table.
+mpm_status build_ranges(mpm_batch* b) {
+  std::vector<int4> ranges;
+  const int64_t chunk = 32 * (int64_t)b->steps_per_warp;
+  for (int i = 0; i < b->nscenes; ++i)
+    for (int64_t p = 0; p < b->scenes[i].count; p += chunk)
+      ranges.push_back(make_int4(i, (int)(b->start[i] + p), (int)(b->start[i] + std::min(p + chunk, b->scenes[i].count)),
+                                 0));
+  cudaFree(b->d_ranges);
+  b->d_ranges = nullptr;
+  b->nranges = 0;
+  BCUDA(b, cudaMalloc(&b->d_ranges, sizeof(int4) * std::max<size_t>(ranges.size(), 1)));
+  if (!ranges.empty())
+    BCUDA(b, cudaMemcpy(b->d_ranges, ranges.data(), sizeof(int4) * ranges.size(), cudaMemcpyHostToDevice));
+  b->nranges = (int)ranges.size();
+  for (int k = 0; k < 2; ++k) {
+    const StepKind kind = k ? kStepFused : kStepP2GOnly;
+    const int bps = step_blocks_per_sm(kind, false, false, step_smem_bytes(kind, true), true);
+    const int blocks = std::max(1, std::min((b->nranges + kStepWarps - 1) / kStepWarps, b->num_sms * bps));
+    (k ? b->blocks_fused : b->blocks_p2g) = blocks;
+  }
+  return MPM_OK;
+}
+
 mpm_status launch(mpm_batch* b, StepKind kind) {
   StepArgs a{};
   a.s = b->sA;
@@ -160,6 +189,17 @@ mpm_status sort(mpm_batch* b, bool g2p_next) {
   return MPM_OK;
 }
 
+// Zero P2G grids and empty box slots, as after an upload (synchronises: the box table
+// is copied from the host).
+mpm_status fresh_grids(mpm_batch* b) {
+  for (auto& g : b->grid) BCUDA(b, cudaMemsetAsync(g, 0, sizeof(float4) * b->cells, b->stream));
+  std::vector<int> boxes(6 * kBoxSlots * b->nscenes);
+  for (size_t i = 0; i < boxes.size(); ++i) boxes[i] = (i % 6 < 3) ? INT_MAX : INT_MIN;
+  BCUDA(b, cudaMemcpyAsync(b->boxes, boxes.data(), sizeof(int) * boxes.size(), cudaMemcpyHostToDevice, b->stream));
+  BCUDA(b, cudaStreamSynchronize(b->stream));
+  return MPM_OK;
+}
+
 mpm_status advance(mpm_batch* b, int32_t nsteps) {
   for (int32_t i = 0; i < nsteps; ++i) {
     if (b->sort_interval > 0 && b->since_sort >= b->sort_interval) {
@@ -214,8 +254,6 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
   b->start.resize(nscenes + 1);
   std::vector<SceneDev> sd(nscenes);
   std::vector<uint32_t> key_base(nscenes);
-  std::vector<int4> ranges;
-  const int chunk = 32 * b->steps_per_warp;
   int64_t off = 0, cells = 0, keys = 0, vcells = 0;
   for (int i = 0; i < nscenes; ++i) {
     b->start[i] = off;
@@ -229,8 +267,6 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
     const int64_t nb = (N + 3) / 4;
     key_base[i] = (uint32_t)keys;
     keys += nb * nb * nb * 64;
-    for (int64_t p = 0; p < scenes[i].count; p += chunk)
-      ranges.push_back(make_int4(i, (int)(off + p), (int)(off + std::min<int64_t>(p + chunk, scenes[i].count)), 0));
     off += scenes[i].count;
   }
   b->start[nscenes] = off;
@@ -240,13 +276,7 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
   b->cells = cells;
   b->vcells = vcells;
   b->key_space = keys;
-  b->nranges = (int)ranges.size();
-  for (int k = 0; k < 2; ++k) {
-    const StepKind kind = k ? kStepFused : kStepP2GOnly;
-    const int bps = step_blocks_per_sm(kind, false, false, step_smem_bytes(kind, true), true);
-    const int blocks = std::max(1, std::min((b->nranges + kStepWarps - 1) / kStepWarps, b->num_sms * bps));
-    (k ? b->blocks_fused : b->blocks_p2g) = blocks;
-  }
+  if (build_ranges(b) != MPM_OK) return bail(MPM_ERR_NOMEM);
 
   const size_t fb = sizeof(float) * (size_t)kNumComps * b->stride;
   if (cudaMalloc(&b->sA, fb) || cudaMalloc(&b->sB, fb) || cudaMalloc(&b->matA, b->stride) ||
@@ -262,8 +292,7 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
   const int64_t nbs = (keys + kThreads * 8 - 1) / (kThreads * 8);
   if (cudaMalloc(&b->counts, 4 * keys) || cudaMalloc(&b->block_sums, 4 * std::max<int64_t>(nbs, 1)) ||
       cudaMalloc(&b->d_scenes, sizeof(SceneDev) * nscenes) || cudaMalloc(&b->d_start, 8 * (nscenes + 1)) ||
-      cudaMalloc(&b->d_key_base, 4 * nscenes) || cudaMalloc(&b->d_ranges, sizeof(int4) * std::max(b->nranges, 1)) ||
-      cudaMalloc(&b->boxes, sizeof(int) * 6 * kBoxSlots * nscenes) ||
+      cudaMalloc(&b->d_key_base, 4 * nscenes) || cudaMalloc(&b->boxes, sizeof(int) * 6 * kBoxSlots * nscenes) ||
       cudaMalloc(&b->status, sizeof(int)))
     return bail(MPM_ERR_NOMEM);
   std::vector<int> boxes(6 * kBoxSlots * nscenes);
@@ -271,7 +300,6 @@ mpm_status mpm_batch_create(const mpm_scene* scenes, int32_t nscenes, int32_t so
   if (cudaMemcpy(b->d_scenes, sd.data(), sizeof(SceneDev) * nscenes, cudaMemcpyHostToDevice) ||
       cudaMemcpy(b->d_start, b->start.data(), 8 * (nscenes + 1), cudaMemcpyHostToDevice) ||
       cudaMemcpy(b->d_key_base, key_base.data(), 4 * nscenes, cudaMemcpyHostToDevice) ||
-      (b->nranges && cudaMemcpy(b->d_ranges, ranges.data(), sizeof(int4) * b->nranges, cudaMemcpyHostToDevice)) ||
       cudaMemcpy(b->boxes, boxes.data(), sizeof(int) * boxes.size(), cudaMemcpyHostToDevice) ||
       cudaMemset(b->status, 0, sizeof(int)) ||
       cudaStreamSynchronize(b->stream))
@@ -326,12 +354,9 @@ mpm_status mpm_batch_upload_soa(mpm_batch* b, const float* x, const float* v, co
   BCUDA(b, launch_deinterleave(b->stage, b->sA, b->stride, n, v != nullptr, C != nullptr, F != nullptr,
                                Jp != nullptr, b->stream));
   BCUDA(b, launch_iota(b->idA, n, b->stream));
-  // fresh grids and box slots
-  for (auto& g : b->grid) BCUDA(b, cudaMemsetAsync(g, 0, sizeof(float4) * b->cells, b->stream));
-  std::vector<int> boxes(6 * kBoxSlots * b->nscenes);
-  for (size_t i = 0; i < boxes.size(); ++i) boxes[i] = (i % 6 < 3) ? INT_MAX : INT_MIN;
-  BCUDA(b, cudaMemcpyAsync(b->boxes, boxes.data(), sizeof(int) * boxes.size(), cudaMemcpyHostToDevice, b->stream));
   b->launches += 2;
+  const mpm_status st = fresh_grids(b);
+  if (st != MPM_OK) return st;
   BCUDA(b, cudaStreamSynchronize(b->stream));
   return MPM_OK;
 }
@@ -450,6 +475,159 @@ int64_t mpm_batch_launch_count(const mpm_batch* b) { return b ? b->launches : -1
 mpm_status mpm_batch_last_error(const mpm_batch* b, char* buf, size_t len) {
   if (!b || !buf || len == 0) return MPM_ERR_INVALID;
   std::snprintf(buf, len, "%s", b->last_error.c_str());
+  return MPM_OK;
+}
+
+mpm_status mpm_batch_set_steps_per_warp(mpm_batch* b, int32_t steps_per_warp) {
+  if (!b) return MPM_ERR_INVALID;
+  if (steps_per_warp < 1 || steps_per_warp > 256) return bfail(b, MPM_ERR_INVALID, "steps_per_warp must be 1..256");
+  if (steps_per_warp == b->steps_per_warp) return MPM_OK;
+  BCUDA(b, cudaStreamSynchronize(b->stream));  // launches in flight read the old range table
+  free_graphs(b);
+  b->steps_per_warp = steps_per_warp;
+  return build_ranges(b);
+}
+
+mpm_status mpm_batch_get_tuning(const mpm_batch* b, mpm_tuning* out) {
+  if (!b || !out) return MPM_ERR_INVALID;
+  *out = mpm_tuning{b->steps_per_warp, kStepWarps, 0, b->sort_interval, 0.0, 0, 0};
+  return MPM_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Autotuner of a batch: the range size of the batched kernel (steps per warp), timed as
+// replayed graphs on a copy of the batch, cached like the single-scene shapes.
+// ---------------------------------------------------------------------------
+namespace {
+
+std::string batch_device_key(int dev) {
+  cudaDeviceProp p{};
+  if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return "unknown device";
+  char b[320];
+  std::snprintf(b, sizeof(b), "%s (%d SMs, cc %d.%d)", p.name, p.multiProcessorCount, p.major, p.minor);
+  return b;
+}
+
+// Changes with every build of this file, so a rebuilt library measures again.
+const char* batch_build_key() { return "mpm_gb300 batch " __DATE__ " " __TIME__; }
+
+// Workload class of a batch: scene count, particle count to the nearest power of two, the
+// grid sides and the material kinds present.
+std::string batch_class_key(const mpm_batch* b) {
+  std::set<unsigned> sides;
+  unsigned kinds = 0;
+  for (const auto& sc : b->scenes) {
+    sides.insert(sc.params.N);
+    kinds |= 1u << sc.material.kind;
+  }
+  std::string ns;
+  for (unsigned n : sides) ns += (ns.empty() ? "" : ",") + std::to_string(n);
+  const int lg = b->n > 0 ? (int)std::lround(std::log2((double)b->n)) : 0;
+  char buf[96];
+  std::snprintf(buf, sizeof(buf), "batch scenes=%d n~2^%d kinds=0x%x N=", b->nscenes, lg, kinds);
+  return buf + ns;
+}
+
+// The trial batch t gets b's particles (same scenes, so the same layout) and fresh grids.
+mpm_status restore_from(mpm_batch* t, const mpm_batch* b) {
+  BCUDA(t, cudaMemcpyAsync(t->sA, b->sA, sizeof(float) * (size_t)kNumComps * (size_t)b->stride,
+                           cudaMemcpyDeviceToDevice, t->stream));
+  BCUDA(t, cudaMemcpyAsync(t->idA, b->idA, sizeof(uint32_t) * (size_t)b->n, cudaMemcpyDeviceToDevice, t->stream));
+  t->pending = false;
+  t->launch_index = 0;
+  t->since_sort = t->sort_interval;
+  return fresh_grids(t);
+}
+
+}  // namespace
+
+extern "C" {
+
+mpm_status mpm_batch_autotune(mpm_batch* b, const char* cache_path, int32_t flags, int32_t budget_substeps,
+                              mpm_tuning* out) {
+  if (!b) return MPM_ERR_INVALID;
+  if (b->n <= 0) return bfail(b, MPM_ERR_INVALID, "autotune needs uploaded particles");
+  if (budget_substeps < 0 || budget_substeps > 4096) return bfail(b, MPM_ERR_INVALID, "budget_substeps out of range");
+  if (flags & ~MPM_TUNE_IGNORE_CACHE) return bfail(b, MPM_ERR_INVALID, "unknown flags");
+  const std::string dkey = batch_device_key(b->device), bkey = batch_build_key(), ckey = batch_class_key(b);
+  if (cache_path && !(flags & MPM_TUNE_IGNORE_CACHE)) {
+    TuningEntry e;
+    if (find_tuning(read_tuning_cache(cache_path), dkey, bkey, ckey, &e) && e.steps_per_warp >= 1 &&
+        e.steps_per_warp <= 256) {
+      const mpm_status st = mpm_batch_set_steps_per_warp(b, e.steps_per_warp);
+      if (st != MPM_OK) return st;
+      if (out) *out = mpm_tuning{b->steps_per_warp, kStepWarps, 0, b->sort_interval, e.us_per_substep, 1, 0};
+      return MPM_OK;
+    }
+  }
+  BCUDA(b, cudaStreamSynchronize(b->stream));  // the trial batch copies the current particles
+  mpm_batch* t = nullptr;
+  mpm_status st = mpm_batch_create(b->scenes.data(), b->nscenes, b->sort_interval, &t);
+  if (st != MPM_OK) return bfail(b, st, "tuning: cannot create the trial batch");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    mpm_batch_destroy(t);
+    return bfail(b, MPM_ERR_CUDA, "tuning: cannot create events");
+  }
+  // replays of a multiple of 6 substeps keep the box-slot phase, so a graph is captured
+  // once per buffer role: two replays capture both, the next two are timed
+  const int steps = std::max(6, ((budget_substeps > 0 ? budget_substeps : 24) + 5) / 6 * 6);
+  int timed = 0;
+  auto time_spw = [&](int spw, double* us) -> mpm_status {
+    ++timed;
+    mpm_status s2 = mpm_batch_set_steps_per_warp(t, spw);
+    if (s2 == MPM_OK) s2 = restore_from(t, b);
+    for (int r = 0; r < 2 && s2 == MPM_OK; ++r) s2 = mpm_batch_substep_graph(t, steps);
+    if (s2 != MPM_OK) return s2;
+    if (cudaEventRecord(e0, t->stream) != cudaSuccess) return MPM_ERR_CUDA;
+    for (int r = 0; r < 2 && s2 == MPM_OK; ++r) s2 = mpm_batch_substep_graph(t, steps);
+    if (s2 != MPM_OK) return s2;
+    if (cudaEventRecord(e1, t->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) return MPM_ERR_CUDA;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) return MPM_ERR_CUDA;
+    *us = 1e3 * (double)ms / (2.0 * steps);
+    return mpm_batch_sync(t);
+  };
+  int best = b->steps_per_warp;
+  double best_us = 0.0;
+  st = time_spw(best, &best_us);
+  const double base_us = best_us;
+  for (int spw : {1, 2, 4, 8, 16}) {
+    if (st != MPM_OK) break;
+    if (spw == b->steps_per_warp) continue;
+    double us = 0.0;
+    st = time_spw(spw, &us);
+    // a knob moves only for a gain above 1 %, so timing noise does not flip it
+    if (st == MPM_OK && us < 0.99 * best_us && us < 0.99 * base_us) {
+      best = spw;
+      best_us = us;
+    }
+  }
+  std::string why = st != MPM_OK ? t->last_error : std::string();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  mpm_batch_destroy(t);
+  if (st != MPM_OK) return bfail(b, st, "tuning: " + why);
+  st = mpm_batch_set_steps_per_warp(b, best);
+  if (st != MPM_OK) return st;
+  const mpm_tuning res{best, kStepWarps, 0, b->sort_interval, best_us, 0, timed};
+  if (out) *out = res;
+  if (cache_path) {
+    TuningEntry e;
+    e.device = dkey;
+    e.build = bkey;
+    e.klass = ckey;
+    e.steps_per_warp = best;
+    e.warps_per_cta = kStepWarps;
+    e.tile_box = MPM_TILE_4x4x6;  // unused by a batch (no G2P tile); a valid value for the file
+    e.sort_interval = b->sort_interval;
+    e.us_per_substep = best_us;
+    if (!store_tuning(cache_path, e))
+      return bfail(b, MPM_ERR_IO, std::string("tuning: cannot write the cache file ") + cache_path);
+  }
   return MPM_OK;
 }
 

@@ -114,3 +114,53 @@ def test_autotune_search_cache_and_parity(gpu_lib, oracle_lib, tmp_path):
     errs = compare_states(out, ref, cfg3["params"], cfg3["state"])
     assert max(errs.values()) < 1e-5, (t3, errs)
     assert len(json.load(open(cache))["entries"]) == 2
+
+
+def test_batch_autotune_picks_a_range_size_and_keeps_parity(gpu_lib, oracle_lib, tmp_path):
+    """mpm_batch_autotune times the batched kernel's range sizes on a copy of the batch
+    (the batch's own particles do not change), applies the fastest, stores it in the
+    cache (a second search is a lookup), and the tuned batch still matches the oracle per
+    scene."""
+    from mpm_gb300 import autotune, scenes
+    from mpm_gb300.batch import Batch
+
+    scs = scenes.config_batched(nscenes=8, seed=21, count_range=(2_000, 30_000))
+    cache = str(tmp_path / "tuning.json")
+    with Batch(scs, sort_interval=4) as b:
+        b.upload([s["state"] for s in scs])
+        before = b.download()
+        t = autotune.tune_batch(b, cache, budget_substeps=12)
+        assert t["steps_per_warp"] in (1, 2, 4, 8, 16) and not t["from_cache"] and t["candidates"] == 5
+        assert t["us_per_substep"] > 0
+        assert autotune.current_batch(b)["steps_per_warp"] == t["steps_per_warp"]
+        after = b.download()
+        for k in before:
+            assert np.array_equal(before[k], after[k]), k
+        t2 = autotune.tune_batch(b, cache, budget_substeps=12)
+        assert t2["from_cache"] and t2["steps_per_warp"] == t["steps_per_warp"]
+        b.advance(3)
+        outs = b.split(b.download())
+    for sc, out in zip(scs, outs):
+        ref = oracle_after(oracle_lib, {"state": sc["state"], "params": sc["params"], "materials": [sc["material"]]}, 3)
+        errs = compare_states(out, ref, sc["params"], sc["state"])
+        assert max(errs.values()) < 2e-5, (sc["params"]["N"], sc["material"].name, errs)
+    entries = json.load(open(cache))["entries"]
+    assert any(e["class"].startswith("batch scenes=8") for e in entries)
+
+
+@pytest.mark.parametrize("spw", [1, 16])
+def test_batch_range_sizes_match_oracle(gpu_lib, oracle_lib, spw):
+    """Any range size gives the oracle's result (ranges only split the work)."""
+    from mpm_gb300 import scenes
+    from mpm_gb300.batch import Batch
+
+    scs = scenes.config_batched(nscenes=6, seed=22, count_range=(1_500, 20_000))
+    with Batch(scs, sort_interval=2) as b:
+        b.set_steps_per_warp(spw)
+        b.upload([s["state"] for s in scs])
+        b.advance(3, graph=True)
+        outs = b.split(b.download())
+    for sc, out in zip(scs, outs):
+        ref = oracle_after(oracle_lib, {"state": sc["state"], "params": sc["params"], "materials": [sc["material"]]}, 3)
+        errs = compare_states(out, ref, sc["params"], sc["state"])
+        assert max(errs.values()) < 2e-5, (spw, sc["params"]["N"], errs)
