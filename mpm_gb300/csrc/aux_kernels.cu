@@ -220,7 +220,11 @@ __global__ void sort_rank(SortArgs a) {
     int start = 0;
     if (valid && lane == leader) start = atomicAdd(a.counts + key_slot(a, key), __popc(same));
     start = __shfl_sync(kFull, start, leader);
-    if (valid) a.perm[(int64_t)start + __popc(same & ((1u << lane) - 1u))] = (uint32_t)p;
+    if (valid) {
+      const int64_t q = (int64_t)start + __popc(same & ((1u << lane) - 1u));
+      a.perm[q] = (uint32_t)p;
+      if (a.inv) a.inv[p] = (uint32_t)q;  // coalesced: p is this thread's particle
+    }
   }
 }
 
@@ -578,9 +582,10 @@ cudaError_t launch_presort(const float* x, float* xcopy, const SortArgs& a, uint
   if (e != cudaSuccess) return e;
   const int blocks = (int)std::min<int64_t>((a.n + kThreads - 1) / kThreads, (int64_t)num_sms * 8);
   presort_keys_kernel<<<blocks, kThreads, 0, st>>>(x, xcopy, a, bad);
-  int n_launch = 3 + scan_cell_counts(a, st);
-  sort_rank<<<blocks, kThreads, 0, st>>>(a);
-  inverse_kernel<<<grid_for(a.n), 256, 0, st>>>(a.perm, a.n, dest);
+  int n_launch = 2 + scan_cell_counts(a, st);
+  SortArgs r = a;
+  r.inv = dest;  // the ranking writes the inverse too
+  sort_rank<<<blocks, kThreads, 0, st>>>(r);
   if (launches) *launches += n_launch;
   return cudaGetLastError();
 }

@@ -141,6 +141,7 @@ struct SortArgs {
   uint32_t* idB;
   uint32_t* keys;
   uint32_t* perm;  // n words, or null: with it the sort ranks, then gathers (for unsorted input)
+  uint32_t* inv;   // with perm, optional: the inverse permutation (particle p -> its slot)
   int* counts;   // one per sort key
   int* block_sums;
   int64_t cells;  // sort key space (bricked cell index range)
