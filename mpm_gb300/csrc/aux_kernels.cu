@@ -574,6 +574,43 @@ cudaError_t launch_inverse(const uint32_t* id, int64_t n, uint32_t* inv, cudaStr
   return cudaGetLastError();
 }
 
+// Cell-order check of an upload that kept the particle order: counts the slots whose cell
+// key is below the previous slot's.  The block that finishes last writes the count to *out
+// (host-visible memory) and resets the two device counters (count, ticket) for the next call.
+__global__ void order_check_kernel(const float* __restrict__ s, int64_t st, int64_t n, float dx_inv, int N,
+                                   int* counters, int* out) {
+  __shared__ int block_count;
+  if (threadIdx.x == 0) block_count = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  int mine = 0;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = base + threadIdx.x;
+    const bool valid = q < n;
+    const uint32_t key = valid ? cell_key(s, st, q, dx_inv, N) : 0u;
+    uint32_t prev = __shfl_up_sync(kFull, key, 1);
+    if (lane == 0 && valid && q > 0) prev = cell_key(s, st, q - 1, dx_inv, N);
+    mine += __popc(__ballot_sync(kFull, valid && q > 0 && key < prev));
+  }
+  if (lane == 0 && mine) atomicAdd(&block_count, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (block_count) atomicAdd(counters, block_count);
+    __threadfence();
+    if (atomicAdd(counters + 1, 1) == (int)gridDim.x - 1) {
+      *out = atomicExch(counters, 0);
+      counters[1] = 0;
+    }
+  }
+}
+
+cudaError_t launch_order_check(const float* s, int64_t stride, int64_t n, float dx_inv, int N, int* counters, int* out,
+                               cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  order_check_kernel<<<grid_for(n), 256, 0, st>>>(s, stride, n, dx_inv, N, counters, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_presort(const float* x, float* xcopy, const SortArgs& a, uint32_t* dest, int* bad, int num_sms,
                            cudaStream_t st, int64_t* launches, bool bad_zeroed) {
   if (a.n == 0) return cudaSuccess;

@@ -425,6 +425,19 @@ mpm_status check_ready(mpm_ctx* c) {
   return MPM_OK;
 }
 
+// The inverse of the id permutation (the slot of each particle in upload order): the
+// cached one while the ids are unchanged, else computed into the spare id copy.
+cudaError_t inverse_ids(mpm_ctx* c, const uint32_t** inv) {
+  if (!c->inv) {
+    const cudaError_t e = launch_inverse(c->idA, c->n, c->idB, c->stream);
+    if (e != cudaSuccess) return e;
+    c->launches += c->n > 0;
+    c->inv = c->idB;
+  }
+  *inv = c->inv;
+  return cudaSuccess;
+}
+
 }  // namespace
 
 namespace mpm {
@@ -621,14 +634,17 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   // buffer with copies.  When the particle arrays keep their size, the conversion writes
   // the spare copy, which replaces the current one after the check.
   const bool grow = n > c->capacity || !c->sA;
-  c->inv = nullptr;  // every path below writes the spare id copy or the sort scratch
   // a per-particle material array keeps the upload order (its bytes are copied as given),
   // so only uploads without one are put in cell order on the way in
   bool mixed = !c->liquid_layout && c->n_materials > 1;
   if (mat)
     for (int64_t p = 0; p < n && !mixed; ++p) mixed = mat[p] != 0;
   const bool presort = n > 0 && !grow && !mixed;
-  bool presorted = false;
+  // the same particle count again: each particle goes to the slot its id holds, keeping the
+  // device order and the ids
+  const bool in_place = presort && n == c->n;
+  if (!in_place) c->inv = nullptr;  // the paths below write the spare id copy or the sort scratch
+  bool presorted = false, kept_order = false, in_place_done = false;
   HostArrays arr{};
   bool direct = false;
   if (n > 0 && !grow) {
@@ -666,6 +682,28 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
       st = ensure_particles(c, n);
       if (st != MPM_OK) return st;
       MPM_CUDA(c, launch_deinterleave_arrays(arr, c->sA, c->stride, n, c->work + 2, c->stream));
+    } else if (in_place) {
+      // The particles keep the device order (cell order as of the last sort) and their ids:
+      // particle p goes to slot inv[p], read over the host link in one pass.  A count of the
+      // slots whose cell key falls below their predecessor's tells whether the new positions
+      // still follow that order; when they do not (a different scene of the same size), the
+      // next substep sorts first.
+      if (direct) MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // earlier work may read the spare copy
+      const uint32_t* inv = nullptr;
+      MPM_CUDA(c, inverse_ids(c, &inv));
+      volatile int* flags = c->host_flags;  // no kernel still writes them: synchronised above
+      flags[0] = 0;
+      flags[2] = 0;
+      MPM_CUDA(c, launch_deinterleave_arrays(arr, c->sB, c->stride, n, c->host_flags_dev, c->stream, inv, true));
+      MPM_CUDA(c, launch_order_check(c->sB, c->stride, n, c->K.g.dx_inv, (int)c->params.N, c->work,
+                                     c->host_flags_dev + 2, c->stream));
+      MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // also: the caller may reuse the host arrays on return
+      if (flags[0]) return fail(c, MPM_ERR_INVALID, "non-finite particle position");
+      std::swap(c->sA, c->sB);
+      c->launches += 1;
+      // more than one slot in 8 out of cell order: sort before the next substep
+      kept_order = (int64_t)flags[2] * 8 <= n;
+      in_place_done = true;
     } else if (presort) {
       if (direct) MPM_CUDA(c, cudaStreamSynchronize(c->stream));  // earlier work may read the stage
       // Cell order from the positions first, then each particle goes straight to its slot:
@@ -727,12 +765,14 @@ mpm_status mpm_upload_soa(mpm_ctx* c, int64_t n, const float* x, const float* v,
   c->pending = false;
   c->prev = -1;
   c->substeps = 0;
-  c->since_sort = presorted ? 0 : c->params.sort_interval;  // otherwise sort before the first substep
-  c->unsorted = !presorted;
+  // a cell-ordered upload starts the sort interval afresh; one that kept the order keeps
+  // its schedule; otherwise sort before the first substep
+  if (!kept_order) c->since_sort = presorted ? 0 : c->params.sort_interval;
+  c->unsorted = !presorted && !kept_order;
   c->t = 0.0;
   free_objects(c);
   if (n == 0) return MPM_OK;
-  if (!presorted) {
+  if (!presorted && !in_place_done) {
     MPM_CUDA(c, launch_iota(c->idA, n, c->stream));
     c->launches += 1;
   }
@@ -875,19 +915,6 @@ mpm_status mpm_sync(mpm_ctx* c) {
     return fail(c, MPM_ERR_STATE, "device index check failed");
   }
   return MPM_OK;
-}
-
-// The inverse of the id permutation (the slot of each particle in upload order): the
-// cached one while the ids are unchanged, else computed into the spare id copy.
-cudaError_t inverse_ids(mpm_ctx* c, const uint32_t** inv) {
-  if (!c->inv) {
-    const cudaError_t e = launch_inverse(c->idA, c->n, c->idB, c->stream);
-    if (e != cudaSuccess) return e;
-    c->launches += c->n > 0;
-    c->inv = c->idB;
-  }
-  *inv = c->inv;
-  return cudaSuccess;
 }
 
 mpm_status mpm_download_soa(mpm_ctx* c, float* x, float* v, float* C, float* F, float* Jp, uint8_t* mat) {

@@ -185,6 +185,11 @@ cudaError_t launch_deinterleave_arrays(HostArrays a, float* s, int64_t stride, i
 // *bad = 1 when a position is not finite (zeroed first unless bad_zeroed, as above).
 cudaError_t launch_presort(const float* x, float* xcopy, const SortArgs& a, uint32_t* dest, int* bad, int num_sms,
                            cudaStream_t st, int64_t* launches, bool bad_zeroed = false);
+// Number of slots q of the component-major arrays whose cell key (the sort's bricked key)
+// is below slot q - 1's, written to *out (host-visible) by the kernel; counters: two ints
+// of device memory, zero between calls.
+cudaError_t launch_order_check(const float* s, int64_t stride, int64_t n, float dx_inv, int N, int* counters, int* out,
+                               cudaStream_t st);
 // Component-major particle arrays -> the non-null arrays in upload order (inv as from
 // launch_inverse, null for the identity).
 cudaError_t launch_interleave_arrays(const float* s, int64_t stride, const uint32_t* inv, int64_t n, OutArrays o,

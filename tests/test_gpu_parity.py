@@ -391,10 +391,11 @@ def test_pinned_host_arrays_take_the_direct_path(gpu_lib):
 
 @pytest.mark.parametrize("liquid", [False, True])
 def test_reupload_in_cell_order_matches_a_fresh_upload(gpu_lib, liquid):
-    """An upload into arrays that keep their size puts the particles in cell order on the way
-    in (no sort at the next substep): downloads still return the upload order exactly, and
-    the trajectory matches a context that uploaded the same state into new arrays and sorted
-    at its first substep (float atomics make the two agree to rounding, not bit for bit)."""
+    """An upload of the same particle count keeps the device order: each particle goes to the
+    slot its id holds (no sort at the next substep). Downloads still return the upload order
+    exactly, and the trajectory matches a context that uploaded the same state into new arrays
+    and sorted at its first substep (float atomics make the two agree to rounding, not bit for
+    bit)."""
     from mpm_gb300 import scenes
     from mpm_gb300.simulation import Simulation
 
@@ -420,6 +421,43 @@ def test_reupload_in_cell_order_matches_a_fresh_upload(gpu_lib, liquid):
                 assert np.abs(ra[k] - rb[k]).max() <= 1e-5 * scale[k], k
         if "mat" in ra:
             assert np.array_equal(ra["mat"], rb["mat"])
+
+
+@pytest.mark.parametrize("shuffled", [False, True])
+def test_same_count_upload_keeps_or_restores_cell_order(gpu_lib, shuffled):
+    """A same-count upload keeps the device order and counts the slots whose cell key falls
+    below their predecessor's. The same scene again keeps the sort schedule (no sort at the
+    next substep). The scene's states permuted among the particle indices put the positions
+    out of that order: the next substep then sorts first. Either way the download returns the
+    upload exactly and the next substep matches a context that uploaded the same state into
+    new arrays."""
+    from mpm_gb300 import scenes
+    from mpm_gb300.simulation import Simulation
+
+    cfg = scenes.config_liquid(n=8000, seed=14)
+    st = {k: np.asarray(v).copy() for k, v in cfg["state"].items()}
+    perm = np.random.default_rng(15).permutation(len(st["x"]))
+    new = {k: v[perm].copy() for k, v in st.items()} if shuffled else st
+    with Simulation.from_config(cfg) as a, Simulation.from_config(cfg) as b:
+        a.upload(st)
+        a.advance(3)
+        a.upload(new)
+        back = a.download()
+        for k in back:
+            assert np.array_equal(back[k], np.asarray(new[k], np.float32).reshape(back[k].shape)), k
+        l0 = a.launches
+        a.advance(1)
+        step_launches = a.launches - l0
+        # P2G-only, velocity pass, G2P-only; a sort adds its histogram, scan, ranking and gather
+        assert step_launches == (7 if shuffled else 3), step_launches
+        b.upload(new)
+        b.advance(1)
+        ra, rb = a.download(), b.download()
+        p = cfg["params"]
+        vmax = max(float(np.abs(rb["v"]).max()), abs(p["dt"] * p["gravity"]))
+        scale = {"x": 1.0, "v": vmax, "C": 4.0 * p["N"] * vmax, "Jp": 1.0}
+        for k, sc in scale.items():
+            assert np.abs(ra[k] - rb[k]).max() <= 1e-5 * sc, k
 
 
 def test_upload_loop_ending_without_prefetch_matches_plain_substeps(gpu_lib):
