@@ -20,6 +20,10 @@ constexpr int kThreads = 256;  // CTA size of the auxiliary kernels (8 warps)
 constexpr int kWarps = kThreads / 32;
 constexpr int kStepThreads = 384;  // CTA size of the substep kernel (12 warps, <= 168 registers)
 constexpr int kStepWarps = kStepThreads / 32;
+// CTA of the P2G-only substep kernel (the first P2G of a run, the adjoint's recomputed P2G):
+// it needs no G2P tiles and fits 128 registers, so 15 warps share an SM's shared memory
+// (15 P2G transpose buffers, 209 KB) where the fused kernel's 168 registers allow 12.
+constexpr int kP2GWarps = 15;
 constexpr unsigned kFull = 0xffffffffu;
 
 enum MatKind { kSnow = 0, kFixedCorotated = 1, kJelly = 2, kLiquid = 3 };

@@ -396,9 +396,11 @@ static void* scene_kernel() {
 
 StepTuning step_tuning(StepKind kind, bool guard, bool batch, StepTuning want) {
   // The fused substep of the plain layouts comes in every CTA size with tile box 0, and
-  // with boxes 1 and 2 at 12 warps; the launches that start or end a run, the G2P-guard
-  // variants and batches use 12 warps and box 0.
+  // with boxes 1 and 2 at 12 warps; the P2G-only launch of the plain layouts uses
+  // kP2GWarps; the G2P-only launch, the G2P-guard variants and batches use 12 warps and
+  // box 0.
   StepTuning t{kStepWarps, 0};
+  if (!batch && !guard && kind == kStepP2GOnly) return StepTuning{kP2GWarps, 0};
   if (batch || guard || kind != kStepFused) return t;
   if (want.tile == 1 || want.tile == 2) {
     t.tile = want.tile;
@@ -426,7 +428,7 @@ static void* select_kernel(StepKind kind, bool liquid, bool guard, bool batch, S
   }
 #define MPM_SEL(L, G)                                                                \
   if (liquid == L && guard == G) {                                                   \
-    if (kind == kStepP2GOnly) return scene_kernel<L, false, true, G, kStepWarps>();  \
+    if (kind == kStepP2GOnly) return scene_kernel<L, false, true, G, G ? kStepWarps : kP2GWarps>(); \
     if (kind == kStepFused) return scene_kernel<L, true, true, G, kStepWarps>();     \
     return scene_kernel<L, true, false, G, kStepWarps>();                            \
   }

@@ -123,7 +123,8 @@ __device__ __forceinline__ float4* align_smem128(float4* p) {
 // plus the 14.3 KB P2G transpose buffer, 17.3 KB (12 warps: 207 KB of the SM's 228 KB).
 // TILE: the tile box (TileBox).  MAT: the material policy (particle_ops.cuh).
 template <bool LIQ, bool G2P, bool P2G, bool GUARD, int WARPS, int TILE, class MAT = BuiltinMaterials>
-__global__ void __launch_bounds__(WARPS * 32, kStepWarps / WARPS) scene_step_kernel(const __grid_constant__ StepArgs A) {
+__global__ void __launch_bounds__(WARPS * 32, WARPS >= kStepWarps ? 1 : kStepWarps / WARPS)
+    scene_step_kernel(const __grid_constant__ StepArgs A) {
   using TB = TileBox<TILE>;
   constexpr int kTileNodes = TB::kNodes, kTileY = TB::Y, kTileZ = TB::Z;
   extern __shared__ float4 smem_dyn[];
