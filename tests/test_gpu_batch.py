@@ -111,6 +111,33 @@ def test_batch_graph_replay_matches_launches(gpu_lib):
     assert max(errs.values()) < 2e-5, errs
 
 
+@pytest.mark.parametrize("interval", [4, 6])
+def test_batch_graph_sorts_at_the_interval(gpu_lib, interval):
+    """A replayed graph sorts before its first substep and then every sort_interval
+    substeps, as launched substeps do: 12 replayed substeps hold 3 sorts (an odd count, which
+    swaps the particle buffers) with interval 4 and 2 with interval 6. Two replays equal 24
+    launched substeps to rounding."""
+    from mpm_gb300.batch import Batch
+
+    scs = small_batch(seed=6, nscenes=8)
+    states = [s["state"] for s in scs]
+    with Batch(scs, sort_interval=interval) as b:
+        b.upload(states)
+        b.advance(24)
+        ref = b.download()
+    with Batch(scs, sort_interval=interval) as b:
+        b.upload(states)
+        l0 = b.launches
+        b.advance(12, graph=True)
+        b.advance(12, graph=True)
+        b.sync()
+        out = b.download()
+        assert b.launches > l0
+    p = scs[0]["params"]
+    errs = compare_states(out, ref, p, {"v": np.concatenate([s["v"] for s in states])})
+    assert max(errs.values()) < 2e-5, errs
+
+
 def test_batch_long_run_clears_grids(gpu_lib, oracle_lib):
     """40 substeps with the sparse grid clearing: the batch stays on the single-scene
     trajectory (stale grid data would show up as drift)."""
