@@ -487,7 +487,7 @@ def batched_section(args, stream, scs=None, rank=0, world=1):
     # the range size of the batched kernel, chosen by the batch autotuner on a copy of the batch
     from mpm_gb300 import autotune
 
-    tuning = autotune.tune_batch(b, autotune.default_cache_path(), budget_substeps=24)
+    tuning = autotune.tune_batch(b, autotune.default_cache_path(), budget_substeps=24, tune_sort_interval=True)
     for _ in range(max(args.warmup, 3)):
         b.advance(sub, graph=True)
     torch.cuda.synchronize()

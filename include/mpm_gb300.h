@@ -411,14 +411,19 @@ mpm_status mpm_batch_last_error(const mpm_batch* batch, char* buf, size_t len);
  * particles of one scene (1..256; default 8).  Rebuilds the range table and drops the
  * captured graphs; synchronises the batch's stream. */
 mpm_status mpm_batch_set_steps_per_warp(mpm_batch* batch, int32_t steps_per_warp);
+/* Sort interval of a batch (0: never); captured graphs, which sort before their first
+ * substep and then every sort_interval substeps, are dropped.  Synchronises the batch's
+ * stream. */
+mpm_status mpm_batch_set_sort_interval(mpm_batch* batch, int32_t sort_interval);
 /* The batch's launch shape: steps_per_warp, warps_per_cta (fixed), tile_box 0 (the batched
  * kernel gathers through L1, without a G2P tile) and the sort interval. */
 mpm_status mpm_batch_get_tuning(const mpm_batch* batch, mpm_tuning* out);
 /* Autotuner of a batch (no counterpart in the reference): times the batched kernel's range
  * sizes (1, 2, 4, 8, 16 steps per warp) as replayed graphs of budget_substeps substeps
  * (0: 24; rounded up to a multiple of 6) on a temporary copy of the batch, so the batch's own
- * state does not change, and applies the fastest (a change needs a gain above 1%).  The
- * cache file, flags (MPM_TUNE_IGNORE_CACHE only) and *out are as for mpm_autotune; the
+ * state does not change, and applies the fastest (a change needs a gain above 1%).  With
+ * MPM_TUNE_SORT_INTERVAL it then times sort intervals of 8, 12, 16 and 24 substeps over
+ * replays of 48.  The cache file, flags and *out are as for mpm_autotune; the
  * workload class is the scene count, the particle count to the nearest power of two, the
  * grid sides and the material kinds.  Synchronises; allocates a second batch while it runs. */
 mpm_status mpm_batch_autotune(mpm_batch* batch, const char* cache_path, int32_t flags, int32_t budget_substeps,

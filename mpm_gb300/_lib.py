@@ -146,6 +146,7 @@ SIGNATURES = [
     ("mpm_batch_launch_count", I64, [P]),
     ("mpm_batch_last_error", I32, [P, ctypes.c_char_p, ctypes.c_size_t]),
     ("mpm_batch_set_steps_per_warp", I32, [P, I32]),
+    ("mpm_batch_set_sort_interval", I32, [P, I32]),
     ("mpm_batch_get_tuning", I32, [P, ctypes.POINTER(MpmTuning)]),
     ("mpm_batch_autotune", I32, [P, ctypes.c_char_p, I32, I32, ctypes.POINTER(MpmTuning)]),
     ("mpm_diff_create", I32, [ctypes.POINTER(MpmParams), ctypes.POINTER(MpmMaterial), I64, I32, I32,

@@ -52,11 +52,13 @@ def _batch_dict(t: _lib.MpmTuning) -> dict:
             "us_per_substep": t.us_per_substep, "from_cache": bool(t.from_cache), "candidates": t.candidates}
 
 
-def tune_batch(batch, cache_path: str | None = None, budget_substeps: int = 0, ignore_cache: bool = False) -> dict:
-    """Chooses and applies the range size (steps per warp) of a Batch with particles, timed
-    as replayed graphs on a copy of the batch (mpm_batch_autotune).  Returns the choice."""
+def tune_batch(batch, cache_path: str | None = None, budget_substeps: int = 0, ignore_cache: bool = False,
+               tune_sort_interval: bool = False) -> dict:
+    """Chooses and applies the range size (steps per warp) of a Batch with particles, and
+    with tune_sort_interval its sort interval, timed as replayed graphs on a copy of the
+    batch (mpm_batch_autotune).  Returns the choice."""
     t = _lib.MpmTuning()
-    flags = _lib.TUNE_IGNORE_CACHE if ignore_cache else 0
+    flags = (_lib.TUNE_IGNORE_CACHE if ignore_cache else 0) | (_lib.TUNE_SORT_INTERVAL if tune_sort_interval else 0)
     path = cache_path.encode() if cache_path else None
     batch._check(batch.L.mpm_batch_autotune(batch.h, path, flags, int(budget_substeps), ctypes.byref(t)))
     return _batch_dict(t)

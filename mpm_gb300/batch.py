@@ -59,6 +59,10 @@ class Batch:
         """Range size of the batched kernel in 32-particle steps (1..256)."""
         self._check(self.L.mpm_batch_set_steps_per_warp(self.h, int(steps_per_warp)))
 
+    def set_sort_interval(self, sort_interval: int):
+        """Substeps between cell sorts (0: never)."""
+        self._check(self.L.mpm_batch_set_sort_interval(self.h, int(sort_interval)))
+
     def upload(self, states):
         """states: one state dict per scene (or one concatenated dict)."""
         if isinstance(states, dict):

@@ -501,6 +501,17 @@ mpm_status mpm_batch_set_steps_per_warp(mpm_batch* b, int32_t steps_per_warp) {
   return build_ranges(b);
 }
 
+mpm_status mpm_batch_set_sort_interval(mpm_batch* b, int32_t sort_interval) {
+  if (!b) return MPM_ERR_INVALID;
+  if (sort_interval < 0) return bfail(b, MPM_ERR_INVALID, "sort_interval must be >= 0");
+  if (sort_interval == b->sort_interval) return MPM_OK;
+  BCUDA(b, cudaStreamSynchronize(b->stream));  // captured graphs bake the old schedule in
+  free_graphs(b);
+  b->sort_interval = sort_interval;
+  b->since_sort = std::min<int64_t>(b->since_sort, sort_interval);
+  return MPM_OK;
+}
+
 mpm_status mpm_batch_get_tuning(const mpm_batch* b, mpm_tuning* out) {
   if (!b || !out) return MPM_ERR_INVALID;
   *out = mpm_tuning{b->steps_per_warp, kStepWarps, 0, b->sort_interval, 0.0, 0, 0};
@@ -563,13 +574,16 @@ mpm_status mpm_batch_autotune(mpm_batch* b, const char* cache_path, int32_t flag
   if (!b) return MPM_ERR_INVALID;
   if (b->n <= 0) return bfail(b, MPM_ERR_INVALID, "autotune needs uploaded particles");
   if (budget_substeps < 0 || budget_substeps > 4096) return bfail(b, MPM_ERR_INVALID, "budget_substeps out of range");
-  if (flags & ~MPM_TUNE_IGNORE_CACHE) return bfail(b, MPM_ERR_INVALID, "unknown flags");
-  const std::string dkey = batch_device_key(b->device), bkey = batch_build_key(), ckey = batch_class_key(b);
+  if (flags & ~(MPM_TUNE_IGNORE_CACHE | MPM_TUNE_SORT_INTERVAL)) return bfail(b, MPM_ERR_INVALID, "unknown flags");
+  const bool with_sort = (flags & MPM_TUNE_SORT_INTERVAL) != 0;
+  const std::string dkey = batch_device_key(b->device), bkey = batch_build_key();
+  const std::string ckey = batch_class_key(b) + (with_sort ? " +sort" : "");
   if (cache_path && !(flags & MPM_TUNE_IGNORE_CACHE)) {
     TuningEntry e;
     if (find_tuning(read_tuning_cache(cache_path), dkey, bkey, ckey, &e) && e.steps_per_warp >= 1 &&
-        e.steps_per_warp <= 256) {
-      const mpm_status st = mpm_batch_set_steps_per_warp(b, e.steps_per_warp);
+        e.steps_per_warp <= 256 && e.sort_interval >= 0) {
+      mpm_status st = mpm_batch_set_steps_per_warp(b, e.steps_per_warp);
+      if (st == MPM_OK && with_sort) st = mpm_batch_set_sort_interval(b, e.sort_interval);
       if (st != MPM_OK) return st;
       if (out) *out = mpm_tuning{b->steps_per_warp, kStepWarps, 0, b->sort_interval, e.us_per_substep, 1, 0};
       return MPM_OK;
@@ -589,19 +603,21 @@ mpm_status mpm_batch_autotune(mpm_batch* b, const char* cache_path, int32_t flag
   // once per buffer role: two replays capture both, the next two are timed
   const int steps = std::max(6, ((budget_substeps > 0 ? budget_substeps : 24) + 5) / 6 * 6);
   int timed = 0;
-  auto time_spw = [&](int spw, double* us) -> mpm_status {
+  auto time_spw = [&](int spw, double* us, int sort_interval = -1, int n_steps = 0) -> mpm_status {
     ++timed;
+    const int len = n_steps > 0 ? n_steps : steps;
     mpm_status s2 = mpm_batch_set_steps_per_warp(t, spw);
+    if (s2 == MPM_OK && sort_interval >= 0) s2 = mpm_batch_set_sort_interval(t, sort_interval);
     if (s2 == MPM_OK) s2 = restore_from(t, b);
-    for (int r = 0; r < 2 && s2 == MPM_OK; ++r) s2 = mpm_batch_substep_graph(t, steps);
+    for (int r = 0; r < 2 && s2 == MPM_OK; ++r) s2 = mpm_batch_substep_graph(t, len);
     if (s2 != MPM_OK) return s2;
     if (cudaEventRecord(e0, t->stream) != cudaSuccess) return MPM_ERR_CUDA;
-    for (int r = 0; r < 2 && s2 == MPM_OK; ++r) s2 = mpm_batch_substep_graph(t, steps);
+    for (int r = 0; r < 2 && s2 == MPM_OK; ++r) s2 = mpm_batch_substep_graph(t, len);
     if (s2 != MPM_OK) return s2;
     if (cudaEventRecord(e1, t->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) return MPM_ERR_CUDA;
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) return MPM_ERR_CUDA;
-    *us = 1e3 * (double)ms / (2.0 * steps);
+    *us = 1e3 * (double)ms / (2.0 * len);
     return mpm_batch_sync(t);
   };
   int best = b->steps_per_warp;
@@ -619,12 +635,32 @@ mpm_status mpm_batch_autotune(mpm_batch* b, const char* cache_path, int32_t flag
       best_us = us;
     }
   }
+  int best_sort = b->sort_interval;
+  if (with_sort && st == MPM_OK) {
+    // sort intervals over replays of 48 substeps (a multiple of each), against the current
+    // interval re-timed over the same length
+    double base = 0.0;
+    st = time_spw(best, &base, b->sort_interval, 48);
+    double cur = base;
+    for (int si : {8, 12, 16, 24}) {
+      if (st != MPM_OK) break;
+      if (si == b->sort_interval) continue;
+      double us = 0.0;
+      st = time_spw(best, &us, si, 48);
+      if (st == MPM_OK && us < 0.99 * cur && us < 0.99 * base) {
+        best_sort = si;
+        cur = us;
+      }
+    }
+    if (st == MPM_OK && best_sort != b->sort_interval) best_us = cur;
+  }
   std::string why = st != MPM_OK ? t->last_error : std::string();
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   mpm_batch_destroy(t);
   if (st != MPM_OK) return bfail(b, st, "tuning: " + why);
   st = mpm_batch_set_steps_per_warp(b, best);
+  if (st == MPM_OK) st = mpm_batch_set_sort_interval(b, best_sort);
   if (st != MPM_OK) return st;
   const mpm_tuning res{best, kStepWarps, 0, b->sort_interval, best_us, 0, timed};
   if (out) *out = res;

@@ -164,3 +164,25 @@ def test_batch_range_sizes_match_oracle(gpu_lib, oracle_lib, spw):
         ref = oracle_after(oracle_lib, {"state": sc["state"], "params": sc["params"], "materials": [sc["material"]]}, 3)
         errs = compare_states(out, ref, sc["params"], sc["state"])
         assert max(errs.values()) < 2e-5, (spw, sc["params"]["N"], errs)
+
+
+def test_batch_autotune_sort_interval(gpu_lib, oracle_lib):
+    """With the sort interval among the knobs, the batch tuner also times intervals of 8, 12,
+    16 and 24 substeps (replays of 48) and applies the fastest; the tuned batch still
+    matches the oracle per scene."""
+    from mpm_gb300 import autotune, scenes
+    from mpm_gb300.batch import Batch
+
+    scs = scenes.config_batched(nscenes=6, seed=23, count_range=(2_000, 20_000))
+    with Batch(scs, sort_interval=4) as b:
+        b.upload([s["state"] for s in scs])
+        t = autotune.tune_batch(b, None, budget_substeps=6, tune_sort_interval=True)
+        assert t["candidates"] == 10 and not t["from_cache"]
+        assert t["sort_interval"] in (4, 8, 12, 16, 24)
+        assert autotune.current_batch(b)["sort_interval"] == t["sort_interval"]
+        b.advance(3, graph=True)
+        outs = b.split(b.download())
+    for sc, out in zip(scs, outs):
+        ref = oracle_after(oracle_lib, {"state": sc["state"], "params": sc["params"], "materials": [sc["material"]]}, 3)
+        errs = compare_states(out, ref, sc["params"], sc["state"])
+        assert max(errs.values()) < 2e-5, (t, sc["params"]["N"], errs)
