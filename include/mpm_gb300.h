@@ -400,7 +400,8 @@ mpm_status mpm_batch_upload_soa(mpm_batch* batch, const float* x, const float* v
 /* nsteps substeps of every scene, one launch each (plus the periodic cell sort). */
 mpm_status mpm_batch_substep(mpm_batch* batch, int32_t nsteps);
 /* The same as one CUDA graph (captured on first use per phase, then replayed); the
- * particles are cell-sorted once at the start of each replayed run. */
+ * particles are cell-sorted at the start of each replayed run and then every sort_interval
+ * substeps of it. */
 mpm_status mpm_batch_substep_graph(mpm_batch* batch, int32_t nsteps);
 mpm_status mpm_batch_sync(mpm_batch* batch);
 mpm_status mpm_batch_download_soa(mpm_batch* batch, float* x, float* v, float* C, float* F, float* Jp);
