@@ -535,7 +535,14 @@ struct mpm_diff {
   float* adj = nullptr;
   double* pgrad = nullptr;
   float* stage = nullptr;
-  uint32_t* id = nullptr;
+  uint32_t* id = nullptr;   // slot q holds particle id[q] (the cell order of the initial state)
+  uint32_t* inv = nullptr;  // particle p sits in slot inv[p]
+  // cell sort of the initial positions (keys, counts, scan block sums, a check flag)
+  uint32_t* keys = nullptr;
+  int* counts = nullptr;
+  int* block_sums = nullptr;
+  int* bad = nullptr;
+  int64_t sort_keys = 0;
   int* status = nullptr;
   int64_t cells = 0;
   std::string last_error;
@@ -610,13 +617,24 @@ mpm_status mpm_diff_create(const mpm_params* params, const mpm_material* materia
       cudaMalloc(&d->grid3, sizeof(float4) * d->cells * 3) || cudaMalloc(&d->vgrid, sizeof(float4) * d->cells) ||
       cudaMalloc(&d->gadj, sizeof(float4) * d->cells) || cudaMalloc(&d->adj, sf) ||
       cudaMalloc(&d->pgrad, 2 * sizeof(double)) || cudaMalloc(&d->stage, sf) ||
-      cudaMalloc(&d->id, sizeof(uint32_t) * d->stride) ||
+      cudaMalloc(&d->id, sizeof(uint32_t) * d->stride) || cudaMalloc(&d->inv, sizeof(uint32_t) * d->stride) ||
+      cudaMalloc(&d->keys, sizeof(uint32_t) * d->stride) || cudaMalloc(&d->bad, sizeof(int)) ||
       cudaMalloc(&d->status, sizeof(int)) ||
       cudaMemset(d->status, 0, sizeof(int)) || cudaMemset(d->ckpt, 0, sf * nck) || cudaMemset(d->seg, 0, sf) ||
       cudaMemset(d->adj, 0, sf) ||
       cudaMalloc(&d->step_vgrid, sizeof(float4) * vgrid_nodes((int)params->N))) {
     mpm_diff_destroy(d);
     return MPM_ERR_NOMEM;
+  }
+  {
+    const int64_t nb = (params->N + 3) / 4;
+    d->sort_keys = nb * nb * nb * 64;
+    const int64_t per = 256 * 8;  // counts per block of the blocked scan
+    if (cudaMalloc(&d->counts, sizeof(int) * d->sort_keys) ||
+        cudaMalloc(&d->block_sums, sizeof(int) * std::max<int64_t>((d->sort_keys + per - 1) / per, 1))) {
+      mpm_diff_destroy(d);
+      return MPM_ERR_NOMEM;
+    }
   }
   if (vgrid_bind(d->vel, d->step_vgrid, (int)params->N) != cudaSuccess) {
     mpm_diff_destroy(d);
@@ -635,6 +653,7 @@ mpm_status mpm_diff_destroy(mpm_diff* d) {
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (void* p : {(void*)d->ckpt, (void*)d->seg, (void*)d->seg_grid, (void*)d->grid3, (void*)d->vgrid,
                   (void*)d->step_vgrid, (void*)d->gadj, (void*)d->adj, (void*)d->pgrad, (void*)d->stage, (void*)d->id,
+                  (void*)d->inv, (void*)d->keys, (void*)d->counts, (void*)d->block_sums, (void*)d->bad,
                   (void*)d->status})
     cudaFree(p);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -670,8 +689,22 @@ mpm_status mpm_diff_forward(mpm_diff* d, const float* x0, const float* v0, const
       (F0 && cudaMemcpyAsync(Fs, F0, 36 * n, cudaMemcpyHostToDevice, s)) ||
       (Jp0 && cudaMemcpyAsync(Js, Jp0, 4 * n, cudaMemcpyHostToDevice, s)))
     return MPM_ERR_CUDA;
-  if (launch_deinterleave(d->stage, d->ckpt, d->stride, n, v0 != nullptr, C0 != nullptr, F0 != nullptr,
-                          Jp0 != nullptr, s) != cudaSuccess)
+  // The particles run in the cell order of their initial positions (as a context's periodic
+  // sort keeps them): P2G then merges a warp's contributions per cell and the gathers stay
+  // local.  id / inv map between that order and the caller's; over one run the particles
+  // move a fraction of a cell, so the order is kept to its end.
+  SortArgs so{};
+  so.n = n;
+  so.keys = d->keys;
+  so.perm = d->id;
+  so.counts = d->counts;
+  so.block_sums = d->block_sums;
+  so.cells = d->sort_keys;
+  so.N = (int)d->params.N;
+  so.dx_inv = d->K.g.dx_inv;
+  if (launch_presort(xs, nullptr, so, d->inv, d->bad, d->num_sms, s, nullptr) != cudaSuccess) return MPM_ERR_CUDA;
+  const HostArrays staged{xs, v0 ? vs : nullptr, C0 ? Cs : nullptr, F0 ? Fs : nullptr, Jp0 ? Js : nullptr};
+  if (launch_deinterleave_arrays(staged, d->ckpt, d->stride, n, d->bad, s, d->inv) != cudaSuccess)
     return MPM_ERR_CUDA;
   // work copy of the state; fused launches with three rotating grids, checkpoints copied out
   const size_t sb = state_floats(d) * sizeof(float);
@@ -710,8 +743,8 @@ mpm_status mpm_diff_forward(mpm_diff* d, const float* x0, const float* v0, const
   }
   d->nsteps = nsteps;
   if (x_out || v_out) {
-    // the differentiable context never reorders its particles (d->id is the identity)
-    if (launch_interleave(work, d->stride, nullptr, n, d->stage, 0, kFieldX | kFieldV, s) != cudaSuccess)
+    // back to the caller's order
+    if (launch_interleave(work, d->stride, d->inv, n, d->stage, 0, kFieldX | kFieldV, s) != cudaSuccess)
       return MPM_ERR_CUDA;
     if (x_out && cudaMemcpyAsync(x_out, d->stage, 12 * n, cudaMemcpyDeviceToHost, s)) return MPM_ERR_CUDA;
     if (v_out && cudaMemcpyAsync(v_out, d->stage + 3 * n, 12 * n, cudaMemcpyDeviceToHost, s)) return MPM_ERR_CUDA;
@@ -736,8 +769,14 @@ mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv
       (gx_final && cudaMemcpyAsync(xs, gx_final, 12 * n, cudaMemcpyHostToDevice, s)) ||
       (gv_final && cudaMemcpyAsync(vs, gv_final, 12 * n, cudaMemcpyHostToDevice, s)))
     return MPM_ERR_CUDA;
-  // adjoint state = (gx, gv, 0, 0, 0); the stage holds interleaved x, v, C, F, Jp slots
-  if (launch_deinterleave(d->stage, d->adj, d->stride, n, 1, 1, 1, 1, s) != cudaSuccess) return MPM_ERR_CUDA;
+  // adjoint state = (gx, gv, 0, 0, 0) in the run's cell order; the stage holds interleaved
+  // x, v, C, F, Jp slots (all read, so no component takes a rest value)
+  {
+    float* Cz = vs + 3 * n;
+    float* Fz = Cz + 9 * n;
+    const HostArrays g{xs, vs, Cz, Fz, Fz + 9 * n};
+    if (launch_deinterleave_arrays(g, d->adj, d->stride, n, d->bad, s, d->inv) != cudaSuccess) return MPM_ERR_CUDA;
+  }
   const int nseg = (d->nsteps + d->ckpt_every - 1) / d->ckpt_every;
   AdjArgs A{};
   A.stride = d->stride;
@@ -777,8 +816,8 @@ mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv
       if (cudaGetLastError() != cudaSuccess) return MPM_ERR_CUDA;
     }
   }
-  // out: adjoint of the initial state, host interleaved
-  if (launch_interleave(d->adj, d->stride, nullptr, n, d->stage, 0, kFieldAll, s) != cudaSuccess) return MPM_ERR_CUDA;
+  // out: adjoint of the initial state, host interleaved, in the caller's order
+  if (launch_interleave(d->adj, d->stride, d->inv, n, d->stage, 0, kFieldAll, s) != cudaSuccess) return MPM_ERR_CUDA;
   float* Cs = vs + 3 * n;
   float* Fs = Cs + 9 * n;
   if ((gx0 && cudaMemcpyAsync(gx0, xs, 12 * n, cudaMemcpyDeviceToHost, s)) ||
