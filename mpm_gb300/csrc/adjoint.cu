@@ -576,12 +576,19 @@ mpm_status dlaunch(mpm_diff* d, StepKind kind, float* state, const float4* gin, 
   return MPM_OK;
 }
 
-// One recomputed substep: P2G of `state` into `grid` (cleared beforehand), which also
-// clears `next_grid` for the following substep, then G2P from it into `state_out`.
-mpm_status forward_substep(mpm_diff* d, float* state, float* state_out, float4* grid, float4* next_grid) {
-  mpm_status st = dlaunch(d, kStepP2GOnly, state, nullptr, grid, next_grid);
+// Recomputes a segment of len substeps from the state in states[0], keeping every state
+// (states + j * sf) and every P2G grid (grids + j * cells, the first one cleared
+// beforehand): P2G of the first state, then fused launches (G2P of substep j into state
+// j + 1, out of place, and P2G of j + 1, clearing the grid after), then the last G2P.
+mpm_status recompute_segment(mpm_diff* d, float* states, float4* grids, int len) {
+  const size_t sf = state_floats(d);
+  auto state = [&](int j) { return states + sf * j; };
+  auto grid = [&](int j) { return j < len ? grids + d->cells * j : nullptr; };
+  mpm_status st = dlaunch(d, kStepP2GOnly, state(0), nullptr, grid(0), grid(1));
+  for (int j = 0; j + 1 < len && st == MPM_OK; ++j)
+    st = dlaunch(d, kStepFused, state(j), grid(j), grid(j + 1), grid(j + 2), state(j + 1));
   if (st != MPM_OK) return st;
-  return dlaunch(d, kStepG2POnly, state, grid, nullptr, nullptr, state_out);
+  return dlaunch(d, kStepG2POnly, state(len - 1), grid(len - 1), nullptr, nullptr, state(len));
 }
 
 int adj_blocks(const mpm_diff* d) {
@@ -799,11 +806,8 @@ mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv
     if (cudaMemcpyAsync(d->seg, d->ckpt + sf * sgi, sb, cudaMemcpyDeviceToDevice, s) ||
         cudaMemsetAsync(d->seg_grid, 0, sizeof(float4) * d->cells, s))
       return MPM_ERR_CUDA;
-    for (int j = 0; j < len; ++j) {
-      mpm_status st = forward_substep(d, d->seg + sf * j, d->seg + sf * (j + 1), d->seg_grid + d->cells * j,
-                                      j + 1 < len ? d->seg_grid + d->cells * (j + 1) : nullptr);
-      if (st != MPM_OK) return st;
-    }
+    mpm_status st = recompute_segment(d, d->seg, d->seg_grid, len);
+    if (st != MPM_OK) return st;
     // adjoint substeps in reverse
     for (int j = len - 1; j >= 0; --j) {
       A.s = d->seg + sf * j;

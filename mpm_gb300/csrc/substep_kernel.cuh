@@ -142,8 +142,9 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS >= kStepWarps ? 1 : kStepWar
   const int N = K.N;
   const float ddx = K.dinv * K.dx;  // D dx of the node-offset gather
   float* __restrict__ s = A.s;
-  // a G2P-only launch may write the new state out of place (the adjoint's recompute)
-  float* const s_w = (!P2G && A.s_out) ? A.s_out : s;
+  // a G2P-only launch, or a fused launch of the general layout, may write the new state out
+  // of place (the adjoint's recompute keeps every state of a segment)
+  float* const s_w = ((!P2G || !LIQ) && A.s_out) ? A.s_out : s;
   const int64_t st = A.stride;
   const int64_t n = A.n, chunk = A.chunk;
 
