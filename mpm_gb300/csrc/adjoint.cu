@@ -545,6 +545,10 @@ struct mpm_diff {
   int64_t sort_keys = 0;
   int* status = nullptr;
   int64_t cells = 0;
+  // a full segment of the backward (recompute and adjoint substeps) as a CUDA graph: every
+  // full segment launches the same kernels on the same buffers; dropped when the material
+  // changes (its constants are kernel parameters)
+  cudaGraphExec_t seg_graph = nullptr;
   std::string last_error;
 };
 
@@ -658,6 +662,7 @@ mpm_status mpm_diff_create(const mpm_params* params, const mpm_material* materia
 mpm_status mpm_diff_destroy(mpm_diff* d) {
   if (!d) return MPM_ERR_INVALID;
   if (d->stream) cudaStreamSynchronize(d->stream);
+  if (d->seg_graph) cudaGraphExecDestroy(d->seg_graph);
   for (void* p : {(void*)d->ckpt, (void*)d->seg, (void*)d->seg_grid, (void*)d->grid3, (void*)d->vgrid,
                   (void*)d->step_vgrid, (void*)d->gadj, (void*)d->adj, (void*)d->pgrad, (void*)d->stage, (void*)d->id,
                   (void*)d->inv, (void*)d->keys, (void*)d->counts, (void*)d->block_sums, (void*)d->bad,
@@ -674,6 +679,11 @@ mpm_status mpm_diff_set_material(mpm_diff* d, const mpm_material* material) {
   if (material->kind != d->material.kind) return MPM_ERR_INVALID;  // the recompute needs the same model
   d->material = *material;
   make_sim_consts(d->params, material, 1, d->K);
+  if (d->seg_graph) {
+    cudaStreamSynchronize(d->stream);
+    cudaGraphExecDestroy(d->seg_graph);
+    d->seg_graph = nullptr;
+  }
   return MPM_OK;
 }
 
@@ -799,16 +809,12 @@ mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv
   if (cudaFuncSetAttribute(adj_g2p_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))
     return MPM_ERR_CUDA;
   const int gblocks = (int)std::min<int64_t>((d->cells + 255) / 256, 4096);
-  for (int sgi = nseg - 1; sgi >= 0; --sgi) {
-    const int s0 = sgi * d->ckpt_every;
-    const int len = std::min(d->ckpt_every, d->nsteps - s0);
-    // recompute the segment, keeping every state and P2G grid
-    if (cudaMemcpyAsync(d->seg, d->ckpt + sf * sgi, sb, cudaMemcpyDeviceToDevice, s) ||
-        cudaMemsetAsync(d->seg_grid, 0, sizeof(float4) * d->cells, s))
-      return MPM_ERR_CUDA;
+  // one segment after its checkpoint is in d->seg: recompute it, keeping every state and P2G
+  // grid, then the adjoint substeps in reverse
+  auto segment = [&](int len) -> mpm_status {
+    if (cudaMemsetAsync(d->seg_grid, 0, sizeof(float4) * d->cells, s)) return MPM_ERR_CUDA;
     mpm_status st = recompute_segment(d, d->seg, d->seg_grid, len);
     if (st != MPM_OK) return st;
-    // adjoint substeps in reverse
     for (int j = len - 1; j >= 0; --j) {
       A.s = d->seg + sf * j;
       A.s1 = d->seg + sf * (j + 1);
@@ -819,6 +825,36 @@ mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv
       adj_p2g_kernel<<<blocks, kAdjThreads, 0, s>>>(A);
       if (cudaGetLastError() != cudaSuccess) return MPM_ERR_CUDA;
     }
+    return MPM_OK;
+  };
+  bool warmed = d->seg_graph != nullptr;  // the first full segment runs eagerly (kernel set-up)
+  for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+    const int s0 = sgi * d->ckpt_every;
+    const int len = std::min(d->ckpt_every, d->nsteps - s0);
+    if (cudaMemcpyAsync(d->seg, d->ckpt + sf * sgi, sb, cudaMemcpyDeviceToDevice, s)) return MPM_ERR_CUDA;
+    if (len < d->ckpt_every || !warmed) {
+      const mpm_status st = segment(len);
+      if (st != MPM_OK) return st;
+      warmed = warmed || len == d->ckpt_every;
+      continue;
+    }
+    if (!d->seg_graph) {
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) return MPM_ERR_CUDA;
+      const mpm_status st = segment(len);
+      const cudaError_t e = cudaStreamEndCapture(s, &g);
+      if (st != MPM_OK || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return st != MPM_OK ? st : MPM_ERR_CUDA;
+      }
+      const cudaError_t ei = cudaGraphInstantiate(&d->seg_graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ei != cudaSuccess) {
+        d->seg_graph = nullptr;
+        return MPM_ERR_CUDA;
+      }
+    }
+    if (cudaGraphLaunch(d->seg_graph, s)) return MPM_ERR_CUDA;
   }
   // out: adjoint of the initial state, host interleaved, in the caller's order
   if (launch_interleave(d->adj, d->stride, d->inv, n, d->stage, 0, kFieldAll, s) != cudaSuccess) return MPM_ERR_CUDA;
