@@ -15,14 +15,17 @@
 //              gathers the grid velocity and SCATTERS the grid-velocity adjoint (the
 //              G2P adjoint is a cell-sorted scatter, reduced per warp like P2G);
 //   adj_gridop per node: back through the grid operation (division by the mass,
-//              gravity, walls) to adjoints of the P2G momentum and mass;
+//              gravity, walls) to adjoints of the P2G momentum and mass; also clears
+//              the grid-velocity adjoint and computes the grid velocities of the
+//              previous substep for its adj_g2p;
 //   adj_p2g    per particle: GATHERS the momentum/mass adjoints (the P2G adjoint is a
 //              gather) and goes back through the affine term, the stress (with the
 //              polar decomposition's adjoint and the hardening factor's dependence on
 //              Jp) and the weights; accumulates dL/dmu0 and dL/dlambda0.
 // The forward run stores the state every `checkpoint_every` substeps; the backward
-// pass recomputes each segment forward (keeping every state and P2G grid of the
-// segment) and then runs the adjoint substeps in reverse.
+// pass recomputes each segment forward (keeping every state, P2G grid and the polar
+// rotation each P2G used, so adj_p2g needs no SVD) and then runs the adjoint substeps
+// in reverse.
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -40,14 +43,22 @@ struct AdjArgs {
   int64_t stride, n;
   const float4* grid;  // P2G grid of substep n: (m v, m)
   const float4* vgrid; // grid velocity of substep n (grid op applied)
-  float4* gadj;        // grid adjoint: velocity adjoint (adj_g2p), then (m v, m) adjoints
+  float4* gvel;        // grid-velocity adjoint, scattered by adj_g2p
+  const float4* gmom;  // (m v, m) adjoints, written by adj_gridop, gathered by adj_p2g
+  const float* rot;    // polar rotation R of each particle's F in state_n, kept by the
+                       // recompute's P2G (9 components, the state's stride)
   double* pgrad;       // [dL/dmu, dL/dlambda]
   GridConsts K;
   DevMaterial M;
 };
 
-constexpr int kAdjThreads = 256;
-constexpr int kAdjWarps = kAdjThreads / 32;
+// Launch shapes, one particle per thread. adj_g2p: 4-warp blocks, three per SM (12 warps,
+// 14 KB of shared memory per warp); at one 8-warp block per SM (its shared memory and 136
+// registers) the backward of 100k particles took 3.5 % longer (snow). adj_p2g: 4-warp
+// blocks, four per SM (16 warps at 127 registers); capping it at 96 or 80 registers for 20
+// or 21 warps per SM spilled and ran slower.
+constexpr int kAdjG2PWarps = 4, kAdjG2PBlocksPerSM = 3;
+constexpr int kAdjP2GWarps = 4, kAdjP2GBlocksPerSM = 4;
 
 // d w_a / d f for the quadratic B-spline (include/InterpolationKernel.cuh:64-66)
 __device__ __forceinline__ void weight_derivs(float x, float dx_inv, float dw[3]) {
@@ -61,8 +72,9 @@ __device__ __forceinline__ void weight_derivs(float x, float dx_inv, float dw[3]
 
 __device__ __forceinline__ float ld(const float* s, int64_t st, int comp, int64_t p) { return s[comp * st + p]; }
 
-// Grid velocities of substep n for the adjoint kernels; also clears the grid adjoint
-// that adj_g2p accumulates into.
+// Grid velocities of the last substep of a segment for the adjoint kernels; also clears
+// the grid-velocity adjoint that adj_g2p accumulates into.  (adj_gridop does both for the
+// other substeps.)
 __global__ void adj_velocity_kernel(const float4* grid, float4* vgrid, float4* gadj, GridConsts K) {
   const int N = K.N;
   const int64_t cells = (int64_t)N * N * N;
@@ -151,7 +163,7 @@ __device__ __forceinline__ void snow_plasticity_adjoint(const float Fh[3][3], fl
 
 // Back through x' = x + dt v', the snow plasticity (above), F^ = (I + dt C') F and the G2P
 // gather (src/mpm.cu:136-176).
-__global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(const AdjArgs A) {
+__global__ void __launch_bounds__(kAdjG2PWarps * 32, kAdjG2PBlocksPerSM) adj_g2p_kernel(const AdjArgs A) {
   extern __shared__ float4 smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float4* wbuf = smem + warp * kRedFloat4;
@@ -159,7 +171,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(const AdjArgs A) {
   const int N = K.N;
   const int64_t st = A.stride;
   const int64_t nsteps = (A.n + 31) / 32;
-  for (int64_t ws = (int64_t)blockIdx.x * kAdjWarps + warp; ws < nsteps; ws += (int64_t)gridDim.x * kAdjWarps) {
+  for (int64_t ws = (int64_t)blockIdx.x * kAdjG2PWarps + warp; ws < nsteps; ws += (int64_t)gridDim.x * kAdjG2PWarps) {
     const int64_t p = ws * 32 + lane;
     const bool valid = p < A.n;
     int key = -1;
@@ -260,19 +272,28 @@ __global__ void __launch_bounds__(kAdjThreads) adj_g2p_kernel(const AdjArgs A) {
         for (int q = 0; q < 9; ++q) A.a[(kF + q) * st + p] = Fa[q / 3][q % 3];
       }
     }
-    if (__ballot_sync(kFull, key >= 0)) warp_scatter_runs(wbuf, lane, key, A.gadj, N);
+    if (__ballot_sync(kFull, key >= 0)) warp_scatter_runs(wbuf, lane, key, A.gvel, N);
   }
 }
 
-// Back through gridOpKernel (src/mpm.cu:76-107): velocity adjoint -> (m v, m) adjoints.
-__global__ void adj_gridop_kernel(const float4* grid, float4* gadj, GridConsts K) {
+// Back through gridOpKernel (src/mpm.cu:76-107): the velocity adjoint gvel -> (m v, m)
+// adjoints in gmom.  In the same pass, per node: gvel is cleared for the adj_g2p of the
+// previous substep, and when prev_grid (that substep's P2G grid) is given, its grid
+// velocity goes to vgrid (adj_g2p of this substep has finished reading it).
+__global__ void adj_gridop_kernel(const float4* grid, float4* gvel, float4* gmom, const float4* prev_grid,
+                                  float4* vgrid, GridConsts K) {
   const int N = K.N;
   const int64_t cells = (int64_t)N * N * N;
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x) {
     const float4 g = grid[c];
-    float4 ga = gadj[c];
+    float4 ga = gvel[c];
+    gvel[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int i = (int)(c / ((int64_t)N * N)), j = (int)((c / N) % N), k = (int)(c % N);
+    if (prev_grid) {
+      const float3 v = grid_node_velocity(prev_grid[c], i, j, k, K);
+      vgrid[c] = make_float4(v.x, v.y, v.z, 0.f);
+    }
     if (g.w > 0.f) {
-      const int i = (int)(c / ((int64_t)N * N)), j = (int)((c / N) % N), k = (int)(c % N);
       bool sticky, floor_;
       if (K.boundary_mode == kBoundaryRefFraction) {
         const float bnd = 0.05f, fN = (float)N;
@@ -293,9 +314,9 @@ __global__ void adj_gridop_kernel(const float4* grid, float4* gadj, GridConsts K
       if (floor_ && !(g.y * inv + K.dtg > 0.f)) ga.y = 0.f;
       // v = m v / m (+ gravity): d/d(mv) = 1/m, d/dm = -(m v)/m^2
       const float mb = -(ga.x * g.x + ga.y * g.y + ga.z * g.z) * inv * inv;
-      gadj[c] = make_float4(ga.x * inv, ga.y * inv, ga.z * inv, mb);
+      gmom[c] = make_float4(ga.x * inv, ga.y * inv, ga.z * inv, mb);
     } else {
-      gadj[c] = make_float4(ga.x, ga.y, ga.z, 0.f);  // raw value passed through (v = m v)
+      gmom[c] = make_float4(ga.x, ga.y, ga.z, 0.f);  // raw value passed through (v = m v)
     }
   }
 }
@@ -316,7 +337,7 @@ __device__ __forceinline__ void cross_mat(const float y[3], float Y[3][3]) {
 // MMFixedCorotated::computePF, with the polar decomposition's adjoint:
 //   F = R S, dR = R [w]x with (tr(S) I - S) w = axial(R^T dF - dF^T R), so for a
 //   rotation adjoint Rbar: Fbar = R [y]x, y = (tr(S) I - S)^-1 k, k = axial part of R^T Rbar.
-__global__ void __launch_bounds__(kAdjThreads) adj_p2g_kernel(const AdjArgs A) {
+__global__ void __launch_bounds__(kAdjP2GWarps * 32, kAdjP2GBlocksPerSM) adj_p2g_kernel(const AdjArgs A) {
   const GridConsts& K = A.K;
   const DevMaterial& M = A.M;
   const int N = K.N;
@@ -339,8 +360,9 @@ __global__ void __launch_bounds__(kAdjThreads) adj_p2g_kernel(const AdjArgs A) {
     float w[3][3], d[3][3];
     stencil(x, K, b, w, d);
     if (outside_domain(b[0], b[1], b[2], N)) continue;  // frozen: adjoint passes through
-    float R[3][3], S[3][3];
-    polar_decomposition(F, R, S);
+    float R[3][3];  // the rotation the forward's P2G used
+#pragma unroll
+    for (int q = 0; q < 9; ++q) R[q / 3][q % 3] = A.rot[q * st + p];
     float PF[3][3];
     compute_PF(M, F, R, Jp, PF);
     const float m = M.mass;
@@ -363,7 +385,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_p2g_kernel(const AdjArgs A) {
         for (int c = 0; c < 3; ++c) {
           const int i = b[0] + a, j = b[1] + bb, k = b[2] + c;
           if ((unsigned)i >= (unsigned)N || (unsigned)j >= (unsigned)N || (unsigned)k >= (unsigned)N) continue;
-          const float4 g = __ldg(A.gadj + ((int64_t)i * N + j) * N + k);
+          const float4 g = __ldg(A.gmom + ((int64_t)i * N + j) * N + k);
           const float gm[3] = {g.x, g.y, g.z};
           const float wt = w[0][a] * w[1][bb] * w[2][c];
           const float dd[3] = {d[0][a], d[1][bb], d[2][c]};
@@ -490,7 +512,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_p2g_kernel(const AdjArgs A) {
     A.a[kJp * st + p] += jbar;
   }
   // block reduction of the parameter gradients
-  __shared__ double red[2][kAdjWarps];
+  __shared__ double red[2][kAdjP2GWarps];
   for (int o = 16; o; o >>= 1) {
     mubar += __shfl_xor_sync(kFull, mubar, o);
     lambar += __shfl_xor_sync(kFull, lambar, o);
@@ -503,7 +525,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_p2g_kernel(const AdjArgs A) {
   __syncthreads();
   if (threadIdx.x == 0) {
     double a0 = 0.0, a1 = 0.0;
-    for (int q = 0; q < kAdjWarps; ++q) {
+    for (int q = 0; q < kAdjP2GWarps; ++q) {
       a0 += red[0][q];
       a1 += red[1][q];
     }
@@ -527,11 +549,13 @@ struct mpm_diff {
   float* ckpt = nullptr;       // (max_steps / ckpt_every + 1) states
   float* seg = nullptr;        // (ckpt_every + 1) states
   float4* seg_grid = nullptr;  // ckpt_every P2G grids
+  float* seg_rot = nullptr;     // ckpt_every x 9 components: the polar rotation of each P2G
   float4* grid3 = nullptr;     // 3 rotating grids for the forward run
   float4* vgrid = nullptr;      // grid velocities of the adjoint kernels
   float4* step_vgrid = nullptr; // padded velocity grid of the forward substep kernels
   VelocityGrid vel;
-  float4* gadj = nullptr;
+  float4* gadj = nullptr;       // grid-velocity adjoint
+  float4* gmom = nullptr;       // grid (m v, m) adjoints
   float* adj = nullptr;
   double* pgrad = nullptr;
   float* stage = nullptr;
@@ -557,10 +581,11 @@ namespace {
 size_t state_floats(const mpm_diff* d) { return (size_t)kNumComps * d->stride; }
 
 mpm_status dlaunch(mpm_diff* d, StepKind kind, float* state, const float4* gin, float4* gout,
-                   float4* gzero = nullptr, float* state_out = nullptr) {
+                   float4* gzero = nullptr, float* state_out = nullptr, float* rot = nullptr) {
   StepArgs a{};
   a.s = state;
   a.s_out = state_out;
+  a.rot = rot;
   a.stride = d->stride;
   a.mat = nullptr;
   a.id = d->id;
@@ -584,19 +609,24 @@ mpm_status dlaunch(mpm_diff* d, StepKind kind, float* state, const float4* gin, 
 // (states + j * sf) and every P2G grid (grids + j * cells, the first one cleared
 // beforehand): P2G of the first state, then fused launches (G2P of substep j into state
 // j + 1, out of place, and P2G of j + 1, clearing the grid after), then the last G2P.
-mpm_status recompute_segment(mpm_diff* d, float* states, float4* grids, int len) {
+// Each P2G also keeps the polar rotation of its F in rots + j * 9 * stride.
+mpm_status recompute_segment(mpm_diff* d, float* states, float4* grids, float* rots, int len) {
   const size_t sf = state_floats(d);
   auto state = [&](int j) { return states + sf * j; };
   auto grid = [&](int j) { return j < len ? grids + d->cells * j : nullptr; };
-  mpm_status st = dlaunch(d, kStepP2GOnly, state(0), nullptr, grid(0), grid(1));
+  auto rot = [&](int j) { return rots + (size_t)9 * d->stride * j; };
+  mpm_status st = dlaunch(d, kStepP2GOnly, state(0), nullptr, grid(0), grid(1), nullptr, rot(0));
   for (int j = 0; j + 1 < len && st == MPM_OK; ++j)
-    st = dlaunch(d, kStepFused, state(j), grid(j), grid(j + 1), grid(j + 2), state(j + 1));
+    st = dlaunch(d, kStepFused, state(j), grid(j), grid(j + 1), grid(j + 2), state(j + 1), rot(j + 1));
   if (st != MPM_OK) return st;
   return dlaunch(d, kStepG2POnly, state(len - 1), grid(len - 1), nullptr, nullptr, state(len));
 }
 
-int adj_blocks(const mpm_diff* d) {
-  return (int)std::max<int64_t>(1, std::min<int64_t>((d->n + kAdjThreads - 1) / kAdjThreads, (int64_t)d->num_sms * 2));
+// One warp per 32 particles, blocks of `warps` warps, at most 8 rounds of the resident blocks
+// (the kernels loop over the rest).
+int adj_blocks(const mpm_diff* d, int warps, int per_sm) {
+  const int64_t need = ((d->n + 31) / 32 + warps - 1) / warps;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)d->num_sms * per_sm * 8));
 }
 
 }  // namespace
@@ -625,8 +655,10 @@ mpm_status mpm_diff_create(const mpm_params* params, const mpm_material* materia
       cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) || cudaMalloc(&d->ckpt, sf * nck) ||
       cudaMalloc(&d->seg, sf * (checkpoint_every + 1)) ||
       cudaMalloc(&d->seg_grid, sizeof(float4) * d->cells * checkpoint_every) ||
+      cudaMalloc(&d->seg_rot, sizeof(float) * 9 * d->stride * checkpoint_every) ||
       cudaMalloc(&d->grid3, sizeof(float4) * d->cells * 3) || cudaMalloc(&d->vgrid, sizeof(float4) * d->cells) ||
-      cudaMalloc(&d->gadj, sizeof(float4) * d->cells) || cudaMalloc(&d->adj, sf) ||
+      cudaMalloc(&d->gadj, sizeof(float4) * d->cells) || cudaMalloc(&d->gmom, sizeof(float4) * d->cells) ||
+      cudaMalloc(&d->adj, sf) ||
       cudaMalloc(&d->pgrad, 2 * sizeof(double)) || cudaMalloc(&d->stage, sf) ||
       cudaMalloc(&d->id, sizeof(uint32_t) * d->stride) || cudaMalloc(&d->inv, sizeof(uint32_t) * d->stride) ||
       cudaMalloc(&d->keys, sizeof(uint32_t) * d->stride) || cudaMalloc(&d->bad, sizeof(int)) ||
@@ -663,8 +695,8 @@ mpm_status mpm_diff_destroy(mpm_diff* d) {
   if (!d) return MPM_ERR_INVALID;
   if (d->stream) cudaStreamSynchronize(d->stream);
   if (d->seg_graph) cudaGraphExecDestroy(d->seg_graph);
-  for (void* p : {(void*)d->ckpt, (void*)d->seg, (void*)d->seg_grid, (void*)d->grid3, (void*)d->vgrid,
-                  (void*)d->step_vgrid, (void*)d->gadj, (void*)d->adj, (void*)d->pgrad, (void*)d->stage, (void*)d->id,
+  for (void* p : {(void*)d->ckpt, (void*)d->seg, (void*)d->seg_grid, (void*)d->seg_rot, (void*)d->grid3, (void*)d->vgrid,
+                  (void*)d->step_vgrid, (void*)d->gadj, (void*)d->gmom, (void*)d->adj, (void*)d->pgrad, (void*)d->stage, (void*)d->id,
                   (void*)d->inv, (void*)d->keys, (void*)d->counts, (void*)d->block_sums, (void*)d->bad,
                   (void*)d->status})
     cudaFree(p);
@@ -799,30 +831,35 @@ mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv
   A.stride = d->stride;
   A.n = n;
   A.a = d->adj;
-  A.gadj = d->gadj;
+  A.gvel = d->gadj;
+  A.gmom = d->gmom;
   A.vgrid = d->vgrid;
   A.pgrad = d->pgrad;
   A.K = d->K.g;
   A.M = d->K.mat[0];
-  const int blocks = adj_blocks(d);
-  const size_t smem = (size_t)kAdjWarps * kRedFloat4 * sizeof(float4);
-  if (cudaFuncSetAttribute(adj_g2p_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))
+  const int g2p_blocks = adj_blocks(d, kAdjG2PWarps, kAdjG2PBlocksPerSM);
+  const int p2g_blocks = adj_blocks(d, kAdjP2GWarps, kAdjP2GBlocksPerSM);
+  const size_t smem = (size_t)kAdjG2PWarps * kRedFloat4 * sizeof(float4);
+  if (cudaFuncSetAttribute(adj_g2p_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ||
+      cudaFuncSetAttribute(adj_g2p_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100))
     return MPM_ERR_CUDA;
   const int gblocks = (int)std::min<int64_t>((d->cells + 255) / 256, 4096);
   // one segment after its checkpoint is in d->seg: recompute it, keeping every state and P2G
   // grid, then the adjoint substeps in reverse
   auto segment = [&](int len) -> mpm_status {
     if (cudaMemsetAsync(d->seg_grid, 0, sizeof(float4) * d->cells, s)) return MPM_ERR_CUDA;
-    mpm_status st = recompute_segment(d, d->seg, d->seg_grid, len);
+    mpm_status st = recompute_segment(d, d->seg, d->seg_grid, d->seg_rot, len);
     if (st != MPM_OK) return st;
     for (int j = len - 1; j >= 0; --j) {
       A.s = d->seg + sf * j;
       A.s1 = d->seg + sf * (j + 1);
       A.grid = d->seg_grid + d->cells * j;
-      adj_velocity_kernel<<<gblocks, 256, 0, s>>>(A.grid, d->vgrid, d->gadj, A.K);
-      adj_g2p_kernel<<<blocks, kAdjThreads, smem, s>>>(A);
-      adj_gridop_kernel<<<gblocks, 256, 0, s>>>(A.grid, d->gadj, A.K);
-      adj_p2g_kernel<<<blocks, kAdjThreads, 0, s>>>(A);
+      A.rot = d->seg_rot + (size_t)9 * d->stride * j;
+      if (j == len - 1) adj_velocity_kernel<<<gblocks, 256, 0, s>>>(A.grid, d->vgrid, d->gadj, A.K);
+      adj_g2p_kernel<<<g2p_blocks, kAdjG2PWarps * 32, smem, s>>>(A);
+      adj_gridop_kernel<<<gblocks, 256, 0, s>>>(A.grid, d->gadj, d->gmom, j > 0 ? A.grid - d->cells : nullptr,
+                                                d->vgrid, A.K);
+      adj_p2g_kernel<<<p2g_blocks, kAdjP2GWarps * 32, 0, s>>>(A);
       if (cudaGetLastError() != cudaSuccess) return MPM_ERR_CUDA;
     }
     return MPM_OK;

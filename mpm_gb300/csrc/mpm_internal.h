@@ -25,6 +25,8 @@ constexpr int kBoxSlots = 6;  // per-scene P2G box slots (record / clear / reset
 struct StepArgs {
   float* s;               // component-major particle state
   float* s_out;           // G2P-only launches: where the updated state goes (null: in place)
+  float* rot;             // null, or where P2G writes each particle's polar rotation R of F
+                          // (9 components at the state's stride; particles inside the domain)
   int64_t stride;         // component stride (elements)
   const uint8_t* mat;     // material index per particle (general layout), may be null
   const uint32_t* id;     // original particle index (for the G2P guard)

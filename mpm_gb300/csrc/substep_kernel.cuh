@@ -277,6 +277,18 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS >= kStepWarps ? 1 : kStepWar
           stencil_f(x, K, b, w, f);
           if (!outside_domain(b[0], b[1], b[2], N)) {
             key = pack_key(b[0], b[1], b[2]);
+            if (!LIQ && A.rot) {
+              // keep R for the adjoint; the stress below reuses it (R = R I^T)
+              float R[3][3];
+              polar_rotation(F, pc, R);
+#pragma unroll
+              for (int i = 0; i < 9; ++i) {
+                A.rot[i * st + p] = R[i / 3][i % 3];
+                pc.U[i / 3][i % 3] = R[i / 3][i % 3];
+                pc.V[i / 3][i % 3] = (i / 3 == i % 3) ? 1.f : 0.f;
+              }
+              pc.valid = true;
+            }
             p2g_prepare_f<LIQ, MAT>(M, K, F, Jp, Cm, v, pc, f, E, q0, m);
           }
         }
