@@ -280,17 +280,20 @@ __global__ void __launch_bounds__(kAdjG2PWarps * 32, kAdjG2PBlocksPerSM) adj_g2p
 // adjoints in gmom.  In the same pass, per node: gvel is cleared for the adj_g2p of the
 // previous substep, and when prev_grid (that substep's P2G grid) is given, its grid
 // velocity goes to vgrid (adj_g2p of this substep has finished reading it).
-__global__ void adj_gridop_kernel(const float4* grid, float4* gvel, float4* gmom, const float4* prev_grid,
-                                  float4* vgrid, GridConsts K) {
+__global__ void adj_gridop_kernel(const float4* __restrict__ grid, float4* __restrict__ gvel,
+                                  float4* __restrict__ gmom, const float4* __restrict__ prev_grid,
+                                  float4* __restrict__ vgrid, GridConsts K) {
   const int N = K.N;
-  const int64_t cells = (int64_t)N * N * N;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x) {
+  const int cells = N * N * N;  // N <= 1000
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += gridDim.x * blockDim.x) {
     const float4 g = grid[c];
     float4 ga = gvel[c];
+    const float4 pg = prev_grid ? prev_grid[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int i = c / (N * N), rem = c - i * (N * N);
+    const int j = rem / N, k = rem - j * N;
     gvel[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-    const int i = (int)(c / ((int64_t)N * N)), j = (int)((c / N) % N), k = (int)(c % N);
     if (prev_grid) {
-      const float3 v = grid_node_velocity(prev_grid[c], i, j, k, K);
+      const float3 v = grid_node_velocity(pg, i, j, k, K);
       vgrid[c] = make_float4(v.x, v.y, v.z, 0.f);
     }
     if (g.w > 0.f) {
