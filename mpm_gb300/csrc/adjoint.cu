@@ -22,10 +22,14 @@
 //              gather) and goes back through the affine term, the stress (with the
 //              polar decomposition's adjoint and the hardening factor's dependence on
 //              Jp) and the weights; accumulates dL/dmu0 and dL/dlambda0.
+// The P2G part of substep n and the G2P part of substep n - 1 touch one particle's
+// adjoint only, so adj_step runs them as one pass per particle (the adjoint of state_n
+// stays in registers); per substep the backward launches adj_gridop and adj_step, with
+// adj_g2p and adj_p2g alone at the two ends of a segment.
 // The forward run stores the state every `checkpoint_every` substeps; the backward
 // pass recomputes each segment forward (keeping every state, P2G grid and the polar
-// rotation each P2G used, so adj_p2g needs no SVD) and then runs the adjoint substeps
-// in reverse.
+// rotation each P2G used, so the P2G adjoint needs no SVD) and then runs the adjoint
+// substeps in reverse.
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -162,117 +166,161 @@ __device__ __forceinline__ void snow_plasticity_adjoint(const float Fh[3][3], fl
 }
 
 // Back through x' = x + dt v', the snow plasticity (above), F^ = (I + dt C') F and the G2P
-// gather (src/mpm.cu:136-176).
+// gather (src/mpm.cu:136-176) for particle p of substep n (A.s = state_n, A.s1 = state_{n+1}).
+// In: the adjoint of the particle's state_{n+1} (ax, av, aC, aF, jb).  Returns false, with
+// nothing written, when the particle is outside the domain at state_n (frozen: its adjoint
+// passes through).  Else out: the adjoint of state_n's x, F and Jp through this part of the
+// substep (gx, Fa, jo; v and C of state_n get theirs from the P2G adjoint alone), the
+// velocity adjoints of its 27 nodes in wbuf (lane's column) and its cell key.
+__device__ __forceinline__ bool g2p_adjoint(const AdjArgs& A, int64_t p, int lane, float4* wbuf, const float ax[3],
+                                            const float av[3], const float aC[3][3], const float aF_in[3][3], float jb,
+                                            float gx[3], float Fa[3][3], float& jo, int& key) {
+  const GridConsts& K = A.K;
+  const int N = K.N;
+  const int64_t st = A.stride;
+  float x[3], w[3][3], d[3][3];
+  int b[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) x[q] = ld(A.s, st, kX + q, p);
+  stencil(x, K, b, w, d);
+  if (outside_domain(b[0], b[1], b[2], N)) return false;
+  key = pack_key(b[0], b[1], b[2]);
+  float F[3][3], C1[3][3], aF[3][3];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    F[q / 3][q % 3] = ld(A.s, st, kF + q, p);
+    C1[q / 3][q % 3] = ld(A.s1, st, kC + q, p);
+    aF[q / 3][q % 3] = aF_in[q / 3][q % 3];
+  }
+  jo = jb;
+  if (A.M.kind == kSnow) {
+    // aF holds the adjoint of F' = U clamp(S) V^T: take it back to F^ = (I + dt C') F,
+    // and the Jp' adjoint back to Jp
+    float Fh[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        Fh[r][c] = F[r][c] + K.dt * (C1[r][0] * F[0][c] + C1[r][1] * F[1][c] + C1[r][2] * F[2][c]);
+    const float Jp = ld(A.s, st, kJp, p);
+    float Fhb[3][3], ratio;
+    bool unclamped;
+    snow_plasticity_adjoint(Fh, Jp, A.M.clamp_lo, A.M.clamp_hi, aF, jb, Fhb, ratio, unclamped);
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) aF[r][c] = Fhb[r][c];
+    jo = unclamped ? jb * ratio : 0.f;
+  }
+  // v' total adjoint, C' total adjoint
+  float vt[3], Ct[3][3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) vt[q] = av[q] + K.dt * ax[q];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      Ct[r][c] = aC[r][c] + K.dt * (aF[r][0] * F[c][0] + aF[r][1] * F[c][1] + aF[r][2] * F[c][2]);
+  // F adjoint: (I + dt C')^T F'adj
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      Fa[r][c] = aF[r][c] + K.dt * (C1[0][r] * aF[0][c] + C1[1][r] * aF[1][c] + C1[2][r] * aF[2][c]);
+  // gather grid velocity; x adjoint through the weights and dpos; node velocity adjoints
+  float dwd[3][3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) weight_derivs(x[q], K.dx_inv, dwd[q]);
+#pragma unroll
+  for (int q = 0; q < 3; ++q) gx[q] = ax[q];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int i = b[0] + a, j = b[1] + bb, k = b[2] + c;
+        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+        if ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N)
+          g = __ldg(A.vgrid + ((int64_t)i * N + j) * N + k);
+        const float wt = w[0][a] * w[1][bb] * w[2][c];
+        const float dd[3] = {d[0][a], d[1][bb], d[2][c]};
+        const float vi[3] = {g.x, g.y, g.z};
+        float Cd[3], CTv[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          Cd[r] = Ct[r][0] * dd[0] + Ct[r][1] * dd[1] + Ct[r][2] * dd[2];
+          CTv[r] = Ct[0][r] * vi[0] + Ct[1][r] * vi[1] + Ct[2][r] * vi[2];
+        }
+        // w-adjoint = v'adj . v_i + D v_i . (C'adj d)
+        const float wbar = vt[0] * vi[0] + vt[1] * vi[1] + vt[2] * vi[2] +
+                           K.dinv * (vi[0] * Cd[0] + vi[1] * Cd[1] + vi[2] * Cd[2]);
+        const float gw[3] = {dwd[0][a] * w[1][bb] * w[2][c], w[0][a] * dwd[1][bb] * w[2][c],
+                             w[0][a] * w[1][bb] * dwd[2][c]};
+#pragma unroll
+        for (int r = 0; r < 3; ++r) gx[r] += wbar * gw[r] - K.dinv * wt * CTv[r];
+        // velocity adjoint of node i
+        wbuf[(a * 9 + bb * 3 + c) * kRedStride + lane] =
+            make_float4(wt * (vt[0] + K.dinv * Cd[0]), wt * (vt[1] + K.dinv * Cd[1]), wt * (vt[2] + K.dinv * Cd[2]), 0.f);
+      }
+  return true;
+}
+
+__device__ __forceinline__ void load_adjoint(const AdjArgs& A, int64_t p, float ax[3], float av[3], float aC[3][3],
+                                             float aF[3][3], float& aJp) {
+  const int64_t st = A.stride;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    ax[q] = ld(A.a, st, kX + q, p);
+    av[q] = ld(A.a, st, kV + q, p);
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    aC[q / 3][q % 3] = ld(A.a, st, kC + q, p);
+    aF[q / 3][q % 3] = ld(A.a, st, kF + q, p);
+  }
+  aJp = ld(A.a, st, kJp, p);
+}
+
+__device__ __forceinline__ void store_adjoint(const AdjArgs& A, int64_t p, const float ax[3], const float av[3],
+                                              const float aC[3][3], const float aF[3][3], float aJp) {
+  const int64_t st = A.stride;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    A.a[(kX + q) * st + p] = ax[q];
+    A.a[(kV + q) * st + p] = av[q];
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    A.a[(kC + q) * st + p] = aC[q / 3][q % 3];
+    A.a[(kF + q) * st + p] = aF[q / 3][q % 3];
+  }
+  A.a[kJp * st + p] = aJp;
+}
+
+// The G2P part of substep n alone (the last substep of a segment): A.a holds the adjoint
+// of state_{n+1}; x, F and Jp of it are replaced by their G2P-part adjoints of state_n.
 __global__ void __launch_bounds__(kAdjG2PWarps * 32, kAdjG2PBlocksPerSM) adj_g2p_kernel(const AdjArgs A) {
   extern __shared__ float4 smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float4* wbuf = smem + warp * kRedFloat4;
-  const GridConsts& K = A.K;
-  const int N = K.N;
   const int64_t st = A.stride;
   const int64_t nsteps = (A.n + 31) / 32;
   for (int64_t ws = (int64_t)blockIdx.x * kAdjG2PWarps + warp; ws < nsteps; ws += (int64_t)gridDim.x * kAdjG2PWarps) {
     const int64_t p = ws * 32 + lane;
-    const bool valid = p < A.n;
     int key = -1;
-    float w[3][3], d[3][3], vt[3], Ct[3][3];
-    if (valid) {
-      float x[3], F[3][3], C1[3][3], ax[3], av[3], aC[3][3], aF[3][3];
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        x[q] = ld(A.s, st, kX + q, p);
-        ax[q] = ld(A.a, st, kX + q, p);
-        av[q] = ld(A.a, st, kV + q, p);
-      }
-#pragma unroll
-      for (int q = 0; q < 9; ++q) {
-        F[q / 3][q % 3] = ld(A.s, st, kF + q, p);
-        C1[q / 3][q % 3] = ld(A.s1, st, kC + q, p);
-        aC[q / 3][q % 3] = ld(A.a, st, kC + q, p);
-        aF[q / 3][q % 3] = ld(A.a, st, kF + q, p);
-      }
-      int b[3];
-      stencil(x, K, b, w, d);
-      if (!outside_domain(b[0], b[1], b[2], N)) {
-        key = pack_key(b[0], b[1], b[2]);
-        if (A.M.kind == kSnow) {
-          // aF holds the adjoint of F' = U clamp(S) V^T: take it back to F^ = (I + dt C') F,
-          // and the Jp' adjoint back to Jp
-          float Fh[3][3];
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-              Fh[r][c] = F[r][c] + K.dt * (C1[r][0] * F[0][c] + C1[r][1] * F[1][c] + C1[r][2] * F[2][c]);
-          const float Jp = ld(A.s, st, kJp, p);
-          const float jb = ld(A.a, st, kJp, p);
-          float Fhb[3][3], ratio;
-          bool unclamped;
-          snow_plasticity_adjoint(Fh, Jp, A.M.clamp_lo, A.M.clamp_hi, aF, jb, Fhb, ratio, unclamped);
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) aF[r][c] = Fhb[r][c];
-          A.a[kJp * st + p] = unclamped ? jb * ratio : 0.f;
-        }
-        // v' total adjoint, C' total adjoint
-#pragma unroll
-        for (int q = 0; q < 3; ++q) vt[q] = av[q] + K.dt * ax[q];
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            Ct[r][c] = aC[r][c] + K.dt * (aF[r][0] * F[c][0] + aF[r][1] * F[c][1] + aF[r][2] * F[c][2]);
-        // F adjoint: (I + dt C')^T F'adj
-        float Fa[3][3];
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            Fa[r][c] = aF[r][c] + K.dt * (C1[0][r] * aF[0][c] + C1[1][r] * aF[1][c] + C1[2][r] * aF[2][c]);
-        // gather grid velocity; x adjoint through the weights and dpos; node velocity adjoints
-        float dwd[3][3];
-#pragma unroll
-        for (int q = 0; q < 3; ++q) weight_derivs(x[q], K.dx_inv, dwd[q]);
-        float gx[3] = {ax[0], ax[1], ax[2]};
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int bb = 0; bb < 3; ++bb)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              const int i = b[0] + a, j = b[1] + bb, k = b[2] + c;
-              float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-              if ((unsigned)i < (unsigned)N && (unsigned)j < (unsigned)N && (unsigned)k < (unsigned)N)
-                g = __ldg(A.vgrid + ((int64_t)i * N + j) * N + k);
-              const float wt = w[0][a] * w[1][bb] * w[2][c];
-              const float dd[3] = {d[0][a], d[1][bb], d[2][c]};
-              const float vi[3] = {g.x, g.y, g.z};
-              float Cd[3], CTv[3];
-#pragma unroll
-              for (int r = 0; r < 3; ++r) {
-                Cd[r] = Ct[r][0] * dd[0] + Ct[r][1] * dd[1] + Ct[r][2] * dd[2];
-                CTv[r] = Ct[0][r] * vi[0] + Ct[1][r] * vi[1] + Ct[2][r] * vi[2];
-              }
-              // w-adjoint = v'adj . v_i + D v_i . (C'adj d)
-              const float wbar = vt[0] * vi[0] + vt[1] * vi[1] + vt[2] * vi[2] +
-                                 K.dinv * (vi[0] * Cd[0] + vi[1] * Cd[1] + vi[2] * Cd[2]);
-              const float gw[3] = {dwd[0][a] * w[1][bb] * w[2][c], w[0][a] * dwd[1][bb] * w[2][c],
-                                   w[0][a] * w[1][bb] * dwd[2][c]};
-#pragma unroll
-              for (int r = 0; r < 3; ++r) gx[r] += wbar * gw[r] - K.dinv * wt * CTv[r];
-              // velocity adjoint of node i
-              wbuf[(a * 9 + bb * 3 + c) * kRedStride + lane] =
-                  make_float4(wt * (vt[0] + K.dinv * Cd[0]), wt * (vt[1] + K.dinv * Cd[1]),
-                              wt * (vt[2] + K.dinv * Cd[2]), 0.f);
-            }
+    if (p < A.n) {
+      float ax[3], av[3], aC[3][3], aF[3][3], aJp, gx[3], Fa[3][3], jo;
+      load_adjoint(A, p, ax, av, aC, aF, aJp);
+      if (g2p_adjoint(A, p, lane, wbuf, ax, av, aC, aF, aJp, gx, Fa, jo, key)) {
 #pragma unroll
         for (int q = 0; q < 3; ++q) A.a[(kX + q) * st + p] = gx[q];
 #pragma unroll
         for (int q = 0; q < 9; ++q) A.a[(kF + q) * st + p] = Fa[q / 3][q % 3];
+        A.a[kJp * st + p] = jo;
       }
     }
-    if (__ballot_sync(kFull, key >= 0)) warp_scatter_runs(wbuf, lane, key, A.gvel, N);
+    if (__ballot_sync(kFull, key >= 0)) warp_scatter_runs(wbuf, lane, key, A.gvel, A.K.N);
   }
 }
 
@@ -340,182 +388,189 @@ __device__ __forceinline__ void cross_mat(const float y[3], float Y[3][3]) {
 // MMFixedCorotated::computePF, with the polar decomposition's adjoint:
 //   F = R S, dR = R [w]x with (tr(S) I - S) w = axial(R^T dF - dF^T R), so for a
 //   rotation adjoint Rbar: Fbar = R [y]x, y = (tr(S) I - S)^-1 k, k = axial part of R^T Rbar.
-__global__ void __launch_bounds__(kAdjP2GWarps * 32, kAdjP2GBlocksPerSM) adj_p2g_kernel(const AdjArgs A) {
+// One particle p of substep n (A.s = state_n).  In: ax, aF, aJp hold the G2P-part adjoints
+// of state_n's x, F and Jp.  Returns false, with nothing changed, when the particle is
+// outside the domain at state_n.  Else out: the full adjoint of state_n in (ax, av, aC, aF,
+// aJp); dL/dmu0 and dL/dlambda0 accumulate into mubar and lambar.
+__device__ __forceinline__ bool p2g_adjoint(const AdjArgs& A, int64_t p, float ax[3], float av[3], float aC[3][3],
+                                            float aF[3][3], float& aJp, double& mubar, double& lambar) {
   const GridConsts& K = A.K;
   const DevMaterial& M = A.M;
   const int N = K.N;
   const int64_t st = A.stride;
-  double mubar = 0.0, lambar = 0.0;
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < A.n; p += (int64_t)gridDim.x * blockDim.x) {
-    float x[3], v[3], C[3][3], F[3][3];
+  float x[3], v[3], C[3][3], F[3][3];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      x[q] = ld(A.s, st, kX + q, p);
-      v[q] = ld(A.s, st, kV + q, p);
-    }
+  for (int q = 0; q < 3; ++q) {
+    x[q] = ld(A.s, st, kX + q, p);
+    v[q] = ld(A.s, st, kV + q, p);
+  }
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
-      C[q / 3][q % 3] = ld(A.s, st, kC + q, p);
-      F[q / 3][q % 3] = ld(A.s, st, kF + q, p);
-    }
-    const float Jp = ld(A.s, st, kJp, p);
-    int b[3];
-    float w[3][3], d[3][3];
-    stencil(x, K, b, w, d);
-    if (outside_domain(b[0], b[1], b[2], N)) continue;  // frozen: adjoint passes through
-    float R[3][3];  // the rotation the forward's P2G used
+  for (int q = 0; q < 9; ++q) {
+    C[q / 3][q % 3] = ld(A.s, st, kC + q, p);
+    F[q / 3][q % 3] = ld(A.s, st, kF + q, p);
+  }
+  const float Jp = ld(A.s, st, kJp, p);
+  int b[3];
+  float w[3][3], d[3][3];
+  stencil(x, K, b, w, d);
+  if (outside_domain(b[0], b[1], b[2], N)) return false;  // frozen: adjoint passes through
+  float R[3][3];  // the rotation the forward's P2G used
 #pragma unroll
-    for (int q = 0; q < 9; ++q) R[q / 3][q % 3] = A.rot[q * st + p];
-    float PF[3][3];
-    compute_PF(M, F, R, Jp, PF);
-    const float m = M.mass;
-    const float sc = ((-K.dinv) * K.dt) * M.vol;
-    float Aff[3][3];
+  for (int q = 0; q < 9; ++q) R[q / 3][q % 3] = A.rot[q * st + p];
+  float PF[3][3];
+  compute_PF(M, F, R, Jp, PF);
+  const float m = M.mass;
+  const float sc = ((-K.dinv) * K.dt) * M.vol;
+  float Aff[3][3];
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
+  for (int r = 0; r < 3; ++r)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) Aff[r][c] = sc * PF[r][c] + m * C[r][c];
-    float dwd[3][3];
+    for (int c = 0; c < 3; ++c) Aff[r][c] = sc * PF[r][c] + m * C[r][c];
+  float dwd[3][3];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) weight_derivs(x[q], K.dx_inv, dwd[q]);
-    float vb[3] = {0.f, 0.f, 0.f}, Ab[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    float xb[3] = {0.f, 0.f, 0.f};
+  for (int q = 0; q < 3; ++q) weight_derivs(x[q], K.dx_inv, dwd[q]);
+  float vb[3] = {0.f, 0.f, 0.f}, Ab[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+  float xb[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+  for (int a = 0; a < 3; ++a)
 #pragma unroll
-      for (int bb = 0; bb < 3; ++bb)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const int i = b[0] + a, j = b[1] + bb, k = b[2] + c;
-          if ((unsigned)i >= (unsigned)N || (unsigned)j >= (unsigned)N || (unsigned)k >= (unsigned)N) continue;
-          const float4 g = __ldg(A.gmom + ((int64_t)i * N + j) * N + k);
-          const float gm[3] = {g.x, g.y, g.z};
-          const float wt = w[0][a] * w[1][bb] * w[2][c];
-          const float dd[3] = {d[0][a], d[1][bb], d[2][c]};
-          float contrib[3], ATg[3];
-#pragma unroll
-          for (int r = 0; r < 3; ++r) {
-            contrib[r] = m * v[r] + Aff[r][0] * dd[0] + Aff[r][1] * dd[1] + Aff[r][2] * dd[2];
-            ATg[r] = Aff[0][r] * gm[0] + Aff[1][r] * gm[1] + Aff[2][r] * gm[2];
-            vb[r] += wt * m * gm[r];
-          }
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int cc = 0; cc < 3; ++cc) Ab[r][cc] += wt * gm[r] * dd[cc];
-          const float wbar = gm[0] * contrib[0] + gm[1] * contrib[1] + gm[2] * contrib[2] + g.w * m;
-          const float gw[3] = {dwd[0][a] * w[1][bb] * w[2][c], w[0][a] * dwd[1][bb] * w[2][c],
-                               w[0][a] * w[1][bb] * dwd[2][c]};
-#pragma unroll
-          for (int r = 0; r < 3; ++r) xb[r] += wbar * gw[r] - wt * ATg[r];
-        }
-    // affine = sc PF + m C
-    float PFb[3][3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) PFb[r][c] = sc * Ab[r][c];
-    // PF = e (2 mu0 G + lambda0 (Jp - 1) Jp I), G = (F - R) F^T, e = exp(h (1 - Jp)) for snow
-    // and jelly with h != 0 (compute_PF), else 1
-    const bool hardens = (M.kind == kSnow || M.kind == kJelly) && M.hardening != 0.f;
-    const float e = hardens ? expf(M.hardening * (1.f - Jp)) : 1.f;
-    const float mu = M.mu0 * e;
-    float G[3][3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-        G[r][c] = (F[r][0] - R[r][0]) * F[c][0] + (F[r][1] - R[r][1]) * F[c][1] + (F[r][2] - R[r][2]) * F[c][2];
-    float pg = 0.f;  // <PFb, G>
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) pg += PFb[r][c] * G[r][c];
-    const float trb = PFb[0][0] + PFb[1][1] + PFb[2][2];
-    // dL/dmu0 = e <PFb, 2 G>, dL/dlambda0 = e tr(PFb) (Jp - 1) Jp
-    mubar += (double)(2.f * e * pg);
-    lambar += (double)(e * trb * ((Jp - 1.f) * Jp));
-    // dL/dJp: de/dJp = -h e on both terms, and d((Jp - 1) Jp)/dJp = 2 Jp - 1
-    const float jbar = (hardens ? -M.hardening * e * (2.f * M.mu0 * pg + M.lambda0 * ((Jp - 1.f) * Jp) * trb) : 0.f) +
-                       M.lambda0 * e * (2.f * Jp - 1.f) * trb;
-    // F adjoint of G(F) = (F - R) F^T with Gbar = 2 mu PFb
-    float Gb[3][3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) Gb[r][c] = 2.f * mu * PFb[r][c];
-    float Fb[3][3], Rb[3][3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
+    for (int bb = 0; bb < 3; ++bb)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        float gf = 0.f, gtf = 0.f, gtr = 0.f;
+        const int i = b[0] + a, j = b[1] + bb, k = b[2] + c;
+        if ((unsigned)i >= (unsigned)N || (unsigned)j >= (unsigned)N || (unsigned)k >= (unsigned)N) continue;
+        const float4 g = __ldg(A.gmom + ((int64_t)i * N + j) * N + k);
+        const float gm[3] = {g.x, g.y, g.z};
+        const float wt = w[0][a] * w[1][bb] * w[2][c];
+        const float dd[3] = {d[0][a], d[1][bb], d[2][c]};
+        float contrib[3], ATg[3];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          gf += Gb[r][q] * F[q][c];
-          gtf += Gb[q][r] * F[q][c];
-          gtr += Gb[q][r] * R[q][c];
+        for (int r = 0; r < 3; ++r) {
+          contrib[r] = m * v[r] + Aff[r][0] * dd[0] + Aff[r][1] * dd[1] + Aff[r][2] * dd[2];
+          ATg[r] = Aff[0][r] * gm[0] + Aff[1][r] * gm[1] + Aff[2][r] * gm[2];
+          vb[r] += wt * m * gm[r];
         }
-        Fb[r][c] = gf + gtf - gtr;
-        Rb[r][c] = -gf;
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) Ab[r][cc] += wt * gm[r] * dd[cc];
+        const float wbar = gm[0] * contrib[0] + gm[1] * contrib[1] + gm[2] * contrib[2] + g.w * m;
+        const float gw[3] = {dwd[0][a] * w[1][bb] * w[2][c], w[0][a] * dwd[1][bb] * w[2][c],
+                             w[0][a] * w[1][bb] * dwd[2][c]};
+#pragma unroll
+        for (int r = 0; r < 3; ++r) xb[r] += wbar * gw[r] - wt * ATg[r];
       }
-    // polar adjoint
-    float Kr[3][3];
+  // affine = sc PF + m C
+  float PFb[3][3];
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
+  for (int r = 0; r < 3; ++r)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) Kr[r][c] = R[0][r] * Rb[0][c] + R[1][r] * Rb[1][c] + R[2][r] * Rb[2][c];
-    const float kv[3] = {Kr[2][1] - Kr[1][2], Kr[0][2] - Kr[2][0], Kr[1][0] - Kr[0][1]};
-    float Sp[3][3];
+    for (int c = 0; c < 3; ++c) PFb[r][c] = sc * Ab[r][c];
+  // PF = e (2 mu0 G + lambda0 (Jp - 1) Jp I), G = (F - R) F^T, e = exp(h (1 - Jp)) for snow
+  // and jelly with h != 0 (compute_PF), else 1
+  const bool hardens = (M.kind == kSnow || M.kind == kJelly) && M.hardening != 0.f;
+  const float e = hardens ? expf(M.hardening * (1.f - Jp)) : 1.f;
+  const float mu = M.mu0 * e;
+  float G[3][3];
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
+  for (int r = 0; r < 3; ++r)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) Sp[r][c] = R[0][r] * F[0][c] + R[1][r] * F[1][c] + R[2][r] * F[2][c];
-    const float tr = Sp[0][0] + Sp[1][1] + Sp[2][2];
-    float T[3][3];
+    for (int c = 0; c < 3; ++c)
+      G[r][c] = (F[r][0] - R[r][0]) * F[c][0] + (F[r][1] - R[r][1]) * F[c][1] + (F[r][2] - R[r][2]) * F[c][2];
+  float pg = 0.f;  // <PFb, G>
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
+  for (int r = 0; r < 3; ++r)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) T[r][c] = (r == c ? tr : 0.f) - 0.5f * (Sp[r][c] + Sp[c][r]);
-    // y = T^-1 k by the adjugate
-    const float det = det3(T);
-    float y[3] = {0.f, 0.f, 0.f};
-    if (fabsf(det) > 1e-30f) {
-      float adj[3][3];
-      adj[0][0] = T[1][1] * T[2][2] - T[1][2] * T[2][1];
-      adj[0][1] = T[0][2] * T[2][1] - T[0][1] * T[2][2];
-      adj[0][2] = T[0][1] * T[1][2] - T[0][2] * T[1][1];
-      adj[1][0] = T[1][2] * T[2][0] - T[1][0] * T[2][2];
-      adj[1][1] = T[0][0] * T[2][2] - T[0][2] * T[2][0];
-      adj[1][2] = T[0][2] * T[1][0] - T[0][0] * T[1][2];
-      adj[2][0] = T[1][0] * T[2][1] - T[1][1] * T[2][0];
-      adj[2][1] = T[0][1] * T[2][0] - T[0][0] * T[2][1];
-      adj[2][2] = T[0][0] * T[1][1] - T[0][1] * T[1][0];
-      const float id = 1.f / det;
+    for (int c = 0; c < 3; ++c) pg += PFb[r][c] * G[r][c];
+  const float trb = PFb[0][0] + PFb[1][1] + PFb[2][2];
+  // dL/dmu0 = e <PFb, 2 G>, dL/dlambda0 = e tr(PFb) (Jp - 1) Jp
+  mubar += (double)(2.f * e * pg);
+  lambar += (double)(e * trb * ((Jp - 1.f) * Jp));
+  // dL/dJp: de/dJp = -h e on both terms, and d((Jp - 1) Jp)/dJp = 2 Jp - 1
+  const float jbar = (hardens ? -M.hardening * e * (2.f * M.mu0 * pg + M.lambda0 * ((Jp - 1.f) * Jp) * trb) : 0.f) +
+                     M.lambda0 * e * (2.f * Jp - 1.f) * trb;
+  // F adjoint of G(F) = (F - R) F^T with Gbar = 2 mu PFb
+  float Gb[3][3];
 #pragma unroll
-      for (int r = 0; r < 3; ++r) y[r] = id * (adj[r][0] * kv[0] + adj[r][1] * kv[1] + adj[r][2] * kv[2]);
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Gb[r][c] = 2.f * mu * PFb[r][c];
+  float Fb[3][3], Rb[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float gf = 0.f, gtf = 0.f, gtr = 0.f;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        gf += Gb[r][q] * F[q][c];
+        gtf += Gb[q][r] * F[q][c];
+        gtr += Gb[q][r] * R[q][c];
+      }
+      Fb[r][c] = gf + gtf - gtr;
+      Rb[r][c] = -gf;
     }
-    float Y[3][3];
-    cross_mat(y, Y);
+  // polar adjoint
+  float Kr[3][3];
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
+  for (int r = 0; r < 3; ++r)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) Fb[r][c] += R[r][0] * Y[0][c] + R[r][1] * Y[1][c] + R[r][2] * Y[2][c];
-    // write the adjoint of state_n (x and F add to the adj_g2p parts)
+    for (int c = 0; c < 3; ++c) Kr[r][c] = R[0][r] * Rb[0][c] + R[1][r] * Rb[1][c] + R[2][r] * Rb[2][c];
+  const float kv[3] = {Kr[2][1] - Kr[1][2], Kr[0][2] - Kr[2][0], Kr[1][0] - Kr[0][1]};
+  float Sp[3][3];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      A.a[(kX + q) * st + p] += xb[q];
-      A.a[(kV + q) * st + p] = vb[q];
-    }
+  for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
-      A.a[(kC + q) * st + p] = m * Ab[q / 3][q % 3];
-      A.a[(kF + q) * st + p] += Fb[q / 3][q % 3];
-    }
-    A.a[kJp * st + p] += jbar;
+    for (int c = 0; c < 3; ++c) Sp[r][c] = R[0][r] * F[0][c] + R[1][r] * F[1][c] + R[2][r] * F[2][c];
+  const float tr = Sp[0][0] + Sp[1][1] + Sp[2][2];
+  float T[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) T[r][c] = (r == c ? tr : 0.f) - 0.5f * (Sp[r][c] + Sp[c][r]);
+  // y = T^-1 k by the adjugate
+  const float det = det3(T);
+  float y[3] = {0.f, 0.f, 0.f};
+  if (fabsf(det) > 1e-30f) {
+    float adj[3][3];
+    adj[0][0] = T[1][1] * T[2][2] - T[1][2] * T[2][1];
+    adj[0][1] = T[0][2] * T[2][1] - T[0][1] * T[2][2];
+    adj[0][2] = T[0][1] * T[1][2] - T[0][2] * T[1][1];
+    adj[1][0] = T[1][2] * T[2][0] - T[1][0] * T[2][2];
+    adj[1][1] = T[0][0] * T[2][2] - T[0][2] * T[2][0];
+    adj[1][2] = T[0][2] * T[1][0] - T[0][0] * T[1][2];
+    adj[2][0] = T[1][0] * T[2][1] - T[1][1] * T[2][0];
+    adj[2][1] = T[0][1] * T[2][0] - T[0][0] * T[2][1];
+    adj[2][2] = T[0][0] * T[1][1] - T[0][1] * T[1][0];
+    const float id = 1.f / det;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) y[r] = id * (adj[r][0] * kv[0] + adj[r][1] * kv[1] + adj[r][2] * kv[2]);
   }
-  // block reduction of the parameter gradients
-  __shared__ double red[2][kAdjP2GWarps];
+  float Y[3][3];
+  cross_mat(y, Y);
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Fb[r][c] += R[r][0] * Y[0][c] + R[r][1] * Y[1][c] + R[r][2] * Y[2][c];
+  // the adjoint of state_n (x and F add to the G2P parts)
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    ax[q] += xb[q];
+    av[q] = vb[q];
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    aC[q / 3][q % 3] = m * Ab[q / 3][q % 3];
+    aF[q / 3][q % 3] += Fb[q / 3][q % 3];
+  }
+  aJp += jbar;
+  return true;
+}
+
+// Block reduction of the parameter gradients into A.pgrad (every thread of the block calls it).
+template <int WARPS>
+__device__ __forceinline__ void reduce_pgrad(const AdjArgs& A, double mubar, double lambar) {
+  __shared__ double red[2][WARPS];
   for (int o = 16; o; o >>= 1) {
     mubar += __shfl_xor_sync(kFull, mubar, o);
     lambar += __shfl_xor_sync(kFull, lambar, o);
@@ -528,13 +583,70 @@ __global__ void __launch_bounds__(kAdjP2GWarps * 32, kAdjP2GBlocksPerSM) adj_p2g
   __syncthreads();
   if (threadIdx.x == 0) {
     double a0 = 0.0, a1 = 0.0;
-    for (int q = 0; q < kAdjP2GWarps; ++q) {
+    for (int q = 0; q < WARPS; ++q) {
       a0 += red[0][q];
       a1 += red[1][q];
     }
     atomicAdd(A.pgrad, a0);
     atomicAdd(A.pgrad + 1, a1);
   }
+}
+
+// The P2G part of substep n alone (the first substep of a segment): A.a holds the G2P-part
+// adjoints of state_n's x, F and Jp; it ends with the full adjoint of state_n.
+__global__ void __launch_bounds__(kAdjP2GWarps * 32, kAdjP2GBlocksPerSM) adj_p2g_kernel(const AdjArgs A) {
+  double mubar = 0.0, lambar = 0.0;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < A.n; p += (int64_t)gridDim.x * blockDim.x) {
+    float ax[3], av[3], aC[3][3], aF[3][3], aJp;
+    load_adjoint(A, p, ax, av, aC, aF, aJp);
+    if (p2g_adjoint(A, p, ax, av, aC, aF, aJp, mubar, lambar)) store_adjoint(A, p, ax, av, aC, aF, aJp);
+  }
+  reduce_pgrad<kAdjP2GWarps>(A, mubar, lambar);
+}
+
+// P2G part of substep n (An) and G2P part of substep n - 1 (Ap, the substep before) in one
+// pass per particle: the adjoint of the particle's state_n stays in registers between them.
+// A.a holds the G2P-part adjoints of state_n's x, F and Jp on entry and those of
+// state_{n-1} on exit (the whole adjoint where the particle is outside the domain).
+__global__ void __launch_bounds__(kAdjG2PWarps * 32, kAdjG2PBlocksPerSM) adj_step_kernel(const AdjArgs An,
+                                                                                         const AdjArgs Ap) {
+  extern __shared__ float4 smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float4* wbuf = smem + warp * kRedFloat4;
+  const int64_t st = An.stride;
+  const int64_t nsteps = (An.n + 31) / 32;
+  double mubar = 0.0, lambar = 0.0;
+  for (int64_t ws = (int64_t)blockIdx.x * kAdjG2PWarps + warp; ws < nsteps; ws += (int64_t)gridDim.x * kAdjG2PWarps) {
+    const int64_t p = ws * 32 + lane;
+    int key = -1;
+    if (p < An.n) {
+      float ax[3], av[3], aC[3][3], aF[3][3], aJp;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) ax[q] = ld(An.a, st, kX + q, p);
+#pragma unroll
+      for (int q = 0; q < 9; ++q) aF[q / 3][q % 3] = ld(An.a, st, kF + q, p);
+      aJp = ld(An.a, st, kJp, p);
+      if (!p2g_adjoint(An, p, ax, av, aC, aF, aJp, mubar, lambar)) {
+        // outside at state_n: the stored adjoint passes through whole
+#pragma unroll
+        for (int q = 0; q < 3; ++q) av[q] = ld(An.a, st, kV + q, p);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) aC[q / 3][q % 3] = ld(An.a, st, kC + q, p);
+      }
+      float gx[3], Fa[3][3], jo;
+      if (g2p_adjoint(Ap, p, lane, wbuf, ax, av, aC, aF, aJp, gx, Fa, jo, key)) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) An.a[(kX + q) * st + p] = gx[q];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) An.a[(kF + q) * st + p] = Fa[q / 3][q % 3];
+        An.a[kJp * st + p] = jo;
+      } else {
+        store_adjoint(An, p, ax, av, aC, aF, aJp);  // outside at state_{n-1}
+      }
+    }
+    if (__ballot_sync(kFull, key >= 0)) warp_scatter_runs(wbuf, lane, key, Ap.gvel, Ap.K.N);
+  }
+  reduce_pgrad<kAdjG2PWarps>(An, mubar, lambar);
 }
 
 }  // namespace mpm
@@ -844,7 +956,9 @@ mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv
   const int p2g_blocks = adj_blocks(d, kAdjP2GWarps, kAdjP2GBlocksPerSM);
   const size_t smem = (size_t)kAdjG2PWarps * kRedFloat4 * sizeof(float4);
   if (cudaFuncSetAttribute(adj_g2p_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ||
-      cudaFuncSetAttribute(adj_g2p_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100))
+      cudaFuncSetAttribute(adj_g2p_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) ||
+      cudaFuncSetAttribute(adj_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ||
+      cudaFuncSetAttribute(adj_step_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100))
     return MPM_ERR_CUDA;
   const int gblocks = (int)std::min<int64_t>((d->cells + 255) / 256, 4096);
   // one segment after its checkpoint is in d->seg: recompute it, keeping every state and P2G
@@ -853,16 +967,27 @@ mpm_status mpm_diff_backward(mpm_diff* d, const float* gx_final, const float* gv
     if (cudaMemsetAsync(d->seg_grid, 0, sizeof(float4) * d->cells, s)) return MPM_ERR_CUDA;
     mpm_status st = recompute_segment(d, d->seg, d->seg_grid, d->seg_rot, len);
     if (st != MPM_OK) return st;
+    auto args = [&](int j) {
+      AdjArgs a = A;
+      a.s = d->seg + sf * j;
+      a.s1 = d->seg + sf * (j + 1);
+      a.grid = d->seg_grid + d->cells * j;
+      a.rot = d->seg_rot + (size_t)9 * d->stride * j;
+      return a;
+    };
+    // the G2P part of the last substep, then per substep the grid-op adjoint and the fused
+    // P2G part of substep j with the G2P part of j - 1; the P2G part of substep 0 alone
+    const AdjArgs last = args(len - 1);
+    adj_velocity_kernel<<<gblocks, 256, 0, s>>>(last.grid, d->vgrid, d->gadj, A.K);
+    adj_g2p_kernel<<<g2p_blocks, kAdjG2PWarps * 32, smem, s>>>(last);
     for (int j = len - 1; j >= 0; --j) {
-      A.s = d->seg + sf * j;
-      A.s1 = d->seg + sf * (j + 1);
-      A.grid = d->seg_grid + d->cells * j;
-      A.rot = d->seg_rot + (size_t)9 * d->stride * j;
-      if (j == len - 1) adj_velocity_kernel<<<gblocks, 256, 0, s>>>(A.grid, d->vgrid, d->gadj, A.K);
-      adj_g2p_kernel<<<g2p_blocks, kAdjG2PWarps * 32, smem, s>>>(A);
-      adj_gridop_kernel<<<gblocks, 256, 0, s>>>(A.grid, d->gadj, d->gmom, j > 0 ? A.grid - d->cells : nullptr,
+      const AdjArgs An = args(j);
+      adj_gridop_kernel<<<gblocks, 256, 0, s>>>(An.grid, d->gadj, d->gmom, j > 0 ? An.grid - d->cells : nullptr,
                                                 d->vgrid, A.K);
-      adj_p2g_kernel<<<p2g_blocks, kAdjP2GWarps * 32, 0, s>>>(A);
+      if (j > 0)
+        adj_step_kernel<<<g2p_blocks, kAdjG2PWarps * 32, smem, s>>>(An, args(j - 1));
+      else
+        adj_p2g_kernel<<<p2g_blocks, kAdjP2GWarps * 32, 0, s>>>(An);
       if (cudaGetLastError() != cudaSuccess) return MPM_ERR_CUDA;
     }
     return MPM_OK;

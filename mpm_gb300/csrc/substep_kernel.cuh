@@ -267,6 +267,10 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS >= kStepWarps ? 1 : kStepWar
         particle_update<LIQ, MAT>(M, K, x, v, Cm, F, Jp, pc);
         store_particle<LIQ>(s_w, st, p, x, v, Cm, F, Jp);
         if (A.check_finite && !isfinite(x[0] + x[1] + x[2] + v[0] + v[1] + v[2])) atomicOr(A.status, kStatusNonFinite);
+      } else if (!LIQ && G2P && valid && s_w != s) {
+        // out-of-place launch: a particle that G2P leaves alone keeps its state in the output
+#pragma unroll 1
+        for (int c = 0; c < kNumComps; ++c) s_w[c * st + p] = s[c * st + p];
       }
       // ---- P2G of the next substep (particleToGrid)
       if (P2G) {

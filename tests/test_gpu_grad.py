@@ -251,3 +251,38 @@ def test_full_size_differentiable_config(gpu_lib, oracle_lib):
         negligible = 1e-3 * abs(fd2) / L2 * L
         assert abs(fd1) < negligible and abs(g[name]) < negligible, (name, g[name], fd1, negligible)
     assert np.isfinite([gE, gnu, g2E, g2nu]).all()
+
+
+def test_frozen_particles_pass_the_adjoint_through(gpu_lib):
+    """Particles completely outside the domain are frozen in the forward (no G2P, no P2G),
+    so their adjoint passes through every substep unchanged and they touch nobody else's.
+    With a linear loss r . x_final on 20 such particles added to the sheared body (spread
+    loss), over 8 substeps in segments of 3, 3 and 2 (every kernel of the backward, both
+    segment ends included): their dL/dx0 is exactly r and their dL/dv0 exactly 0, and the
+    body's gradients equal those of the body alone to rounding (the extra particles change
+    the cell order, so the P2G sums round differently)."""
+    base = sheared_case()
+    g0, _ = gpu_grads(base, 8, 3, "spread")
+    n0 = base["state"]["x"].shape[0]
+    rng = np.random.default_rng(11)
+    k = 20
+    extra = {"x": rng.uniform(1.3, 1.9, (k, 3)), "v": rng.standard_normal((k, 3)),
+             "C": 0.1 * rng.standard_normal((k, 3, 3)), "F": np.tile(np.eye(3), (k, 1, 1)), "Jp": np.ones(k)}
+    cfg = sheared_case()
+    for f, a in extra.items():
+        cfg["state"][f] = np.concatenate([cfg["state"][f], a.astype(np.float32)])
+    from mpm_gb300.autograd import DiffSim
+
+    m = cfg["materials"][0]
+    sim = DiffSim(cfg["params"], m, n0 + k, 8, 3)
+    xo, _ = sim.forward(cfg["state"], 8)
+    assert np.array_equal(xo[n0:], cfg["state"]["x"][n0:])  # frozen in the forward
+    gx, _ = loss_grad_x(xo[:n0], "spread")
+    r = rng.standard_normal((k, 3)).astype(np.float32)
+    g = sim.backward(np.concatenate([gx, r]))
+    sim.close()
+    assert np.array_equal(g["x"][n0:], r)
+    assert not g["v"][n0:].any()
+    assert rel(g["x"][:n0], g0["x"]) < 1e-4, rel(g["x"][:n0], g0["x"])
+    assert rel(g["v"][:n0], g0["v"]) < 1e-4, rel(g["v"][:n0], g0["v"])
+    assert abs(g["mu0"] - g0["mu0"]) < 1e-4 * abs(g0["mu0"]), (g["mu0"], g0["mu0"])
