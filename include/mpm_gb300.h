@@ -432,16 +432,19 @@ mpm_status mpm_batch_autotune(mpm_batch* batch, const char* cache_path, int32_t 
 
 /* ---------------------------------------------------------------------------
  * Differentiable substeps (no counterpart in the reference, which has no gradients).
- * A fixed-corotated scene (MMFixedCorotated, include/MaterialModel.cuh:40-62) is run
- * forward with a checkpoint every `checkpoint_every` substeps; the backward pass
- * recomputes each segment and runs hand-written adjoint kernels in reverse.  Host
- * arrays use the interleaved layout of mpm_upload_soa.
+ * A fixed-corotated (MMFixedCorotated, include/MaterialModel.cuh:40-62) or snow (MMSnow,
+ * :67-116) scene is run forward with a checkpoint every `checkpoint_every` substeps; the
+ * backward pass recomputes each segment (keeping its states, P2G grids and the polar
+ * rotation of each particle's P2G: per segment, checkpoint_every x (34 floats per particle
+ * + one N^3 float4 grid) of device memory) and runs hand-written adjoint kernels in
+ * reverse.  Host arrays use the interleaved layout of mpm_upload_soa.
  * ------------------------------------------------------------------------- */
 typedef struct mpm_diff mpm_diff;
 mpm_status mpm_diff_create(const mpm_params* params, const mpm_material* material, int64_t n, int32_t max_steps,
                            int32_t checkpoint_every, mpm_diff** out);
 mpm_status mpm_diff_destroy(mpm_diff* diff);
-/* Change E / nu (the material must stay fixed-corotated). */
+/* Change E / nu and the other material constants (the material kind must stay the same:
+ * MPM_ERR_INVALID otherwise). */
 mpm_status mpm_diff_set_material(mpm_diff* diff, const mpm_material* material);
 /* nsteps substeps from the initial state; writes the final x and v (either may be NULL). */
 mpm_status mpm_diff_forward(mpm_diff* diff, const float* x0, const float* v0, const float* C0, const float* F0,
